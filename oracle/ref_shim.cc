@@ -1,0 +1,172 @@
+// C entry points over the reference's own CPU classes -- TEST INFRASTRUCTURE.
+//
+// Compiled (oracle/Makefile, target "ref") together with the reference's
+// src/*.cc straight from the reference checkout, into oracle/_ref/.  It gives
+// tests/golden/make_golden.py and the pin tests the reference's own outputs
+// through the same signatures as ctr_oracle.h (prefix ref_ instead of orc_).
+// Only methods whose reference code is well defined are exposed: the
+// parallel-BP grad (src/bp_par_2d.cc:145-199, uninitialised pointers) and the
+// fan-angle grad (src/bp_fan_2d_angle.cc:124-169, uninitialised ypos) are not.
+#include <vector>
+
+#include "include/bp_fan_2d.h"
+#include "include/bp_fan_2d_angle.h"
+#include "include/bp_par_2d.h"
+#include "include/bp_par_2d_sv.h"
+#include "include/fan_weighting.h"
+#include "include/filter.h"
+#include "include/fp_par_2d.h"
+
+#include "ctr_oracle.h"
+
+using namespace ct_recon;
+
+namespace {
+
+FanBackprojection2DParam fan_param(const orc_geom* g)
+{
+    return FanBackprojection2DParam(g->ns, g->na, g->ds, g->orbit, g->offset_s, g->orbit_start,
+                                    g->nx, g->ny, g->dx, g->dy, g->offset_x, g->offset_y,
+                                    g->dso, g->dsd, g->fov);
+}
+
+FanBackprojection2DAngleParam angle_param(const orc_geom* g)
+{
+    return FanBackprojection2DAngleParam(g->ns, g->na, g->ds, g->offset_s, g->nx, g->ny, g->dx,
+                                         g->dy, g->offset_x, g->offset_y, g->dso, g->dsd,
+                                         g->fov);
+}
+
+ParallelBackprojection2DParam par_param(const orc_geom* g)
+{
+    return ParallelBackprojection2DParam(g->ns, g->na, g->ds, g->orbit, g->offset_s,
+                                         g->orbit_start, g->nx, g->ny, g->dx, g->dy,
+                                         g->offset_x, g->offset_y, g->fov);
+}
+
+ParallelSingleViewBp2DParam sv_param(const orc_geom* g)
+{
+    return ParallelSingleViewBp2DParam(g->ns, g->na, g->ds, g->orbit, g->offset_s,
+                                       g->orbit_start, g->nx, g->ny, g->dx, g->dy, g->offset_x,
+                                       g->offset_y, g->fov);
+}
+
+ParallelProjection2DParam fp_param(const orc_geom* g)
+{
+    return ParallelProjection2DParam(g->ns, g->na, g->ds, g->orbit, g->offset_s, g->orbit_start,
+                                     g->nx, g->ny, g->dx, g->dy, g->offset_x, g->offset_y,
+                                     g->fov);
+}
+
+}  // namespace
+
+#define REF_T(T, SFX)                                                                          \
+    extern "C" int ref_fan_weighting_##SFX(unsigned ns, unsigned nrow, double ds,              \
+                                           double offset, double dso, double dsd, int type,    \
+                                           const T* in, T* out)                                \
+    {                                                                                          \
+        return FanWeighting<T>(FanWeightingParam(ns, nrow, ds, offset, dso, dsd, type))        \
+            .calculate_on_cpu(in, out);                                                        \
+    }                                                                                          \
+    extern "C" int ref_fan_weighting_grad_##SFX(unsigned ns, unsigned nrow, double ds,         \
+                                                double offset, double dso, double dsd,         \
+                                                int type, const T* in, T* out)                 \
+    {                                                                                          \
+        return FanWeightingGrad<T>(FanWeightingParam(ns, nrow, ds, offset, dso, dsd, type))    \
+            .calculate_on_cpu(in, out);                                                        \
+    }                                                                                          \
+    extern "C" int ref_ramp_filter_##SFX(unsigned ns, unsigned nrow, double ds, const T* in,   \
+                                         const double* filter, T* out)                         \
+    {                                                                                          \
+        return RampFilter<T>(FilterParam(ns, nrow, ds)).calculate_on_cpu(in, filter, out);     \
+    }                                                                                          \
+    extern "C" int ref_ramp_filter_grad_##SFX(unsigned ns, unsigned nrow, double ds,           \
+                                              const T* in, const double* filter, T* out)       \
+    {                                                                                          \
+        return RampFilterGrad<T>(FilterParam(ns, nrow, ds)).calculate_on_cpu(in, filter, out); \
+    }                                                                                          \
+    extern "C" int ref_bp_fan_2d_##SFX(const orc_geom* g, const T* proj, T* img,               \
+                                       const double* xpos, const double* ypos,                 \
+                                       const double* sc)                                       \
+    {                                                                                          \
+        return FanBackprojection2DPixDriven<T>(fan_param(g))                                   \
+            .calculate_on_cpu(proj, img, xpos, ypos, sc);                                      \
+    }                                                                                          \
+    extern "C" int ref_bp_fan_2d_grad_##SFX(const orc_geom* g, const T* img, T* grad,          \
+                                            const double* xpos, const double* ypos,            \
+                                            const double* sc)                                  \
+    {                                                                                          \
+        return FanBackprojection2DPixDrivenGrad<T>(fan_param(g))                               \
+            .calculate_on_cpu(img, grad, xpos, ypos, sc);                                      \
+    }                                                                                          \
+    extern "C" int ref_bp_fan_2d_angle_##SFX(const orc_geom* g, const T* proj, T* img,         \
+                                             const double* xpos, const double* ypos,           \
+                                             const double* sc)                                 \
+    {                                                                                          \
+        return FanBackprojection2DAnglePixDriven<T>(angle_param(g))                            \
+            .calculate_on_cpu(proj, img, xpos, ypos, sc);                                      \
+    }                                                                                          \
+    extern "C" int ref_bp_par_2d_##SFX(const orc_geom* g, const T* proj, T* img,               \
+                                       const double* xcos, const double* ysin)                 \
+    {                                                                                          \
+        return ParallelBackprojection2DPixDriven<T>(par_param(g))                              \
+            .calculate_on_cpu(proj, img, xcos, ysin, nullptr);                                 \
+    }                                                                                          \
+    extern "C" int ref_bp_par_2d_sv_##SFX(const orc_geom* g, const T* proj, T* img,            \
+                                          const double* xcos, const double* ysin)              \
+    {                                                                                          \
+        return ParallelSingleViewBp2DPixDriven<T>(sv_param(g))                                 \
+            .calculate_on_cpu(proj, img, xcos, ysin, nullptr);                                 \
+    }                                                                                          \
+    extern "C" int ref_fp_par_2d_##SFX(const orc_geom* g, const T* img, T* proj,               \
+                                       const double* sc, const double* bo, const int* usex)    \
+    {                                                                                          \
+        return ParallelProjection2DRayDriven<T>(fp_param(g))                                   \
+            .calculate_on_cpu(img, proj, sc, bo, usex);                                        \
+    }                                                                                          \
+    extern "C" int ref_fp_par_2d_grad_##SFX(const orc_geom* g, const T* proj, T* img,          \
+                                            const double* weights, const double* pos,          \
+                                            const int* usex)                                   \
+    {                                                                                          \
+        return ParallelProjection2DRayDrivenGrad<T>(fp_param(g))                               \
+            .calculate_on_cpu(proj, img, weights, pos, usex);                                  \
+    }
+
+REF_T(float, f32)
+REF_T(double, f64)
+
+extern "C" int ref_ramp_filter_prep(unsigned ns, double ds, double dsd, int type,
+                                    double* filter)
+{
+    return RampFilterPrep(FilterParam(ns, 1, ds, dsd, type)).calculate_on_cpu(filter);
+}
+
+extern "C" int ref_bp_fan_2d_prep(const orc_geom* g, double* xpos, double* ypos, double* sc)
+{
+    return FanBackprojection2DPixDrivenPrep(fan_param(g)).calculate_on_cpu(xpos, ypos, sc);
+}
+
+extern "C" int ref_bp_fan_2d_angle_prep(const orc_geom* g, const double* angles, double* xpos,
+                                        double* ypos, double* sc)
+{
+    return FanBackprojection2DAnglePixDrivenPrep(angle_param(g))
+        .calculate_on_cpu(angles, xpos, ypos, sc);
+}
+
+extern "C" int ref_bp_par_2d_prep(const orc_geom* g, double* xcos, double* ysin)
+{
+    return ParallelBackprojection2DPixDrivenPrep(par_param(g)).calculate_on_cpu(xcos, ysin,
+                                                                                nullptr);
+}
+
+extern "C" int ref_fp_par_2d_prep(const orc_geom* g, double* sc, double* bo, int* usex)
+{
+    return ParallelProjection2DRayDrivenPrepare(fp_param(g)).calculate_on_cpu(sc, bo, usex);
+}
+
+extern "C" int ref_fp_par_2d_grad_prep(const orc_geom* g, double* weights, double* pos,
+                                       int* usex)
+{
+    return ParallelProjection2DRayDrivenGradPrep(fp_param(g)).calculate_on_cpu(weights, pos,
+                                                                               usex);
+}

@@ -1,0 +1,120 @@
+"""Pin the oracle port (oracle/ctr_oracle.c) to the reference's own outputs.
+
+The fixtures were produced by the reference's src/ code compiled unmodified
+(tests/golden/make_golden.py); the port must reproduce them bit for bit.  The
+two adjoints without a reference fixture are pinned by the dot test against
+their pinned forward operators.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import golden_cases as gc
+
+SFX = [("f32", np.float32), ("f64", np.float64)]
+
+
+@pytest.mark.parametrize("name", gc.names(("fan", "fan_angle")))
+@pytest.mark.parametrize("sfx,dt", SFX)
+def test_fan_chain(port, name, sfx, dt):
+    c = gc.load(name)
+    g = gc.geom(c)
+    p = c[f"sino_{sfx}"]
+    for wt in (1, 2):
+        w = port.fan_weighting(p, g.ds, g.offset_s, g.dso, g.dsd, wt)
+        assert np.array_equal(w, c[f"weighted{wt}_{sfx}"])
+        wg = port.fan_weighting(p, g.ds, g.offset_s, g.dso, g.dsd, wt, grad=True)
+        assert np.array_equal(wg, c[f"weighted{wt}_grad_{sfx}"])
+    assert np.array_equal(port.ramp_taps(g.ns, g.ds, g.dsd, 1), c["taps_fan"])
+    assert np.array_equal(port.ramp_taps(g.ns, g.ds, g.dsd, 2), c["taps_flat"])
+    filt = port.ramp_filter(c[f"weighted1_{sfx}"], g.ds, g.dsd, 1)
+    assert np.array_equal(filt, c[f"filtered_{sfx}"])
+    assert np.array_equal(port.ramp_filter(p, g.ds, g.dsd, 1, grad=True), c[f"filtered_grad_{sfx}"])
+    assert np.array_equal(port.ramp_filter(c[f"weighted2_{sfx}"], g.ds, g.dsd, 2),
+                          c[f"filtered_flat_{sfx}"])
+    if c["kind"] == "fan":
+        assert np.array_equal(port.bp_fan_2d(filt, g), c[f"bp_{sfx}"])
+        assert np.array_equal(port.bp_fan_2d_grad(c[f"img_in_{sfx}"], g), c[f"bp_grad_{sfx}"])
+    else:
+        assert np.array_equal(port.bp_fan_2d_angle(filt, g, c["angles"]), c[f"bp_{sfx}"])
+
+
+@pytest.mark.parametrize("name", gc.names("par"))
+@pytest.mark.parametrize("sfx,dt", SFX)
+def test_par_bp(port, name, sfx, dt):
+    c = gc.load(name)
+    g = gc.geom(c)
+    assert np.array_equal(port.ramp_taps(g.ns, g.ds, -1.0, 0), c["taps_par"])
+    filt = port.ramp_filter(c[f"sino_{sfx}"], g.ds, -1.0, 0)
+    assert np.array_equal(filt, c[f"filtered_{sfx}"])
+    assert np.array_equal(port.bp_par_2d(filt, g), c[f"bp_{sfx}"])
+
+
+@pytest.mark.parametrize("sfx,dt", SFX)
+def test_single_view(port, sfx, dt):
+    c = gc.load("sv")
+    g = gc.geom(c)
+    assert np.array_equal(port.bp_par_2d_sv(c[f"sino_{sfx}"], g), c[f"sv_{sfx}"])
+
+
+@pytest.mark.parametrize("name", gc.names("fp"))
+@pytest.mark.parametrize("sfx,dt", SFX)
+def test_fp_ray_driven(port, name, sfx, dt):
+    c = gc.load(name)
+    g = gc.geom(c)
+    assert np.array_equal(port.fp_par_2d(c[f"img_{sfx}"], g), c[f"fp_{sfx}"])
+    assert np.array_equal(port.fp_par_2d_grad(c[f"proj_in_{sfx}"], g), c[f"fp_grad_{sfx}"])
+
+
+def _dot_rel(a_x, y, x, at_y):
+    lhs = float(np.vdot(a_x.astype(np.float64), y.astype(np.float64)))
+    rhs = float(np.vdot(x.astype(np.float64), at_y.astype(np.float64)))
+    return abs(lhs - rhs) / abs(lhs)
+
+
+@pytest.mark.parametrize("name", gc.names("par"))
+def test_par_bp_adjoint_dot(port, name):
+    c = gc.load(name)
+    g = gc.geom(c)
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((g.na, g.ns))
+    y = rng.standard_normal((g.ny, g.nx))
+    assert _dot_rel(port.bp_par_2d(x, g), y, x, port.bp_par_2d_grad(y, g)) < 1e-12
+
+
+def test_fan_angle_adjoint_dot(port):
+    c = gc.load("fan_angle")
+    g = gc.geom(c)
+    rng = np.random.default_rng(6)
+    x = rng.standard_normal((g.na, g.ns))
+    y = rng.standard_normal((g.ny, g.nx))
+    lhs = port.bp_fan_2d_angle(x, g, c["angles"])
+    assert _dot_rel(lhs, y, x, port.bp_fan_2d_angle_grad(y, g, c["angles"])) < 1e-12
+
+
+@pytest.mark.parametrize("name", gc.names("fan"))
+def test_fan_bp_adjoint_dot(port, name):
+    c = gc.load(name)
+    g = gc.geom(c)
+    rng = np.random.default_rng(7)
+    x = rng.standard_normal((g.na, g.ns))
+    y = rng.standard_normal((g.ny, g.nx))
+    assert _dot_rel(port.bp_fan_2d(x, g), y, x, port.bp_fan_2d_grad(y, g)) < 1e-12
+
+
+def test_row_threads_identical():
+    from oracle import Oracle
+    c = gc.load("fan_full")
+    g = gc.geom(c)
+    one = Oracle("port", threads=1).bp_fan_2d(c["filtered_f32"], g)
+    many = Oracle("port", threads=7).bp_fan_2d(c["filtered_f32"], g)
+    assert np.array_equal(one, many)
+
+
+def test_invalid_types_rejected(port):
+    p = np.zeros((3, 8), np.float32)
+    with pytest.raises(ValueError):
+        port.fan_weighting(p, 1.0, 0.0, 500.0, 1000.0, 3)
+    with pytest.raises(ValueError):
+        port.ramp_taps(8, 1.0, 1000.0, 5)
