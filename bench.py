@@ -1,0 +1,559 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 CT reconstruction hot path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one step): the parallel-beam drop-in at its headline size -- a
+512x512 image at 0.5 mm is forward projected (fp_par_2d, ray-driven) to a
+720-view sinogram over pi with 729 bins at 0.5 mm, ramp filtered (par) and
+backprojected (bp_par_2d) -- on one slice (batch 1).  Steps cycle through a
+pool of distinct seeded phantom slices whose total size exceeds the 129 MB L2,
+so every step reads its input from HBM.
+
+Reported: slices/s (value) and pixel-view updates/s; ``e2e`` repeats the
+workload through the C ABI with the slice copied from pinned host memory and
+the reconstruction read back every step; ``roofline`` is the dominant
+kernel's algorithmic FP32 FLOP/s (per-launch CUDA-event durations inside the
+timed region) against the FP32 peak; ``cpu_baseline`` times the oracle port
+(the reference's CPU algorithm restated in C) on this host's cores.  The fan
+FBP at its headline size (fan weighting -> ramp(fan) -> bp_fan_2d, 720 x 736
+-> 512x512) is measured the same way and reported under ``extra``.
+
+``--impl reference`` times the reference's CPU implementation of the same
+workload on this host (the compiled reference when its build is present,
+else the oracle port), all host threads, one slice per step.
+
+Under torchrun (N > 1) every rank runs the same workload on its own GPU as an
+independent replica (no data exchange); value is the sum over ranks of the
+slices processed divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FBP slices/s and pixel-view updates/s at rel-L2<=1e-4 vs FP64; batched vs plain"
+SM_COUNT = 152
+FP32_LANES_PER_SM = 128
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--pool", type=int, default=160, help="distinct slices cycled through")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas only)
+# ---------------------------------------------------------------------------
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self, backend):
+        import torch
+        import torch.distributed as dist
+        self.ws, self.rank, self.local = dist_env()
+        self.dist = dist if self.ws > 1 else None
+        if self.dist:
+            dist.init_process_group(backend)
+        self.torch = torch
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.dist:
+            return v
+        t = self.torch.tensor([v], dtype=self.torch.float64,
+                              device="cuda" if self.dist.get_backend() == "nccl" else "cpu")
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+
+def par_geometry():
+    from ct_recon_extensions_gb300 import synthetic as syn
+    return syn.parallel_config_2()
+
+
+def fan_geometry():
+    from ct_recon_extensions_gb300 import synthetic as syn
+    return syn.fan_config_1()
+
+
+def make_pool(kind, g, n, seed0):
+    """n distinct float32 inputs (images for the parallel workload, analytic
+    sinograms for the fan workload): 16 seeded phantoms, each item a
+    distinct scaled copy."""
+    from ct_recon_extensions_gb300 import synthetic as syn
+    base = []
+    for i in range(16):
+        e = syn.random_ellipses(seed0 + i)
+        if kind == "par":
+            base.append(syn.rasterize(e, g["nx"], g["ny"], g["dx"], g["dy"]))
+        else:
+            base.append(syn.fan_sinogram(e, g["na"], g["ns"], g["ds"], g["orbit"], g["dso"], g["dsd"]))
+    return base
+
+
+class ParPipeline:
+    """fp_par_2d -> ramp(par) -> bp_par_2d through the C ABI on preallocated buffers."""
+
+    def __init__(self, g, device):
+        import torch
+        from ct_recon_extensions_gb300 import _lib
+        from ct_recon_extensions_gb300 import torch_ctrecon as tc
+        self.torch = torch
+        self.lib = _lib.load()
+        self.g = g
+        self.fp = tc.ParallelProjection2DOp(g["ns"], g["na"], g["ds"], g["orbit"], g["offset_s"],
+                                            g["orbit_start"], g["nx"], g["ny"], g["dx"], g["dy"],
+                                            g["offset_x"], g["offset_y"], g["fov"])
+        self.ramp = tc.RampFilterOp(g["ns"], g["na"], g["ds"], -1.0, 0)
+        self.bp = tc.ParallelBackprojection2DOp(g["ns"], g["na"], g["ds"], g["orbit"],
+                                                g["offset_s"], g["orbit_start"], g["nx"], g["ny"],
+                                                g["dx"], g["dy"], g["offset_x"], g["offset_y"],
+                                                g["fov"])
+        self.fpt = [ctypes.c_void_p(t.data_ptr()) for t in self.fp.tables(device)]
+        self.taps = ctypes.c_void_p(self.ramp.taps(device).data_ptr())
+        self.bpt = [ctypes.c_void_p(t.data_ptr()) for t in self.bp.tables(device)]
+        f32 = dict(dtype=torch.float32, device=device)
+        self.sino = torch.empty((g["na"], g["ns"]), **f32)
+        self.filt = torch.empty((g["na"], g["ns"]), **f32)
+        self.names = ["fp_par_2d", "ramp_filter", "bp_par_2d"]
+        # algorithmic FP32 FLOPs per launch (fixed conventions)
+        self.flops = {"fp_par_2d": 6.0 * g["na"] * g["ns"] * g["ny"],
+                      "ramp_filter": 2.0 * g["ns"] * g["na"] * g["ns"],
+                      "bp_par_2d": 9.0 * g["nx"] * g["ny"] * g["na"]}
+        self.bytes = {"fp_par_2d": 4.0 * (g["nx"] * g["ny"] + g["na"] * g["ns"]),
+                      "ramp_filter": 8.0 * g["na"] * g["ns"],
+                      "bp_par_2d": 4.0 * (g["nx"] * g["ny"] + g["na"] * g["ns"])}
+        self.updates = float(g["nx"] * g["ny"] * g["na"])
+
+    def launches(self, img, out, stream):
+        L = self.lib
+        s = ctypes.c_void_p(stream)
+        p = ctypes.byref(self.fp.p)
+        yield lambda: L.ctr_fp_par_2d_f32(p, ctypes.c_void_p(img.data_ptr()),
+                                          ctypes.c_void_p(self.sino.data_ptr()), *self.fpt, 1, s)
+        yield lambda: L.ctr_ramp_filter_f32(ctypes.byref(self.ramp.p),
+                                            ctypes.c_void_p(self.sino.data_ptr()), self.taps,
+                                            ctypes.c_void_p(self.filt.data_ptr()), 1, s)
+        yield lambda: L.ctr_bp_par_2d_f32(ctypes.byref(self.bp.p),
+                                          ctypes.c_void_p(self.filt.data_ptr()),
+                                          ctypes.c_void_p(out.data_ptr()), *self.bpt, None, 1, s)
+
+
+class FanPipeline:
+    """fan_weighting -> ramp(fan) -> bp_fan_2d through the C ABI."""
+
+    def __init__(self, g, device):
+        import torch
+        from ct_recon_extensions_gb300 import _lib
+        from ct_recon_extensions_gb300 import torch_ctrecon as tc
+        self.lib = _lib.load()
+        self.g = g
+        self.w = tc.FanWeightingOp(g["ns"], g["na"], g["ds"], g["offset_s"], g["dso"], g["dsd"], 1)
+        self.ramp = tc.RampFilterOp(g["ns"], g["na"], g["ds"], g["dsd"], 1)
+        self.bp = tc.FanBackprojection2DOp(g["ns"], g["na"], g["ds"], g["orbit"], g["offset_s"],
+                                           g["orbit_start"], g["nx"], g["ny"], g["dx"], g["dy"],
+                                           g["offset_x"], g["offset_y"], g["dso"], g["dsd"], g["fov"])
+        self.taps = ctypes.c_void_p(self.ramp.taps(device).data_ptr())
+        self.bpt = [ctypes.c_void_p(t.data_ptr()) for t in self.bp.tables(device)]
+        f32 = dict(dtype=torch.float32, device=device)
+        self.wt = torch.empty((g["na"], g["ns"]), **f32)
+        self.filt = torch.empty((g["na"], g["ns"]), **f32)
+        self.names = ["fan_weighting", "ramp_filter", "bp_fan_2d"]
+        self.flops = {"fan_weighting": 1.0 * g["na"] * g["ns"],
+                      "ramp_filter": 2.0 * g["ns"] * g["na"] * g["ns"],
+                      "bp_fan_2d": 32.0 * g["nx"] * g["ny"] * g["na"]}
+        self.bytes = {"fan_weighting": 8.0 * g["na"] * g["ns"],
+                      "ramp_filter": 8.0 * g["na"] * g["ns"],
+                      "bp_fan_2d": 4.0 * (g["nx"] * g["ny"] + g["na"] * g["ns"])}
+        self.updates = float(g["nx"] * g["ny"] * g["na"])
+
+    def launches(self, sino, out, stream):
+        L = self.lib
+        s = ctypes.c_void_p(stream)
+        yield lambda: L.ctr_fan_weighting_f32(ctypes.byref(self.w.p), ctypes.c_void_p(sino.data_ptr()),
+                                              ctypes.c_void_p(self.wt.data_ptr()), 1, s)
+        yield lambda: L.ctr_ramp_filter_f32(ctypes.byref(self.ramp.p), ctypes.c_void_p(self.wt.data_ptr()),
+                                            self.taps, ctypes.c_void_p(self.filt.data_ptr()), 1, s)
+        yield lambda: L.ctr_bp_fan_2d_f32(ctypes.byref(self.bp.p), ctypes.c_void_p(self.filt.data_ptr()),
+                                          ctypes.c_void_p(out.data_ptr()), *self.bpt, 1, s)
+
+
+def run_device(pipe, pool_dev, outs, steps, warmup, dist, per_kernel=True):
+    """Time `steps` pipeline steps on device-resident inputs; returns (seconds,
+    per-kernel mean ms, launches)."""
+    import torch
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    P = len(pool_dev)
+
+    def step(k, rec):
+        for i, fn in enumerate(pipe.launches(pool_dev[k % P], outs[k % len(outs)], sp)):
+            if rec is not None:
+                rec[i][0].record(stream)
+            st = fn()
+            if st != 0:
+                raise RuntimeError(f"{pipe.names[i]} failed: {pipe.lib.ctr_last_error().decode()}")
+            if rec is not None:
+                rec[i][1].record(stream)
+
+    for k in range(warmup):
+        step(k, None)
+    torch.cuda.synchronize()
+    ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in pipe.names] for _ in range(steps)] if per_kernel else None
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    dist.barrier()
+    torch.cuda.synchronize()
+    t0.record(stream)
+    for k in range(steps):
+        step(warmup + k, ev[k] if per_kernel else None)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    dist.barrier()
+    secs = t0.elapsed_time(t1) / 1e3
+    kern = {}
+    if per_kernel:
+        for i, n in enumerate(pipe.names):
+            kern[n] = statistics.fmean(ev[k][i][0].elapsed_time(ev[k][i][1]) for k in range(steps))
+    return secs, kern, len(pipe.names) * steps
+
+
+def run_e2e(pipe, pool_host, steps, warmup, in_shape, out_shape, device):
+    """Through the C ABI with host buffers: per step H2D of the input from
+    pinned memory, the three operators, D2H of the result, stream sync."""
+    import torch
+    stream = torch.cuda.current_stream()
+    din = torch.empty(in_shape, dtype=torch.float32, device=device)
+    dout = torch.empty(out_shape, dtype=torch.float32, device=device)
+    hout = torch.empty(out_shape, dtype=torch.float32, pin_memory=True)
+    P = len(pool_host)
+
+    def step(k):
+        din.copy_(pool_host[k % P], non_blocking=True)
+        for fn in pipe.launches(din, dout, stream.cuda_stream):
+            if fn() != 0:
+                raise RuntimeError(pipe.lib.ctr_last_error().decode())
+        hout.copy_(dout, non_blocking=True)
+        stream.synchronize()
+
+    for k in range(warmup):
+        step(k)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for k in range(steps):
+        step(warmup + k)
+    secs = time.perf_counter() - t
+    return secs, din.numel() * 4, dout.numel() * 4
+
+
+def fp32_peak_tflops(device):
+    """Measured FP32 (non-tensor) throughput: cuBLAS SGEMM with TF32 off,
+    best of 5 at 8192^3."""
+    import torch
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        n = 8192
+        a = torch.randn(n, n, device=device)
+        b = torch.randn(n, n, device=device)
+        c = a @ b
+        torch.cuda.synchronize()
+        best = math.inf
+        for _ in range(5):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b, out=c)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1) / 1e3)
+        del a, b, c
+        return 2.0 * n ** 3 / best / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
+def read_traffic():
+    """Per-launch DRAM bytes measured by ncu, from profiles/ncu_traffic.txt
+    (lines: '<kernel> <bytes per launch> <workload>')."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    out = {}
+    if os.path.exists(path):
+        for ln in open(path):
+            f = ln.split()
+            if len(f) >= 2 and not ln.startswith("#"):
+                try:
+                    out[f[0]] = float(f[1])
+                except ValueError:
+                    pass
+    return out
+
+
+# ---------------------------------------------------------------------------
+# CPU side (oracle port / reference build)
+# ---------------------------------------------------------------------------
+
+def cpu_slices_per_s(kind, g, n_slices, threads):
+    """Time the reference CPU algorithm of one step on n_slices slices."""
+    from oracle import Geom, Oracle, REF_LIB
+    from ct_recon_extensions_gb300 import synthetic as syn
+    use_ref = kind == "reference" and os.path.exists(REF_LIB)
+    gm = Geom.make(**g)
+    e = syn.random_ellipses(2000)
+    img = syn.rasterize(e, g["nx"], g["ny"], g["dx"], g["dy"])
+    if use_ref:
+        # the reference's own code is single-threaded per call: run one slice per thread
+        from concurrent.futures import ThreadPoolExecutor
+        orc = Oracle("reference")
+
+        def one(_):
+            s = orc.fp_par_2d(img, gm)
+            return orc.bp_par_2d(orc.ramp_filter(s, gm.ds, -1.0, 0), gm)
+        t = time.perf_counter()
+        with ThreadPoolExecutor(threads) as ex:
+            list(ex.map(one, range(n_slices)))
+        secs = time.perf_counter() - t
+        return n_slices / secs, "reference", threads
+    orc = Oracle("port", threads=threads)
+    t = time.perf_counter()
+    for _ in range(n_slices):
+        s = orc.fp_par_2d(img, gm)
+        orc.bp_par_2d(orc.ramp_filter(s, gm.ds, -1.0, 0), gm)
+    secs = time.perf_counter() - t
+    return n_slices / secs, "port", threads
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    try:
+        oracle.build(ref=False)
+    except Exception as e:  # pragma: no cover
+        print(json.dumps({"impl": "reference", "unavailable": f"oracle build failed: {e}"}))
+        return
+    g = par_geometry()
+    threads = os.cpu_count() or 1
+    kind = "reference" if os.path.exists(oracle.REF_LIB) else "port"
+    # warm-up steps, then `steps` timed steps of one slice each
+    for _ in range(min(args.warmup, 3)):
+        cpu_slices_per_s(kind, g, 1, threads)
+    t = time.perf_counter()
+    steps = max(1, min(args.steps, 20))
+    v, k, c = cpu_slices_per_s(kind, g, steps, threads)
+    secs = time.perf_counter() - t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "slices/s",
+        "n_gpus": ws, "steps": steps, "warmup": min(args.warmup, 3),
+        "ms_per_step": 1e3 * secs / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded random-ellipse phantom)",
+        "config": {"workload": "parallel drop-in: fp_par_2d 512x512 @0.5mm -> 720 views x 729 bins "
+                               "over pi -> ramp(par) -> bp_par_2d", "batch": 1},
+        "cpu_baseline": {"value": v, "unit": "slices/s", "cores": c, "kind": k,
+                         "sample": f"{steps} slices, one per step"},
+        "e2e": {"value": v, "unit": "slices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "updates_per_s": v * g["nx"] * g["ny"] * g["na"],
+    }
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    dist = Dist("nccl")
+    from ct_recon_extensions_gb300 import build as b
+    b.build()
+    from ct_recon_extensions_gb300 import _lib
+    lib = _lib.load()
+    if lib.ctr_device_check() != 0:
+        raise SystemExit(lib.ctr_last_error().decode())
+
+    # ---- parallel drop-in (headline) ----
+    g = par_geometry()
+    pipe = ParPipeline(g, device)
+    base = make_pool("par", g, args.pool, 2000 + 100 * rank)
+    pool_dev = [torch.from_numpy(base[i % 16] * (1.0 + 1e-3 * i)).to(device) for i in range(args.pool)]
+    outs = [torch.empty((g["ny"], g["nx"]), dtype=torch.float32, device=device) for _ in range(4)]
+
+    clk = ClockSampler(local)
+    clk.start()
+    secs, kern, launches = run_device(pipe, pool_dev, outs, args.steps, args.warmup, dist)
+    clocks = clk.stop()
+    secs = dist.max(secs)
+    value = ws * args.steps / secs
+
+    # ---- e2e through the C ABI with pinned host buffers ----
+    pool_host = [t.cpu().pin_memory() for t in pool_dev[:32]]
+    e_secs, hb, db = run_e2e(pipe, pool_host, args.steps, args.warmup, (g["ny"], g["nx"]),
+                             (g["ny"], g["nx"]), device)
+    e_secs = dist.max(e_secs)
+    e2e = {"value": ws * args.steps / e_secs, "unit": "slices/s", "h2d_bytes_per_step": hb,
+           "d2h_bytes_per_step": db}
+
+    # ---- fan FBP at its headline size (extra) ----
+    gf = fan_geometry()
+    fpipe = FanPipeline(gf, device)
+    fbase = make_pool("fan", gf, 64, 1000 + 100 * rank)
+    fpool = [torch.from_numpy(fbase[i % 16] * (1.0 + 1e-3 * i)).to(device) for i in range(64)]
+    fouts = [torch.empty((gf["ny"], gf["nx"]), dtype=torch.float32, device=device) for _ in range(4)]
+    f_secs, f_kern, f_launches = run_device(fpipe, fpool, fouts, args.steps, args.warmup, dist)
+    f_secs = dist.max(f_secs)
+
+    # ---- roofline of the dominant kernel ----
+    peak_meas = fp32_peak_tflops(device)
+    clk_max = clocks.get("sm_max_mhz") or 2070.0
+    peak_nominal = SM_COUNT * FP32_LANES_PER_SM * 2 * clk_max * 1e6 / 1e12
+    dom = max(kern, key=kern.get)
+    achieved = pipe.flops[dom] / (kern[dom] / 1e3) / 1e12
+    traffic = read_traffic()
+    plausible = peak_meas <= 1.1 * peak_nominal
+    peak = peak_meas if plausible else peak_nominal
+    roofline = {
+        "bound": "fp32", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+        "frac": achieved / peak, "traffic": traffic.get(dom),
+        "algorithmic_bytes": pipe.bytes[dom],
+        "peak_source": ("measured: cuBLAS SGEMM 8192^3, TF32 off, best of 5" if plausible else
+                        "nominal: 152 SMs x 128 FP32 lanes x 2 x max SM clock"),
+        "peak_nominal": peak_nominal,
+        "kernel_ms": kern,
+    }
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            v, k, c = cpu_slices_per_s("port", g, 2, os.cpu_count() or 1)
+            cpu = {"value": v, "unit": "slices/s", "cores": c, "kind": k,
+                   "sample": "2 slices of the same workload (fp_par_2d -> ramp -> bp_par_2d)"}
+        fdom = max(f_kern, key=f_kern.get)
+        line = {
+            "metric": METRIC, "value": value, "unit": "slices/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded random-ellipse phantoms, analytic fan sinograms)",
+            "config": {"workload": "parallel drop-in: fp_par_2d 512x512 @0.5mm -> 720 views x 729 "
+                                   "bins over pi -> ramp(par) -> bp_par_2d", "batch": 1,
+                       "pool_slices": args.pool,
+                       "l2": f"inputs larger than L2: {args.pool} distinct 1 MiB slices cycled"},
+            "updates_per_s": value * pipe.updates,
+            "gpu_launches": launches,
+            "e2e": e2e, "roofline": roofline, "clocks": clocks, "cpu_baseline": cpu,
+            "extra": {
+                "fan_fbp_config1": {
+                    "workload": "fan_weighting -> ramp(fan) -> bp_fan_2d, 720 views x 736 ch -> 512x512",
+                    "slices_per_s": ws * args.steps / f_secs,
+                    "updates_per_s": ws * args.steps / f_secs * fpipe.updates,
+                    "kernel_ms": f_kern,
+                    "dominant": fdom,
+                    "dominant_tflops": fpipe.flops[fdom] / (f_kern[fdom] / 1e3) / 1e12,
+                    "dominant_frac": fpipe.flops[fdom] / (f_kern[fdom] / 1e3) / 1e12 / peak,
+                    "gpu_launches": f_launches,
+                },
+            },
+        }
+        print(json.dumps(line))
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,79 @@
+// Shared internals of libctrecon_gb300: status plumbing, launch helpers and
+// the small device-math pieces every operator uses.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+
+#include "ctrecon_gb300.h"
+
+namespace ctr {
+
+// ---- host-side status handling -------------------------------------------
+
+// Records `msg` as this thread's last error and returns `status`.
+int fail(int status, const char* fmt, ...);
+// Maps the last launch error (cudaGetLastError) to a status.
+int check_launch(const char* what);
+// Validates the common (batch, stream) arguments and the current device.
+int check_common(int batch);
+
+inline bool bad_ptr(const void* p) { return p == nullptr; }
+
+// ---- kernel self-checks ----------------------------------------------------
+// Kernels that detect an internal inconsistency (a detector window larger
+// than its shared-memory slot) set a bit here instead of trapping; the bit is
+// readable with ctr_kernel_flags().
+enum KernelFlag : unsigned int {
+    kFlagWindowOverflow = 1u << 0,
+    kFlagQueueOverflow = 1u << 1,
+    kFlagWaitTimeout = 1u << 2,
+    kFlagMisaligned = 1u << 3,
+};
+extern __device__ unsigned int g_kernel_flags;
+
+__device__ __forceinline__ void raise_flag(unsigned int f) { atomicOr(&g_kernel_flags, f); }
+
+// ---- launch geometry --------------------------------------------------------
+constexpr int kSmCount = 152;  // GB300: 2 dies x 76 SMs
+
+inline unsigned int div_up(unsigned long long a, unsigned long long b)
+{
+    return static_cast<unsigned int>((a + b - 1) / b);
+}
+
+// ---- device math -------------------------------------------------------------
+template <typename T>
+struct DevMath;
+
+template <>
+struct DevMath<float> {
+    static __device__ __forceinline__ float atan2_(float y, float x) { return atan2f(y, x); }
+    static __device__ __forceinline__ float floor_(float x) { return floorf(x); }
+    static __device__ __forceinline__ float rcp_(float x) { return __frcp_rn(x); }
+    static __device__ __forceinline__ float abs_(float x) { return fabsf(x); }
+};
+
+template <>
+struct DevMath<double> {
+    static __device__ __forceinline__ double atan2_(double y, double x) { return atan2(y, x); }
+    static __device__ __forceinline__ double floor_(double x) { return floor(x); }
+    static __device__ __forceinline__ double rcp_(double x) { return 1.0 / x; }
+    static __device__ __forceinline__ double abs_(double x) { return fabs(x); }
+};
+
+template <typename T>
+struct Pair;
+template <>
+struct Pair<float> {
+    using type = float2;
+};
+template <>
+struct Pair<double> {
+    using type = double2;
+};
+
+}  // namespace ctr

@@ -1,0 +1,213 @@
+// Fan weighting and ramp filtering (reference src/fan_weighting.cc:19-59,
+// src/filter.cc:67-124).
+//
+// Fan weighting is an HBM-bound diagonal scaling: one thread per channel
+// computes the FP64 weight once and streams a block of rows, multiplying in
+// FP64 exactly as the reference does (results are bit-identical to its CPU
+// code for both T).
+//
+// The ramp filter is a linear (zero-padded) convolution with 2ns+1 taps.  A
+// CTA stages kRows rows and the taps in shared memory; each thread produces
+// one output column for all staged rows, so a tap load is shared by kRows
+// multiply-adds.  The reference kernels have zero even taps (k != 0); when
+// the caller's table has that structure (checked in-kernel) only the odd
+// taps are visited.  Left and right halves accumulate
+// separately, which keeps FP32 partial sums small.
+#include "ctr_common.cuh"
+
+namespace ctr {
+namespace {
+
+constexpr int kWeightThreads = 128;
+constexpr int kWeightRows = 8;
+
+template <typename T>
+__global__ void __launch_bounds__(kWeightThreads)
+    fan_weight_kernel(const T* __restrict__ in, T* __restrict__ out, unsigned ns,
+                      unsigned long long rows, double ds, double cents, double dso, double dsd,
+                      int type)
+{
+    const unsigned is = blockIdx.x * kWeightThreads + threadIdx.x;
+    if (is >= ns) return;
+    const double s = ds * (static_cast<double>(is) - cents);
+    const double w = type == 2 ? dso * fabs(cos(atan2(s, dsd))) / dsd : dso * fabs(cos(s / dsd)) / dsd;
+    const unsigned long long r0 = static_cast<unsigned long long>(blockIdx.y) * kWeightRows;
+    const unsigned long long r1 = r0 + kWeightRows < rows ? r0 + kWeightRows : rows;
+    for (unsigned long long r = r0; r < r1; ++r) {
+        const size_t k = r * ns + is;
+        out[k] = static_cast<T>(w * static_cast<double>(in[k]));
+    }
+}
+
+template <typename T>
+int launch_fan_weighting(const ctr_fan_weighting_param* p, const T* in, T* out, int batch,
+                         cudaStream_t stream)
+{
+    if (!p || bad_ptr(in) || bad_ptr(out)) return fail(CTR_ERR_INVALID_ARG, "null argument");
+    int st = check_common(batch);
+    if (st) return st;
+    if (p->type != 1 && p->type != 2)
+        return fail(CTR_ERR_INVALID_ARG, "fan weighting type %d (1 fan, 2 flat)", p->type);
+    if (p->ns < 1 || p->nrow < 1) return fail(CTR_ERR_INVALID_ARG, "empty sinogram");
+    const unsigned long long rows = static_cast<unsigned long long>(p->nrow) * batch;
+    const double cents = static_cast<double>(p->ns - 1) / 2 + p->offset;
+    dim3 grid(div_up(p->ns, kWeightThreads), div_up(rows, kWeightRows));
+    if (grid.y > 65535u) return fail(CTR_ERR_UNSUPPORTED, "too many rows for one launch");
+    fan_weight_kernel<T><<<grid, kWeightThreads, 0, stream>>>(in, out, p->ns, rows, p->ds, cents,
+                                                              p->dso, p->dsd, p->type);
+    return check_launch("fan_weighting");
+}
+
+// ---- ramp filter ---------------------------------------------------------
+
+constexpr int kFilterThreads = 256;
+constexpr int kFilterRows = 4;
+
+// Shared layout: tpos[ns] (h[+k], k = 0..ns-1), tneg[ns] (h[-k]), rows[kFilterRows][ns].
+template <typename T, bool kGrad>
+__global__ void __launch_bounds__(kFilterThreads)
+    ramp_filter_kernel(const T* __restrict__ in, const double* __restrict__ filter,
+                       T* __restrict__ out, const float* __restrict__ weight, unsigned ns,
+                       unsigned long long rows, double ds)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* tpos = reinterpret_cast<T*>(smem_raw);
+    T* tneg = tpos + ns;
+    T* xs = tneg + ns;
+    __shared__ int s_fast;
+
+    const int n = static_cast<int>(ns);
+    const double* h = filter + ns;  // h[k], k in [-ns, ns]
+    if (threadIdx.x == 0) s_fast = 1;
+    __syncthreads();
+    bool fast = true;
+    for (int k = threadIdx.x; k < n; k += kFilterThreads) {
+        // the convolution uses h[i - j]; the correlation (grad) h[j - i]
+        const double hp = kGrad ? h[-k] : h[k];
+        const double hn = kGrad ? h[k] : h[-k];
+        tpos[k] = static_cast<T>(hp * ds);
+        tneg[k] = static_cast<T>(hn * ds);
+        if (k > 0 && (k & 1) == 0 && (hp != 0.0 || hn != 0.0)) fast = false;
+    }
+    if (!fast) s_fast = 0;
+    const unsigned long long r0 = static_cast<unsigned long long>(blockIdx.x) * kFilterRows;
+    const int nr = static_cast<int>(rows - r0 < kFilterRows ? rows - r0 : kFilterRows);
+    for (int idx = threadIdx.x; idx < kFilterRows * n; idx += kFilterThreads) {
+        const int r = idx / n, j = idx - r * n;
+        T v = 0;
+        if (r < nr) {
+            v = in[(r0 + r) * ns + j];
+            if (weight) v = static_cast<T>(v * static_cast<T>(weight[j]));
+        }
+        xs[idx] = v;
+    }
+    __syncthreads();
+    const int step = s_fast ? 2 : 1;
+    for (int i = threadIdx.x; i < n; i += kFilterThreads) {
+        T left[kFilterRows], right[kFilterRows];
+#pragma unroll
+        for (int r = 0; r < kFilterRows; ++r) {
+            left[r] = 0;
+            right[r] = 0;
+        }
+        // j = i - k  (k >= 1) uses h[+k];  j = i + k uses h[-k]
+        for (int k = 1; k <= i; k += step) {
+            const T t = tpos[k];
+#pragma unroll
+            for (int r = 0; r < kFilterRows; ++r) left[r] += t * xs[r * n + i - k];
+        }
+        for (int k = 1; k < n - i; k += step) {
+            const T t = tneg[k];
+#pragma unroll
+            for (int r = 0; r < kFilterRows; ++r) right[r] += t * xs[r * n + i + k];
+        }
+        const T t0 = tpos[0];
+#pragma unroll
+        for (int r = 0; r < kFilterRows; ++r) {
+            if (r < nr) out[(r0 + r) * ns + i] = t0 * xs[r * n + i] + (left[r] + right[r]);
+        }
+    }
+}
+
+template <typename T, bool kGrad>
+int launch_ramp_filter(const ctr_filter_param* p, const T* in, const double* filter, T* out,
+                       const float* weight, int batch, cudaStream_t stream)
+{
+    if (!p || bad_ptr(in) || bad_ptr(filter) || bad_ptr(out))
+        return fail(CTR_ERR_INVALID_ARG, "null argument");
+    int st = check_common(batch);
+    if (st) return st;
+    if (p->ns < 1 || p->nrow < 1) return fail(CTR_ERR_INVALID_ARG, "empty sinogram");
+    if (in == out) return fail(CTR_ERR_INVALID_ARG, "ramp filter cannot run in place");
+    const unsigned long long rows = static_cast<unsigned long long>(p->nrow) * batch;
+    const size_t smem = sizeof(T) * static_cast<size_t>(p->ns) * (2 + kFilterRows);
+    if (smem > 200 * 1024)
+        return fail(CTR_ERR_UNSUPPORTED, "ns=%u exceeds the filter's shared-memory tile", p->ns);
+    auto kern = ramp_filter_kernel<T, kGrad>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "filter smem: %s", cudaGetErrorString(e));
+    const unsigned blocks = div_up(rows, kFilterRows);
+    kern<<<blocks, kFilterThreads, smem, stream>>>(in, filter, out, weight, p->ns, rows, p->ds);
+    return check_launch("ramp_filter");
+}
+
+}  // namespace
+
+int ramp_filter_weighted_f32(const ctr_filter_param* p, const float* in, const double* filter,
+                             float* out, const float* weight, int batch, cudaStream_t stream)
+{
+    return launch_ramp_filter<float, false>(p, in, filter, out, weight, batch, stream);
+}
+
+}  // namespace ctr
+
+using namespace ctr;
+
+extern "C" {
+
+int ctr_fan_weighting_f32(const ctr_fan_weighting_param* p, const float* in, float* out,
+                          int batch, cudaStream_t stream)
+{
+    return launch_fan_weighting<float>(p, in, out, batch, stream);
+}
+int ctr_fan_weighting_f64(const ctr_fan_weighting_param* p, const double* in, double* out,
+                          int batch, cudaStream_t stream)
+{
+    return launch_fan_weighting<double>(p, in, out, batch, stream);
+}
+// The reference's grad applies the same diagonal weight (src/fan_weighting.cc:40-59).
+int ctr_fan_weighting_grad_f32(const ctr_fan_weighting_param* p, const float* in, float* out,
+                               int batch, cudaStream_t stream)
+{
+    return launch_fan_weighting<float>(p, in, out, batch, stream);
+}
+int ctr_fan_weighting_grad_f64(const ctr_fan_weighting_param* p, const double* in,
+                               double* out, int batch, cudaStream_t stream)
+{
+    return launch_fan_weighting<double>(p, in, out, batch, stream);
+}
+
+int ctr_ramp_filter_f32(const ctr_filter_param* p, const float* in, const double* filter,
+                        float* out, int batch, cudaStream_t stream)
+{
+    return launch_ramp_filter<float, false>(p, in, filter, out, nullptr, batch, stream);
+}
+int ctr_ramp_filter_f64(const ctr_filter_param* p, const double* in, const double* filter,
+                        double* out, int batch, cudaStream_t stream)
+{
+    return launch_ramp_filter<double, false>(p, in, filter, out, nullptr, batch, stream);
+}
+int ctr_ramp_filter_grad_f32(const ctr_filter_param* p, const float* in, const double* filter,
+                             float* out, int batch, cudaStream_t stream)
+{
+    return launch_ramp_filter<float, true>(p, in, filter, out, nullptr, batch, stream);
+}
+int ctr_ramp_filter_grad_f64(const ctr_filter_param* p, const double* in,
+                             const double* filter, double* out, int batch,
+                             cudaStream_t stream)
+{
+    return launch_ramp_filter<double, true>(p, in, filter, out, nullptr, batch, stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,501 @@
+"""PyTorch front end of the GB300 CT reconstruction path.
+
+Mirrors the reference's TensorFlow front end (python/tf_ctrecon.py): the same
+function names, argument names, defaults and tensor layout (NHWC with C = 1,
+i.e. [batch, height, width, 1]; [batch, H, W] and [H, W] are accepted too),
+and the same gradient wiring (tf_ctrecon.py:29-108): every forward operator
+is a ``torch.autograd.Function`` whose backward runs the operator's
+hand-written adjoint kernel.
+
+Each distinct set of attributes builds one operator object that owns its
+FP64 geometry tables on the device, as the reference's TF op kernels keep
+persistent buffers (tensorflow/bp_fan_2d_ops.cu:167-169).  Computation goes
+through the C ABI of libctrecon_gb300.so on the current CUDA stream;
+float32 tensors take the FP32 kernels, float64 tensors the FP64 kernels.
+There is no CPU implementation: CPU tensors are rejected.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from functools import lru_cache
+
+import torch
+
+from . import _lib
+from ._lib import (FanBpAngleParam, FanBpParam, FanWeightingParam, FilterParam, ParParam,
+                   call)
+
+_FILTER_TYPES = {"par": 0, "fan": 1, "flat": 2}
+_WEIGHT_TYPES = {"fan": 1, "flat": 2}
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t: torch.Tensor):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _sfx(t: torch.Tensor) -> str:
+    if t.dtype == torch.float32:
+        return "f32"
+    if t.dtype == torch.float64:
+        return "f64"
+    raise TypeError(f"ct_recon operators take float32 or float64 tensors, got {t.dtype}")
+
+
+def _as_batch(x: torch.Tensor, h: int, w: int, what: str):
+    """[B,H,W,1] / [B,H,W] / [H,W] -> contiguous [B,H,W] and a function that
+    restores the caller's layout for an output of shape [B,h2,w2]."""
+    if not x.is_cuda:
+        raise ValueError(f"{what}: input must be a CUDA tensor (no CPU implementation)")
+    shape = tuple(x.shape)
+    if x.dim() == 4:
+        if shape[3] != 1:
+            raise ValueError(f"{what}: channel dimension must be 1, got {shape}")
+        xb = x.reshape(shape[0], shape[1], shape[2])
+        restore = lambda y: y.unsqueeze(-1)  # noqa: E731
+    elif x.dim() == 3:
+        xb = x
+        restore = lambda y: y  # noqa: E731
+    elif x.dim() == 2:
+        xb = x.unsqueeze(0)
+        restore = lambda y: y[0]  # noqa: E731
+    else:
+        raise ValueError(f"{what}: expected [B,H,W,1], [B,H,W] or [H,W], got {shape}")
+    if xb.shape[1] != h or xb.shape[2] != w:
+        raise ValueError(f"{what}: expected height {h} and width {w}, got {shape}")
+    return xb.contiguous(), restore
+
+
+class _Tables:
+    """Device FP64 tables of one operator, built once per device."""
+
+    def __init__(self):
+        self._per_device = {}
+
+    def get(self, device, build):
+        key = device.index if device.index is not None else torch.cuda.current_device()
+        t = self._per_device.get(key)
+        if t is None:
+            with torch.cuda.device(key):
+                t = build(torch.device("cuda", key))
+            self._per_device[key] = t
+        return t
+
+
+# ---------------------------------------------------------------------------
+# operator objects
+# ---------------------------------------------------------------------------
+
+class FanWeightingOp:
+    """FanWeighting / FanWeightingGrad (reference include/fan_weighting.h)."""
+
+    def __init__(self, ns, nrow, ds, offset=0.0, dso=-1.0, dsd=-1.0, type=1):
+        if type not in (1, 2):
+            raise ValueError("fan weighting type must be 1 ('fan') or 2 ('flat')")
+        self.p = FanWeightingParam(ns, nrow, ds, offset, dso, dsd, type)
+        self.ns, self.nrow = ns, nrow
+
+    def _run(self, name, x):
+        xb, restore = _as_batch(x, self.nrow, self.ns, name)
+        out = torch.empty_like(xb)
+        call(f"ctr_{name}_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(out), xb.shape[0],
+             _stream())
+        return restore(out)
+
+    def forward(self, x):
+        return self._run("fan_weighting", x)
+
+    def adjoint(self, y):
+        return self._run("fan_weighting_grad", y)
+
+
+class RampFilterOp:
+    """RampFilterPrep + RampFilter / RampFilterGrad (reference include/filter.h)."""
+
+    def __init__(self, ns, nrow, ds, dsd=-1.0, type=0, window=0):
+        if type not in (0, 1, 2):
+            raise ValueError("ramp filter type must be 0 ('par'), 1 ('fan') or 2 ('flat')")
+        self.p = FilterParam(ns, nrow, ds, dsd, type, window)
+        self.ns, self.nrow = ns, nrow
+        self._tables = _Tables()
+
+    def taps(self, device):
+        def build(dev):
+            f = torch.empty(2 * self.ns + 1, dtype=torch.float64, device=dev)
+            call("ctr_ramp_filter_prep", ctypes.byref(self.p), _ptr(f), _stream())
+            return f
+        return self._tables.get(device, build)
+
+    def _run(self, name, x):
+        xb, restore = _as_batch(x, self.nrow, self.ns, name)
+        out = torch.empty_like(xb)
+        call(f"ctr_{name}_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(self.taps(xb.device)),
+             _ptr(out), xb.shape[0], _stream())
+        return restore(out)
+
+    def forward(self, x):
+        return self._run("ramp_filter", x)
+
+    def adjoint(self, y):
+        return self._run("ramp_filter_grad", y)
+
+
+class FanBackprojection2DOp:
+    """FanBackprojection2DPixDriven{Prep,,GradPrep,Grad} (reference
+    include/bp_fan_2d.h:151-225)."""
+
+    def __init__(self, ns, na, ds, orbit, offset_s, orbit_start, nx, ny, dx, dy, offset_x,
+                 offset_y, dso, dsd, fov=-1.0):
+        self.p = FanBpParam(ns, na, ds, orbit, offset_s, orbit_start, nx, ny, dx, dy, offset_x,
+                            offset_y, dso, dsd, fov)
+        self.ns, self.na, self.nx, self.ny = ns, na, nx, ny
+        self._tables = _Tables()
+
+    def tables(self, device):
+        def build(dev):
+            xpos = torch.empty(self.nx, dtype=torch.float64, device=dev)
+            ypos = torch.empty(self.ny, dtype=torch.float64, device=dev)
+            sc = torch.empty(2 * self.na, dtype=torch.float64, device=dev)
+            call("ctr_bp_fan_2d_prep", ctypes.byref(self.p), _ptr(xpos), _ptr(ypos), _ptr(sc),
+                 _stream())
+            return xpos, ypos, sc
+        return self._tables.get(device, build)
+
+    _fwd, _adj = "bp_fan_2d", "bp_fan_2d_grad"
+
+    def forward(self, proj):
+        xb, restore = _as_batch(proj, self.na, self.ns, self._fwd)
+        img = torch.empty((xb.shape[0], self.ny, self.nx), dtype=xb.dtype, device=xb.device)
+        t = self.tables(xb.device)
+        call(f"ctr_{self._fwd}_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(img),
+             *map(_ptr, t), xb.shape[0], _stream())
+        return restore(img)
+
+    def adjoint(self, img):
+        xb, restore = _as_batch(img, self.ny, self.nx, self._adj)
+        grad = torch.empty((xb.shape[0], self.na, self.ns), dtype=xb.dtype, device=xb.device)
+        t = self.tables(xb.device)
+        call(f"ctr_{self._adj}_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(grad),
+             *map(_ptr, t), xb.shape[0], _stream())
+        return restore(grad)
+
+
+class FanBackprojection2DAngleOp(FanBackprojection2DOp):
+    """FanBackprojection2DAnglePixDriven{Prep,} (reference include/bp_fan_2d_angle.h):
+    explicit view angles, no output scale."""
+
+    _fwd, _adj = "bp_fan_2d_angle", "bp_fan_2d_angle_grad"
+
+    def __init__(self, angles, ns, ds, offset_s, nx, ny, dx, dy, offset_x, offset_y, dso, dsd,
+                 fov=-1.0):
+        angles = torch.as_tensor(angles, dtype=torch.float64).flatten().cpu()
+        na = int(angles.numel())
+        self.angles = angles
+        self.p = FanBpAngleParam(ns, na, ds, offset_s, nx, ny, dx, dy, offset_x, offset_y, dso,
+                                 dsd, fov)
+        self.ns, self.na, self.nx, self.ny = ns, na, nx, ny
+        self._tables = _Tables()
+
+    def tables(self, device):
+        def build(dev):
+            ang = self.angles.to(dev)
+            xpos = torch.empty(self.nx, dtype=torch.float64, device=dev)
+            ypos = torch.empty(self.ny, dtype=torch.float64, device=dev)
+            sc = torch.empty(2 * self.na, dtype=torch.float64, device=dev)
+            call("ctr_bp_fan_2d_angle_prep", ctypes.byref(self.p), _ptr(ang), _ptr(xpos),
+                 _ptr(ypos), _ptr(sc), _stream())
+            return xpos, ypos, sc
+        return self._tables.get(device, build)
+
+
+class ParallelBackprojection2DOp:
+    """ParallelBackprojection2DPixDriven (reference include/bp_par_2d.h) and its
+    exact adjoint."""
+
+    def __init__(self, ns, na, ds, orbit, offset_s, orbit_start, nx, ny, dx, dy, offset_x,
+                 offset_y, fov=-1.0):
+        self.p = ParParam(ns, na, ds, orbit, offset_s, orbit_start, nx, ny, dx, dy, offset_x,
+                          offset_y, fov)
+        self.ns, self.na, self.nx, self.ny = ns, na, nx, ny
+        self._tables = _Tables()
+
+    def tables(self, device):
+        def build(dev):
+            xcos = torch.empty((self.nx, self.na), dtype=torch.float64, device=dev)
+            ysin = torch.empty((self.ny, self.na), dtype=torch.float64, device=dev)
+            call("ctr_bp_par_2d_prep", ctypes.byref(self.p), _ptr(xcos), _ptr(ysin), None,
+                 _stream())
+            return xcos, ysin
+        return self._tables.get(device, build)
+
+    def forward(self, proj):
+        xb, restore = _as_batch(proj, self.na, self.ns, "bp_par_2d")
+        img = torch.empty((xb.shape[0], self.ny, self.nx), dtype=xb.dtype, device=xb.device)
+        xcos, ysin = self.tables(xb.device)
+        call(f"ctr_bp_par_2d_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(img), _ptr(xcos),
+             _ptr(ysin), None, xb.shape[0], _stream())
+        return restore(img)
+
+    def adjoint(self, img):
+        xb, restore = _as_batch(img, self.ny, self.nx, "bp_par_2d_grad")
+        grad = torch.empty((xb.shape[0], self.na, self.ns), dtype=xb.dtype, device=xb.device)
+        xcos, ysin = self.tables(xb.device)
+        call(f"ctr_bp_par_2d_grad_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(grad),
+             _ptr(xcos), _ptr(ysin), xb.shape[0], _stream())
+        return restore(grad)
+
+    def single_view(self, proj):
+        """ParallelSingleViewBp2DPixDriven: [B,na,ns] -> [B,ny,nx,na]."""
+        xb, _ = _as_batch(proj, self.na, self.ns, "bp_par_2d_sv")
+        img = torch.empty((xb.shape[0], self.ny, self.nx, self.na), dtype=xb.dtype,
+                          device=xb.device)
+        xcos, ysin = self.tables(xb.device)
+        call(f"ctr_bp_par_2d_sv_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(img),
+             _ptr(xcos), _ptr(ysin), None, xb.shape[0], _stream())
+        return img
+
+
+class ParallelProjection2DOp:
+    """ParallelProjection2DRayDriven{Prepare,,GradPrep,Grad} (reference
+    include/fp_par_2d.h:209-278)."""
+
+    def __init__(self, ns, na, ds, orbit, offset_s, orbit_start, nx, ny, dx, dy, offset_x,
+                 offset_y, fov=-1.0, method="raydriven"):
+        if method != "raydriven":
+            raise ValueError(f"projection method {method!r}: only 'raydriven' is implemented")
+        if nx != ny:
+            raise ValueError("Image should have same width and height for raydriven projection.")
+        self.p = ParParam(ns, na, ds, orbit, offset_s, orbit_start, nx, ny, dx, dy, offset_x,
+                          offset_y, fov)
+        self.ns, self.na, self.nx, self.ny = ns, na, nx, ny
+        self._fwd_tables = _Tables()
+        self._adj_tables = _Tables()
+
+    def tables(self, device):
+        def build(dev):
+            sc = torch.empty((self.na, 2), dtype=torch.float64, device=dev)
+            bo = torch.empty((self.na, self.ns, 2), dtype=torch.float64, device=dev)
+            ux = torch.empty(self.na, dtype=torch.int32, device=dev)
+            call("ctr_fp_par_2d_prep", ctypes.byref(self.p), _ptr(sc), _ptr(bo), _ptr(ux),
+                 _stream())
+            return sc, bo, ux
+        return self._fwd_tables.get(device, build)
+
+    def grad_tables(self, device):
+        def build(dev):
+            w = torch.empty(self.na, dtype=torch.float64, device=dev)
+            pos = torch.empty((self.na, self.nx, 2), dtype=torch.float64, device=dev)
+            ux = torch.empty(self.na, dtype=torch.int32, device=dev)
+            call("ctr_fp_par_2d_grad_prep", ctypes.byref(self.p), _ptr(w), _ptr(pos), _ptr(ux),
+                 _stream())
+            return w, pos, ux
+        return self._adj_tables.get(device, build)
+
+    def forward(self, img):
+        xb, restore = _as_batch(img, self.ny, self.nx, "fp_par_2d")
+        proj = torch.empty((xb.shape[0], self.na, self.ns), dtype=xb.dtype, device=xb.device)
+        call(f"ctr_fp_par_2d_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(proj),
+             *map(_ptr, self.tables(xb.device)), xb.shape[0], _stream())
+        return restore(proj)
+
+    def adjoint(self, proj):
+        xb, restore = _as_batch(proj, self.na, self.ns, "fp_par_2d_grad")
+        img = torch.empty((xb.shape[0], self.ny, self.nx), dtype=xb.dtype, device=xb.device)
+        call(f"ctr_fp_par_2d_grad_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(img),
+             *map(_ptr, self.grad_tables(xb.device)), xb.shape[0], _stream())
+        return restore(img)
+
+
+# ---------------------------------------------------------------------------
+# autograd: forward op + adjoint kernel as backward
+# ---------------------------------------------------------------------------
+
+class _LinearOp(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, op):
+        ctx.op = op
+        return op.forward(x)
+
+    @staticmethod
+    def backward(ctx, g):
+        return ctx.op.adjoint(g.contiguous()), None
+
+
+class _AdjointOp(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, op):
+        ctx.op = op
+        return op.adjoint(x)
+
+    @staticmethod
+    def backward(ctx, g):
+        return ctx.op.forward(g.contiguous()), None
+
+
+def apply(op, x):
+    """Differentiable forward of an operator object."""
+    return _LinearOp.apply(x, op)
+
+
+def apply_adjoint(op, x):
+    """Differentiable adjoint of an operator object."""
+    return _AdjointOp.apply(x, op)
+
+
+# ---------------------------------------------------------------------------
+# tf_ctrecon.py-compatible functions (attributes are (y, x) ordered there)
+# ---------------------------------------------------------------------------
+
+@lru_cache(maxsize=256)
+def _fan_weighting_op(ns, nrow, ds, offset, dso, dsd, tp):
+    return FanWeightingOp(ns, nrow, ds, offset, dso, dsd, _WEIGHT_TYPES[tp])
+
+
+@lru_cache(maxsize=256)
+def _ramp_op(ns, nrow, ds, dsd, ftype):
+    return RampFilterOp(ns, nrow, ds, dsd, _FILTER_TYPES[ftype])
+
+
+@lru_cache(maxsize=256)
+def _fan_bp_op(*args):
+    return FanBackprojection2DOp(*args)
+
+
+@lru_cache(maxsize=256)
+def _par_bp_op(*args):
+    return ParallelBackprojection2DOp(*args)
+
+
+@lru_cache(maxsize=256)
+def _par_fp_op(*args):
+    return ParallelProjection2DOp(*args)
+
+
+def _par_args(img_shape, img_space, img_offset, proj_shape, channel_space, channel_offset,
+              orbit_start, orbit, fov):
+    # reference tensorflow/bp_par_2d_ops.cu: (nx, ny) = (img_shape[1], img_shape[0])
+    return (int(proj_shape[1]), int(proj_shape[0]), float(channel_space), float(orbit),
+            float(channel_offset), float(orbit_start), int(img_shape[1]), int(img_shape[0]),
+            float(img_space[1]), float(img_space[0]), float(img_offset[1]), float(img_offset[0]),
+            float(fov))
+
+
+def ramp_filter(proj, n_channel, n_row, channel_space, dsd=-1, type="par", window="None"):
+    """Ramp filter (tf_ctrecon.py:112-129); differentiable, backward = correlation."""
+    if type not in _FILTER_TYPES:
+        raise ValueError("Unrecognised geometry type. Only par, fan or flat are available for ramp filter.")
+    return apply(_ramp_op(int(n_channel), int(n_row), float(channel_space), float(dsd), type), proj)
+
+
+def ramp_filter_grad(grad_in, n_channel, n_row, channel_space, dsd=-1, type="par", window="None"):
+    return apply_adjoint(_ramp_op(int(n_channel), int(n_row), float(channel_space), float(dsd), type),
+                         grad_in)
+
+
+def fan_weighting(proj, proj_shape, channel_space, channel_offset=0, dso=1000, dsd=1500, tp="fan"):
+    """Fan / flat pre-weighting (tf_ctrecon.py:268-281)."""
+    if tp not in _WEIGHT_TYPES:
+        raise ValueError("fan weighting tp must be 'fan' or 'flat'")
+    op = _fan_weighting_op(int(proj_shape[1]), int(proj_shape[0]), float(channel_space),
+                           float(channel_offset), float(dso), float(dsd), tp)
+    return apply(op, proj)
+
+
+def fan_weighting_grad(grad_in, proj_shape, channel_space, channel_offset=0, dso=1000, dsd=1500,
+                       tp="fan"):
+    op = _fan_weighting_op(int(proj_shape[1]), int(proj_shape[0]), float(channel_space),
+                           float(channel_offset), float(dso), float(dsd), tp)
+    return apply_adjoint(op, grad_in)
+
+
+def parallel_backprojection_2d(proj, img_shape, img_space, proj_shape, channel_space,
+                               img_offset=(0, 0), channel_offset=0, orbit_start=0,
+                               orbit=math.pi / 180, fov=-1, method="pixdriven"):
+    """Pixel-driven parallel BP (tf_ctrecon.py:149-170)."""
+    if method != "pixdriven":
+        raise ValueError("Unrecognised backprojection method. Only pixdriven is available now.")
+    op = _par_bp_op(*_par_args(img_shape, img_space, img_offset, proj_shape, channel_space,
+                               channel_offset, orbit_start, orbit, fov))
+    return apply(op, proj)
+
+
+def parallel_backprojection_2d_grad(grad_in, img_shape, img_space, proj_shape, channel_space,
+                                    img_offset=(0, 0), channel_offset=0, orbit_start=0,
+                                    orbit=math.pi / 180, fov=-1, method="pixdriven"):
+    op = _par_bp_op(*_par_args(img_shape, img_space, img_offset, proj_shape, channel_space,
+                               channel_offset, orbit_start, orbit, fov))
+    return apply_adjoint(op, grad_in)
+
+
+def parallel_projection_2d(img, img_shape, img_space, proj_shape, channel_space,
+                           img_offset=(0, 0), channel_offset=0, orbit_start=0,
+                           orbit=math.pi / 180, fov=-1, method="raydriven"):
+    """Ray-driven parallel forward projection (tf_ctrecon.py:173-195)."""
+    op = _par_fp_op(*_par_args(img_shape, img_space, img_offset, proj_shape, channel_space,
+                               channel_offset, orbit_start, orbit, fov), method)
+    return apply(op, img)
+
+
+def parallel_projection_2d_grad(grad_in, img_shape, img_space, proj_shape, channel_space,
+                                img_offset=(0, 0), channel_offset=0, orbit_start=0,
+                                orbit=math.pi / 180, fov=-1, method="raydriven"):
+    op = _par_fp_op(*_par_args(img_shape, img_space, img_offset, proj_shape, channel_space,
+                               channel_offset, orbit_start, orbit, fov), method)
+    return apply_adjoint(op, grad_in)
+
+
+def parallel_single_view_bp_2d(proj, img_shape, img_space, proj_shape, channel_space,
+                               img_offset=(0, 0), channel_offset=0, orbit_start=0,
+                               orbit=math.pi / 180, fov=-1, method="pixdriven"):
+    """Single-view BP (tf_ctrecon.py:198-219): [B,na,ns(,1)] -> [B,ny,nx,na]."""
+    if method != "pixdriven":
+        raise ValueError("Unrecognised backprojection method. Only pixdriven is available now.")
+    op = _par_bp_op(*_par_args(img_shape, img_space, img_offset, proj_shape, channel_space,
+                               channel_offset, orbit_start, orbit, fov))
+    return op.single_view(proj)
+
+
+def _fan_args(img_shape, img_space, img_offset, proj_shape, channel_space, channel_offset,
+              orbit_start, orbit, dso, dsd, fov):
+    # reference tensorflow/bp_fan_2d_ops.cu:156-159
+    return (int(proj_shape[1]), int(proj_shape[0]), float(channel_space), float(orbit),
+            float(channel_offset), float(orbit_start), int(img_shape[1]), int(img_shape[0]),
+            float(img_space[1]), float(img_space[0]), float(img_offset[1]), float(img_offset[0]),
+            float(dso), float(dsd), float(fov))
+
+
+def fan_backprojection_2d(proj, img_shape, img_space, proj_shape, channel_space,
+                          img_offset=(0, 0), channel_offset=0, orbit_start=0,
+                          orbit=math.pi / 180, dso=1000, dsd=1500, fov=-1, method="pixdriven"):
+    """Pixel-driven fan BP (tf_ctrecon.py:221-244)."""
+    if method != "pixdriven":
+        raise ValueError("Unrecognised backprojection method. Only pixdriven is available for fan geometry now.")
+    op = _fan_bp_op(*_fan_args(img_shape, img_space, img_offset, proj_shape, channel_space,
+                               channel_offset, orbit_start, orbit, dso, dsd, fov))
+    return apply(op, proj)
+
+
+def fan_backprojection_2d_grad(grad_in, img_shape, img_space, proj_shape, channel_space,
+                               img_offset=(0, 0), channel_offset=0, orbit_start=0,
+                               orbit=math.pi / 180, dso=1000, dsd=1500, fov=-1,
+                               method="pixdriven"):
+    """Adjoint of fan_backprojection_2d (tf_ctrecon.py:246-266)."""
+    op = _fan_bp_op(*_fan_args(img_shape, img_space, img_offset, proj_shape, channel_space,
+                               channel_offset, orbit_start, orbit, dso, dsd, fov))
+    return apply_adjoint(op, grad_in)
+
+
+def fan_backprojection_2d_angle(proj, angles, img_shape, img_space, proj_shape, channel_space,
+                                img_offset=(0, 0), channel_offset=0, dso=1000, dsd=1500, fov=-1):
+    """Fan BP over an explicit angle list, unscaled (the reference's numpy
+    FanFBP2DAngle path, numpy_ext/np_ctrecon.py:66-99)."""
+    op = FanBackprojection2DAngleOp(angles, int(proj_shape[1]), float(channel_space),
+                                    float(channel_offset), int(img_shape[1]), int(img_shape[0]),
+                                    float(img_space[1]), float(img_space[0]),
+                                    float(img_offset[1]), float(img_offset[0]), float(dso),
+                                    float(dsd), float(fov))
+    return apply(op, proj)

@@ -1,0 +1,232 @@
+/*
+ * ctrecon_gb300 -- C ABI of the GB300 (sm_103a) CT reconstruction hot path.
+ *
+ * Drop-in boundary for the filtered-backprojection / projection path of
+ * CT_RECON_EXTENSIONS.  Every entry point replaces one GPU method of the
+ * reference's operator API (the headers under its include/) with the same buffers and the
+ * same meaning: the caller owns every buffer (input, output, geometry tables),
+ * all pointers are device pointers unless stated otherwise, images are
+ * [ny][nx] (row 0 on top), sinograms [na][ns] (view-major).
+ *
+ * Differences from the reference's GPU methods, by design:
+ *   - the return value is a status code (CTR_OK == 0) instead of bool, and no
+ *     C++ exception ever crosses this boundary;
+ *   - work is stream-ordered on the given stream; entry points do not call
+ *     cudaDeviceSynchronize (the C++ mirror classes in include/ct_recon/ add
+ *     the blocking semantics of the reference methods);
+ *   - results follow the reference's CPU code where its GPU code diverges
+ *     (fan weighting offset and grad weight, single-view BP, ray-driven edge
+ *     test);
+ *   - *_f32 entry points compute in FP32 (geometry tables are read in FP64 and
+ *     rounded once); *_f64 entry points compute in FP64.
+ *
+ * A batch of B independent items with the same geometry is passed with
+ * `batch` = B; item b lives at in + b*in_size, out + b*out_size.
+ */
+#ifndef CTRECON_GB300_H
+#define CTRECON_GB300_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <cuda_runtime_api.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ----------------------------------------------------- */
+#define CTR_OK 0
+#define CTR_ERR_INVALID_ARG 1  /* bad size, pointer, type or method       */
+#define CTR_ERR_UNSUPPORTED 2  /* valid request this build does not handle */
+#define CTR_ERR_CUDA 3         /* a CUDA runtime call failed               */
+#define CTR_ERR_DEVICE 4       /* no sm_103 device / kernel image missing   */
+#define CTR_ERR_KERNEL 5       /* a kernel reported an internal check       */
+
+const char* ctr_status_string(int status);
+/* Message of the last failing call on this host thread ("" if none). */
+const char* ctr_last_error(void);
+/* Library version, major*10000 + minor*100 + patch. */
+int ctr_version(void);
+/* CTR_OK when the current device is a compute-capability 10.3 GPU that can
+ * run this library's kernels. */
+int ctr_device_check(void);
+/* Reads (and optionally clears) the kernel self-check flags: bit 0 = a
+ * detector window wider than its shared-memory slot, bit 1 = work-queue
+ * overflow, bit 2 = a bounded wait gave up, bit 3 = a copy destination
+ * failed its alignment check (the kernel then skips its work).  Synchronises
+ * the device. */
+int ctr_kernel_flags(unsigned int* flags, int reset);
+
+/* ---- parameter structs (field order of the reference Param structs) ---- */
+
+/* FanWeightingParam, reference include/fan_weighting.h:21-39 */
+typedef struct ctr_fan_weighting_param {
+    unsigned int ns, nrow;
+    double ds, offset, dso, dsd;
+    int type; /* 1 "fan" (equiangular), 2 "flat" */
+} ctr_fan_weighting_param;
+
+/* FilterParam, reference include/filter.h:21-36 */
+typedef struct ctr_filter_param {
+    unsigned int ns, nrow;
+    double ds, dsd;
+    int type;   /* 0 "par", 1 "fan", 2 "flat" */
+    int window; /* unused, as in the reference */
+} ctr_filter_param;
+
+/* FanBackprojection2DParam, reference include/bp_fan_2d.h:20-58 */
+typedef struct ctr_fan_bp_param {
+    unsigned int ns, na;
+    double ds, orbit, offset_s, orbit_start;
+    unsigned int nx, ny;
+    double dx, dy, offset_x, offset_y, dso, dsd, fov;
+} ctr_fan_bp_param;
+
+/* FanBackprojection2DAngleParam, reference include/bp_fan_2d_angle.h:20-55 */
+typedef struct ctr_fan_bp_angle_param {
+    unsigned int ns, na;
+    double ds, offset_s;
+    unsigned int nx, ny;
+    double dx, dy, offset_x, offset_y, dso, dsd, fov;
+} ctr_fan_bp_angle_param;
+
+/* ParallelBackprojection2DParam / ParallelSingleViewBp2DParam /
+ * ParallelProjection2DParam (identical layouts), reference
+ * include/bp_par_2d.h:20-55, include/bp_par_2d_sv.h:19-54,
+ * include/fp_par_2d.h:20-55 */
+typedef struct ctr_par_param {
+    unsigned int ns, na;
+    double ds, orbit, offset_s, orbit_start;
+    unsigned int nx, ny;
+    double dx, dy, offset_x, offset_y, fov;
+} ctr_par_param;
+
+/* ---- fan weighting: FanWeighting<T> / FanWeightingGrad<T>::calculate_on_gpu
+ *      (reference include/fan_weighting.h:41-77).  in == out is allowed. ---- */
+int ctr_fan_weighting_f32(const ctr_fan_weighting_param* p, const float* in, float* out,
+                          int batch, cudaStream_t stream);
+int ctr_fan_weighting_f64(const ctr_fan_weighting_param* p, const double* in, double* out,
+                          int batch, cudaStream_t stream);
+int ctr_fan_weighting_grad_f32(const ctr_fan_weighting_param* p, const float* in, float* out,
+                               int batch, cudaStream_t stream);
+int ctr_fan_weighting_grad_f64(const ctr_fan_weighting_param* p, const double* in,
+                               double* out, int batch, cudaStream_t stream);
+
+/* ---- ramp filter (reference include/filter.h:38-92) ----
+ * filter: device double[2*ns+1], tap n at filter[n+ns] (RampFilterPrep).
+ * RampFilter<T>: linear convolution out[r][i] = ds * sum_j in[r][j]*h[i-j];
+ * RampFilterGrad<T>: the correlation (its adjoint).  in != out. */
+int ctr_ramp_filter_prep(const ctr_filter_param* p, double* filter, cudaStream_t stream);
+int ctr_ramp_filter_f32(const ctr_filter_param* p, const float* in, const double* filter,
+                        float* out, int batch, cudaStream_t stream);
+int ctr_ramp_filter_f64(const ctr_filter_param* p, const double* in, const double* filter,
+                        double* out, int batch, cudaStream_t stream);
+int ctr_ramp_filter_grad_f32(const ctr_filter_param* p, const float* in, const double* filter,
+                             float* out, int batch, cudaStream_t stream);
+int ctr_ramp_filter_grad_f64(const ctr_filter_param* p, const double* in,
+                             const double* filter, double* out, int batch,
+                             cudaStream_t stream);
+
+/* ---- fan-beam pixel-driven backprojection, uniform orbit
+ *      (reference include/bp_fan_2d.h:151-225) ----
+ * Tables (FanBackprojection2DPixDrivenPrep / ...GradPrep): xpos double[nx],
+ * ypos double[ny], sincostbl double[2*na] = (sin b, cos b) per view.
+ * Forward: proj [na][ns] -> img [ny][nx], scaled by |orbit| / round(|na*orbit|/pi).
+ * Grad: the exact adjoint, img [ny][nx] -> grad [na][ns]. */
+int ctr_bp_fan_2d_prep(const ctr_fan_bp_param* p, double* xpos, double* ypos,
+                       double* sincostbl, cudaStream_t stream);
+int ctr_bp_fan_2d_f32(const ctr_fan_bp_param* p, const float* proj, float* img,
+                      const double* xpos, const double* ypos, const double* sincostbl,
+                      int batch, cudaStream_t stream);
+int ctr_bp_fan_2d_f64(const ctr_fan_bp_param* p, const double* proj, double* img,
+                      const double* xpos, const double* ypos, const double* sincostbl,
+                      int batch, cudaStream_t stream);
+int ctr_bp_fan_2d_grad_f32(const ctr_fan_bp_param* p, const float* img, float* grad,
+                           const double* xpos, const double* ypos, const double* sincostbl,
+                           int batch, cudaStream_t stream);
+int ctr_bp_fan_2d_grad_f64(const ctr_fan_bp_param* p, const double* img, double* grad,
+                           const double* xpos, const double* ypos, const double* sincostbl,
+                           int batch, cudaStream_t stream);
+
+/* ---- fan-beam backprojection with an explicit angle list
+ *      (reference include/bp_fan_2d_angle.h:145-223) ----
+ * angles: device double[na].  No output scale (the caller multiplies by the
+ * orbit step, as the reference's numpy front end does). */
+int ctr_bp_fan_2d_angle_prep(const ctr_fan_bp_angle_param* p, const double* angles,
+                             double* xpos, double* ypos, double* sincostbl,
+                             cudaStream_t stream);
+int ctr_bp_fan_2d_angle_f32(const ctr_fan_bp_angle_param* p, const float* proj, float* img,
+                            const double* xpos, const double* ypos, const double* sincostbl,
+                            int batch, cudaStream_t stream);
+int ctr_bp_fan_2d_angle_f64(const ctr_fan_bp_angle_param* p, const double* proj, double* img,
+                            const double* xpos, const double* ypos, const double* sincostbl,
+                            int batch, cudaStream_t stream);
+int ctr_bp_fan_2d_angle_grad_f32(const ctr_fan_bp_angle_param* p, const float* img,
+                                 float* grad, const double* xpos, const double* ypos,
+                                 const double* sincostbl, int batch, cudaStream_t stream);
+int ctr_bp_fan_2d_angle_grad_f64(const ctr_fan_bp_angle_param* p, const double* img,
+                                 double* grad, const double* xpos, const double* ypos,
+                                 const double* sincostbl, int batch, cudaStream_t stream);
+
+/* ---- parallel-beam pixel-driven backprojection
+ *      (reference include/bp_par_2d.h:153-224) ----
+ * Tables (ParallelBackprojection2DPixDrivenPrep): xcos double[nx][na] = x cos t,
+ * ysin double[ny][na] = y sin t; `buffer` is unused, as in the reference.
+ * Forward scale is the signed orbit.  Grad is the exact adjoint of the
+ * forward and takes the forward's tables (the reference's grad pair,
+ * include/bp_par_2d.h:181-224, is not well defined and is replaced). */
+int ctr_bp_par_2d_prep(const ctr_par_param* p, double* xcos, double* ysin, int* buffer,
+                       cudaStream_t stream);
+int ctr_bp_par_2d_f32(const ctr_par_param* p, const float* proj, float* img,
+                      const double* xcos, const double* ysin, const int* buffer, int batch,
+                      cudaStream_t stream);
+int ctr_bp_par_2d_f64(const ctr_par_param* p, const double* proj, double* img,
+                      const double* xcos, const double* ysin, const int* buffer, int batch,
+                      cudaStream_t stream);
+int ctr_bp_par_2d_grad_f32(const ctr_par_param* p, const float* img, float* grad,
+                           const double* xcos, const double* ysin, int batch,
+                           cudaStream_t stream);
+int ctr_bp_par_2d_grad_f64(const ctr_par_param* p, const double* img, double* grad,
+                           const double* xcos, const double* ysin, int batch,
+                           cudaStream_t stream);
+
+/* ---- parallel-beam single-view backprojection
+ *      (reference include/bp_par_2d_sv.h:112-138) ----
+ * proj [na][ns] -> img [ny][nx][na]: the interpolated value of every view,
+ * 0 where the pixel projects off the detector.  Same tables as bp_par_2d. */
+int ctr_bp_par_2d_sv_f32(const ctr_par_param* p, const float* proj, float* img,
+                         const double* xcos, const double* ysin, const int* buffer, int batch,
+                         cudaStream_t stream);
+int ctr_bp_par_2d_sv_f64(const ctr_par_param* p, const double* proj, double* img,
+                         const double* xcos, const double* ysin, const int* buffer, int batch,
+                         cudaStream_t stream);
+
+/* ---- parallel-beam ray-driven forward projection
+ *      (reference include/fp_par_2d.h:209-278) ----
+ * Prep (ParallelProjection2DRayDrivenPrepare): sincostbl double[na][2],
+ * beginoffset double[na][ns][2], usex int[na].  Grad prep
+ * (...RayDrivenGradPrep): weights double[na], pos double[na][nx][2],
+ * usex int[na].  Requires nx == ny, as the reference op does. */
+int ctr_fp_par_2d_prep(const ctr_par_param* p, double* sincostbl, double* beginoffset,
+                       int* usex, cudaStream_t stream);
+int ctr_fp_par_2d_f32(const ctr_par_param* p, const float* img, float* proj,
+                      const double* sincostbl, const double* beginoffset, const int* usex,
+                      int batch, cudaStream_t stream);
+int ctr_fp_par_2d_f64(const ctr_par_param* p, const double* img, double* proj,
+                      const double* sincostbl, const double* beginoffset, const int* usex,
+                      int batch, cudaStream_t stream);
+int ctr_fp_par_2d_grad_prep(const ctr_par_param* p, double* weights, double* pos, int* usex,
+                            cudaStream_t stream);
+int ctr_fp_par_2d_grad_f32(const ctr_par_param* p, const float* proj, float* img,
+                           const double* weights, const double* pos, const int* usex,
+                           int batch, cudaStream_t stream);
+int ctr_fp_par_2d_grad_f64(const ctr_par_param* p, const double* proj, double* img,
+                           const double* weights, const double* pos, const int* usex,
+                           int batch, cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

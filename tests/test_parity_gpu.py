@@ -1,0 +1,191 @@
+"""Parity of the CUDA path (through the C ABI) with the reference.
+
+* small cases: every operator against the fixtures the reference's own CPU
+  code produced (tests/golden), T=float kernels at rel-L2 <= 1e-5 and
+  T=double kernels at rel-L2 <= 1e-11;
+* full benchmark sizes: the FP32 FBP chains against the oracle port, at
+  rel-L2 <= 1e-5 against its T=float output and <= 1e-4 against FP64;
+* adjoint dot tests, batching and the kernels' self-check flags.
+"""
+import ctypes
+import math
+
+import numpy as np
+import pytest
+
+import golden_cases as gc
+from gpu_helpers import (angle_op, cuda, dot_rel, fan_op, fp_op, host, par_op, ramp_op,
+                         rel_l2, tol, weight_op)
+
+pytestmark = pytest.mark.gpu
+
+DT = [("f32", np.float32), ("f64", np.float64)]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib_ready():
+    import torch
+    from ct_recon_extensions_gb300 import build, _lib
+    build.build()
+    assert torch.cuda.is_available()
+    assert _lib.load().ctr_device_check() == 0, _lib.load().ctr_last_error()
+    flags = ctypes.c_uint(0)
+    _lib.load().ctr_kernel_flags(ctypes.byref(flags), 1)
+    yield
+    _lib.load().ctr_kernel_flags(ctypes.byref(flags), 1)
+    assert flags.value == 0, f"kernel self-check flags raised: {flags.value:#x}"
+
+
+@pytest.mark.parametrize("name", gc.names(("fan", "fan_angle")))
+@pytest.mark.parametrize("sfx,dt", DT)
+def test_fan_chain(name, sfx, dt):
+    c = gc.load(name)
+    g = c["geom"]
+    p = cuda(c[f"sino_{sfx}"])
+    for wt in (1, 2):
+        op = weight_op(g, g["na"], wt)
+        w = host(op.forward(p))
+        assert rel_l2(w, c[f"weighted{wt}_{sfx}"]) <= 1e-7
+        assert rel_l2(host(op.adjoint(p)), c[f"weighted{wt}_grad_{sfx}"]) <= 1e-7
+    filt = host(ramp_op(g, g["na"], 1).forward(cuda(c[f"weighted1_{sfx}"])))
+    assert rel_l2(filt, c[f"filtered_{sfx}"]) <= tol(dt)
+    assert rel_l2(host(ramp_op(g, g["na"], 1).adjoint(p)), c[f"filtered_grad_{sfx}"]) <= tol(dt)
+    flat = host(ramp_op(g, g["na"], 2).forward(cuda(c[f"weighted2_{sfx}"])))
+    assert rel_l2(flat, c[f"filtered_flat_{sfx}"]) <= tol(dt)
+    if c["kind"] == "fan":
+        op = fan_op(g)
+        assert rel_l2(host(op.forward(cuda(c[f"filtered_{sfx}"]))), c[f"bp_{sfx}"]) <= tol(dt)
+        assert rel_l2(host(op.adjoint(cuda(c[f"img_in_{sfx}"]))), c[f"bp_grad_{sfx}"]) <= tol(dt)
+    else:
+        op = angle_op(g, c["angles"])
+        assert rel_l2(host(op.forward(cuda(c[f"filtered_{sfx}"]))), c[f"bp_{sfx}"]) <= tol(dt)
+
+
+@pytest.mark.parametrize("name", gc.names("par"))
+@pytest.mark.parametrize("sfx,dt", DT)
+def test_par_bp(name, sfx, dt):
+    c = gc.load(name)
+    g = c["geom"]
+    filt = host(ramp_op(g, g["na"], 0, dsd=-1.0).forward(cuda(c[f"sino_{sfx}"])))
+    assert rel_l2(filt, c[f"filtered_{sfx}"]) <= tol(dt)
+    img = host(par_op(g).forward(cuda(c[f"filtered_{sfx}"])))
+    assert rel_l2(img, c[f"bp_{sfx}"]) <= tol(dt)
+
+
+@pytest.mark.parametrize("sfx,dt", DT)
+def test_single_view(sfx, dt):
+    c = gc.load("sv")
+    g = c["geom"]
+    out = host(par_op(g).single_view(cuda(c[f"sino_{sfx}"])))[0]
+    assert out.shape == c[f"sv_{sfx}"].shape
+    assert rel_l2(out, c[f"sv_{sfx}"]) <= tol(dt)
+
+
+@pytest.mark.parametrize("name", gc.names("fp"))
+@pytest.mark.parametrize("sfx,dt", DT)
+def test_fp_ray_driven(name, sfx, dt):
+    c = gc.load(name)
+    g = c["geom"]
+    op = fp_op(g)
+    assert rel_l2(host(op.forward(cuda(c[f"img_{sfx}"]))), c[f"fp_{sfx}"]) <= tol(dt)
+    assert rel_l2(host(op.adjoint(cuda(c[f"proj_in_{sfx}"]))), c[f"fp_grad_{sfx}"]) <= tol(dt)
+
+
+# ---- adjoint dot tests --------------------------------------------------------
+
+def _dot(op, x_shape, y_shape, dt, seed=0):
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal(x_shape).astype(dt)
+    y = rng.standard_normal(y_shape).astype(dt)
+    ax = host(op.forward(cuda(x)))
+    aty = host(op.adjoint(cuda(y)))
+    return dot_rel(ax, y, x, aty)
+
+
+@pytest.mark.parametrize("sfx,dt", DT)
+def test_adjoint_dot(sfx, dt):
+    lim = 1e-6 if dt == np.float32 else 1e-10
+    c = gc.load("fan_full")["geom"]
+    assert _dot(fan_op(c), (c["na"], c["ns"]), (c["ny"], c["nx"]), dt) < lim
+    p = gc.load("par_rect_cw")["geom"]
+    assert _dot(par_op(p), (p["na"], p["ns"]), (p["ny"], p["nx"]), dt) < lim
+    f = gc.load("fp_half")["geom"]
+    assert _dot(fp_op(f), (f["ny"], f["nx"]), (f["na"], f["ns"]), dt) < lim
+    assert _dot(ramp_op(c, c["na"], 1), (c["na"], c["ns"]), (c["na"], c["ns"]), dt) < lim
+    assert _dot(weight_op(c, c["na"], 1), (c["na"], c["ns"]), (c["na"], c["ns"]), dt) < lim
+
+
+# ---- batching ----------------------------------------------------------------
+
+def test_batch_matches_items():
+    import torch
+    c = gc.load("fan_full")
+    g = c["geom"]
+    op = fan_op(g)
+    rng = np.random.default_rng(3)
+    stack = np.stack([c["filtered_f32"], rng.standard_normal(c["filtered_f32"].shape).astype(np.float32),
+                      np.zeros_like(c["filtered_f32"])])
+    out = host(op.forward(cuda(stack)[..., None]))[..., 0]
+    for i in range(3):
+        one = host(op.forward(cuda(stack[i])))
+        assert np.array_equal(out[i], one)
+    assert np.all(out[2] == 0)
+
+
+# ---- full benchmark sizes against the oracle ---------------------------------
+
+@pytest.fixture(scope="module")
+def oracle_port():
+    import os
+    from oracle import Oracle
+    return Oracle("port", threads=os.cpu_count() or 1)
+
+
+def test_fan_fbp_config1(oracle_port):
+    from oracle import Geom
+    from ct_recon_extensions_gb300 import synthetic as syn
+    d = syn.fan_config_1()
+    g = Geom.make(**d)
+    e = syn.random_ellipses(1000)
+    sino = syn.fan_sinogram(e, g.na, g.ns, g.ds, g.orbit, g.dso, g.dsd)
+    ref32 = oracle_port.fbp_fan(sino, g)
+    ref64 = oracle_port.fbp_fan(sino.astype(np.float64), g)
+    w = weight_op(d, d["na"], 1).forward(cuda(sino))
+    f = ramp_op(d, d["na"], 1).forward(w)
+    img = host(fan_op(d).forward(f))
+    assert rel_l2(img, ref32) <= 1e-5
+    assert rel_l2(img, ref64) <= 1e-4
+
+
+def test_parallel_config2(oracle_port):
+    from oracle import Geom
+    from ct_recon_extensions_gb300 import synthetic as syn
+    d = syn.parallel_config_2()
+    g = Geom.make(**d)
+    img0 = syn.rasterize(syn.random_ellipses(2000), 512, 512, 0.5, 0.5)
+    sino_ref = oracle_port.fp_par_2d(img0, g)
+    sino = fp_op(d).forward(cuda(img0))
+    assert rel_l2(host(sino), sino_ref) <= 1e-5
+    filt_ref = oracle_port.ramp_filter(sino_ref, g.ds, -1.0, 0)
+    rec_ref = oracle_port.bp_par_2d(filt_ref, g)
+    filt = ramp_op(d, d["na"], 0, dsd=-1.0).forward(cuda(sino_ref))
+    rec = host(par_op(d).forward(filt))
+    assert rel_l2(rec, rec_ref) <= 1e-5
+    rec64 = oracle_port.bp_par_2d(oracle_port.ramp_filter(sino_ref.astype(np.float64), g.ds, -1.0, 0), g)
+    assert rel_l2(rec, rec64) <= 1e-4
+
+
+def test_fp_adjoint_config2_dot():
+    from ct_recon_extensions_gb300 import synthetic as syn
+    d = syn.parallel_config_2()
+    assert _dot(fp_op(d), (d["ny"], d["nx"]), (d["na"], d["ns"]), np.float32) < 1e-6
+    assert _dot(par_op(d), (d["na"], d["ns"]), (d["ny"], d["nx"]), np.float32) < 1e-6
+    f = syn.fan_config_1()
+    assert _dot(fan_op(f), (f["na"], f["ns"]), (f["ny"], f["nx"]), np.float32) < 1e-6
+
+
+def test_cpu_tensor_rejected():
+    import torch
+    c = gc.load("par")["geom"]
+    with pytest.raises(ValueError):
+        par_op(c).forward(torch.zeros((c["na"], c["ns"])))
