@@ -66,6 +66,16 @@ class ParParam(ctypes.Structure):
                 ("offset_y", c_double), ("fov", c_double)]
 
 
+class PlanInfo(ctypes.Structure):
+    _fields_ = [("n_items", c_int), ("work_items", ctypes.c_longlong), ("tile_rows", c_int),
+                ("view_block", c_int), ("ctas", c_int), ("autotuned", c_int),
+                ("tuned_ms", c_double), ("graph", c_int), ("workspace_bytes", ctypes.c_ulonglong),
+                ("launches_per_run", ctypes.c_longlong)]
+
+
+CTR_PLAN_AUTOTUNE = 1
+CTR_PLAN_GRAPH = 2
+
 _P = c_void_p  # device pointers and the stream travel as void*
 _S = ctypes.POINTER
 
@@ -82,6 +92,10 @@ PROTOTYPES = {
     "ctr_bp_par_2d_prep": [_S(ParParam), _P, _P, _P, _P],
     "ctr_fp_par_2d_prep": [_S(ParParam), _P, _P, _P, _P],
     "ctr_fp_par_2d_grad_prep": [_S(ParParam), _P, _P, _P, _P],
+    "ctr_fbp_fan_plan_create": [_S(FanBpParam), c_int, c_int, c_int, ctypes.POINTER(c_void_p)],
+    "ctr_fbp_fan_plan_run": [c_void_p, ctypes.POINTER(c_void_p), ctypes.POINTER(c_void_p), _P],
+    "ctr_fbp_fan_plan_info": [c_void_p, _S(PlanInfo)],
+    "ctr_fbp_fan_plan_destroy": [c_void_p],
 }
 for _t in ("f32", "f64"):
     PROTOTYPES.update({

@@ -1,0 +1,622 @@
+// Device side of the FP32 pixel-driven backprojectors, shared by the
+// single-geometry entry points (bp.cu) and the batched plan (batch.cu): view
+// parameters, detector windows, the fast interior and exact edge tap paths,
+// and the tile bodies.  Everything here has internal linkage per file.
+#pragma once
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+
+#include "ctr_async.cuh"
+#include "ctr_common.cuh"
+
+namespace ctr {
+namespace {
+
+constexpr int kBpThreads = 256;
+constexpr int kTileX = 32;
+constexpr int kRowsPerThread = 4;
+constexpr int kTileY = (kBpThreads / 32) * kRowsPerThread;
+constexpr int kViewBlock = 16;
+
+enum class Geo { kFan, kPar };
+
+// Per-launch constants of the FP32 tile kernels.
+struct TileConst {
+    int ns, na, nx, ny;
+    int W;                 // staged window length (channels)
+    float cents;           // (ns-1)/2 + offset_s
+    float nsm1;            // ns - 1
+    float dso, K;          // fan: source distance, dsd/ds
+    float scale;           // applied once to the final sum
+    double orbit_start, orbit;  // parallel: view angle = orbit_start + ia*orbit
+    double inv_ds;         // parallel: 1/ds
+    double centx, centy, dx, dy;  // parallel pixel grid
+    double ds_d, cents_d, dso_d, dsd_d;  // FP64 geometry for the exact edge test
+    float poly[6];         // fan: atan polynomial scaled by dsd/ds
+    int WB;                // TMA box (elements) per view: >= W + 4, multiple of 4
+    int WS;                // shared slot stride per view: WB rounded up to 128 bytes
+    long long total4;      // sinogram elements of the launch, rounded down to 4
+    size_t proj_stride, img_stride;
+};
+
+// FP32 channel positions are within ~3e-4 channels of the reference's FP64
+// value (s up to ~2e3, plus atan2f error).  Within kEdgeEps of a detector end
+// the inclusion decision is recomputed in FP64 from the caller's tables.
+constexpr float kEdgeEps = 2e-3f;
+
+// ---- per-view parameters ---------------------------------------------------
+// Fan: (sin b, cos b) from the caller's table.  Parallel: (cos t / ds,
+// sin t / ds) from the geometry, with t = orbit_start + ia*orbit.
+template <Geo G>
+__device__ __forceinline__ float2 view_params(const double* __restrict__ sincos, int ia,
+                                              const TileConst& c)
+{
+    if constexpr (G == Geo::kFan) {
+        return make_float2(static_cast<float>(sincos[2 * ia]), static_cast<float>(sincos[2 * ia + 1]));
+    } else {
+        double sa, ca;
+        ::sincos(c.orbit_start + ia * c.orbit, &sa, &ca);
+        return make_float2(static_cast<float>(ca * c.inv_ds), static_cast<float>(sa * c.inv_ds));
+    }
+}
+
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Channel position of pixel (x, y) for a view, and the fan distance weight
+// 1/(d^2 + r^2) (dsd^2 is applied with the final scale).
+template <Geo G>
+__device__ __forceinline__ float channel_of(float x, float y, float2 vp, const TileConst& c,
+                                            float* w)
+{
+    if constexpr (G == Geo::kFan) {
+        const float d = fmaf(-y, vp.y, fmaf(x, vp.x, c.dso));
+        const float r = fmaf(x, vp.y, y * vp.x);
+        *w = rcp_approx(fmaf(d, d, r * r));
+        return fmaf(atan2f(r, d), c.K, c.cents);
+    } else {
+        *w = 1.0f;
+        return fmaf(y, vp.y, fmaf(x, vp.x, c.cents));
+    }
+}
+
+// The reference's FP64 channel position (src/bp_fan_2d.cc:66-69,
+// src/bp_par_2d.cc:70) from the caller's tables: t0/t1/t2 are xpos/ypos/
+// sincostbl (fan) or xcos/ysin (parallel).
+template <Geo G>
+__device__ __noinline__ double channel_exact(int ix, int iy, int ia, const double* __restrict__ t0,
+                                             const double* __restrict__ t1,
+                                             const double* __restrict__ t2, const TileConst& c)
+{
+    if constexpr (G == Geo::kFan) {
+        const double x = t0[ix], y = t1[iy], sb = t2[2 * ia], cb = t2[2 * ia + 1];
+        const double d = __dadd_rn(c.dso_d, __dadd_rn(__dmul_rn(x, sb), -__dmul_rn(y, cb)));
+        const double r = __dadd_rn(__dmul_rn(x, cb), __dmul_rn(y, sb));
+        return __dadd_rn(__ddiv_rn(__dmul_rn(atan2(r, d), c.dsd_d), c.ds_d), c.cents_d);
+    } else {
+        const double xc = t0[static_cast<size_t>(ix) * c.na + ia];
+        const double ys = t1[static_cast<size_t>(iy) * c.na + ia];
+        return __dadd_rn(__ddiv_rn(__dadd_rn(xc, ys), c.ds_d), c.cents_d);
+    }
+}
+
+// One pixel-view tap on an edge view: inclusion decided as the reference does
+// (exactly, in FP64, near the detector ends); returns false when excluded.
+template <Geo G>
+__device__ __forceinline__ bool edge_tap(float s, int ix, int iy, int ia, int lo,
+                                         const double* t0, const double* t1, const double* t2,
+                                         const TileConst& c, int* k, float* u)
+{
+    float fs;
+    if (fabsf(s) < kEdgeEps || fabsf(s - c.nsm1) < kEdgeEps) {
+        const double sd = channel_exact<G>(ix, iy, ia, t0, t1, t2, c);
+        if (!(sd >= 0.0 && sd <= static_cast<double>(c.ns - 1))) return false;
+        const double fd = floor(sd);
+        fs = static_cast<float>(fd);
+        *u = static_cast<float>(sd - fd);
+    } else {
+        if (!(s >= 0.0f && s <= c.nsm1)) return false;
+        fs = floorf(s);
+        *u = s - fs;
+    }
+    *k = min(max(static_cast<int>(fs) - lo, 0), c.W - 2);
+    return true;
+}
+
+// Detector window [lo, lo+W) that covers every tap of the tile for one view;
+// *interior is set when every pixel of the tile projects at least one channel
+// inside the detector (no inclusion test needed) and the window fits.
+template <Geo G>
+__device__ int window_start(float2 vp, float x0, float x1, float y0, float y1, const TileConst& c,
+                            bool* interior)
+{
+    float smin = FLT_MAX, smax = -FLT_MAX;
+    bool full = false;
+    const float xs[2] = {x0, x1}, ys[2] = {y0, y1};
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            if constexpr (G == Geo::kFan) {
+                const float d = fmaf(-ys[j], vp.y, fmaf(xs[i], vp.x, c.dso));
+                if (d <= 0.0f) full = true;
+            }
+            float w;
+            const float s = channel_of<G>(xs[i], ys[j], vp, c, &w);
+            smin = fminf(smin, s);
+            smax = fmaxf(smax, s);
+        }
+    }
+    *interior = false;
+    if (full || !(smin == smin) || !(smax == smax)) return -1;
+    int lo = static_cast<int>(floorf(smin)) - 2;
+    int hi = static_cast<int>(floorf(smax)) + 3;
+    const bool fits = hi - lo + 1 <= c.W;
+    *interior = fits && smin >= 1.0f && smax <= c.nsm1 - 1.0f;
+    lo = max(lo, -1);
+    hi = min(hi, c.ns);
+    if (hi - lo + 1 > c.W && lo <= c.ns && hi >= -1) raise_flag(kFlagWindowOverflow);
+    return min(lo, c.ns);
+}
+
+// Forward FP32 tile kernel with cooperative (plain-load) staging: proj [na][ns]
+// -> img [ny][nx] (batch in grid.z).  t0/t1/t2: fan xpos/ypos/sincostbl,
+// parallel xcos/ysin/unused.  Used where the TMA kernel below does not apply
+// (windows wider than one 256-element box, unaligned buffers).
+template <Geo G>
+__global__ void __launch_bounds__(kBpThreads, 2)
+    bp_tile_f32_coop(const float* __restrict__ proj, float* __restrict__ img,
+                const double* __restrict__ t0, const double* __restrict__ t1,
+                const double* __restrict__ t2, const TileConst c)
+{
+    extern __shared__ float2 win[];  // [kViewBlock][W]
+    __shared__ float2 s_vp[kViewBlock];
+    __shared__ int s_lo[kViewBlock];
+    __shared__ int s_in[kViewBlock];
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int tx0 = blockIdx.x * kTileX, ty0 = blockIdx.y * kTileY;
+    const float* P = proj + blockIdx.z * c.proj_stride;
+
+    auto px = [&](int ix) -> float {
+        if constexpr (G == Geo::kFan) return static_cast<float>(t0[ix]);
+        else return static_cast<float>((ix - c.centx) * c.dx);
+    };
+    auto py = [&](int iy) -> float {
+        if constexpr (G == Geo::kFan) return static_cast<float>(t1[iy]);
+        else return static_cast<float>((c.centy - iy) * c.dy);
+    };
+    const int ixc = min(tx0 + lane, c.nx - 1);
+    const float x = px(ixc);
+    float y[kRowsPerThread], acc[kRowsPerThread];
+#pragma unroll
+    for (int r = 0; r < kRowsPerThread; ++r) {
+        y[r] = py(min(ty0 + warp * kRowsPerThread + r, c.ny - 1));
+        acc[r] = 0.0f;
+    }
+    const float cx0 = px(tx0), cx1 = px(min(tx0 + kTileX - 1, c.nx - 1));
+    const float cy0 = py(ty0), cy1 = py(min(ty0 + kTileY - 1, c.ny - 1));
+
+    for (int v0 = 0; v0 < c.na; v0 += kViewBlock) {
+        const int nv = min(kViewBlock, c.na - v0);
+        if (threadIdx.x < nv) {
+            const float2 vp = view_params<G>(t2, v0 + threadIdx.x, c);
+            bool inner;
+            s_vp[threadIdx.x] = vp;
+            s_lo[threadIdx.x] = window_start<G>(vp, cx0, cx1, cy0, cy1, c, &inner);
+            s_in[threadIdx.x] = inner;
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < nv * c.W; idx += kBpThreads) {
+            const int j = idx / c.W, k = idx - j * c.W;
+            const int g = s_lo[j] + k;
+            const float* row = P + static_cast<size_t>(v0 + j) * c.ns;
+            const float p0 = (g >= 0 && g < c.ns) ? __ldg(row + g) : 0.0f;
+            const float p1 = (g + 1 >= 0 && g + 1 < c.ns) ? __ldg(row + g + 1) : 0.0f;
+            win[idx] = make_float2(p0, p1 - p0);
+        }
+        __syncthreads();
+        for (int j = 0; j < nv; ++j) {
+            const float2 vp = s_vp[j];
+            const int lo = s_lo[j];
+            const float2* wj = win + j * c.W;
+            if (s_in[j]) {
+                // every tap of the tile is on the detector and inside the window
+#pragma unroll
+                for (int r = 0; r < kRowsPerThread; ++r) {
+                    float w;
+                    const float s = channel_of<G>(x, y[r], vp, c, &w);
+                    const float fs = floorf(s);
+                    const float2 pv = wj[static_cast<int>(fs) - lo];
+                    const float v = fmaf(s - fs, pv.y, pv.x);
+                    if constexpr (G == Geo::kFan) acc[r] = fmaf(v, w, acc[r]);
+                    else acc[r] += v;
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < kRowsPerThread; ++r) {
+                    float w, u;
+                    int k;
+                    const float s = channel_of<G>(x, y[r], vp, c, &w);
+                    const int iyc = min(ty0 + warp * kRowsPerThread + r, c.ny - 1);
+                    if (edge_tap<G>(s, ixc, iyc, v0 + j, lo, t0, t1, t2, c, &k, &u)) {
+                        const float2 pv = wj[k];
+                        const float v = fmaf(u, pv.y, pv.x);
+                        if constexpr (G == Geo::kFan) acc[r] = fmaf(v, w, acc[r]);
+                        else acc[r] += v;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    float* I = img + blockIdx.z * c.img_stride;
+    const int ix = tx0 + lane;
+#pragma unroll
+    for (int r = 0; r < kRowsPerThread; ++r) {
+        const int iy = ty0 + warp * kRowsPerThread + r;
+        if (ix < c.nx && iy < c.ny) I[static_cast<size_t>(iy) * c.nx + ix] = acc[r] * c.scale;
+    }
+}
+
+// ---- TMA-fed forward kernel ---------------------------------------------------
+//
+// Same tile as bp_tile_f32_coop, but a CTA runs two view groups of 256 threads
+// on the same 32x32 tile (each group takes half of every block of
+// 2*kViewBlock views; the two partial sums are added in a fixed order at the
+// end), and the detector windows reach shared memory through the TMA engine:
+// one cp.async.bulk copy per view (16-byte aligned start in the flattened
+// sinogram, a 128-byte aligned shared slot), issued two view blocks ahead
+// into double-buffered raw slots, each block completed on its own mbarrier
+// (waits are bounded and report kFlagWaitTimeout).  Once a slot
+// has landed, the CTA rewrites it as (p[i], p[i+1]-p[i]) pairs, zero off the
+// detector, so an interpolation is one 8-byte shared load and one FMA.
+//
+// Interior fast path (every tap of the tile on the detector): the floor and
+// fraction of s come from adding 2^23 - 0.5 (round-to-nearest of s - 1/2 lands
+// the integer part in the low mantissa bits; s in [1, 2^22)), and for the fan
+// atan(r/d) is the minimax polynomial below when |r/d| <= kAtanTmax on the
+// whole tile, with an approximate reciprocal of d.
+
+// atan(t) ~= t*P(t^2), |t| <= 0.6, max relative error 3.28e-08 (Remez, degree 5
+// in t^2; coefficients from gen_atan_poly.py).
+constexpr double kAtanPoly[6] = {9.99999967214467378e-01, -3.33326573611355148e-01,
+                                 1.99772013637297047e-01, -1.39992597733896912e-01,
+                                 9.42086263445095634e-02, -4.04465160162714304e-02};
+constexpr float kAtanTmax = 0.6f;
+constexpr float kMagic = 8388608.0f;       // 2^23
+constexpr float kMagicHalf = 8388607.5f;   // 2^23 - 1/2
+constexpr unsigned kMagicBits = 0x4B000000u;
+constexpr int kGroups = 2;
+constexpr int kBlockViews = kGroups * kViewBlock;
+constexpr int kTmaThreads = kGroups * kBpThreads;
+constexpr int kModeEdge = 0, kModeFast = 2;
+
+struct ViewP {
+    float2 vp;
+    int lo;     // first staged channel
+    int mode;   // kModeEdge or kModeFast
+};
+
+__device__ __forceinline__ float2 lds_f2(unsigned addr)
+{
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
+    return v;
+}
+
+// Channel position on the interior fast path (shared by the forward and the
+// adjoint so that both take bit-identical taps).  Fan: xs = dso + x sin b,
+// xc = x cos b; parallel: xs = x cos t / ds + cents.  Returns s; *w is the fan
+// distance weight 1/(d^2+r^2).
+template <Geo G>
+__device__ __forceinline__ float fast_s(float xs, float xc, float y, float2 vp, const TileConst& c,
+                                        float* w)
+{
+    if constexpr (G == Geo::kFan) {
+        const float d = fmaf(-y, vp.y, xs);
+        const float rr = fmaf(y, vp.x, xc);
+        const float t = rr * rcp_approx(d);
+        const float z = t * t;
+        float p = fmaf(z, c.poly[5], c.poly[4]);
+        p = fmaf(z, p, c.poly[3]);
+        p = fmaf(z, p, c.poly[2]);
+        p = fmaf(z, p, c.poly[1]);
+        p = fmaf(z, p, c.poly[0]);
+        *w = rcp_approx(fmaf(d, d, rr * rr));
+        return fmaf(t, p, c.cents);
+    } else {
+        *w = 1.0f;
+        return fmaf(y, vp.y, xs);
+    }
+}
+
+template <Geo G>
+__device__ __forceinline__ void fast_xs(float x, float2 vp, const TileConst& c, float* xs, float* xc)
+{
+    if constexpr (G == Geo::kFan) {
+        *xs = fmaf(x, vp.x, c.dso);
+        *xc = x * vp.y;
+    } else {
+        *xs = fmaf(x, vp.x, c.cents);
+        *xc = 0.0f;
+    }
+}
+
+// Per-view parameters, window and path for one tile (thread-local).
+template <Geo G>
+__device__ ViewP view_setup(const double* __restrict__ t2, int ia, float x0, float x1,
+                            float y0, float y1, const TileConst& c)
+{
+    ViewP P;
+    P.vp = view_params<G>(t2, ia, c);
+    bool inner;
+    P.lo = window_start<G>(P.vp, x0, x1, y0, y1, c, &inner);
+    bool fast = inner;
+    if constexpr (G == Geo::kFan) {
+        // polynomial atan needs d > 0 and |r/d| <= kAtanTmax on the whole tile
+        // (r/d is a linear-fractional function: extremes at the corners)
+        const float xs[2] = {x0, x1}, ys[2] = {y0, y1};
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const float d = fmaf(-ys[j], P.vp.y, fmaf(xs[i], P.vp.x, c.dso));
+                const float r = fmaf(xs[i], P.vp.y, ys[j] * P.vp.x);
+                fast = fast && d > 0.0f && fabsf(r) <= kAtanTmax * d;
+            }
+    }
+    P.mode = fast ? kModeFast : kModeEdge;
+    return P;
+}
+
+// One tile (tile_x, tile_y) of item `item`; all 512 threads of the CTA call it.
+// Re-entrant across calls of a persistent CTA: the mbarriers are
+// (re)initialised here and every copy issued is waited on before returning.
+// Returns false (uniformly) when a check or a bounded wait failed.
+template <Geo G, int R = kRowsPerThread, int VB = kViewBlock>
+__device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, float* __restrict__ img,
+                                             const double* __restrict__ t0,
+                                             const double* __restrict__ t1,
+                                             const double* __restrict__ t2, const TileConst& c,
+                                             int tile_x, int tile_y, int item)
+{
+    constexpr int kTY = (kBpThreads / 32) * R;  // tile height
+    constexpr int kBV = kGroups * VB;           // views per staged block
+    // Dynamic shared memory, 128-byte aligned here: raw slots [2][kBV][WS]
+    // (every slot stride a 128-byte multiple), pairs [2][kBV][W], then one
+    // ViewP per view of the whole scan.
+    extern __shared__ __align__(128) unsigned char smem_dyn[];
+    unsigned char* smem = smem_dyn + ((128u - (smem_u32(smem_dyn) & 127u)) & 127u);
+    float* raw = reinterpret_cast<float*>(smem);
+    float2* pairs = reinterpret_cast<float2*>(smem + 2 * kBV * c.WS * sizeof(float));
+    ViewP* views = reinterpret_cast<ViewP*>(pairs + 2 * kBV * c.W);
+    __shared__ __align__(8) unsigned long long s_bar[2];
+    __shared__ int s_ok;
+
+    const int tid = threadIdx.x;
+    const int group = tid / kBpThreads;
+    const int lt = tid - group * kBpThreads;
+    const int lane = lt & 31, warp = lt >> 5;
+    const int tx0 = tile_x * kTileX, ty0 = tile_y * kTY;
+    const int nblocks = (c.na + kBV - 1) / kBV;
+
+    auto px = [&](int ix) -> float {
+        if constexpr (G == Geo::kFan) return static_cast<float>(t0[ix]);
+        else return static_cast<float>((ix - c.centx) * c.dx);
+    };
+    auto py = [&](int iy) -> float {
+        if constexpr (G == Geo::kFan) return static_cast<float>(t1[iy]);
+        else return static_cast<float>((c.centy - iy) * c.dy);
+    };
+    const float cx0 = px(tx0), cx1 = px(min(tx0 + kTileX - 1, c.nx - 1));
+    const float cy0 = py(ty0), cy1 = py(min(ty0 + kTY - 1, c.ny - 1));
+
+    // Slot j of block b receives sinogram elements [gx, gx + WB) of the flattened
+    // array (gx = window start rounded down to 4 elements, so the source is
+    // 16-byte aligned), clipped to [0, total4) where total4 = total rounded down
+    // to 4 elements; the conversion below reads the clipped-away elements from
+    // global directly.
+    auto slot_start = [&](int ia) -> long long {
+        return (static_cast<long long>(item) * c.na + ia) * c.ns + views[ia].lo;
+    };
+    // Issued by warp 0, one lane per view (kBV <= 64: two rounds at most); lane 0
+    // arms the barrier with the block's byte count (a warp sum) first.
+    auto issue_block = [&](int b) {
+        if (b >= nblocks) return;
+        const int v0 = b * kBV;
+        const int nv = min(kBV, c.na - v0);
+        const unsigned bar = smem_u32(&s_bar[b & 1]);
+        float* slot = raw + (b & 1) * kBV * c.WS;
+        unsigned bytes = 0;
+        for (int j = lane; j < nv; j += 32) {
+            const long long gx = slot_start(v0 + j) & ~3ll;
+            const long long g0 = max(gx, 0ll), g1 = min(gx + c.WB, c.total4);
+            if (g1 > g0) bytes += static_cast<unsigned>((g1 - g0) * sizeof(float));
+        }
+        bytes = __reduce_add_sync(0xffffffffu, bytes);
+        if (lane == 0) mbar_expect_tx(bar, bytes);
+        __syncwarp();
+        for (int j = lane; j < nv; j += 32) {
+            const long long gx = slot_start(v0 + j) & ~3ll;
+            const long long g0 = max(gx, 0ll), g1 = min(gx + c.WB, c.total4);
+            if (g1 > g0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                bulk_load(smem_u32(slot + j * c.WS + (g0 - gx)), proj + g0,
+                          static_cast<unsigned>((g1 - g0) * sizeof(float)), bar);
+            }
+        }
+    };
+
+    // per-view parameters, windows and paths of this tile for the whole scan
+    for (int ia = tid; ia < c.na; ia += kTmaThreads)
+        views[ia] = view_setup<G>(t2, ia, cx0, cx1, cy0, cy1, c);
+    if (tid == 0) {
+        // every copy destination must be 128-byte aligned; check before issuing any
+        const bool aligned = (smem_u32(raw) & 127u) == 0 && (c.WS * sizeof(float)) % 128 == 0;
+        s_ok = aligned;
+        if (!aligned) raise_flag(kFlagMisaligned);
+        mbar_init(smem_u32(&s_bar[0]), 1);
+        mbar_init(smem_u32(&s_bar[1]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (!s_ok) return false;
+    if (tid < 32) {
+        issue_block(0);
+        issue_block(1);
+    }
+
+    const int ixc = min(tx0 + lane, c.nx - 1);
+    const float x = px(ixc);
+    float y[R], acc[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        y[r] = py(min(ty0 + warp * R + r, c.ny - 1));
+        acc[r] = 0.0f;
+    }
+    const unsigned pairs_u32 = smem_u32(pairs);
+
+    const int wid = tid >> 5;  // warp of the CTA (0..15)
+    for (int b = 0; b < nblocks; ++b) {
+        // every thread waits for block b's copies (bounded); a timeout is
+        // reported and the block proceeds, so no thread is left at a barrier
+        if (!mbar_wait_bounded(smem_u32(&s_bar[b & 1]), (b >> 1) & 1) && tid == 0)
+            raise_flag(kFlagWaitTimeout);
+        const int nv = min(kBV, c.na - b * kBV);
+        const float* slot = raw + (b & 1) * kBV * c.WS;
+        float2* pb = pairs + (b & 1) * kBV * c.W;
+        // one warp per view: rewrite the raw window as (p[i], p[i+1] - p[i]) pairs
+        for (int j = wid; j < nv; j += kTmaThreads / 32) {
+            const long long st = slot_start(b * kBV + j);
+            const int lo = views[b * kBV + j].lo;
+            const float* src = slot + j * c.WS + static_cast<int>(st & 3ll);
+            float2* dst = pb + j * c.W;
+            if (lo >= 0 && lo + c.W < c.ns && st + c.W < c.total4) {
+                for (int k = lane; k < c.W; k += 32) {
+                    const float p0 = src[k], p1 = src[k + 1];
+                    dst[k] = make_float2(p0, p1 - p0);
+                }
+            } else {  // a detector end or the array's ragged tail is in the window
+                for (int k = lane; k < c.W; k += 32) {
+                    auto at = [&](int gg, long long ii, const float* sp) -> float {
+                        if (gg < 0 || gg >= c.ns) return 0.0f;  // off the detector
+                        return ii < c.total4 ? *sp : __ldg(proj + ii);
+                    };
+                    const float p0 = at(lo + k, st + k, src + k);
+                    const float p1 = at(lo + k + 1, st + k + 1, src + k + 1);
+                    dst[k] = make_float2(p0, p1 - p0);
+                }
+            }
+        }
+        __syncthreads();
+        if (tid < 32) issue_block(b + 2);  // block b's raw slot has been consumed
+
+        const int jb = group * VB;
+        const int je = min(jb + VB, nv);
+        float part[R];  // this block's partial sums (blocked summation)
+#pragma unroll
+        for (int r = 0; r < R; ++r) part[r] = 0.0f;
+        for (int j = jb; j < je; ++j) {
+            const int ia = b * kBV + j;
+            const ViewP P = views[ia];
+            if (P.mode == kModeFast) {
+                // index of s = bits(v) - kMagicBits, v = fl(s + 2^23 - 1/2)
+                const unsigned base = pairs_u32 + 8u * static_cast<unsigned>(((b & 1) * kBV + j) * c.W) -
+                                      8u * (kMagicBits + static_cast<unsigned>(P.lo));
+                float xs, xc;
+                fast_xs<G>(x, P.vp, c, &xs, &xc);
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    float w;
+                    const float s = fast_s<G>(xs, xc, y[r], P.vp, c, &w);
+                    const float v = s + kMagicHalf;
+                    const float u = s - (v - kMagic);
+                    const float2 pv = lds_f2(base + 8u * __float_as_uint(v));
+                    if constexpr (G == Geo::kFan) part[r] = fmaf(fmaf(u, pv.y, pv.x), w, part[r]);
+                    else part[r] = fmaf(u, pv.y, part[r] + pv.x);
+                }
+            } else {
+                const float2* wj = pb + j * c.W;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    float w, u;
+                    int k;
+                    const float s = channel_of<G>(x, y[r], P.vp, c, &w);
+                    const int iyc = min(ty0 + warp * R + r, c.ny - 1);
+                    if (edge_tap<G>(s, ixc, iyc, ia, P.lo, t0, t1, t2, c, &k, &u)) {
+                        const float2 pv = wj[k];
+                        const float v = fmaf(u, pv.y, pv.x);
+                        if constexpr (G == Geo::kFan) part[r] = fmaf(v, w, part[r]);
+                        else part[r] += v;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) acc[r] += part[r];
+    }
+    // add the second group's sums to the first's, in that order; the reduction
+    // uses the pairs buffer of block nblocks-2, which every thread has finished
+    // reading before the last block's barrier
+    float* red = reinterpret_cast<float*>(pairs + (nblocks & 1) * kBV * c.W);
+    if (group == 1) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) red[r * kBpThreads + lt] = acc[r];
+    }
+    __syncthreads();
+    if (group == 0) {
+        float* I = img + static_cast<size_t>(item) * c.img_stride;
+        const int ix = tx0 + lane;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int iy = ty0 + warp * R + r;
+            if (ix < c.nx && iy < c.ny)
+                I[static_cast<size_t>(iy) * c.nx + ix] = (acc[r] + red[r * kBpThreads + lt]) * c.scale;
+        }
+    }
+    return true;
+}
+
+template <Geo G>
+__global__ void __launch_bounds__(kTmaThreads, 2)
+    bp_tile_tma_f32(const float* __restrict__ proj, float* __restrict__ img,
+                    const double* __restrict__ t0, const double* __restrict__ t1,
+                    const double* __restrict__ t2, const TileConst c)
+{
+    tile_forward<G>(proj, img, t0, t1, t2, c, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// ---- host: window bounds --------------------------------------------------
+
+constexpr double kPi = 3.14159265358979323846;
+
+// Bound on the channel span of one tile for any view (in channels).
+int fan_window(int ns, double ds, double dso, double dsd, int nx, int ny, double dx, double dy,
+               double ox, double oy, int tile_y = kTileY)
+{
+    const double hx = ((nx - 1) / 2.0 + std::fabs(ox)) * dx, hy = ((ny - 1) / 2.0 + std::fabs(oy)) * dy;
+    const double rimg = std::sqrt(hx * hx + hy * hy);  // farthest pixel centre from the iso-centre
+    const double rt = 0.5 * std::sqrt(std::pow(kTileX * dx, 2) + std::pow(tile_y * dy, 2));
+    const double dmin = dso - rimg - rt;
+    if (dmin <= rt * 1.05) return ns + 2;  // a tile may reach the source: stage whole rows
+    const double span = 2.0 * std::asin(std::min(1.0, rt / dmin)) * dsd / ds;
+    const int w = static_cast<int>(std::ceil(span)) + 8;
+    return std::min(w, ns + 2);
+}
+
+int par_window(int ns, double ds, double dx, double dy, int tile_y = kTileY)
+{
+    const double span = std::sqrt(std::pow(kTileX * dx, 2) + std::pow(tile_y * dy, 2)) / ds;
+    const int w = static_cast<int>(std::ceil(span)) + 8;
+    return std::min(w, ns + 2);
+}
+
+}  // namespace
+}  // namespace ctr

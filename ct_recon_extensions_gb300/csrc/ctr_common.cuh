@@ -45,6 +45,20 @@ inline unsigned int div_up(unsigned long long a, unsigned long long b)
     return static_cast<unsigned int>((a + b - 1) / b);
 }
 
+// ---- batched filtering (weight_filter.cu) -----------------------------------
+// One item of a batched weighting + ramp-filter launch.
+struct FilterJob {
+    const float* in;
+    float* out;
+    const double* taps;   // 2*ns+1 FP64 taps of the item (RampFilterPrep layout)
+    const float* weight;  // per-channel pre-weight of the item, or null
+    unsigned ns, nrow;
+    double ds;
+};
+int ramp_filter_batch_f32(const FilterJob* jobs, const int2* blocks, int n_blocks, unsigned max_ns,
+                          cudaStream_t stream);
+constexpr int kFilterRowsPerBlock = 4;
+
 // ---- device math -------------------------------------------------------------
 template <typename T>
 struct DevMath;

@@ -23,6 +23,7 @@
 // FP64 kernels follow the reference's arithmetic (one thread per ray / pixel).
 #include <algorithm>
 
+#include "ctr_async.cuh"
 #include "ctr_common.cuh"
 
 namespace ctr {
@@ -32,12 +33,20 @@ namespace {
 
 constexpr int kFpThreads = 512;
 constexpr int kFpMaxRays = 8;  // rays per thread
-// Sample positions are 32.32 fixed point.  Rounding the per-ray start and step
-// to 2^-32 moves a position by at most (k+1)/2 units (< 1100 units for 2048
-// samples); the bias keeps X >= 0 wherever the FP64 position is >= 0, so the
-// integer part is a valid pixel index (it shifts positions by 4.8e-7 px).
-constexpr long long kFpBias = 2048;
+// Sample positions are 32.32 fixed point.  Each ray's line X(k) = X0 + k*S is
+// anchored at its smallest-x valid sample, X(anchor) = round(x(anchor) * 2^32)
+// >= 0, and is monotonic along the ray, so X >= 0 on every valid sample and its
+// integer part is a valid pixel index; rounding S moves a position by at most
+// |k - anchor|/2 units (< 6e-8 px for 512 samples).
 constexpr double kTwo32 = 4294967296.0;
+
+// 32.32 fixed-point line of a ray with FP64 start/step over samples [k0, k1].
+__device__ __forceinline__ long long ray_line(double begin, double step, int k0, int k1, long long* S)
+{
+    *S = llrint(step * kTwo32);
+    const int ka = step < 0.0 ? k1 : k0;  // smallest x
+    return llrint(fma(static_cast<double>(ka), step, begin) * kTwo32) - static_cast<long long>(ka) * *S;
+}
 
 struct FpConst {
     int ns, na, nx, ny;
@@ -127,8 +136,7 @@ __global__ void __launch_bounds__(kFpThreads)
             const int nsamp = ux ? c.ny : c.nx;
             const int lim = ux ? c.nx - 1 : c.ny - 1;
             ray_range(begin, step, nsamp, lim, &k0[j], &k1[j]);
-            X[j] = llrint(begin * kTwo32) + kFpBias;
-            S[j] = llrint(step * kTwo32);
+            X[j] = ray_line(begin, step, k0[j], k1[j], &S[j]);
             cls[j] = ux ? 0 : 1;
             has_cls[cls[j]] = true;
         }
@@ -160,14 +168,14 @@ __global__ void __launch_bounds__(kFpThreads)
                 if (ka > kb) continue;
                 long long x = X[j] + static_cast<long long>(ka) * S[j];
                 const float* line = band + (ka - b0) * ld;
-                float acc = sum[j];
+                float acc = 0.0f;  // this band's partial sum (blocked summation)
                 for (int k = ka; k <= kb; ++k, line += ld, x += S[j]) {
                     const int i1 = static_cast<int>(x >> 32);
                     const float u = frac_of(x);
                     const float p0 = line[i1], p1 = line[i1 + 1];
                     acc = fmaf(u, p1 - p0, acc + p0);
                 }
-                sum[j] = acc;
+                sum[j] += acc;
             }
             __syncthreads();
         }
@@ -181,6 +189,171 @@ __global__ void __launch_bounds__(kFpThreads)
             proj[blockIdx.y * c.proj_stride + static_cast<size_t>(v0) * c.ns + r] =
                 static_cast<float>(sum[j] * dw);
         }
+    }
+}
+
+// ---- FP32 forward, row-band pipeline -------------------------------------------
+//
+// Rays of column-marching views are run on a transposed copy of the image, so
+// every ray marches image rows.  A CTA owns kFrViews views x a chunk of
+// kFrChunk channels (4 rays of one view per thread, so the view's per-sample
+// step S is shared).  The source image streams through shared memory in bands
+// of `band` rows: each band is one contiguous range of the row-major image,
+// brought in by a single TMA bulk copy (16-byte aligned start, 16-byte multiple
+// size; the <= 3 elements of a ragged array tail are loaded directly) into one
+// of two buffers, two bands ahead, completing on that buffer's mbarrier.
+constexpr int kFrThreads = 256;
+constexpr int kFrViews = 4;
+constexpr int kFrRaysPerThread = 4;
+constexpr int kFrLanesPerView = kFrThreads / kFrViews;          // 64
+constexpr int kFrChunk = kFrLanesPerView * kFrRaysPerThread;    // 256 channels
+
+struct FrConst {
+    int ns, na, n;          // n = nx = ny
+    int band;               // rows per band
+    int buf_floats;         // floats per band buffer (>= band*n + 8, multiple of 32)
+    long long total;        // elements of one source array (batch * n * n)
+    long long total4;       // total rounded down to 4
+    double dx, dy;
+    size_t proj_stride;
+};
+
+__global__ void __launch_bounds__(kFrThreads, 4)
+    fp_rows_f32(const float* __restrict__ img, const float* __restrict__ imgT,
+                float* __restrict__ proj, const double* __restrict__ sincos,
+                const double* __restrict__ bo, const int* __restrict__ usex, const FrConst c)
+{
+    extern __shared__ __align__(128) unsigned char fr_dyn[];
+    float* buf = reinterpret_cast<float*>(fr_dyn + ((128u - (smem_u32(fr_dyn) & 127u)) & 127u));
+    __shared__ __align__(8) unsigned long long s_bar[2];
+    __shared__ int s_ok;
+
+    const int tid = threadIdx.x;
+    const int vl = tid / kFrLanesPerView, lv = tid - vl * kFrLanesPerView;
+    const int ia = blockIdx.x * kFrViews + vl;
+    const int item = blockIdx.z;
+    const bool view_ok = ia < c.na;
+    const int cls = view_ok ? (usex[ia] != 0 ? 0 : 1) : -1;
+
+    long long X[kFrRaysPerThread];
+    int k0[kFrRaysPerThread], k1[kFrRaysPerThread];
+    float sum[kFrRaysPerThread];
+    long long S = 0;
+#pragma unroll
+    for (int j = 0; j < kFrRaysPerThread; ++j) {
+        const int is = blockIdx.y * kFrChunk + lv + j * kFrLanesPerView;
+        X[j] = 0;
+        k0[j] = 0;
+        k1[j] = -1;
+        sum[j] = 0.0f;
+        if (view_ok && is < c.ns) {
+            const size_t ray = static_cast<size_t>(ia) * c.ns + is;
+            const double begin = bo[2 * ray], step = bo[2 * ray + 1];
+            ray_range(begin, step, c.n, c.n - 1, &k0[j], &k1[j]);
+            X[j] = ray_line(begin, step, k0[j], k1[j], &S);
+        }
+    }
+    // zero both buffers once: positions never written by a copy then read as 0
+    for (int i = tid; i < 2 * c.buf_floats; i += kFrThreads) buf[i] = 0.0f;
+    if (tid == 0) {
+        mbar_init(smem_u32(&s_bar[0]), 1);
+        mbar_init(smem_u32(&s_bar[1]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    const int nbands = (c.n + c.band - 1) / c.band;
+    unsigned uses0 = 0u, uses1 = 0u;  // completed waits on each barrier (tid 0's count)
+    for (int pass = 0; pass < 2; ++pass) {
+        if (!__syncthreads_or(cls == pass)) continue;
+        const float* src = pass == 0 ? img : imgT;
+        const long long item0 = static_cast<long long>(item) * c.n * c.n;
+        // band t covers rows [t*band, t*band + nb) = elements [g, g + nb*n) of src
+        auto band_start = [&](int t) -> long long {
+            return item0 + static_cast<long long>(t) * c.band * c.n;
+        };
+        auto issue = [&](int t) {
+            if (t >= nbands) return;
+            const int nb = min(c.band, c.n - t * c.band);
+            const long long g = band_start(t), ga = g & ~3ll;
+            const long long g1 = min((g + static_cast<long long>(nb) * c.n + 3) & ~3ll, c.total4);
+            const unsigned bar = smem_u32(&s_bar[t & 1]);
+            const unsigned bytes = g1 > ga ? static_cast<unsigned>((g1 - ga) * sizeof(float)) : 0u;
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_expect_tx(bar, bytes);
+            if (bytes) bulk_load(smem_u32(buf + (t & 1) * c.buf_floats), src + ga, bytes, bar);
+        };
+        if (tid == 0) {
+            issue(0);
+            issue(1);
+        }
+        for (int t = 0; t < nbands; ++t) {
+            const int nb = min(c.band, c.n - t * c.band);
+            const long long g = band_start(t), ga = g & ~3ll;
+            float* bb = buf + (t & 1) * c.buf_floats;
+            if (tid == 0) {
+                const unsigned parity = (t & 1) ? (uses1++ & 1u) : (uses0++ & 1u);
+                s_ok = mbar_wait_bounded(smem_u32(&s_bar[t & 1]), parity);
+                // the ragged tail of the array (not a 16-byte multiple) comes directly
+                const long long gend = g + static_cast<long long>(nb) * c.n;
+                for (long long i = max(c.total4, ga); i < min(gend, c.total); ++i) bb[i - ga] = src[i];
+            }
+            __syncthreads();
+            if (!s_ok) {
+                if (tid == 0) raise_flag(kFlagWaitTimeout);
+                return;
+            }
+            if (cls == pass) {
+                const float* base = bb + (g - ga);
+                const int b0 = t * c.band;
+#pragma unroll
+                for (int j = 0; j < kFrRaysPerThread; ++j) {
+                    const int ka = max(k0[j], b0), kb = min(k1[j], b0 + nb - 1);
+                    if (ka > kb) continue;
+                    long long x = X[j] + static_cast<long long>(ka) * S;
+                    const float* row = base + (ka - b0) * c.n;
+                    float acc = 0.0f;  // this band's partial sum (blocked summation)
+#pragma unroll 4
+                    for (int k = ka; k <= kb; ++k) {
+                        const int i1 = static_cast<int>(x >> 32);
+                        const float u = frac_of(x);
+                        const float p0 = row[i1], p1 = row[i1 + 1];
+                        acc = fmaf(u, p1 - p0, acc + p0);
+                        x += S;
+                        row += c.n;
+                    }
+                    sum[j] += acc;
+                }
+            }
+            __syncthreads();
+            if (tid == 0) issue(t + 2);
+        }
+    }
+    if (view_ok) {
+        const double dw = cls == 0 ? fabs(c.dy / sincos[2 * ia + 1]) : fabs(c.dx / sincos[2 * ia]);
+        float* P = proj + item * c.proj_stride + static_cast<size_t>(ia) * c.ns;
+#pragma unroll
+        for (int j = 0; j < kFrRaysPerThread; ++j) {
+            const int is = blockIdx.y * kFrChunk + lv + j * kFrLanesPerView;
+            if (is < c.ns) P[is] = static_cast<float>(sum[j] * dw);
+        }
+    }
+}
+
+// imgT[b][x][y] = img[b][y][x] for n x n images (32x32 tiles through shared memory).
+__global__ void __launch_bounds__(256) transpose_f32(const float* __restrict__ in, float* __restrict__ out, int n)
+{
+    __shared__ float t[32][33];
+    const size_t off = static_cast<size_t>(blockIdx.z) * n * n;
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        const int y = y0 + r, x = x0 + threadIdx.x;
+        if (x < n && y < n) t[r][threadIdx.x] = in[off + static_cast<size_t>(y) * n + x];
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        const int x = x0 + r, y = y0 + threadIdx.x;
+        if (x < n && y < n) out[off + static_cast<size_t>(x) * n + y] = t[threadIdx.x][r];
     }
 }
 
@@ -227,6 +400,9 @@ __global__ void __launch_bounds__(256)
             }
         }
         __syncthreads();
+        float blk[kFaRows];  // this view block's partial sums (blocked summation)
+#pragma unroll
+        for (int r = 0; r < kFaRows; ++r) blk[r] = 0.0f;
         for (int j = 0; j < nv; ++j) {
             const int ux = s_ux[j];
             const long long O1 = s_o1[j];
@@ -254,9 +430,11 @@ __global__ void __launch_bounds__(256)
                     const float d = fabsf(mf - static_cast<float>(is - mi));
                     part = fmaf(fmaf(-d, inv, 1.0f), __ldg(row + is), part);
                 }
-                acc[r] = fmaf(part, w, acc[r]);
+                blk[r] = fmaf(part, w, blk[r]);
             }
         }
+#pragma unroll
+        for (int r = 0; r < kFaRows; ++r) acc[r] += blk[r];
         __syncthreads();
     }
     float* O = img + blockIdx.z * c.img_stride;
@@ -377,6 +555,38 @@ int fp_forward(const ctr_par_param* p, const T* img, T* proj, const double* sc,
     int st = check_fp(p, img, proj, sc, bo, usex, batch);
     if (st) return st;
     if constexpr (sizeof(T) == 4) {
+        const int n = static_cast<int>(p->nx);
+        FrConst r{};
+        r.ns = p->ns; r.na = p->na; r.n = n;
+        r.band = std::max(2, std::min(32, 4096 / n));
+        r.buf_floats = (r.band * n + 8 + 31) / 32 * 32;
+        r.total = static_cast<long long>(batch) * n * n;
+        r.total4 = r.total & ~3ll;
+        r.dx = p->dx; r.dy = p->dy;
+        r.proj_stride = static_cast<size_t>(p->ns) * p->na;
+        const size_t smem = 128 + 2 * static_cast<size_t>(r.buf_floats) * sizeof(float);
+        if (smem <= 160 * 1024 && reinterpret_cast<uintptr_t>(img) % 16 == 0 && r.total < (1ll << 40)) {
+            // column-marching views run on the transposed image (stream-ordered scratch)
+            float* imgT = nullptr;
+            cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&imgT), r.total * sizeof(float), stream);
+            if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp_par_2d scratch: %s", cudaGetErrorString(e));
+            transpose_f32<<<dim3(div_up(n, 32), div_up(n, 32), batch), dim3(32, 8), 0, stream>>>(img, imgT, n);
+            int st2 = check_launch("fp_par_2d transpose");
+            if (st2 == CTR_OK) {
+                e = cudaFuncSetAttribute(fp_rows_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+                if (e != cudaSuccess) {
+                    st2 = fail(CTR_ERR_CUDA, "fp smem: %s", cudaGetErrorString(e));
+                } else {
+                    dim3 grid(div_up(p->na, kFrViews), div_up(p->ns, kFrChunk), batch);
+                    fp_rows_f32<<<grid, kFrThreads, smem, stream>>>(img, imgT, proj, sc, bo, usex, r);
+                    st2 = check_launch("fp_par_2d");
+                }
+            }
+            cudaFreeAsync(imgT, stream);
+            return st2;
+        }
+        // fallback: image bands staged with plain loads
         FpConst c = fp_const(p);
         c.views = std::max(1, std::min(4, kFpThreads * kFpMaxRays / static_cast<int>(p->ns)));
         if (c.views * static_cast<long long>(p->ns) > kFpThreads * kFpMaxRays)
@@ -384,12 +594,12 @@ int fp_forward(const ctr_par_param* p, const T* img, T* proj, const double* sc,
                         kFpThreads * kFpMaxRays);
         const int len = std::max(p->nx, p->ny) + 1;
         c.band = std::max(1, std::min(32, 16384 / len));
-        const size_t smem = sizeof(float) * static_cast<size_t>(c.band) * len;
+        const size_t smem2 = sizeof(float) * static_cast<size_t>(c.band) * len;
         cudaError_t e = cudaFuncSetAttribute(fp_band_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             static_cast<int>(smem));
+                                             static_cast<int>(smem2));
         if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp smem: %s", cudaGetErrorString(e));
         dim3 grid(div_up(p->na, c.views), batch);
-        fp_band_f32<<<grid, kFpThreads, smem, stream>>>(img, proj, sc, bo, usex, c);
+        fp_band_f32<<<grid, kFpThreads, smem2, stream>>>(img, proj, sc, bo, usex, c);
     } else {
         dim3 grid(div_up(p->ns, kFp64Threads), p->na, batch);
         fp_ray_kernel<T><<<grid, kFp64Threads, 0, stream>>>(img, proj, sc, bo, usex, p->ns, p->na,

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "ctr_common.cuh"
+#include "host_geometry.h"
 
 namespace ctr {
 
@@ -33,10 +34,15 @@ int upload(V* dst, const std::vector<V>& src, cudaStream_t stream, const char* w
     return CTR_OK;
 }
 
+bool views_along_x(double angle)
+{
+    return !((angle >= kPi4 && angle < 3 * kPi4) || (angle >= 5 * kPi4 && angle < 7 * kPi4));
+}
+}  // namespace
+
 void pixel_positions(unsigned nx, unsigned ny, double dx, double dy, double ox, double oy,
                      std::vector<double>& xpos, std::vector<double>& ypos)
 {
-    // reference src/bp_fan_2d.cc:22-42
     const double centx = static_cast<double>(nx - 1) / 2 + ox;
     const double centy = static_cast<double>(ny - 1) / 2 + oy;
     xpos.resize(nx);
@@ -52,11 +58,60 @@ void pixel_positions(unsigned nx, unsigned ny, double dx, double dy, double ox, 
     }
 }
 
-bool views_along_x(double angle)
+void fan_sincos(unsigned na, double orbit_start, double orbit, std::vector<double>& sc)
 {
-    return !((angle >= kPi4 && angle < 3 * kPi4) || (angle >= 5 * kPi4 && angle < 7 * kPi4));
+    sc.resize(2 * static_cast<size_t>(na));
+    double angle = orbit_start;
+    for (unsigned ia = 0; ia < na; ++ia) {
+        sc[2 * ia] = std::sin(angle);
+        sc[2 * ia + 1] = std::cos(angle);
+        angle += orbit;
+    }
 }
-}  // namespace
+
+bool ramp_taps(unsigned ns, double ds, double dsd, int type, std::vector<double>& taps)
+{
+    const int n = static_cast<int>(ns);
+    taps.assign(2 * static_cast<size_t>(n) + 1, 0.0);
+    double* h = taps.data() + n;
+    if (type == 0 || type == 2) {
+        const double ds2_inv = 1.0 / (ds * ds);
+        const double pi2_inv = 1.0 / (kPi * kPi);
+        for (int k = -n; k <= n; ++k)
+            h[k] = k == 0 ? 0.25 * ds2_inv
+                          : (k % 2 == 0 ? 0.0 : -pi2_inv * ds2_inv / static_cast<double>(k * k));
+        return true;
+    }
+    if (type == 1) {
+        const double pidsd2_inv = 1.0 / (kPi * kPi * dsd * dsd);
+        for (int k = -n; k <= n; ++k) {
+            if (k == 0) {
+                h[k] = 0.25 / (ds * ds);
+            } else if (k % 2 == 0) {
+                h[k] = 0.0;
+            } else {
+                const double sa = std::sin(static_cast<double>(k) * ds / dsd);
+                h[k] = -pidsd2_inv / (sa * sa);
+            }
+        }
+        return true;
+    }
+    return false;
+}
+
+bool fan_weights(unsigned ns, double ds, double offset, double dso, double dsd, int type,
+                 std::vector<double>& w)
+{
+    if (type != 1 && type != 2) return false;
+    w.resize(ns);
+    const double cents = static_cast<double>(ns - 1) / 2 + offset;
+    for (unsigned is = 0; is < ns; ++is) {
+        const double s = ds * (static_cast<double>(is) - cents);
+        w[is] = type == 2 ? dso * std::fabs(std::cos(std::atan2(s, dsd))) / dsd
+                          : dso * std::fabs(std::cos(s / dsd)) / dsd;
+    }
+    return true;
+}
 
 int fail(int status, const char* fmt, ...)
 {
@@ -141,30 +196,9 @@ int ctr_ramp_filter_prep(const ctr_filter_param* p, double* filter, cudaStream_t
     // reference src/filter.cc:18-65
     if (!p || bad_ptr(filter)) return fail(CTR_ERR_INVALID_ARG, "null argument");
     if (p->ns < 1) return fail(CTR_ERR_INVALID_ARG, "ns must be >= 1");
-    const int n = static_cast<int>(p->ns);
-    std::vector<double> taps(2 * n + 1);
-    double* h = taps.data() + n;
-    if (p->type == 0 || p->type == 2) {
-        const double ds2_inv = 1.0 / (p->ds * p->ds);
-        const double pi2_inv = 1.0 / (kPi * kPi);
-        for (int k = -n; k <= n; ++k)
-            h[k] = k == 0 ? 0.25 * ds2_inv
-                          : (k % 2 == 0 ? 0.0 : -pi2_inv * ds2_inv / static_cast<double>(k * k));
-    } else if (p->type == 1) {
-        const double pidsd2_inv = 1.0 / (kPi * kPi * p->dsd * p->dsd);
-        for (int k = -n; k <= n; ++k) {
-            if (k == 0) {
-                h[k] = 0.25 / (p->ds * p->ds);
-            } else if (k % 2 == 0) {
-                h[k] = 0.0;
-            } else {
-                const double sa = std::sin(static_cast<double>(k) * p->ds / p->dsd);
-                h[k] = -pidsd2_inv / (sa * sa);
-            }
-        }
-    } else {
+    std::vector<double> taps;
+    if (!ramp_taps(p->ns, p->ds, p->dsd, p->type, taps))
         return fail(CTR_ERR_INVALID_ARG, "ramp filter type %d (0 par, 1 fan, 2 flat)", p->type);
-    }
     return upload(filter, taps, stream, "ramp filter taps");
 }
 
@@ -175,13 +209,8 @@ int ctr_bp_fan_2d_prep(const ctr_fan_bp_param* p, double* xpos, double* ypos,
     if (!p || bad_ptr(xpos) || bad_ptr(ypos) || bad_ptr(sincostbl))
         return fail(CTR_ERR_INVALID_ARG, "null argument");
     if (p->na < 1 || p->nx < 1 || p->ny < 1) return fail(CTR_ERR_INVALID_ARG, "empty geometry");
-    std::vector<double> sc(2 * p->na), xp, yp;
-    double angle = p->orbit_start;
-    for (unsigned ia = 0; ia < p->na; ++ia) {
-        sc[2 * ia] = std::sin(angle);
-        sc[2 * ia + 1] = std::cos(angle);
-        angle += p->orbit;
-    }
+    std::vector<double> sc, xp, yp;
+    fan_sincos(p->na, p->orbit_start, p->orbit, sc);
     pixel_positions(p->nx, p->ny, p->dx, p->dy, p->offset_x, p->offset_y, xp, yp);
     int st = upload(sincostbl, sc, stream, "sincostbl");
     if (st == CTR_OK) st = upload(xpos, xp, stream, "xpos");

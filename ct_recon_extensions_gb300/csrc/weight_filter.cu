@@ -61,16 +61,16 @@ int launch_fan_weighting(const ctr_fan_weighting_param* p, const T* in, T* out, 
 // ---- ramp filter ---------------------------------------------------------
 
 constexpr int kFilterThreads = 256;
-constexpr int kFilterRows = 4;
+constexpr int kFilterRows = kFilterRowsPerBlock;
 
-// Shared layout: tpos[ns] (h[+k], k = 0..ns-1), tneg[ns] (h[-k]), rows[kFilterRows][ns].
+// Filters rows [r0, r0 + nr) (nr <= kFilterRows) of one item.  Shared layout:
+// tpos[ns] (h[+k], k = 0..ns-1), tneg[ns] (h[-k]), rows[kFilterRows][ns].
 template <typename T, bool kGrad>
-__global__ void __launch_bounds__(kFilterThreads)
-    ramp_filter_kernel(const T* __restrict__ in, const double* __restrict__ filter,
-                       T* __restrict__ out, const float* __restrict__ weight, unsigned ns,
-                       unsigned long long rows, double ds)
+__device__ __forceinline__ void filter_rows(const T* __restrict__ in, const double* __restrict__ filter,
+                                            T* __restrict__ out, const float* __restrict__ weight,
+                                            unsigned ns, unsigned long long r0, int nr, double ds,
+                                            unsigned char* smem_raw)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     T* tpos = reinterpret_cast<T*>(smem_raw);
     T* tneg = tpos + ns;
     T* xs = tneg + ns;
@@ -90,8 +90,6 @@ __global__ void __launch_bounds__(kFilterThreads)
         if (k > 0 && (k & 1) == 0 && (hp != 0.0 || hn != 0.0)) fast = false;
     }
     if (!fast) s_fast = 0;
-    const unsigned long long r0 = static_cast<unsigned long long>(blockIdx.x) * kFilterRows;
-    const int nr = static_cast<int>(rows - r0 < kFilterRows ? rows - r0 : kFilterRows);
     for (int idx = threadIdx.x; idx < kFilterRows * n; idx += kFilterThreads) {
         const int r = idx / n, j = idx - r * n;
         T v = 0;
@@ -127,6 +125,30 @@ __global__ void __launch_bounds__(kFilterThreads)
             if (r < nr) out[(r0 + r) * ns + i] = t0 * xs[r * n + i] + (left[r] + right[r]);
         }
     }
+    __syncthreads();  // shared buffers are free for the caller's next call
+}
+
+template <typename T, bool kGrad>
+__global__ void __launch_bounds__(kFilterThreads)
+    ramp_filter_kernel(const T* __restrict__ in, const double* __restrict__ filter,
+                       T* __restrict__ out, const float* __restrict__ weight, unsigned ns,
+                       unsigned long long rows, double ds)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const unsigned long long r0 = static_cast<unsigned long long>(blockIdx.x) * kFilterRows;
+    const int nr = static_cast<int>(rows - r0 < kFilterRows ? rows - r0 : kFilterRows);
+    filter_rows<T, kGrad>(in, filter, out, weight, ns, r0, nr, ds, smem_raw);
+}
+
+// Batched FP32 filtering with pre-weighting: one CTA per (job, row block).
+__global__ void __launch_bounds__(kFilterThreads)
+    ramp_filter_batch_kernel(const FilterJob* __restrict__ jobs, const int2* __restrict__ blocks)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int2 b = blocks[blockIdx.x];  // (job, first row)
+    const FilterJob J = jobs[b.x];
+    const int nr = min(kFilterRows, static_cast<int>(J.nrow) - b.y);
+    filter_rows<float, false>(J.in, J.taps, J.out, J.weight, J.ns, b.y, nr, J.ds, smem_raw);
 }
 
 template <typename T, bool kGrad>
@@ -158,6 +180,21 @@ int ramp_filter_weighted_f32(const ctr_filter_param* p, const float* in, const d
                              float* out, const float* weight, int batch, cudaStream_t stream)
 {
     return launch_ramp_filter<float, false>(p, in, filter, out, weight, batch, stream);
+}
+
+// Batched weighting + filtering of a job list (see FilterJob); `blocks` lists
+// (job, first row) pairs, one CTA each; max_ns sizes the shared memory.
+int ramp_filter_batch_f32(const FilterJob* jobs, const int2* blocks, int n_blocks, unsigned max_ns,
+                          cudaStream_t stream)
+{
+    const size_t smem = sizeof(float) * static_cast<size_t>(max_ns) * (2 + kFilterRows);
+    if (smem > 200 * 1024) return fail(CTR_ERR_UNSUPPORTED, "ns=%u too wide for the filter tile", max_ns);
+    cudaError_t e = cudaFuncSetAttribute(ramp_filter_batch_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "filter smem: %s", cudaGetErrorString(e));
+    if (n_blocks > 0)
+        ramp_filter_batch_kernel<<<n_blocks, kFilterThreads, smem, stream>>>(jobs, blocks);
+    return check_launch("ramp_filter_batch");
 }
 
 }  // namespace ctr

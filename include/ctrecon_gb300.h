@@ -226,6 +226,61 @@ int ctr_fp_par_2d_grad_f64(const ctr_par_param* p, const double* proj, double* i
                            const double* weights, const double* pos, const int* usex,
                            int batch, cudaStream_t stream);
 
+
+/* ---- batched uneven fan-beam FBP (no reference counterpart: the reference
+ *      loops over batch items of one geometry, tensorflow/bp_fan_2d_ops.h:119-125) ----
+ * A plan reconstructs n items, each with its own FanBackprojection2DParam:
+ * fan weighting (type 1 fan / 2 flat) -> ramp filter (matching type) ->
+ * bp_fan_2d, as one batched filter launch and ONE persistent backprojection
+ * launch over all (item, tile) pairs, optionally captured in a CUDA graph and
+ * autotuned (tile shape, view-block depth) on the batch at creation.  The plan
+ * owns its tables and a filtered-sinogram workspace; run() takes HOST arrays
+ * of n DEVICE pointers (sinogram [na][ns] and image [ny][nx] per item) and is
+ * stream-ordered.  A plan serves one stream at a time. */
+typedef struct ctr_fbp_plan ctr_fbp_plan;
+typedef struct ctr_fbp_plan_info {
+    int n_items;
+    long long work_items;        /* (item, tile) pairs */
+    int tile_rows;               /* tile is 32 x tile_rows pixels */
+    int view_block;              /* views per group per staged block */
+    int ctas;                    /* persistent CTAs */
+    int autotuned;
+    double tuned_ms;             /* autotuner's time of the chosen config */
+    int graph;                   /* run() replays a CUDA graph */
+    unsigned long long workspace_bytes;
+    long long launches_per_run;  /* kernels (and memset) per run */
+} ctr_fbp_plan_info;
+#define CTR_PLAN_AUTOTUNE 1
+#define CTR_PLAN_GRAPH 2
+int ctr_fbp_fan_plan_create(const ctr_fan_bp_param* geoms, int n_items, int weighting, int flags,
+                            ctr_fbp_plan** plan);
+int ctr_fbp_fan_plan_run(ctr_fbp_plan* plan, const float* const* proj, float* const* img,
+                         cudaStream_t stream);
+int ctr_fbp_fan_plan_info(const ctr_fbp_plan* plan, ctr_fbp_plan_info* info);
+int ctr_fbp_fan_plan_destroy(ctr_fbp_plan* plan);
+
+/* ---- numpy extension ABI (reference numpy_ext, the *_npext.cu files and common.cu) ----
+ * Same names and signatures as the reference's libnumpy_ctext: handles over
+ * HOST double arrays, FP64 kernels, blocking.  set_device(-1) (the reference's
+ * CPU mode) returns false: this library is the GPU implementation only.
+ * Failures return false (or -1 from *_create) with ctr_last_error(). */
+bool set_device(const int device);                                /* common.cu:29-49 */
+bool clear(void);                                                 /* common.cu:51-60 */
+int fan_weighting_create(unsigned int ns, unsigned int nrow, double ds, double offset,
+                         double dso, double dsd, int type);       /* fan_weighting_npext.cu:86-93 */
+bool fan_weighting_run(int handle, double* in, double* out);      /* :95-100 */
+bool fan_weighting_destroy(int handle);                           /* :102-106 */
+int ramp_filter_create(unsigned int ns, unsigned int nrow, double ds, double dsd,
+                       int type);                                 /* filter_npext.cu:104-111 */
+bool ramp_filter_run(int handle, double* in, double* out);        /* :113-118 */
+bool ramp_filter_destroy(int handle);                             /* :120-124 */
+int fan_bp_2d_angle_create(double* angles, unsigned int ns, unsigned int na, double ds,
+                           double offset_s, unsigned int nx, unsigned int ny, double dx,
+                           double dy, double offset_x, double offset_y, double dso, double dsd,
+                           double fov);                           /* bp_fan_2d_angle_npext.cu:136-146 */
+bool fan_bp_2d_angle_run(int handle, double* in, double* out);    /* :148-153 */
+bool fan_bp_2d_angle_destroy(int handle);                         /* :155-159 */
+
 #ifdef __cplusplus
 }
 #endif
