@@ -96,6 +96,7 @@ PROTOTYPES = {
     "ctr_fbp_fan_plan_run": [c_void_p, ctypes.POINTER(c_void_p), ctypes.POINTER(c_void_p), _P],
     "ctr_fbp_fan_plan_info": [c_void_p, _S(PlanInfo)],
     "ctr_fbp_fan_plan_destroy": [c_void_p],
+    "ctr_fp_par_2d_f32_noalloc": [_S(ParParam), _P, _P, _P, _P, _P, c_int, _P],
 }
 for _t in ("f32", "f64"):
     PROTOTYPES.update({

@@ -22,6 +22,7 @@
 //
 // FP64 kernels follow the reference's arithmetic (one thread per ray / pixel).
 #include <algorithm>
+#include <mutex>
 
 #include "ctr_async.cuh"
 #include "ctr_common.cuh"
@@ -630,6 +631,84 @@ int fp_adjoint(const ctr_par_param* p, const T* proj, T* img, const double* w,
     return check_launch("fp_par_2d_grad");
 }
 
+// ---- allocation-free FP32 forward projection ---------------------------------
+// For callers that must not allocate device memory inside a call: a host
+// framework that hands out all device memory itself (its own pool, a fixed
+// arena), or a real-time loop that cannot wait on the allocator.  The
+// transposed image that column-marching views read lives in this fixed
+// file-scope array instead of stream-ordered scratch: at most
+// kFpNoAllocFloats = 4,194,304 floats (16 MiB), i.e. batch * nx * ny <= 2^22
+// (one 2048^2 image, or 16 images of 512^2).  The transpose overwrites every
+// element it later reads, so nothing in the array has to start at zero.
+// All calls on a device share the one array: calls ordered on one stream are
+// safe, calls that can overlap (two streams, two host threads without
+// ordering) race on it and give wrong results.
+constexpr long long kFpNoAllocFloats = 1ll << 22;
+static __device__ __align__(256) float g_fp_noalloc_scratch[kFpNoAllocFloats];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+float* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// The array's device address on the current device, looked up once per device
+// (cudaGetSymbolAddress; the first call on a device does this set-up).
+int noalloc_scratch(float** out)
+{
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(CTR_ERR_DEVICE, "cudaGetDevice: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= kNoAllocMaxDevices)
+        return fail(CTR_ERR_UNSUPPORTED, "device %d >= %d", dev, kNoAllocMaxDevices);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* ptr = nullptr;
+        e = cudaGetSymbolAddress(&ptr, g_fp_noalloc_scratch);
+        if (e != cudaSuccess || !ptr)
+            return fail(CTR_ERR_CUDA, "fp_par_2d_f32_noalloc scratch address: %s",
+                        cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = static_cast<float*>(ptr);
+    }
+    *out = g_noalloc_ptr[dev];
+    return CTR_OK;
+}
+
+int fp_forward_noalloc(const ctr_par_param* p, const float* img, float* proj, const double* sc,
+                       const double* bo, const int* usex, int batch, cudaStream_t stream)
+{
+    int st = check_fp(p, img, proj, sc, bo, usex, batch);
+    if (st) return st;
+    const long long n = p->nx;
+    if (n > 2048 || batch * n * n > kFpNoAllocFloats)
+        return fail(CTR_ERR_UNSUPPORTED,
+                    "fp_par_2d_f32_noalloc: batch*nx*ny = %d*%lld*%lld exceeds its fixed scratch of "
+                    "%lld floats (16 MiB); split the batch or call ctr_fp_par_2d_f32",
+                    batch, n, n, kFpNoAllocFloats);
+    if (reinterpret_cast<uintptr_t>(img) % 16 != 0)
+        return fail(CTR_ERR_INVALID_ARG, "fp_par_2d_f32_noalloc: img must be 16-byte aligned");
+    FrConst r{};
+    r.ns = p->ns; r.na = p->na; r.n = static_cast<int>(n);
+    r.band = std::max(2, std::min(32, static_cast<int>(4096 / n)));
+    r.buf_floats = (r.band * r.n + 8 + 31) / 32 * 32;
+    r.total = batch * n * n;
+    r.total4 = r.total & ~3ll;
+    r.dx = p->dx; r.dy = p->dy;
+    r.proj_stride = static_cast<size_t>(p->ns) * p->na;
+    const size_t smem = 128 + 2 * static_cast<size_t>(r.buf_floats) * sizeof(float);
+    float* imgT = nullptr;
+    st = noalloc_scratch(&imgT);
+    if (st) return st;
+    transpose_f32<<<dim3(div_up(n, 32), div_up(n, 32), batch), dim3(32, 8), 0, stream>>>(
+        img, imgT, r.n);
+    st = check_launch("fp_par_2d_f32_noalloc transpose");
+    if (st) return st;
+    cudaError_t e = cudaFuncSetAttribute(fp_rows_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp smem: %s", cudaGetErrorString(e));
+    dim3 grid(div_up(p->na, kFrViews), div_up(p->ns, kFrChunk), batch);
+    fp_rows_f32<<<grid, kFrThreads, smem, stream>>>(img, imgT, proj, sc, bo, usex, r);
+    return check_launch("fp_par_2d_f32_noalloc");
+}
+
 }  // namespace
 }  // namespace ctr
 
@@ -660,6 +739,12 @@ int ctr_fp_par_2d_grad_f64(const ctr_par_param* p, const double* proj, double* i
                            int batch, cudaStream_t stream)
 {
     return fp_adjoint<double>(p, proj, img, weights, pos, usex, batch, stream);
+}
+int ctr_fp_par_2d_f32_noalloc(const ctr_par_param* p, const float* img, float* proj,
+                              const double* sincostbl, const double* beginoffset, const int* usex,
+                              int batch, cudaStream_t stream)
+{
+    return fp_forward_noalloc(p, img, proj, sincostbl, beginoffset, usex, batch, stream);
 }
 
 }  // extern "C"

@@ -226,6 +226,24 @@ int ctr_fp_par_2d_grad_f64(const ctr_par_param* p, const double* proj, double* i
                            const double* weights, const double* pos, const int* usex,
                            int batch, cudaStream_t stream);
 
+/* ---- allocation-free FP32 forward projection (no counterpart in the
+ *      reference; same arguments and results as ctr_fp_par_2d_f32) ----
+ * For callers that cannot allocate device memory inside a call: a host that
+ * owns all device memory (its own pool or a fixed arena), or a real-time loop
+ * that must not wait on the allocator.  The scratch the projector needs (the
+ * transposed image) is a fixed 16 MiB array inside the library, so this call
+ * allocates nothing.  Limits: batch * nx * ny <= 4,194,304 floats (one
+ * 2048 x 2048 image, or 16 of 512 x 512); larger inputs return
+ * CTR_ERR_UNSUPPORTED.  img must be 16-byte aligned.
+ * The first call on each device looks up the array's address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls on a device share the array: calls
+ * ordered on one stream are fine, calls that may overlap (other streams,
+ * other host threads) race on it. */
+int ctr_fp_par_2d_f32_noalloc(const ctr_par_param* p, const float* img, float* proj,
+                              const double* sincostbl, const double* beginoffset,
+                              const int* usex, int batch, cudaStream_t stream);
+
 
 /* ---- batched uneven fan-beam FBP (no reference counterpart: the reference
  *      loops over batch items of one geometry, tensorflow/bp_fan_2d_ops.h:119-125) ----
