@@ -7,12 +7,13 @@
 // reference's CPU rule (src/fp_par_2d.cc:237,259); the ray sum is scaled by
 // dy/|cos| or dx/|sin|.
 //
-// FP32 forward: a CTA owns a few consecutive views and all their channels; it
-// streams the image through shared memory in bands of rows (or of columns,
-// stored transposed) that every ray of the CTA reads, so global reads are
-// coalesced and each image byte is fetched from L2 once per CTA.  Each ray's
-// sample range is decided once in FP64; positions are 32.32 fixed point, so
-// a sample costs one 64-bit add, the fraction and an 8-byte shared read pair.
+// FP32 forward: a persistent-style pipeline streams the image (and a
+// transposed copy for column-marching views) through shared memory in bands of
+// rows with TMA bulk copies; each lane keeps a few rays in registers.  Each
+// ray's sample range is decided once, in integer arithmetic with the
+// reference's FP64 rule taken over at ties (fp_setup.cuh); positions are 32.32
+// fixed point, so a sample costs one 64-bit add, two shared loads, the
+// fraction and two FP32 operations.
 //
 // FP32 adjoint: one thread per pixel gathers, for every view, the channels of
 // its footprint with the triangle weights of the reference's grad
@@ -23,9 +24,11 @@
 // FP64 kernels follow the reference's arithmetic (one thread per ray / pixel).
 #include <algorithm>
 #include <mutex>
+#include <numeric>
 
 #include "ctr_async.cuh"
 #include "ctr_common.cuh"
+#include "fp_setup.cuh"
 
 namespace ctr {
 namespace {
@@ -34,20 +37,8 @@ namespace {
 
 constexpr int kFpThreads = 512;
 constexpr int kFpMaxRays = 8;  // rays per thread
-// Sample positions are 32.32 fixed point.  Each ray's line X(k) = X0 + k*S is
-// anchored at its smallest-x valid sample, X(anchor) = round(x(anchor) * 2^32)
-// >= 0, and is monotonic along the ray, so X >= 0 on every valid sample and its
-// integer part is a valid pixel index; rounding S moves a position by at most
-// |k - anchor|/2 units (< 6e-8 px for 512 samples).
+// 2^32: the adjoint's channel positions are 32.32 fixed point.
 constexpr double kTwo32 = 4294967296.0;
-
-// 32.32 fixed-point line of a ray with FP64 start/step over samples [k0, k1].
-__device__ __forceinline__ long long ray_line(double begin, double step, int k0, int k1, long long* S)
-{
-    *S = llrint(step * kTwo32);
-    const int ka = step < 0.0 ? k1 : k0;  // smallest x
-    return llrint(fma(static_cast<double>(ka), step, begin) * kTwo32) - static_cast<long long>(ka) * *S;
-}
 
 struct FpConst {
     int ns, na, nx, ny;
@@ -60,45 +51,6 @@ struct FpConst {
 __device__ __forceinline__ float frac_of(long long X)
 {
     return __uint_as_float(0x3F800000u | (static_cast<unsigned>(X) >> 9)) - 1.0f;
-}
-
-// Sample range [k0, k1] of a ray with FP64 start/step: 0 <= begin + k*step <= lim
-// (the reference's inclusion rule, src/fp_par_2d.cc:237).
-__device__ void ray_range(double begin, double step, int nsamp, int lim, int* k0o, int* k1o)
-{
-    int k0 = 0, k1 = nsamp - 1;
-    if (step == 0.0) {
-        if (!(begin >= 0.0 && begin <= lim)) k1 = -1;
-    } else {
-        double a = (0.0 - begin) / step, b = (lim - begin) / step;
-        if (a > b) {
-            const double t = a;
-            a = b;
-            b = t;
-        }
-        k0 = max(k0, static_cast<int>(fmax(ceil(a), -1.0)));
-        k1 = min(k1, static_cast<int>(fmin(floor(b), static_cast<double>(nsamp))));
-        if (k0 <= k1) {  // settle the divisions' rounding on the samples themselves
-            const double xa = fma(static_cast<double>(k0), step, begin);
-            if (!(xa >= 0.0 && xa <= lim)) {
-                ++k0;
-            } else if (k0 > 0) {
-                const double xp = fma(static_cast<double>(k0 - 1), step, begin);
-                if (xp >= 0.0 && xp <= lim) --k0;
-            }
-        }
-        if (k0 <= k1) {
-            const double xb = fma(static_cast<double>(k1), step, begin);
-            if (!(xb >= 0.0 && xb <= lim)) {
-                --k1;
-            } else if (k1 < nsamp - 1) {
-                const double xn = fma(static_cast<double>(k1 + 1), step, begin);
-                if (xn >= 0.0 && xn <= lim) ++k1;
-            }
-        }
-    }
-    *k0o = k0;
-    *k1o = k1;
 }
 
 // A CTA projects `views` consecutive views (all channels).  Rays of row-marching
@@ -134,10 +86,8 @@ __global__ void __launch_bounds__(kFpThreads)
             const size_t ray = static_cast<size_t>(v0) * c.ns + r;
             const int ux = usex[ia] != 0;
             const double begin = bo[2 * ray], step = bo[2 * ray + 1];
-            const int nsamp = ux ? c.ny : c.nx;
-            const int lim = ux ? c.nx - 1 : c.ny - 1;
-            ray_range(begin, step, nsamp, lim, &k0[j], &k1[j]);
-            X[j] = ray_line(begin, step, k0[j], k1[j], &S[j]);
+            if (!ray_fixed(begin, step, c.nx, &X[j], &S[j], &k0[j], &k1[j]))
+                ray_fp64(begin, step, c.nx, &X[j], &S[j], &k0[j], &k1[j]);
             cls[j] = ux ? 0 : 1;
             has_cls[cls[j]] = true;
         }
@@ -193,152 +143,107 @@ __global__ void __launch_bounds__(kFpThreads)
     }
 }
 
-// ---- FP32 forward, row-band pipeline -------------------------------------------
+// ---- FP32 forward: ray set-up kernel + one pipelined pass over image bands ----
 //
-// Rays of column-marching views are run on a transposed copy of the image, so
-// every ray marches image rows.  A CTA owns kFrViews views x a chunk of
-// kFrChunk channels (4 rays of one view per thread, so the view's per-sample
-// step S is shared).  The source image streams through shared memory in bands
-// of `band` rows: each band is one contiguous range of the row-major image,
-// brought in by a single TMA bulk copy (16-byte aligned start, 16-byte multiple
-// size; the <= 3 elements of a ragged array tail are loaded directly) into one
-// of two buffers, two bands ahead, completing on that buffer's mbarrier.
-constexpr int kFrThreads = 256;
-constexpr int kFrViews = 4;
-constexpr int kFrRaysPerThread = 4;
-constexpr int kFrLanesPerView = kFrThreads / kFrViews;          // 64
-constexpr int kFrChunk = kFrLanesPerView * kFrRaysPerThread;    // 256 channels
+// fpx_setup decides every ray once: its sample range and 32.32 fixed-point
+// line (fp_setup.cuh), written to a per-call table; block 0 also lists the
+// views of each marching class and cuts the slots of each class among the
+// projector's CTAs.  fp_proj_f32 then streams, per CTA, the image (row-marching
+// views, usex) or its transposed copy (column-marching views) once through
+// shared memory in bands of rows, so every ray marches rows of the staged
+// array and every CTA serves one class.
+//
+// Rays are grouped in "slots" of 4 consecutive views of one class x 8
+// consecutive channels, one ray per lane (lane = 8*view + channel), so a
+// warp's 32 samples of one row fall within a few pixels of each other.  Slots
+// are ordered view quad by view quad, and within a quad the channel octets in
+// a strided order (slot_octet), so a contiguous range of slots mixes long
+// central rays and short edge rays.  A class's CTAs cut its slots at equal
+// shares of a per-view weight (samples per row grow with max(|sin|, |cos|)),
+// and a CTA deals its slots, sorted by their exact sample counts, to its warps
+// in snake order.  A round holds up to kFpxRound slots (one more round streams
+// the image again; rare).
+//
+// Pipeline: a producer lane copies band t (one contiguous range of the staged
+// row-major array, one TMA bulk copy) into stage t % 3 once every consumer
+// warp has released that stage, so warps drift up to two bands apart instead
+// of meeting at a CTA barrier per band.  Within a band a sample costs one
+// 64-bit add, the address, two shared loads, the fraction and two FP32
+// operations: the position's high word indexes the stage directly
+// (S2 = S + n * 2^32 steps one row down).
+//
+// Ties: a ray whose end sample lies within a hair of the image border (where
+// the fixed-point rule might differ from the reference's accumulated FP64
+// one) streams only its certain samples; the set-up decides its few border
+// samples by the reference's accumulation (acc_advance) and the ray's lane
+// adds the ones found inside, read from global memory, before writing.
+constexpr int kFpxWarps = 9;                         // consumer warps
+constexpr int kFpxThreads = (kFpxWarps + 1) * 32;    // + one producer warp
+constexpr int kFpxSlots = 8;                         // ray slots per consumer lane and round
+constexpr int kFpxRound = kFpxWarps * kFpxSlots;     // slots per round
+constexpr int kFpxStages = 3;
+constexpr int kFpxStageFloats = 8192;                // nominal stage: 32 KB
+constexpr int kFpxEmpty = 3 << 30;                   // ray code of a ray with no sample
+constexpr int kFpxMaxTies = 8192;                    // tie rays per call
+constexpr int kFpxSetupThreads = 256;
 
-struct FrConst {
-    int ns, na, n;          // n = nx = ny
-    int band;               // rows per band
-    int buf_floats;         // floats per band buffer (>= band*n + 8, multiple of 32)
-    long long total;        // elements of one source array (batch * n * n)
-    long long total4;       // total rounded down to 4
-    double dx, dy;
+struct FpxConst {
+    int ns, na, n;
+    int octets;            // channel octets per view quad
+    int stride;            // octet order within a quad: octet = rank * stride mod octets
+    int quads;             // view quads without class padding: ceil(na / 4)
+    int ctas;              // CTAs per item
+    int band, nbands;      // image rows per stage; stages
+    int stage_floats;      // floats per stage (>= band*n + 8, multiple of 32)
+    long long total;       // elements of one staged array (batch * n * n)
+    long long total4;      // total rounded down to 4
     size_t proj_stride;
+    float dx, dy;
 };
 
-__global__ void __launch_bounds__(kFrThreads, 4)
-    fp_rows_f32(const float* __restrict__ img, const float* __restrict__ imgT,
-                float* __restrict__ proj, const double* __restrict__ sincos,
-                const double* __restrict__ bo, const int* __restrict__ usex, const FrConst c)
+// Global tie entry (a ray the fixed-point rule could not settle).
+struct FpxTie {
+    int namb;
+    unsigned in;  // bit a: amb[a] is inside by the reference's accumulated rule
+    int amb[4];   // ambiguous samples next to the certain range
+};
+
+// The per-call tables (scratch) written by fpx_setup.
+struct FpxRays {
+    long long* X0;   // [na*ns] 32.32 position of sample 0
+    long long* S;    // [na*ns] 32.32 step
+    int* code;       // [na*ns] k0 | k1 << 15 | class << 30, or kFpxEmpty
+    int* tie;        // [na*ns] index into ties, or -1
+    int* views;      // [4 * (quads + 2)] views of class 0, then of class 1, -1 padded to quads
+    int* cuts;       // [ctas + 1] first slot of every CTA; cuts[ctas + 1] = CTAs of class 0
+    FpxTie* ties;    // [kFpxMaxTies]
+    int* nties;      // count (zeroed before fpx_setup)
+};
+
+__host__ __device__ inline size_t fpx_table_bytes(long long rays, int na, int ctas)
 {
-    extern __shared__ __align__(128) unsigned char fr_dyn[];
-    float* buf = reinterpret_cast<float*>(fr_dyn + ((128u - (smem_u32(fr_dyn) & 127u)) & 127u));
-    __shared__ __align__(8) unsigned long long s_bar[2];
-    __shared__ int s_ok;
+    const size_t r = static_cast<size_t>(rays);
+    const size_t views = 4 * (static_cast<size_t>(na) / 4 + 3);
+    return ((r * 24 + views * 4 + (static_cast<size_t>(ctas) + 2) * 4 + 63) & ~static_cast<size_t>(63)) +
+           64 + static_cast<size_t>(kFpxMaxTies) * sizeof(FpxTie);
+}
 
-    const int tid = threadIdx.x;
-    const int vl = tid / kFrLanesPerView, lv = tid - vl * kFrLanesPerView;
-    const int ia = blockIdx.x * kFrViews + vl;
-    const int item = blockIdx.z;
-    const bool view_ok = ia < c.na;
-    const int cls = view_ok ? (usex[ia] != 0 ? 0 : 1) : -1;
+// Channel octet of the slot with rank `r` within its view quad.  Ranks run
+// through the octets with a stride near 0.618 * octets (coprime), so a CTA's
+// contiguous range of slots mixes central rays (long) and edge rays (short or
+// empty).
+__device__ __forceinline__ int slot_octet(unsigned r, const FpxConst& c)
+{
+    return static_cast<int>((r * static_cast<unsigned>(c.stride)) % static_cast<unsigned>(c.octets));
+}
 
-    long long X[kFrRaysPerThread];
-    int k0[kFrRaysPerThread], k1[kFrRaysPerThread];
-    float sum[kFrRaysPerThread];
-    long long S = 0;
-#pragma unroll
-    for (int j = 0; j < kFrRaysPerThread; ++j) {
-        const int is = blockIdx.y * kFrChunk + lv + j * kFrLanesPerView;
-        X[j] = 0;
-        k0[j] = 0;
-        k1[j] = -1;
-        sum[j] = 0.0f;
-        if (view_ok && is < c.ns) {
-            const size_t ray = static_cast<size_t>(ia) * c.ns + is;
-            const double begin = bo[2 * ray], step = bo[2 * ray + 1];
-            ray_range(begin, step, c.n, c.n - 1, &k0[j], &k1[j]);
-            X[j] = ray_line(begin, step, k0[j], k1[j], &S);
-        }
-    }
-    // zero both buffers once: positions never written by a copy then read as 0
-    for (int i = tid; i < 2 * c.buf_floats; i += kFrThreads) buf[i] = 0.0f;
-    if (tid == 0) {
-        mbar_init(smem_u32(&s_bar[0]), 1);
-        mbar_init(smem_u32(&s_bar[1]), 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-
-    const int nbands = (c.n + c.band - 1) / c.band;
-    unsigned uses0 = 0u, uses1 = 0u;  // completed waits on each barrier (tid 0's count)
-    for (int pass = 0; pass < 2; ++pass) {
-        if (!__syncthreads_or(cls == pass)) continue;
-        const float* src = pass == 0 ? img : imgT;
-        const long long item0 = static_cast<long long>(item) * c.n * c.n;
-        // band t covers rows [t*band, t*band + nb) = elements [g, g + nb*n) of src
-        auto band_start = [&](int t) -> long long {
-            return item0 + static_cast<long long>(t) * c.band * c.n;
-        };
-        auto issue = [&](int t) {
-            if (t >= nbands) return;
-            const int nb = min(c.band, c.n - t * c.band);
-            const long long g = band_start(t), ga = g & ~3ll;
-            const long long g1 = min((g + static_cast<long long>(nb) * c.n + 3) & ~3ll, c.total4);
-            const unsigned bar = smem_u32(&s_bar[t & 1]);
-            const unsigned bytes = g1 > ga ? static_cast<unsigned>((g1 - ga) * sizeof(float)) : 0u;
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_expect_tx(bar, bytes);
-            if (bytes) bulk_load(smem_u32(buf + (t & 1) * c.buf_floats), src + ga, bytes, bar);
-        };
-        if (tid == 0) {
-            issue(0);
-            issue(1);
-        }
-        for (int t = 0; t < nbands; ++t) {
-            const int nb = min(c.band, c.n - t * c.band);
-            const long long g = band_start(t), ga = g & ~3ll;
-            float* bb = buf + (t & 1) * c.buf_floats;
-            if (tid == 0) {
-                const unsigned parity = (t & 1) ? (uses1++ & 1u) : (uses0++ & 1u);
-                s_ok = mbar_wait_bounded(smem_u32(&s_bar[t & 1]), parity);
-                // the ragged tail of the array (not a 16-byte multiple) comes directly
-                const long long gend = g + static_cast<long long>(nb) * c.n;
-                for (long long i = max(c.total4, ga); i < min(gend, c.total); ++i) bb[i - ga] = src[i];
-            }
-            __syncthreads();
-            if (!s_ok) {
-                if (tid == 0) raise_flag(kFlagWaitTimeout);
-                return;
-            }
-            if (cls == pass) {
-                const float* base = bb + (g - ga);
-                const int b0 = t * c.band;
-#pragma unroll
-                for (int j = 0; j < kFrRaysPerThread; ++j) {
-                    const int ka = max(k0[j], b0), kb = min(k1[j], b0 + nb - 1);
-                    if (ka > kb) continue;
-                    long long x = X[j] + static_cast<long long>(ka) * S;
-                    const float* row = base + (ka - b0) * c.n;
-                    float acc = 0.0f;  // this band's partial sum (blocked summation)
-#pragma unroll 4
-                    for (int k = ka; k <= kb; ++k) {
-                        const int i1 = static_cast<int>(x >> 32);
-                        const float u = frac_of(x);
-                        const float p0 = row[i1], p1 = row[i1 + 1];
-                        acc = fmaf(u, p1 - p0, acc + p0);
-                        x += S;
-                        row += c.n;
-                    }
-                    sum[j] += acc;
-                }
-            }
-            __syncthreads();
-            if (tid == 0) issue(t + 2);
-        }
-    }
-    if (view_ok) {
-        const double dw = cls == 0 ? fabs(c.dy / sincos[2 * ia + 1]) : fabs(c.dx / sincos[2 * ia]);
-        float* P = proj + item * c.proj_stride + static_cast<size_t>(ia) * c.ns;
-#pragma unroll
-        for (int j = 0; j < kFrRaysPerThread; ++j) {
-            const int is = blockIdx.y * kFrChunk + lv + j * kFrLanesPerView;
-            if (is < c.ns) P[is] = static_cast<float>(sum[j] * dw);
-        }
-    }
+// The ray of slot q on lane `lane`: view ia (-1: padding) and channel is.
+__device__ __forceinline__ void slot_ray(unsigned q, int lane, const FpxConst& c, const int* views,
+                                         int* ia, int* is)
+{
+    const unsigned quad = q / static_cast<unsigned>(c.octets);
+    *ia = views[quad * 4 + (lane >> 3)];
+    *is = slot_octet(q - quad * static_cast<unsigned>(c.octets), c) * 8 + (lane & 7);
 }
 
 // imgT[b][x][y] = img[b][y][x] for n x n images (32x32 tiles through shared memory).
@@ -355,6 +260,331 @@ __global__ void __launch_bounds__(256) transpose_f32(const float* __restrict__ i
     for (int r = threadIdx.y; r < 32; r += 8) {
         const int x = x0 + r, y = y0 + threadIdx.x;
         if (x < n && y < n) out[off + static_cast<size_t>(x) * n + y] = t[threadIdx.x][r];
+    }
+}
+
+// ---- set-up kernel: every ray once; block 0 the class lists and CTA cut ------
+__global__ void __launch_bounds__(kFpxSetupThreads)
+    fpx_setup(const double* __restrict__ sincos, const double* __restrict__ bo,
+              const int* __restrict__ usex, const FpxConst c, const FpxRays r)
+{
+    extern __shared__ float fs_P[];  // block 0: [quads + 3] running quad weights
+    __shared__ int s_cnt[kFpxSetupThreads + 1];
+    const int tid = threadIdx.x;
+    if (blockIdx.x == 0) {
+        // class lists: row-marching views (usex) first, then column-marching ones
+        const int per = (c.na + kFpxSetupThreads - 1) / kFpxSetupThreads;
+        const int v0 = min(tid * per, c.na), v1 = min(v0 + per, c.na);
+        int n0 = 0;
+        for (int v = v0; v < v1; ++v) n0 += usex[v] != 0 ? 1 : 0;
+        s_cnt[tid + 1] = n0;
+        __syncthreads();
+        if (tid == 0) {
+            s_cnt[0] = 0;
+            for (int i = 1; i <= kFpxSetupThreads; ++i) s_cnt[i] += s_cnt[i - 1];
+        }
+        __syncthreads();
+        const int N0 = s_cnt[kFpxSetupThreads], N1 = c.na - N0;
+        const int Q0 = (N0 + 3) / 4, Q1 = (N1 + 3) / 4, Qt = Q0 + Q1;
+        int o0 = s_cnt[tid], o1 = 4 * Q0 + (v0 - s_cnt[tid]);
+        for (int v = v0; v < v1; ++v) {
+            if (usex[v] != 0) r.views[o0++] = v;
+            else r.views[o1++] = v;
+        }
+        for (int i = N0 + tid; i < 4 * Q0; i += kFpxSetupThreads) r.views[i] = -1;
+        for (int i = 4 * Q0 + N1 + tid; i < 4 * Qt; i += kFpxSetupThreads) r.views[i] = -1;
+        __syncthreads();
+        // quad weights: its views (a view costs about the same at every angle:
+        // fewer samples at 45 degrees, but longer shared-memory and lane waits)
+        for (int qd = tid; qd < Qt; qd += kFpxSetupThreads) {
+            float w = 0.0f;
+            for (int k = 0; k < 4; ++k) w += r.views[qd * 4 + k] >= 0 ? 1.0f : 0.0f;
+            fs_P[qd + 1] = w;
+        }
+        __syncthreads();
+        if (tid == 0) {  // running sum (a short serial pass)
+            float acc = 0.0f;
+            fs_P[0] = 0.0f;
+            for (int qd = 1; qd <= Qt; ++qd) {
+                acc += fs_P[qd];
+                fs_P[qd] = acc;
+            }
+        }
+        __syncthreads();
+        // CTAs per class in proportion to the weight, each class cut evenly
+        const float W0 = fs_P[Q0], W1 = fs_P[Qt] - fs_P[Q0];
+        int G0 = 0;
+        if (N0 > 0) G0 = N1 > 0 ? static_cast<int>(rintf(c.ctas * W0 / (W0 + W1))) : c.ctas;
+        if (N0 > 0 && N1 > 0) G0 = max(1, min(c.ctas - 1, G0));
+        const int G1 = c.ctas - G0;
+        for (int i = tid; i <= c.ctas; i += kFpxSetupThreads) {
+            const bool cls1 = i > G0 || (i == G0 && G0 == 0);
+            const int gi = cls1 ? i - G0 : i, G = cls1 ? G1 : G0;
+            const int qa = cls1 ? Q0 : 0, qb = cls1 ? Qt : Q0;  // quads of the class
+            int s;
+            if (gi <= 0) {
+                s = qa * c.octets;
+            } else if (gi >= G) {
+                s = qb * c.octets;
+            } else {
+                const float T = fs_P[qa] + (fs_P[qb] - fs_P[qa]) * (static_cast<float>(gi) / G);
+                int lo = qa, hi = qb - 1;  // largest Q with P[Q] <= T
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (fs_P[mid] <= T) lo = mid;
+                    else hi = mid - 1;
+                }
+                const float f = (T - fs_P[lo]) / (fs_P[lo + 1] - fs_P[lo]);
+                int rank = static_cast<int>(ceilf(f * static_cast<float>(c.octets)));
+                rank = rank < 0 ? 0 : (rank > c.octets ? c.octets : rank);
+                s = min(lo * c.octets + rank, qb * c.octets);
+            }
+            r.cuts[i] = s;
+        }
+        if (tid == 0) r.cuts[c.ctas + 1] = G0;
+    }
+    const int rays = c.na * c.ns;
+    for (int ray = blockIdx.x * kFpxSetupThreads + tid; ray < rays; ray += gridDim.x * kFpxSetupThreads) {
+        const int ia = ray / c.ns;
+        const double begin = bo[2 * static_cast<size_t>(ray)], step = bo[2 * static_cast<size_t>(ray) + 1];
+        long long X0 = 0, S = 0;
+        int k0, k1, tie = -1;
+        if (!ray_fixed(begin, step, c.n, &X0, &S, &k0, &k1)) {
+            int amb[4], namb = 0;
+            bool done = false;
+            if (ray_split(begin, step, c.n, &X0, &S, &k0, &k1, amb, &namb)) {
+                const int e = atomicAdd(r.nties, 1);
+                if (e < kFpxMaxTies) {
+                    // the reference's decisions for the ambiguous samples, walked in order
+                    for (int a = 1; a < namb; ++a)
+                        for (int b = a; b > 0 && amb[b] < amb[b - 1]; --b) {
+                            const int tmp = amb[b];
+                            amb[b] = amb[b - 1];
+                            amb[b - 1] = tmp;
+                        }
+                    AccWalk w{begin, 0};
+                    unsigned in = 0u;
+                    for (int a = 0; a < namb; ++a) {
+                        acc_advance(&w, step, amb[a]);
+                        if (w.x >= 0.0 && w.x <= static_cast<double>(c.n - 1)) in |= 1u << a;
+                    }
+                    FpxTie& t = r.ties[e];
+                    t.namb = namb;
+                    t.in = in;
+                    for (int a = 0; a < 4; ++a) t.amb[a] = a < namb ? amb[a] : 0;
+                    tie = e;
+                    done = true;
+                }
+            }
+            if (!done) ray_fp64(begin, step, c.n, &X0, &S, &k0, &k1);
+        }
+        const int cls = usex[ia] != 0 ? 0 : 1;
+        r.X0[ray] = X0;
+        r.S[ray] = S;
+        r.code[ray] = k0 <= k1 ? (k0 | (k1 << 15) | (cls << 30)) : kFpxEmpty;
+        r.tie[ray] = tie;
+    }
+}
+
+__global__ void __launch_bounds__(kFpxThreads, 2)
+    fp_proj_f32(const float* __restrict__ img, const float* __restrict__ imgT,
+                float* __restrict__ proj, const double* __restrict__ sincos,
+                const int* __restrict__ usex, const FpxConst c, const FpxRays r)
+{
+    extern __shared__ __align__(128) unsigned char fpx_dyn[];
+    float* stage = reinterpret_cast<float*>(fpx_dyn + ((128u - (smem_u32(fpx_dyn) & 127u)) & 127u));
+    __shared__ __align__(8) unsigned long long s_full[kFpxStages], s_empty[kFpxStages];
+    __shared__ int s_work[kFpxRound];
+    __shared__ int s_assign[kFpxWarps][kFpxSlots];  // slot of the round, or -1
+    __shared__ int s_abort;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int n = c.n;
+    const long long item0 = static_cast<long long>(blockIdx.y) * n * n;
+    const float* I = img + item0;
+    const int q_lo = r.cuts[blockIdx.x], q_hi = r.cuts[blockIdx.x + 1];
+    const bool cls1 = static_cast<int>(blockIdx.x) >= r.cuts[c.ctas + 1];
+    const float* src = cls1 ? imgT : img;  // the staged array: rows are the marched lines
+    if (tid == 0) {
+        s_abort = 0;
+        for (int s = 0; s < kFpxStages; ++s) {
+            mbar_init(smem_u32(&s_full[s]), 1);
+            mbar_init(smem_u32(&s_empty[s]), kFpxWarps);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+
+    int g = 0;  // band instances so far (producer and consumers count alike)
+    for (int base = q_lo; base < q_hi; base += kFpxRound) {
+        const int m = min(kFpxRound, q_hi - base);
+        for (int i = tid; i < kFpxRound; i += kFpxThreads) (&s_assign[0][0])[i] = -1;
+        // ---- sample counts of the round's slots
+        if (warp < kFpxWarps) {
+            for (int t = warp; t < m; t += kFpxWarps) {
+                int ia, is, cnt = 0;
+                slot_ray(static_cast<unsigned>(base + t), lane, c, r.views, &ia, &is);
+                if (ia >= 0 && is < c.ns) {
+                    const int code = r.code[ia * c.ns + is];
+                    if (code != kFpxEmpty) cnt = ((code >> 15) & 0x7FFF) - (code & 0x7FFF) + 1;
+                }
+                const unsigned tot = __reduce_add_sync(0xffffffffu, static_cast<unsigned>(cnt));
+                if (lane == 0) s_work[t] = static_cast<int>(tot);
+            }
+        }
+        __syncthreads();
+        // ---- deal the slots, largest first, to the warps in snake order
+        if (tid < m) {
+            const int wt = s_work[tid];
+            int rk = 0;
+            for (int u = 0; u < m; ++u) {
+                const int wu = s_work[u];
+                rk += (wu > wt || (wu == wt && u < tid)) ? 1 : 0;
+            }
+            const int k = rk / kFpxWarps, pos = rk - k * kFpxWarps;
+            s_assign[(k & 1) ? kFpxWarps - 1 - pos : pos][k] = tid;
+        }
+        // zero the stages: the few slack elements past a band read as finite
+        for (int i = tid; i < kFpxStages * c.stage_floats; i += kFpxThreads) stage[i] = 0.0f;
+        __syncthreads();
+
+        if (warp == kFpxWarps) {
+            // ---- producer: one lane issues every band
+            if (lane == 0) {
+                bool alive = true;
+                int g1 = g;
+                for (int t = 0; t < c.nbands; ++t, ++g1) {
+                    const int s = g1 % kFpxStages;
+                    const int use = g1 / kFpxStages;
+                    if (use > 0 && !mbar_wait_bounded(smem_u32(&s_empty[s]), (use - 1) & 1)) {
+                        raise_flag(kFlagWaitTimeout);
+                        alive = false;
+                        break;
+                    }
+                    const int nb = min(c.band, n - t * c.band);
+                    const long long g0 = item0 + static_cast<long long>(t) * c.band * n;
+                    const long long ga = g0 & ~3ll, gend = g0 + static_cast<long long>(nb) * n;
+                    const long long gz = min((gend + 3) & ~3ll, c.total4);
+                    const unsigned bytes = gz > ga ? static_cast<unsigned>((gz - ga) * sizeof(float)) : 0u;
+                    float* dst = stage + s * c.stage_floats;
+                    // the ragged tail of the array (not a 16-byte multiple) comes directly
+                    for (long long i = max(c.total4, ga); i < min(gend, c.total); ++i) dst[i - ga] = src[i];
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    mbar_expect_tx(smem_u32(&s_full[s]), bytes);
+                    if (bytes) bulk_load(smem_u32(dst), src + ga, bytes, smem_u32(&s_full[s]));
+                }
+                if (!alive) {
+                    s_abort = 1;
+                    // let the copies in flight land before the CTA moves on or exits
+                    for (int gg = max(g, g1 - kFpxStages); gg < g1; ++gg)
+                        mbar_wait_bounded(smem_u32(&s_full[gg % kFpxStages]), (gg / kFpxStages) & 1);
+                }
+            }
+        } else {
+            // ---- consumers: the assigned slots' rays in registers
+            long long X0[kFpxSlots], S[kFpxSlots];
+            int code[kFpxSlots];
+            float sum[kFpxSlots];
+#pragma unroll
+            for (int j = 0; j < kFpxSlots; ++j) {
+                X0[j] = 0;
+                S[j] = 0;
+                code[j] = kFpxEmpty;
+                sum[j] = 0.0f;
+                const int t = s_assign[warp][j];
+                if (t >= 0) {
+                    int ia, is;
+                    slot_ray(static_cast<unsigned>(base + t), lane, c, r.views, &ia, &is);
+                    if (ia >= 0 && is < c.ns) {
+                        const int ray = ia * c.ns + is;
+                        code[j] = r.code[ray];
+                        X0[j] = r.X0[ray];
+                        S[j] = r.S[ray];
+                    }
+                }
+            }
+            int g1 = g;
+            bool alive = true;
+            for (int t = 0; t < c.nbands; ++t, ++g1) {
+                const int s = g1 % kFpxStages;
+                int ok = 1;
+                if (lane == 0) ok = mbar_wait_bounded(smem_u32(&s_full[s]), (g1 / kFpxStages) & 1);
+                ok = __shfl_sync(0xffffffffu, ok, 0);
+                if (!ok) {
+                    if (lane == 0) {
+                        raise_flag(kFlagWaitTimeout);
+                        s_abort = 1;
+                    }
+                    alive = false;
+                    break;
+                }
+                const int b0 = t * c.band, b1 = min(b0 + c.band, n) - 1;
+                const long long g0 = item0 + static_cast<long long>(b0) * n;
+                const float* bb = stage + s * c.stage_floats + (g0 & 3ll);
+#pragma unroll
+                for (int j = 0; j < kFpxSlots; ++j) {
+                    const int cj = code[j];
+                    if (cj == kFpxEmpty) continue;
+                    const int ka = max(cj & 0x7FFF, b0), kb = min((cj >> 15) & 0x7FFF, b1);
+                    if (ka > kb) continue;
+                    long long x = X0[j] + static_cast<long long>(ka) * S[j] +
+                                  (static_cast<long long>((ka - b0) * n) << 32);
+                    const long long S2 = S[j] + (static_cast<long long>(n) << 32);
+                    float a = 0.0f, b = 0.0f;  // this band's partial sums (blocked summation)
+#pragma unroll 4
+                    for (int k = ka; k <= kb; ++k) {
+                        const float* p = bb + static_cast<int>(x >> 32);
+                        const float p0 = p[0], p1 = p[1];
+                        a += p0;
+                        b = fmaf(frac_of(x), p1 - p0, b);
+                        x += S2;
+                    }
+                    sum[j] += a + b;
+                }
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(&s_empty[s]));
+            }
+            // ---- results (every ray of an assigned slot, also one with no valid sample)
+#pragma unroll
+            for (int j = 0; j < kFpxSlots; ++j) {
+                const int t = s_assign[warp][j];
+                if (!alive || t < 0) continue;
+                int ia, is;
+                slot_ray(static_cast<unsigned>(base + t), lane, c, r.views, &ia, &is);
+                if (ia < 0 || is >= c.ns) continue;
+                float v = sum[j];
+                const int gi = r.tie[ia * c.ns + is];
+                if (gi >= 0) {
+                    // border samples of a tie ray found inside by the reference's
+                    // rule: read directly
+                    const FpxTie& tt = r.ties[gi];
+                    for (int a = 0; a < tt.namb; ++a) {
+                        if (!((tt.in >> a) & 1u)) continue;
+                        const int k = tt.amb[a];
+                        const long long X = X0[j] + static_cast<long long>(k) * S[j];
+                        int hi = static_cast<int>(X >> 32);
+                        float u = frac_of(X);
+                        if (X < 0) {
+                            hi = 0;
+                            u = 0.0f;
+                        } else if (hi >= n - 1) {
+                            hi = n - 1;
+                            u = 0.0f;
+                        }
+                        // row ray: row k, columns hi, hi + 1; column ray: column k, rows hi, hi + 1
+                        const size_t i0 = cls1 ? static_cast<size_t>(hi) * n + k : static_cast<size_t>(k) * n + hi;
+                        const size_t d1 = cls1 ? static_cast<size_t>(n) : 1;
+                        const float p0 = I[i0], p1 = u > 0.0f ? I[i0 + d1] : p0;
+                        v += p0 + u * (p1 - p0);
+                    }
+                }
+                const float dw = cls1 ? c.dx / fabsf(dbl2flt(sincos[2 * ia]))
+                                      : c.dy / fabsf(dbl2flt(sincos[2 * ia + 1]));
+                proj[blockIdx.y * c.proj_stride + static_cast<size_t>(ia) * c.ns + is] = v * dw;
+            }
+        }
+        g += c.nbands;
+        __syncthreads();  // round end: every copy consumed; the next round may rewrite the tables
+        if (s_abort) break;
     }
 }
 
@@ -422,8 +652,26 @@ __global__ void __launch_bounds__(256)
                     L = R;
                     R = t;
                 }
-                const int lo = max(static_cast<int>((L + 0xFFFFFFFFll) >> 32), 0);
-                const int hi = min(static_cast<int>(R >> 32), c.ns - 1);
+                int lo = max(static_cast<int>((L + 0xFFFFFFFFll) >> 32), 0);
+                int hi = min(static_cast<int>(R >> 32), c.ns - 1);
+                if (along == 0 || along == n - 1) {
+                    // One-sided footprint of a border pixel: its end channel sits at
+                    // the pixel itself with weight ~1, so the range is decided in
+                    // FP64 exactly as the reference does (mid = begin + offset*along).
+                    const int lin = ux ? iy : ix;
+                    const double* pp = pos + (static_cast<size_t>(v0 + j) * n + min(lin, n - 1)) * 2;
+                    const double off = pp[1];
+                    const double mid = __dadd_rn(pp[0], __dmul_rn(off, static_cast<double>(along)));
+                    double left = along == 0 ? mid : __dsub_rn(mid, off);
+                    double right = along == n - 1 ? mid : __dadd_rn(mid, off);
+                    if (left > right) {
+                        const double t = left;
+                        left = right;
+                        right = t;
+                    }
+                    lo = static_cast<int>(fmax(ceil(left), 0.0));
+                    hi = static_cast<int>(fmin(floor(right), static_cast<double>(c.ns - 1)));
+                }
                 const int mi = static_cast<int>(MID >> 32);
                 const float mf = frac_of(MID);
                 float part = 0.0f;
@@ -549,6 +797,100 @@ FpConst fp_const(const ctr_par_param* p)
     return c;
 }
 
+// FpxConst of the pipelined FP32 forward projector, or false when the geometry
+// needs the plain band kernel (very wide images, a misaligned image, more
+// slots than 32-bit slot indices hold).
+bool fpx_const(const ctr_par_param* p, const void* img, int batch, FpxConst* out, size_t* smem)
+{
+    const int n = static_cast<int>(p->nx);
+    if (n > 8192 || reinterpret_cast<uintptr_t>(img) % 16 != 0) return false;
+    FpxConst c{};
+    c.ns = p->ns;
+    c.na = p->na;
+    c.n = n;
+    c.octets = static_cast<int>(div_up(p->ns, 8));
+    c.stride = std::max(1, static_cast<int>(0.618 * c.octets + 0.5));
+    while (std::gcd(c.stride, c.octets) != 1) ++c.stride;
+    c.quads = static_cast<int>(div_up(p->na, 4));
+    const long long slots = static_cast<long long>(c.quads + 2) * c.octets;  // with class padding
+    if (slots >= (1ll << 30) || static_cast<long long>(p->na) * p->ns >= (1ll << 31)) return false;
+    // two CTAs an SM; more when the mean CTA would exceed 7/8 of a round
+    const long long ctas = std::max<long long>(div_up(slots * 8, kFpxRound * 7), 2 * kSmCount);
+    c.ctas = static_cast<int>(std::min<long long>(ctas, slots));
+    c.band = std::max(1, std::min(32, kFpxStageFloats / n));
+    c.nbands = static_cast<int>(div_up(n, c.band));
+    c.stage_floats = (c.band * n + 8 + 31) / 32 * 32;
+    c.total = static_cast<long long>(batch) * n * n;
+    c.total4 = c.total & ~3ll;
+    c.proj_stride = static_cast<size_t>(p->ns) * p->na;
+    c.dx = static_cast<float>(p->dx);
+    c.dy = static_cast<float>(p->dy);
+    *smem = 128 + static_cast<size_t>(kFpxStages) * c.stage_floats * sizeof(float);
+    if (*smem > 200 * 1024) return false;
+    *out = c;
+    return true;
+}
+
+// Bytes of scratch the projector needs: the transposed image, then its tables.
+size_t fpx_scratch_bytes(const FpxConst& c)
+{
+    const size_t imgT = (static_cast<size_t>(c.total) * sizeof(float) + 255) & ~static_cast<size_t>(255);
+    return imgT + fpx_table_bytes(static_cast<long long>(c.na) * c.ns, c.na, c.ctas);
+}
+
+// Carves the tables out of `scratch` (256-byte aligned), after the transposed image.
+FpxRays fpx_rays(void* scratch, const FpxConst& c, float** imgT)
+{
+    const size_t rays = static_cast<size_t>(c.na) * c.ns;
+    unsigned char* b = static_cast<unsigned char*>(scratch);
+    *imgT = reinterpret_cast<float*>(b);
+    b += (static_cast<size_t>(c.total) * sizeof(float) + 255) & ~static_cast<size_t>(255);
+    FpxRays r;
+    r.X0 = reinterpret_cast<long long*>(b);
+    r.S = reinterpret_cast<long long*>(b + rays * 8);
+    r.code = reinterpret_cast<int*>(b + rays * 16);
+    r.tie = reinterpret_cast<int*>(b + rays * 20);
+    r.views = reinterpret_cast<int*>(b + rays * 24);
+    const size_t nviews = 4 * (static_cast<size_t>(c.na) / 4 + 3);
+    r.cuts = reinterpret_cast<int*>(b + rays * 24 + nviews * 4);
+    const size_t off = (rays * 24 + nviews * 4 + (static_cast<size_t>(c.ctas) + 2) * 4 + 63) &
+                       ~static_cast<size_t>(63);
+    r.nties = reinterpret_cast<int*>(b + off);
+    r.ties = reinterpret_cast<FpxTie*>(b + off + 64);
+    return r;
+}
+
+// Transposed copy, ray set-up and the projector, in stream order, on `scratch`.
+int launch_fpx(const FpxConst& c, size_t smem, void* scratch, const float* img, float* proj,
+               const double* sc, const double* bo, const int* usex, int batch, cudaStream_t stream)
+{
+    float* imgT = nullptr;
+    const FpxRays r = fpx_rays(scratch, c, &imgT);
+    const int n = c.n;
+    transpose_f32<<<dim3(div_up(n, 32), div_up(n, 32), batch), dim3(32, 8), 0, stream>>>(img, imgT, n);
+    int st = check_launch("fp_par_2d transpose");
+    if (st) return st;
+    cudaError_t e = cudaMemsetAsync(r.nties, 0, sizeof(int), stream);
+    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp_par_2d: %s", cudaGetErrorString(e));
+    const size_t setup_smem = (static_cast<size_t>(c.quads) + 3) * sizeof(float);
+    if (setup_smem > 48 * 1024) {
+        e = cudaFuncSetAttribute(fpx_setup, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(setup_smem));
+        if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp setup smem: %s", cudaGetErrorString(e));
+    }
+    const long long rays = static_cast<long long>(c.na) * c.ns;
+    const unsigned blocks = static_cast<unsigned>(
+        std::min<long long>(div_up(rays, kFpxSetupThreads), 8 * kSmCount));
+    fpx_setup<<<blocks, kFpxSetupThreads, setup_smem, stream>>>(sc, bo, usex, c, r);
+    st = check_launch("fp_par_2d set-up");
+    if (st) return st;
+    e = cudaFuncSetAttribute(fp_proj_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(smem));
+    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp smem: %s", cudaGetErrorString(e));
+    fp_proj_f32<<<dim3(c.ctas, batch), kFpxThreads, smem, stream>>>(img, imgT, proj, sc, usex, c, r);
+    return check_launch("fp_par_2d");
+}
+
 template <typename T>
 int fp_forward(const ctr_par_param* p, const T* img, T* proj, const double* sc,
                const double* bo, const int* usex, int batch, cudaStream_t stream)
@@ -556,51 +898,32 @@ int fp_forward(const ctr_par_param* p, const T* img, T* proj, const double* sc,
     int st = check_fp(p, img, proj, sc, bo, usex, batch);
     if (st) return st;
     if constexpr (sizeof(T) == 4) {
-        const int n = static_cast<int>(p->nx);
-        FrConst r{};
-        r.ns = p->ns; r.na = p->na; r.n = n;
-        r.band = std::max(2, std::min(32, 4096 / n));
-        r.buf_floats = (r.band * n + 8 + 31) / 32 * 32;
-        r.total = static_cast<long long>(batch) * n * n;
-        r.total4 = r.total & ~3ll;
-        r.dx = p->dx; r.dy = p->dy;
-        r.proj_stride = static_cast<size_t>(p->ns) * p->na;
-        const size_t smem = 128 + 2 * static_cast<size_t>(r.buf_floats) * sizeof(float);
-        if (smem <= 160 * 1024 && reinterpret_cast<uintptr_t>(img) % 16 == 0 && r.total < (1ll << 40)) {
-            // column-marching views run on the transposed image (stream-ordered scratch)
-            float* imgT = nullptr;
-            cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&imgT), r.total * sizeof(float), stream);
+        FpxConst c;
+        size_t smem = 0;
+        if (fpx_const(p, img, batch, &c, &smem)) {
+            // the transposed image and the per-call ray tables live in stream-ordered scratch
+            void* scratch = nullptr;
+            const size_t bytes = fpx_scratch_bytes(c);
+            cudaError_t e = cudaMallocAsync(&scratch, bytes, stream);
             if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp_par_2d scratch: %s", cudaGetErrorString(e));
-            transpose_f32<<<dim3(div_up(n, 32), div_up(n, 32), batch), dim3(32, 8), 0, stream>>>(img, imgT, n);
-            int st2 = check_launch("fp_par_2d transpose");
-            if (st2 == CTR_OK) {
-                e = cudaFuncSetAttribute(fp_rows_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
-                if (e != cudaSuccess) {
-                    st2 = fail(CTR_ERR_CUDA, "fp smem: %s", cudaGetErrorString(e));
-                } else {
-                    dim3 grid(div_up(p->na, kFrViews), div_up(p->ns, kFrChunk), batch);
-                    fp_rows_f32<<<grid, kFrThreads, smem, stream>>>(img, imgT, proj, sc, bo, usex, r);
-                    st2 = check_launch("fp_par_2d");
-                }
-            }
-            cudaFreeAsync(imgT, stream);
-            return st2;
+            st = launch_fpx(c, smem, scratch, img, proj, sc, bo, usex, batch, stream);
+            cudaFreeAsync(scratch, stream);
+            return st;
         }
         // fallback: image bands staged with plain loads
-        FpConst c = fp_const(p);
-        c.views = std::max(1, std::min(4, kFpThreads * kFpMaxRays / static_cast<int>(p->ns)));
-        if (c.views * static_cast<long long>(p->ns) > kFpThreads * kFpMaxRays)
+        FpConst c2 = fp_const(p);
+        c2.views = std::max(1, std::min(4, kFpThreads * kFpMaxRays / static_cast<int>(p->ns)));
+        if (c2.views * static_cast<long long>(p->ns) > kFpThreads * kFpMaxRays)
             return fail(CTR_ERR_UNSUPPORTED, "fp_par_2d: ns=%u exceeds %d channels", p->ns,
                         kFpThreads * kFpMaxRays);
         const int len = std::max(p->nx, p->ny) + 1;
-        c.band = std::max(1, std::min(32, 16384 / len));
-        const size_t smem2 = sizeof(float) * static_cast<size_t>(c.band) * len;
+        c2.band = std::max(1, std::min(32, 16384 / len));
+        const size_t smem2 = sizeof(float) * static_cast<size_t>(c2.band) * len;
         cudaError_t e = cudaFuncSetAttribute(fp_band_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              static_cast<int>(smem2));
         if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp smem: %s", cudaGetErrorString(e));
-        dim3 grid(div_up(p->na, c.views), batch);
-        fp_band_f32<<<grid, kFpThreads, smem2, stream>>>(img, proj, sc, bo, usex, c);
+        dim3 grid(div_up(p->na, c2.views), batch);
+        fp_band_f32<<<grid, kFpThreads, smem2, stream>>>(img, proj, sc, bo, usex, c2);
     } else {
         dim3 grid(div_up(p->ns, kFp64Threads), p->na, batch);
         fp_ray_kernel<T><<<grid, kFp64Threads, 0, stream>>>(img, proj, sc, bo, usex, p->ns, p->na,
@@ -635,24 +958,25 @@ int fp_adjoint(const ctr_par_param* p, const T* proj, T* img, const double* w,
 // For callers that must not allocate device memory inside a call: a host
 // framework that hands out all device memory itself (its own pool, a fixed
 // arena), or a real-time loop that cannot wait on the allocator.  The
-// transposed image that column-marching views read lives in this fixed
-// file-scope array instead of stream-ordered scratch: at most
-// kFpNoAllocFloats = 4,194,304 floats (16 MiB), i.e. batch * nx * ny <= 2^22
-// (one 2048^2 image, or 16 images of 512^2).  The transpose overwrites every
-// element it later reads, so nothing in the array has to start at zero.
+// projector's scratch (the transposed image, 4 bytes a pixel of the batch, and
+// its per-call ray tables, 24 bytes a ray plus ~400 KB) lives in this fixed
+// file-scope array instead of stream-ordered scratch: 16 MiB, e.g. 720 views x
+// 729 bins with up to 3 images of 512^2.  Every call writes all of the scratch
+// it reads (the tie counter by a memset), so nothing in the array has to start
+// at zero.
 // All calls on a device share the one array: calls ordered on one stream are
 // safe, calls that can overlap (two streams, two host threads without
 // ordering) race on it and give wrong results.
-constexpr long long kFpNoAllocFloats = 1ll << 22;
-static __device__ __align__(256) float g_fp_noalloc_scratch[kFpNoAllocFloats];
+constexpr long long kFpNoAllocBytes = 16ll << 20;
+static __device__ __align__(256) unsigned char g_fp_noalloc_scratch[kFpNoAllocBytes];
 
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
-float* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
 
 // The array's device address on the current device, looked up once per device
 // (cudaGetSymbolAddress; the first call on a device does this set-up).
-int noalloc_scratch(float** out)
+int noalloc_scratch(void** out)
 {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
@@ -666,7 +990,7 @@ int noalloc_scratch(float** out)
         if (e != cudaSuccess || !ptr)
             return fail(CTR_ERR_CUDA, "fp_par_2d_f32_noalloc scratch address: %s",
                         cudaGetErrorString(e));
-        g_noalloc_ptr[dev] = static_cast<float*>(ptr);
+        g_noalloc_ptr[dev] = ptr;
     }
     *out = g_noalloc_ptr[dev];
     return CTR_OK;
@@ -677,36 +1001,21 @@ int fp_forward_noalloc(const ctr_par_param* p, const float* img, float* proj, co
 {
     int st = check_fp(p, img, proj, sc, bo, usex, batch);
     if (st) return st;
-    const long long n = p->nx;
-    if (n > 2048 || batch * n * n > kFpNoAllocFloats)
+    FpxConst c;
+    size_t smem = 0;
+    if (!fpx_const(p, img, batch, &c, &smem))
         return fail(CTR_ERR_UNSUPPORTED,
-                    "fp_par_2d_f32_noalloc: batch*nx*ny = %d*%lld*%lld exceeds its fixed scratch of "
-                    "%lld floats (16 MiB); split the batch or call ctr_fp_par_2d_f32",
-                    batch, n, n, kFpNoAllocFloats);
-    if (reinterpret_cast<uintptr_t>(img) % 16 != 0)
-        return fail(CTR_ERR_INVALID_ARG, "fp_par_2d_f32_noalloc: img must be 16-byte aligned");
-    FrConst r{};
-    r.ns = p->ns; r.na = p->na; r.n = static_cast<int>(n);
-    r.band = std::max(2, std::min(32, static_cast<int>(4096 / n)));
-    r.buf_floats = (r.band * r.n + 8 + 31) / 32 * 32;
-    r.total = batch * n * n;
-    r.total4 = r.total & ~3ll;
-    r.dx = p->dx; r.dy = p->dy;
-    r.proj_stride = static_cast<size_t>(p->ns) * p->na;
-    const size_t smem = 128 + 2 * static_cast<size_t>(r.buf_floats) * sizeof(float);
-    float* imgT = nullptr;
-    st = noalloc_scratch(&imgT);
+                    "fp_par_2d_f32_noalloc: needs a 16-byte aligned img and nx <= 8192");
+    const size_t need = fpx_scratch_bytes(c);
+    if (need > static_cast<size_t>(kFpNoAllocBytes))
+        return fail(CTR_ERR_UNSUPPORTED,
+                    "fp_par_2d_f32_noalloc: %zu bytes of scratch (24 per ray, 4 per image pixel) "
+                    "exceed its fixed 16 MiB; split the batch or call ctr_fp_par_2d_f32",
+                    need);
+    void* scratch = nullptr;
+    st = noalloc_scratch(&scratch);
     if (st) return st;
-    transpose_f32<<<dim3(div_up(n, 32), div_up(n, 32), batch), dim3(32, 8), 0, stream>>>(
-        img, imgT, r.n);
-    st = check_launch("fp_par_2d_f32_noalloc transpose");
-    if (st) return st;
-    cudaError_t e = cudaFuncSetAttribute(fp_rows_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
-    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp smem: %s", cudaGetErrorString(e));
-    dim3 grid(div_up(p->na, kFrViews), div_up(p->ns, kFrChunk), batch);
-    fp_rows_f32<<<grid, kFrThreads, smem, stream>>>(img, imgT, proj, sc, bo, usex, r);
-    return check_launch("fp_par_2d_f32_noalloc");
+    return launch_fpx(c, smem, scratch, img, proj, sc, bo, usex, batch, stream);
 }
 
 }  // namespace

@@ -230,11 +230,13 @@ int ctr_fp_par_2d_grad_f64(const ctr_par_param* p, const double* proj, double* i
  *      reference; same arguments and results as ctr_fp_par_2d_f32) ----
  * For callers that cannot allocate device memory inside a call: a host that
  * owns all device memory (its own pool or a fixed arena), or a real-time loop
- * that must not wait on the allocator.  The scratch the projector needs (the
- * transposed image) is a fixed 16 MiB array inside the library, so this call
- * allocates nothing.  Limits: batch * nx * ny <= 4,194,304 floats (one
- * 2048 x 2048 image, or 16 of 512 x 512); larger inputs return
- * CTR_ERR_UNSUPPORTED.  img must be 16-byte aligned.
+ * that must not wait on the allocator.  The scratch the projector needs (a
+ * transposed copy of the image and per-call ray tables) is a fixed 16 MiB
+ * array inside the library, so this call
+ * allocates nothing.  Limits: 24 bytes per ray (na * ns) plus 4 bytes per
+ * image pixel of the batch plus about 400 KB within 16 MiB (720 views x 729
+ * bins with up to 3 images of 512 x 512), nx at most 8192, img 16-byte
+ * aligned; otherwise CTR_ERR_UNSUPPORTED.
  * The first call on each device looks up the array's address
  * (cudaGetSymbolAddress) with that device current; make that first call
  * before any stream capture.  All calls on a device share the array: calls

@@ -63,8 +63,8 @@ def test_noalloc_rejects_oversize():
     from ct_recon_extensions_gb300._lib import CtrError
     from ct_recon_extensions_gb300 import synthetic as syn
     d = dict(syn.parallel_config_2())
-    d["nx"] = d["ny"] = 2048
+    d["na"] = 1000  # 1000 x 729 rays exceed the fixed scratch
     op = fp_op(d)
-    img = torch.zeros((2, 2048, 2048), dtype=torch.float32, device="cuda")
+    img = torch.zeros((1, d["ny"], d["nx"]), dtype=torch.float32, device="cuda")
     with pytest.raises(CtrError, match="16 MiB"):
         _run("ctr_fp_par_2d_f32_noalloc", op, img)
