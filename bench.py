@@ -53,7 +53,7 @@ FP32_LANES_PER_SM = 128
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--pool", type=int, default=160, help="distinct slices cycled through")
@@ -104,6 +104,8 @@ class Dist:
 # ---------------------------------------------------------------------------
 
 class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples every 20 ms, each stamped
+    on arrival; stop() keeps those inside the timed window."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -117,28 +119,35 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except OSError:
             self.proc = None
+            return
+        t = time.perf_counter()
+        while not self.lines and time.perf_counter() - t < 5.0:  # sampling has begun
+            time.sleep(0.01)
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
-    def stop(self):
+    def stop(self, windows=()):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.05)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
+        inside = [ln for ts, ln in self.lines if any(a <= ts <= b for a, b in windows)]
+        lines = inside or [ln for _, ln in self.lines]
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in lines:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -151,7 +160,8 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "window": "timed regions" if inside else "whole run"}
 
 
 # ---------------------------------------------------------------------------
@@ -208,6 +218,8 @@ class ParPipeline:
         self.sino = torch.empty((g["na"], g["ns"]), **f32)
         self.filt = torch.empty((g["na"], g["ns"]), **f32)
         self.names = ["fp_par_2d", "ramp_filter", "bp_par_2d"]
+        # our kernels per call (fp_par_2d: transposed copy, ray set-up, projector)
+        self.kernels = {"fp_par_2d": 3, "ramp_filter": 1, "bp_par_2d": 1}
         # algorithmic FP32 FLOPs per launch (fixed conventions)
         self.flops = {"fp_par_2d": 6.0 * g["na"] * g["ns"] * g["ny"],
                       "ramp_filter": 2.0 * g["ns"] * g["na"] * g["ns"],
@@ -251,6 +263,7 @@ class FanPipeline:
         self.wt = torch.empty((g["na"], g["ns"]), **f32)
         self.filt = torch.empty((g["na"], g["ns"]), **f32)
         self.names = ["fan_weighting", "ramp_filter", "bp_fan_2d"]
+        self.kernels = {"fan_weighting": 1, "ramp_filter": 1, "bp_fan_2d": 1}
         self.flops = {"fan_weighting": 1.0 * g["na"] * g["ns"],
                       "ramp_filter": 2.0 * g["ns"] * g["na"] * g["ns"],
                       "bp_fan_2d": 32.0 * g["nx"] * g["ny"] * g["na"]}
@@ -308,7 +321,67 @@ def run_device(pipe, pool_dev, outs, steps, warmup, dist, per_kernel=True):
     if per_kernel:
         for i, n in enumerate(pipe.names):
             kern[n] = statistics.fmean(ev[k][i][0].elapsed_time(ev[k][i][1]) for k in range(steps))
-    return secs, kern, len(pipe.names) * steps
+    return secs, kern, sum(pipe.kernels.values()) * steps
+
+
+def run_batched(device, steps, warmup, dist):
+    """The uneven fan batch (64 items, image 256^2..1024^2, 360..2304 views,
+    512..1024 channels): one plan run (batched filter launch + one persistent
+    backprojection launch, replayed from a CUDA graph) per step, against the
+    same items through the plain per-item drop-in (3 launches an item)."""
+    import torch
+    from ct_recon_extensions_gb300 import synthetic as syn
+    from ct_recon_extensions_gb300.batch import FanFBPBatch
+    items = syn.batched_config_3()
+    geoms = [{k: v for k, v in it.items() if k != "seed"} for it in items]
+    sinos = [syn.fan_sinogram_torch(syn.random_ellipses(it["seed"]), g["na"], g["ns"], g["ds"],
+                                    g["orbit"], g["dso"], g["dsd"], device).contiguous()
+             for it, g in zip(items, geoms)]
+    outs = [torch.empty((g["ny"], g["nx"]), dtype=torch.float32, device=device) for g in geoms]
+    updates = float(sum(g["nx"] * g["ny"] * g["na"] for g in geoms))
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, k):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        dist.barrier()
+        torch.cuda.synchronize()
+        t0.record(stream)
+        for _ in range(k):
+            fn()
+        t1.record(stream)
+        torch.cuda.synchronize()
+        dist.barrier()
+        return dist.max(t0.elapsed_time(t1) / 1e3)
+
+    plan = FanFBPBatch(geoms)  # autotuned, CUDA graph
+    k = max(3, min(steps, 10))
+    b_secs = timed(lambda: plan.run(sinos, outs), k)
+    info = plan.info()
+    pipes = [FanPipeline(g, device) for g in geoms]
+    sp = stream.cuda_stream
+
+    def plain():
+        for pipe, s, o in zip(pipes, sinos, outs):
+            for fn in pipe.launches(s, o, sp):
+                if fn() != 0:
+                    raise RuntimeError(pipe.lib.ctr_last_error().decode())
+
+    p_secs = timed(plain, k)
+    n = len(geoms)
+    plan.close()
+    return {
+        "workload": "64 fan sinograms of uneven size (image 256^2-1024^2, 360-2304 views, "
+                    "512-1024 channels): weighting -> ramp(fan) -> bp_fan_2d",
+        "slices_per_s": n * k / b_secs, "updates_per_s": updates * k / b_secs,
+        "plain_slices_per_s": n * k / p_secs, "speedup_vs_plain": p_secs / b_secs,
+        "plan": {key: info[key] for key in ("tile_rows", "view_block", "ctas", "autotuned",
+                                            "tuned_ms", "graph", "launches_per_run")},
+        "gpu_launches": int(info["launches_per_run"]) * k, "runs": k,
+    }
 
 
 def run_e2e(pipe, pool_host, steps, warmup, in_shape, out_shape, device):
@@ -479,8 +552,9 @@ def main():
 
     clk = ClockSampler(local)
     clk.start()
+    t_a = time.perf_counter()
     secs, kern, launches = run_device(pipe, pool_dev, outs, args.steps, args.warmup, dist)
-    clocks = clk.stop()
+    clocks = clk.stop([(t_a, time.perf_counter())])
     secs = dist.max(secs)
     value = ws * args.steps / secs
 
@@ -500,6 +574,9 @@ def main():
     fouts = [torch.empty((gf["ny"], gf["nx"]), dtype=torch.float32, device=device) for _ in range(4)]
     f_secs, f_kern, f_launches = run_device(fpipe, fpool, fouts, args.steps, args.warmup, dist)
     f_secs = dist.max(f_secs)
+
+    # ---- batched uneven fan FBP (config 3) against the plain drop-in ----
+    batched = run_batched(device, args.steps, args.warmup, dist)
 
     # ---- roofline of the dominant kernel ----
     peak_meas = fp32_peak_tflops(device)
@@ -549,6 +626,7 @@ def main():
                     "dominant_frac": fpipe.flops[fdom] / (f_kern[fdom] / 1e3) / 1e12 / peak,
                     "gpu_launches": f_launches,
                 },
+                "batched_fan_config3": batched,
             },
         }
         print(json.dumps(line))

@@ -158,10 +158,9 @@ __global__ void __launch_bounds__(kFpThreads)
 // warp's 32 samples of one row fall within a few pixels of each other.  Slots
 // are ordered view quad by view quad, and within a quad the channel octets in
 // a strided order (slot_octet), so a contiguous range of slots mixes long
-// central rays and short edge rays.  A class's CTAs cut its slots at equal
-// shares of a per-view weight (samples per row grow with max(|sin|, |cos|)),
-// and a CTA deals its slots, sorted by their exact sample counts, to its warps
-// in snake order.  A round holds up to kFpxRound slots (one more round streams
+// central rays and short edge rays.  Each class gets CTAs in proportion to its
+// views and cuts its slots into equal ranges, and a CTA deals its slots, sorted
+// by their exact sample counts, to its warps in snake order.  A round holds up to kFpxRound slots (one more round streams
 // the image again; rare).
 //
 // Pipeline: a producer lane copies band t (one contiguous range of the staged
@@ -265,81 +264,62 @@ __global__ void __launch_bounds__(256) transpose_f32(const float* __restrict__ i
 
 // ---- set-up kernel: every ray once; block 0 the class lists and CTA cut ------
 __global__ void __launch_bounds__(kFpxSetupThreads)
-    fpx_setup(const double* __restrict__ sincos, const double* __restrict__ bo,
-              const int* __restrict__ usex, const FpxConst c, const FpxRays r)
+    fpx_setup(const double* __restrict__ bo, const int* __restrict__ usex, const FpxConst c,
+              const FpxRays r)
 {
-    extern __shared__ float fs_P[];  // block 0: [quads + 3] running quad weights
-    __shared__ int s_cnt[kFpxSetupThreads + 1];
+    __shared__ int s_chunk[2049];  // block 0: row-marching views before each chunk of 32
     const int tid = threadIdx.x;
     if (blockIdx.x == 0) {
-        // class lists: row-marching views (usex) first, then column-marching ones
-        const int per = (c.na + kFpxSetupThreads - 1) / kFpxSetupThreads;
-        const int v0 = min(tid * per, c.na), v1 = min(v0 + per, c.na);
-        int n0 = 0;
-        for (int v = v0; v < v1; ++v) n0 += usex[v] != 0 ? 1 : 0;
-        s_cnt[tid + 1] = n0;
-        __syncthreads();
-        if (tid == 0) {
-            s_cnt[0] = 0;
-            for (int i = 1; i <= kFpxSetupThreads; ++i) s_cnt[i] += s_cnt[i - 1];
+        // class lists with warp ballots over chunks of 32 views: row-marching
+        // views (usex) first, then column-marching ones, each padded to quads
+        constexpr int kWarps = kFpxSetupThreads / 32;
+        const int warp = tid >> 5, lane = tid & 31;
+        const int nch = (c.na + 31) / 32;
+        for (int ch = warp; ch < nch; ch += kWarps) {
+            const int v = ch * 32 + lane;
+            const unsigned b = __ballot_sync(0xffffffffu, v < c.na && usex[v] != 0);
+            if (lane == 0) s_chunk[ch + 1] = __popc(b);
         }
         __syncthreads();
-        const int N0 = s_cnt[kFpxSetupThreads], N1 = c.na - N0;
-        const int Q0 = (N0 + 3) / 4, Q1 = (N1 + 3) / 4, Qt = Q0 + Q1;
-        int o0 = s_cnt[tid], o1 = 4 * Q0 + (v0 - s_cnt[tid]);
-        for (int v = v0; v < v1; ++v) {
-            if (usex[v] != 0) r.views[o0++] = v;
-            else r.views[o1++] = v;
-        }
-        for (int i = N0 + tid; i < 4 * Q0; i += kFpxSetupThreads) r.views[i] = -1;
-        for (int i = 4 * Q0 + N1 + tid; i < 4 * Qt; i += kFpxSetupThreads) r.views[i] = -1;
-        __syncthreads();
-        // quad weights: its views (a view costs about the same at every angle:
-        // fewer samples at 45 degrees, but longer shared-memory and lane waits)
-        for (int qd = tid; qd < Qt; qd += kFpxSetupThreads) {
-            float w = 0.0f;
-            for (int k = 0; k < 4; ++k) w += r.views[qd * 4 + k] >= 0 ? 1.0f : 0.0f;
-            fs_P[qd + 1] = w;
-        }
-        __syncthreads();
-        if (tid == 0) {  // running sum (a short serial pass)
-            float acc = 0.0f;
-            fs_P[0] = 0.0f;
-            for (int qd = 1; qd <= Qt; ++qd) {
-                acc += fs_P[qd];
-                fs_P[qd] = acc;
+        if (warp == 0) {  // running count of row-marching views before each chunk
+            int carry = 0;
+            if (lane == 0) s_chunk[0] = 0;
+            for (int base = 0; base < nch; base += 32) {
+                int x = base + lane < nch ? s_chunk[base + lane + 1] : 0;
+                for (int off = 1; off < 32; off <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, x, off);
+                    if (lane >= off) x += y;
+                }
+                if (base + lane < nch) s_chunk[base + lane + 1] = carry + x;
+                carry += __shfl_sync(0xffffffffu, x, 31);
             }
         }
         __syncthreads();
-        // CTAs per class in proportion to the weight, each class cut evenly
-        const float W0 = fs_P[Q0], W1 = fs_P[Qt] - fs_P[Q0];
+        const int N0 = s_chunk[nch], N1 = c.na - N0;
+        const int Q0 = (N0 + 3) / 4, Q1 = (N1 + 3) / 4, Qt = Q0 + Q1;
+        for (int ch = warp; ch < nch; ch += kWarps) {
+            const int v = ch * 32 + lane;
+            const bool row = v < c.na && usex[v] != 0;
+            const unsigned below = __ballot_sync(0xffffffffu, row) & ((1u << lane) - 1u);
+            const int o0 = s_chunk[ch] + __popc(below);                        // row views before v
+            const int o1 = (ch * 32 - s_chunk[ch]) + (lane - __popc(below));  // column views before v
+            if (v < c.na) r.views[row ? o0 : 4 * Q0 + o1] = v;
+        }
+        for (int i = N0 + tid; i < 4 * Q0; i += kFpxSetupThreads) r.views[i] = -1;
+        for (int i = 4 * Q0 + N1 + tid; i < 4 * Qt; i += kFpxSetupThreads) r.views[i] = -1;
+        // CTAs per class in proportion to its views, each class cut into equal
+        // slot ranges (a view costs about the same at every angle: fewer samples
+        // at 45 degrees, but longer shared-memory and lane waits)
         int G0 = 0;
-        if (N0 > 0) G0 = N1 > 0 ? static_cast<int>(rintf(c.ctas * W0 / (W0 + W1))) : c.ctas;
+        if (N0 > 0) G0 = N1 > 0 ? static_cast<int>(rintf(static_cast<float>(c.ctas) * N0 / c.na)) : c.ctas;
         if (N0 > 0 && N1 > 0) G0 = max(1, min(c.ctas - 1, G0));
         const int G1 = c.ctas - G0;
         for (int i = tid; i <= c.ctas; i += kFpxSetupThreads) {
             const bool cls1 = i > G0 || (i == G0 && G0 == 0);
-            const int gi = cls1 ? i - G0 : i, G = cls1 ? G1 : G0;
-            const int qa = cls1 ? Q0 : 0, qb = cls1 ? Qt : Q0;  // quads of the class
-            int s;
-            if (gi <= 0) {
-                s = qa * c.octets;
-            } else if (gi >= G) {
-                s = qb * c.octets;
-            } else {
-                const float T = fs_P[qa] + (fs_P[qb] - fs_P[qa]) * (static_cast<float>(gi) / G);
-                int lo = qa, hi = qb - 1;  // largest Q with P[Q] <= T
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (fs_P[mid] <= T) lo = mid;
-                    else hi = mid - 1;
-                }
-                const float f = (T - fs_P[lo]) / (fs_P[lo + 1] - fs_P[lo]);
-                int rank = static_cast<int>(ceilf(f * static_cast<float>(c.octets)));
-                rank = rank < 0 ? 0 : (rank > c.octets ? c.octets : rank);
-                s = min(lo * c.octets + rank, qb * c.octets);
-            }
-            r.cuts[i] = s;
+            const long long gi = cls1 ? i - G0 : i, G = cls1 ? G1 : G0;
+            const long long s0 = static_cast<long long>(cls1 ? Q0 : 0) * c.octets;
+            const long long ns_ = static_cast<long long>(cls1 ? Q1 : Q0) * c.octets;
+            r.cuts[i] = static_cast<int>(s0 + (G > 0 ? (gi * ns_) / G : 0));
         }
         if (tid == 0) r.cuts[c.ctas + 1] = G0;
     }
@@ -872,16 +852,10 @@ int launch_fpx(const FpxConst& c, size_t smem, void* scratch, const float* img, 
     if (st) return st;
     cudaError_t e = cudaMemsetAsync(r.nties, 0, sizeof(int), stream);
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp_par_2d: %s", cudaGetErrorString(e));
-    const size_t setup_smem = (static_cast<size_t>(c.quads) + 3) * sizeof(float);
-    if (setup_smem > 48 * 1024) {
-        e = cudaFuncSetAttribute(fpx_setup, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(setup_smem));
-        if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp setup smem: %s", cudaGetErrorString(e));
-    }
     const long long rays = static_cast<long long>(c.na) * c.ns;
     const unsigned blocks = static_cast<unsigned>(
         std::min<long long>(div_up(rays, kFpxSetupThreads), 8 * kSmCount));
-    fpx_setup<<<blocks, kFpxSetupThreads, setup_smem, stream>>>(sc, bo, usex, c, r);
+    fpx_setup<<<blocks, kFpxSetupThreads, 0, stream>>>(bo, usex, c, r);
     st = check_launch("fp_par_2d set-up");
     if (st) return st;
     e = cudaFuncSetAttribute(fp_proj_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,

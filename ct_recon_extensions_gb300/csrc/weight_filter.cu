@@ -59,38 +59,58 @@ int launch_fan_weighting(const ctr_fan_weighting_param* p, const T* in, T* out, 
 }
 
 // ---- ramp filter ---------------------------------------------------------
+//
+// out[r][o] = ds * sum_j h[o - j] * x[r][j]   (correlation, the grad: h[j - o]).
+// The ramp taps are zero at even offsets except 0, so output o sums the inputs
+// of the other parity.  A thread computes 4 outputs of one parity, o_m = i0 + 2m,
+// for kRows rows: stepping j by 2, the taps it needs, H[o_m - j], slide by one
+// place (H[o_m - j - 2] = H[o_{m-1} - j]), so each step loads one new tap and
+// one input per row for 4 * kRows FMAs, all from shared memory.  Thread pairs
+// cover 8 consecutive outputs (both parities).  Even taps other than 0, which
+// the ramp filters of the reference never have, take the generic loop.
+constexpr int kFilterMaxThreads = 1024;
+constexpr int kFilterPad = 16;   // zero taps beyond the ends of H
+constexpr int kFilterRowsPlain = 2;
 
-constexpr int kFilterThreads = 256;
-constexpr int kFilterRows = kFilterRowsPerBlock;
+__host__ __device__ inline int filter_threads(unsigned ns)
+{
+    const int t = static_cast<int>((ns + 7) / 8) * 2;
+    return t < 32 ? 32 : (t > kFilterMaxThreads ? kFilterMaxThreads : (t + 31) / 32 * 32);
+}
 
-// Filters rows [r0, r0 + nr) (nr <= kFilterRows) of one item.  Shared layout:
-// tpos[ns] (h[+k], k = 0..ns-1), tneg[ns] (h[-k]), rows[kFilterRows][ns].
-template <typename T, bool kGrad>
+// Shared layout: H[-(ns-1) - kFilterPad .. ns - 1 + kFilterPad] (taps * ds),
+// then xs[kRows][ns].
+template <typename T>
+__host__ __device__ inline size_t filter_smem(unsigned ns, int rows)
+{
+    return sizeof(T) * ((2 * static_cast<size_t>(ns) + 2 * kFilterPad) + static_cast<size_t>(rows) * ns);
+}
+
+template <typename T, int kRows, bool kGrad>
 __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const double* __restrict__ filter,
                                             T* __restrict__ out, const float* __restrict__ weight,
                                             unsigned ns, unsigned long long r0, int nr, double ds,
                                             unsigned char* smem_raw)
 {
-    T* tpos = reinterpret_cast<T*>(smem_raw);
-    T* tneg = tpos + ns;
-    T* xs = tneg + ns;
-    __shared__ int s_fast;
-
     const int n = static_cast<int>(ns);
+    T* H0 = reinterpret_cast<T*>(smem_raw);
+    T* H = H0 + (n - 1) + kFilterPad;  // H[d], d in [-(n-1) - pad, n - 1 + pad]
+    T* xs = H0 + 2 * n + 2 * kFilterPad;
+    __shared__ int s_even;
+
     const double* h = filter + ns;  // h[k], k in [-ns, ns]
-    if (threadIdx.x == 0) s_fast = 1;
+    if (threadIdx.x == 0) s_even = 0;
     __syncthreads();
-    bool fast = true;
-    for (int k = threadIdx.x; k < n; k += kFilterThreads) {
-        // the convolution uses h[i - j]; the correlation (grad) h[j - i]
-        const double hp = kGrad ? h[-k] : h[k];
-        const double hn = kGrad ? h[k] : h[-k];
-        tpos[k] = static_cast<T>(hp * ds);
-        tneg[k] = static_cast<T>(hn * ds);
-        if (k > 0 && (k & 1) == 0 && (hp != 0.0 || hn != 0.0)) fast = false;
+    bool even = false;
+    for (int idx = threadIdx.x; idx < 2 * n + 2 * kFilterPad; idx += blockDim.x) {
+        const int d = idx - (n - 1) - kFilterPad;
+        double v = 0.0;
+        if (d > -n && d < n) v = kGrad ? h[-d] : h[d];
+        H0[idx] = static_cast<T>(v * ds);
+        if (d != 0 && (d & 1) == 0 && v != 0.0) even = true;
     }
-    if (!fast) s_fast = 0;
-    for (int idx = threadIdx.x; idx < kFilterRows * n; idx += kFilterThreads) {
+    if (even) s_even = 1;
+    for (int idx = threadIdx.x; idx < kRows * n; idx += blockDim.x) {
         const int r = idx / n, j = idx - r * n;
         T v = 0;
         if (r < nr) {
@@ -100,55 +120,83 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
         xs[idx] = v;
     }
     __syncthreads();
-    const int step = s_fast ? 2 : 1;
-    for (int i = threadIdx.x; i < n; i += kFilterThreads) {
-        T left[kFilterRows], right[kFilterRows];
+    const int groups = (n + 7) / 8 * 2;  // thread tasks: (8-output block, parity)
+    if (!s_even) {
+        for (int task = threadIdx.x; task < groups; task += blockDim.x) {
+            const int i0 = (task >> 1) * 8 + (task & 1);
+            T acc[kRows][4];
 #pragma unroll
-        for (int r = 0; r < kFilterRows; ++r) {
-            left[r] = 0;
-            right[r] = 0;
+            for (int r = 0; r < kRows; ++r)
+#pragma unroll
+                for (int m = 0; m < 4; ++m) acc[r][m] = 0;
+            const int jb = (i0 + 1) & 1;  // inputs of the other parity
+            T w0 = H[i0 - jb], w1 = H[i0 + 2 - jb], w2 = H[i0 + 4 - jb], w3 = H[i0 + 6 - jb];
+#pragma unroll 4
+            for (int j = jb; j < n; j += 2) {
+#pragma unroll
+                for (int r = 0; r < kRows; ++r) {
+                    const T xv = xs[r * n + j];
+                    acc[r][0] += w0 * xv;
+                    acc[r][1] += w1 * xv;
+                    acc[r][2] += w2 * xv;
+                    acc[r][3] += w3 * xv;
+                }
+                w3 = w2;
+                w2 = w1;
+                w1 = w0;
+                w0 = H[i0 - j - 2];
+            }
+            const T t0 = H[0];
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                const int o = i0 + 2 * m;
+                if (o >= n) continue;
+#pragma unroll
+                for (int r = 0; r < kRows; ++r)
+                    if (r < nr) out[(r0 + r) * ns + o] = t0 * xs[r * n + o] + acc[r][m];
+            }
         }
-        // j = i - k  (k >= 1) uses h[+k];  j = i + k uses h[-k]
-        for (int k = 1; k <= i; k += step) {
-            const T t = tpos[k];
+    } else {
+        // a filter with even taps: the plain sum over every input
+        for (int o = threadIdx.x; o < n; o += blockDim.x) {
+            T acc[kRows];
 #pragma unroll
-            for (int r = 0; r < kFilterRows; ++r) left[r] += t * xs[r * n + i - k];
-        }
-        for (int k = 1; k < n - i; k += step) {
-            const T t = tneg[k];
+            for (int r = 0; r < kRows; ++r) acc[r] = 0;
+            for (int j = 0; j < n; ++j) {
+                const T t = H[o - j];
 #pragma unroll
-            for (int r = 0; r < kFilterRows; ++r) right[r] += t * xs[r * n + i + k];
-        }
-        const T t0 = tpos[0];
+                for (int r = 0; r < kRows; ++r) acc[r] += t * xs[r * n + j];
+            }
 #pragma unroll
-        for (int r = 0; r < kFilterRows; ++r) {
-            if (r < nr) out[(r0 + r) * ns + i] = t0 * xs[r * n + i] + (left[r] + right[r]);
+            for (int r = 0; r < kRows; ++r)
+                if (r < nr) out[(r0 + r) * ns + o] = acc[r];
         }
     }
     __syncthreads();  // shared buffers are free for the caller's next call
 }
 
 template <typename T, bool kGrad>
-__global__ void __launch_bounds__(kFilterThreads)
+__global__ void __launch_bounds__(kFilterMaxThreads)
     ramp_filter_kernel(const T* __restrict__ in, const double* __restrict__ filter,
                        T* __restrict__ out, const float* __restrict__ weight, unsigned ns,
                        unsigned long long rows, double ds)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const unsigned long long r0 = static_cast<unsigned long long>(blockIdx.x) * kFilterRows;
-    const int nr = static_cast<int>(rows - r0 < kFilterRows ? rows - r0 : kFilterRows);
-    filter_rows<T, kGrad>(in, filter, out, weight, ns, r0, nr, ds, smem_raw);
+    const unsigned long long r0 = static_cast<unsigned long long>(blockIdx.x) * kFilterRowsPlain;
+    const int nr = static_cast<int>(rows - r0 < kFilterRowsPlain ? rows - r0 : kFilterRowsPlain);
+    filter_rows<T, kFilterRowsPlain, kGrad>(in, filter, out, weight, ns, r0, nr, ds, smem_raw);
 }
 
 // Batched FP32 filtering with pre-weighting: one CTA per (job, row block).
-__global__ void __launch_bounds__(kFilterThreads)
+__global__ void __launch_bounds__(kFilterMaxThreads)
     ramp_filter_batch_kernel(const FilterJob* __restrict__ jobs, const int2* __restrict__ blocks)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int2 b = blocks[blockIdx.x];  // (job, first row)
     const FilterJob J = jobs[b.x];
-    const int nr = min(kFilterRows, static_cast<int>(J.nrow) - b.y);
-    filter_rows<float, false>(J.in, J.taps, J.out, J.weight, J.ns, b.y, nr, J.ds, smem_raw);
+    const int nr = min(kFilterRowsPerBlock, static_cast<int>(J.nrow) - b.y);
+    filter_rows<float, kFilterRowsPerBlock, false>(J.in, J.taps, J.out, J.weight, J.ns, b.y, nr,
+                                                   J.ds, smem_raw);
 }
 
 template <typename T, bool kGrad>
@@ -162,15 +210,15 @@ int launch_ramp_filter(const ctr_filter_param* p, const T* in, const double* fil
     if (p->ns < 1 || p->nrow < 1) return fail(CTR_ERR_INVALID_ARG, "empty sinogram");
     if (in == out) return fail(CTR_ERR_INVALID_ARG, "ramp filter cannot run in place");
     const unsigned long long rows = static_cast<unsigned long long>(p->nrow) * batch;
-    const size_t smem = sizeof(T) * static_cast<size_t>(p->ns) * (2 + kFilterRows);
+    const size_t smem = filter_smem<T>(p->ns, kFilterRowsPlain);
     if (smem > 200 * 1024)
         return fail(CTR_ERR_UNSUPPORTED, "ns=%u exceeds the filter's shared-memory tile", p->ns);
     auto kern = ramp_filter_kernel<T, kGrad>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "filter smem: %s", cudaGetErrorString(e));
-    const unsigned blocks = div_up(rows, kFilterRows);
-    kern<<<blocks, kFilterThreads, smem, stream>>>(in, filter, out, weight, p->ns, rows, p->ds);
+    const unsigned blocks = div_up(rows, kFilterRowsPlain);
+    kern<<<blocks, filter_threads(p->ns), smem, stream>>>(in, filter, out, weight, p->ns, rows, p->ds);
     return check_launch("ramp_filter");
 }
 
@@ -187,13 +235,13 @@ int ramp_filter_weighted_f32(const ctr_filter_param* p, const float* in, const d
 int ramp_filter_batch_f32(const FilterJob* jobs, const int2* blocks, int n_blocks, unsigned max_ns,
                           cudaStream_t stream)
 {
-    const size_t smem = sizeof(float) * static_cast<size_t>(max_ns) * (2 + kFilterRows);
+    const size_t smem = filter_smem<float>(max_ns, kFilterRowsPerBlock);
     if (smem > 200 * 1024) return fail(CTR_ERR_UNSUPPORTED, "ns=%u too wide for the filter tile", max_ns);
     cudaError_t e = cudaFuncSetAttribute(ramp_filter_batch_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "filter smem: %s", cudaGetErrorString(e));
     if (n_blocks > 0)
-        ramp_filter_batch_kernel<<<n_blocks, kFilterThreads, smem, stream>>>(jobs, blocks);
+        ramp_filter_batch_kernel<<<n_blocks, filter_threads(max_ns), smem, stream>>>(jobs, blocks);
     return check_launch("ramp_filter_batch");
 }
 

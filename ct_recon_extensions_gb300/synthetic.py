@@ -147,3 +147,25 @@ def large_config_5():
     return dict(ns=1472, na=2304, ds=0.6429, orbit=2 * math.pi / 2304, offset_s=0.0,
                 orbit_start=0.0, nx=2048, ny=2048, dx=0.25, dy=0.25, offset_x=0.0,
                 offset_y=0.0, dso=FAN_DSO, dsd=FAN_DSD, fov=-1.0)
+
+
+def fan_sinogram_torch(e: Ellipses, na: int, ns: int, ds: float, orbit: float, dso: float,
+                       dsd: float, device, orbit_start: float = 0.0, offset_s: float = 0.0):
+    """fan_sinogram computed with torch on `device` (FP32), for large batches."""
+    import torch
+    f32 = dict(dtype=torch.float32, device=device)
+    cents = (ns - 1) / 2 + offset_s
+    beta = orbit_start + torch.arange(na, **f32) * orbit
+    gamma = (torch.arange(ns, **f32) - cents) * (ds / dsd)
+    theta = beta[:, None] + gamma[None, :]
+    s = dso * torch.sin(gamma)[None, :]
+    ct, st = torch.cos(theta), torch.sin(theta)
+    out = torch.zeros((na, ns), **f32)
+    for i in range(len(e.mu)):
+        al = theta - float(e.phi[i])
+        r2 = (float(e.a[i]) * torch.cos(al)) ** 2 + (float(e.b[i]) * torch.sin(al)) ** 2
+        sp = s - (float(e.cx[i]) * ct + float(e.cy[i]) * st)
+        arg = r2 - sp * sp
+        out += torch.where(arg > 0, 2.0 * float(e.mu[i] * e.a[i] * e.b[i]) *
+                           torch.sqrt(torch.clamp(arg, min=0.0)) / r2, torch.zeros_like(arg))
+    return out
