@@ -384,6 +384,84 @@ def run_batched(device, steps, warmup, dist):
     }
 
 
+def run_gd(device, steps, warmup, dist):
+    """The differentiable pair: gradient descent on ||A x - y||^2 for a batch of
+    16 images of 512^2 (parallel, 720 views, 729 bins), y = A x_true + Gaussian
+    noise (1 % of max), step 1/||A^T A||.  A step = forward projection of the
+    batch, residual, backward through torch.autograd (the adjoint kernel),
+    update."""
+    import torch
+    from ct_recon_extensions_gb300 import synthetic as syn
+    from ct_recon_extensions_gb300 import torch_ctrecon as tc
+    g = syn.parallel_config_2()
+    op = tc.ParallelProjection2DOp(g["ns"], g["na"], g["ds"], g["orbit"], g["offset_s"],
+                                   g["orbit_start"], g["nx"], g["ny"], g["dx"], g["dy"],
+                                   g["offset_x"], g["offset_y"], g["fov"])
+    B = 16
+    xt = torch.from_numpy(np.stack([syn.rasterize(syn.random_ellipses(4000 + i), g["nx"], g["ny"],
+                                                  g["dx"], g["dy"]) for i in range(B)])).float().to(device)
+    with torch.no_grad():
+        y = op.forward(xt)
+        gen = torch.Generator(device=device).manual_seed(4)
+        y += 0.01 * y.max() * torch.randn(y.shape, generator=gen, device=device)
+        v = torch.ones_like(xt)  # step 1/L, L = ||A^T A|| by power iteration
+        for _ in range(10):
+            v = op.adjoint(op.forward(v))
+            L = float(v.norm()) / math.sqrt(v.numel())
+            v *= math.sqrt(v.numel()) / float(v.norm())
+    x = torch.zeros_like(xt, requires_grad=True)
+    lr = 1.0 / L
+    stream = torch.cuda.current_stream()
+    ev = []
+
+    def step(rec):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)] if rec else None
+        if rec:
+            e[0].record(stream)
+        ax = tc.apply(op, x)
+        if rec:
+            e[1].record(stream)
+        loss = 0.5 * (ax - y).pow(2).sum()
+        if rec:
+            e[2].record(stream)
+        loss.backward()
+        if rec:
+            e[3].record(stream)
+            ev.append(e)
+        with torch.no_grad():
+            x.sub_(lr * x.grad)
+            x.grad = None
+        return loss.detach()
+
+    l0 = None
+    for _ in range(warmup):
+        lw = step(False)
+        l0 = float(lw) if l0 is None else l0
+    k = max(3, min(steps, 20))
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    dist.barrier()
+    torch.cuda.synchronize()
+    t0.record(stream)
+    for _ in range(k):
+        loss = step(True)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    dist.barrier()
+    secs = dist.max(t0.elapsed_time(t1) / 1e3)
+    fwd = statistics.fmean(e[0].elapsed_time(e[1]) for e in ev)
+    bwd = statistics.fmean(e[2].elapsed_time(e[3]) for e in ev)
+    return {
+        "workload": "gradient descent on ||Ax - y||^2, batch 16 x 512^2, fp_par_2d 720 x 729 "
+                    "and its adjoint through torch.autograd",
+        "steps_per_s": k / secs, "images_per_s": B * k / secs,
+        "forward_batch_ms": fwd, "backward_batch_ms": bwd,
+        "loss_first": l0, "loss_last": float(loss), "steps": k,
+        "gpu_launches": k * (3 + 1),
+    }
+
+
 def run_e2e(pipe, pool_host, steps, warmup, in_shape, out_shape, device):
     """Through the C ABI with host buffers: per step H2D of the input from
     pinned memory, the three operators, D2H of the result, stream sync."""
@@ -578,6 +656,9 @@ def main():
     # ---- batched uneven fan FBP (config 3) against the plain drop-in ----
     batched = run_batched(device, args.steps, args.warmup, dist)
 
+    # ---- differentiable pair: gradient descent (config 4) ----
+    gd = run_gd(device, args.steps, args.warmup, dist)
+
     # ---- roofline of the dominant kernel ----
     peak_meas = fp32_peak_tflops(device)
     clk_max = clocks.get("sm_max_mhz") or 2070.0
@@ -627,6 +708,7 @@ def main():
                     "gpu_launches": f_launches,
                 },
                 "batched_fan_config3": batched,
+                "gd_config4": gd,
             },
         }
         print(json.dumps(line))

@@ -160,8 +160,8 @@ __global__ void __launch_bounds__(kFpThreads)
 // a strided order (slot_octet), so a contiguous range of slots mixes long
 // central rays and short edge rays.  Each class gets CTAs in proportion to its
 // views and cuts its slots into equal ranges, and a CTA deals its slots, sorted
-// by their exact sample counts, to its warps in snake order.  A round holds up to kFpxRound slots (one more round streams
-// the image again; rare).
+// by their exact sample counts, to its warps in snake order.  A round holds up
+// to kFpxRound slots (one more round streams the image again; rare).
 //
 // Pipeline: a producer lane copies band t (one contiguous range of the staged
 // row-major array, one TMA bulk copy) into stage t % 3 once every consumer
@@ -570,10 +570,22 @@ __global__ void __launch_bounds__(kFpxThreads, 2)
 
 // ---- FP32 adjoint: per-pixel gather over each view's channel footprint ----
 // Channel positions of pixel centres are 32.32 fixed point built from the
-// caller's grad-prep table (one FP64 conversion per tile line and view); the
-// footprint and triangle weights are those of src/fp_par_2d.cc:339-383.
+// caller's grad-prep table (one conversion per tile line and view); the
+// footprint and triangle weights are those of src/fp_par_2d.cc:339-383:
+// channels within |offset| of the pixel's position mid, weight 1 - |mid - is| /
+// |offset|.  Where |offset| <= 1 (every view when dx, dy <= ds) a pixel-view
+// touches at most the channels floor(mid) and floor(mid) + 1, whose weights
+// follow from the fraction with two FMAs, so the gather is two loads and four
+// FMAs.  Wider footprints, and the one-sided footprints of border pixels
+// (decided in FP64 as the reference does), take the general loop.
 constexpr int kFaViews = 16;
 constexpr int kFaRows = 4;  // pixels per thread (one column), 32x32 tile
+
+// 32.32 fixed point of a table value: integer conversion where exact, FP64 beyond.
+__device__ __forceinline__ long long fix32_any(double v)
+{
+    return ((double_bits(v) >> 52) & 0x7FF) < 1043 ? fix32(v) : llrint(v * kTwo32);
+}
 
 __global__ void __launch_bounds__(256)
     fp_adj_f32(const float* __restrict__ proj, float* __restrict__ img,
@@ -583,7 +595,7 @@ __global__ void __launch_bounds__(256)
     __shared__ long long s_base[kFaViews][32];
     __shared__ long long s_o1[kFaViews];
     __shared__ float s_w[kFaViews], s_inv[kFaViews];
-    __shared__ int s_ux[kFaViews];
+    __shared__ int s_ux[kFaViews], s_two[kFaViews];
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tx0 = blockIdx.x * 32, ty0 = blockIdx.y * 32;
@@ -593,6 +605,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int r = 0; r < kFaRows; ++r) acc[r] = 0.0f;
     const int n = c.nx;  // == ny
+    const unsigned ns = static_cast<unsigned>(c.ns);
 
     for (int v0 = 0; v0 < c.na; v0 += kFaViews) {
         const int nv = min(kFaViews, c.na - v0);
@@ -602,12 +615,14 @@ __global__ void __launch_bounds__(256)
             const int ux = usex[ia] != 0;
             const int lin = min((ux ? ty0 : tx0) + l, n - 1);
             const double* pp = pos + (static_cast<size_t>(ia) * n + lin) * 2;
-            s_base[j][l] = llrint(pp[0] * kTwo32);
+            s_base[j][l] = fix32_any(pp[0]);
             if (l == 0) {
-                s_o1[j] = llrint(pp[1] * kTwo32);
-                s_w[j] = static_cast<float>(weights[ia]);
-                s_inv[j] = static_cast<float>(1.0 / fabs(pp[1]));
+                const float o1 = fabsf(dbl2flt(pp[1]));
+                s_o1[j] = fix32_any(pp[1]);
+                s_w[j] = dbl2flt(weights[ia]);
+                s_inv[j] = 1.0f / o1;
                 s_ux[j] = ux;
+                s_two[j] = o1 <= 1.0f;
             }
         }
         __syncthreads();
@@ -618,6 +633,7 @@ __global__ void __launch_bounds__(256)
             const int ux = s_ux[j];
             const long long O1 = s_o1[j];
             const float inv = s_inv[j], w = s_w[j];
+            const bool two = s_two[j] != 0;
             const float* row = P + static_cast<size_t>(v0 + j) * c.ns;
 #pragma unroll
             for (int r = 0; r < kFaRows; ++r) {
@@ -625,39 +641,49 @@ __global__ void __launch_bounds__(256)
                 const int along = ux ? ix : iy;
                 const long long MID = s_base[j][ux ? warp * kFaRows + r : lane] +
                                       static_cast<long long>(along) * O1;
-                long long L = along == 0 ? MID : MID - O1;
-                long long R = along == n - 1 ? MID : MID + O1;
-                if (L > R) {
-                    const long long t = L;
-                    L = R;
-                    R = t;
-                }
-                int lo = max(static_cast<int>((L + 0xFFFFFFFFll) >> 32), 0);
-                int hi = min(static_cast<int>(R >> 32), c.ns - 1);
-                if (along == 0 || along == n - 1) {
-                    // One-sided footprint of a border pixel: its end channel sits at
-                    // the pixel itself with weight ~1, so the range is decided in
-                    // FP64 exactly as the reference does (mid = begin + offset*along).
-                    const int lin = ux ? iy : ix;
-                    const double* pp = pos + (static_cast<size_t>(v0 + j) * n + min(lin, n - 1)) * 2;
-                    const double off = pp[1];
-                    const double mid = __dadd_rn(pp[0], __dmul_rn(off, static_cast<double>(along)));
-                    double left = along == 0 ? mid : __dsub_rn(mid, off);
-                    double right = along == n - 1 ? mid : __dadd_rn(mid, off);
-                    if (left > right) {
-                        const double t = left;
-                        left = right;
-                        right = t;
-                    }
-                    lo = static_cast<int>(fmax(ceil(left), 0.0));
-                    hi = static_cast<int>(fmin(floor(right), static_cast<double>(c.ns - 1)));
-                }
                 const int mi = static_cast<int>(MID >> 32);
                 const float mf = frac_of(MID);
-                float part = 0.0f;
-                for (int is = lo; is <= hi; ++is) {
-                    const float d = fabsf(mf - static_cast<float>(is - mi));
-                    part = fmaf(fmaf(-d, inv, 1.0f), __ldg(row + is), part);
+                const bool border = along == 0 || along == n - 1;
+                float part;
+                if (two && !border) {
+                    const float w0 = fmaxf(fmaf(-mf, inv, 1.0f), 0.0f);
+                    const float w1 = fmaxf(fmaf(mf, inv, 1.0f - inv), 0.0f);
+                    const float p0 = static_cast<unsigned>(mi) < ns ? __ldg(row + mi) : 0.0f;
+                    const float p1 = static_cast<unsigned>(mi + 1) < ns ? __ldg(row + mi + 1) : 0.0f;
+                    part = fmaf(w0, p0, w1 * p1);
+                } else {
+                    long long L = along == 0 ? MID : MID - O1;
+                    long long R = along == n - 1 ? MID : MID + O1;
+                    if (L > R) {
+                        const long long t = L;
+                        L = R;
+                        R = t;
+                    }
+                    int lo = max(static_cast<int>((L + 0xFFFFFFFFll) >> 32), 0);
+                    int hi = min(static_cast<int>(R >> 32), c.ns - 1);
+                    if (border) {
+                        // One-sided footprint of a border pixel: its end channel sits at
+                        // the pixel itself with weight ~1, so the range is decided in
+                        // FP64 exactly as the reference does (mid = begin + offset*along).
+                        const int lin = ux ? iy : ix;
+                        const double* pp = pos + (static_cast<size_t>(v0 + j) * n + min(lin, n - 1)) * 2;
+                        const double off = pp[1];
+                        const double mid = __dadd_rn(pp[0], __dmul_rn(off, static_cast<double>(along)));
+                        double left = along == 0 ? mid : __dsub_rn(mid, off);
+                        double right = along == n - 1 ? mid : __dadd_rn(mid, off);
+                        if (left > right) {
+                            const double t = left;
+                            left = right;
+                            right = t;
+                        }
+                        lo = static_cast<int>(fmax(ceil(left), 0.0));
+                        hi = static_cast<int>(fmin(floor(right), static_cast<double>(c.ns - 1)));
+                    }
+                    part = 0.0f;
+                    for (int is = lo; is <= hi; ++is) {
+                        const float d = fabsf(mf - static_cast<float>(is - mi));
+                        part = fmaf(fmaf(-d, inv, 1.0f), __ldg(row + is), part);
+                    }
                 }
                 blk[r] = fmaf(part, w, blk[r]);
             }
