@@ -576,10 +576,16 @@ __global__ void __launch_bounds__(kFpxThreads, 2)
 // |offset|.  Where |offset| <= 1 (every view when dx, dy <= ds) a pixel-view
 // touches at most the channels floor(mid) and floor(mid) + 1, whose weights
 // follow from the fraction with two FMAs, so the gather is two loads and four
-// FMAs.  Wider footprints, and the one-sided footprints of border pixels
-// (decided in FP64 as the reference does), take the general loop.
+// FMAs.  A border pixel's footprint is one-sided; its end channel is decided
+// from the fixed-point fraction, or, when mid lies within kFaTie units of a
+// channel, in FP64 exactly as the reference does (the general loop, which
+// also takes the wider footprints).
 constexpr int kFaViews = 16;
 constexpr int kFaRows = 4;  // pixels per thread (one column), 32x32 tile
+// Units of 2^-32 channel within which a border pixel's position counts as on a
+// channel: the fixed-point position is within 0.5 + 0.5*along units of the
+// reference's FP64 one (along < 8192).
+constexpr unsigned kFaTie = 8192;
 
 // 32.32 fixed point of a table value: integer conversion where exact, FP64 beyond.
 __device__ __forceinline__ long long fix32_any(double v)
@@ -644,10 +650,20 @@ __global__ void __launch_bounds__(256)
                 const int mi = static_cast<int>(MID >> 32);
                 const float mf = frac_of(MID);
                 const bool border = along == 0 || along == n - 1;
+                // a border pixel's footprint is one-sided (toward the neighbour
+                // pixel): channels >= mid or <= mid; settled in fixed point unless
+                // mid is within kFaTie units of a channel (then FP64, as the reference)
+                const unsigned frac_bits = static_cast<unsigned>(MID);
+                const bool tie = border && (n == 1 || frac_bits < kFaTie || frac_bits > 0u - kFaTie);
                 float part;
-                if (two && !border) {
-                    const float w0 = fmaxf(fmaf(-mf, inv, 1.0f), 0.0f);
-                    const float w1 = fmaxf(fmaf(mf, inv, 1.0f - inv), 0.0f);
+                if (two && !tie) {
+                    float w0 = fmaxf(fmaf(-mf, inv, 1.0f), 0.0f);
+                    float w1 = fmaxf(fmaf(mf, inv, 1.0f - inv), 0.0f);
+                    if (border) {
+                        const bool ge = (along == 0) != (O1 < 0);  // footprint [mid, mid + |o|]
+                        if (ge) w0 = 0.0f;
+                        else w1 = 0.0f;
+                    }
                     const float p0 = static_cast<unsigned>(mi) < ns ? __ldg(row + mi) : 0.0f;
                     const float p1 = static_cast<unsigned>(mi + 1) < ns ? __ldg(row + mi + 1) : 0.0f;
                     part = fmaf(w0, p0, w1 * p1);
