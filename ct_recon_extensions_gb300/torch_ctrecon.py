@@ -144,6 +144,82 @@ class RampFilterOp:
         return self._run("ramp_filter_grad", y)
 
 
+class RampFilterTCOp:
+    """The ramp filter, optionally after fan weighting, as a Toeplitz GEMM on
+    the BF16 tensor cores with hi/lo split operands and FP32 accumulation.
+
+    Input: float32, bfloat16 or float16 sinograms [B,nrow,ns]; output float32.
+    No reference counterpart: it is the reduced-precision form of RampFilter
+    (src/filter.cc:67-91), with FanWeighting (src/fan_weighting.cc:19-38)
+    fused in front when `weighting` (a FanWeightingOp) is given.  One plan per
+    (device, direction), grown to the largest batch seen."""
+
+    _DTYPES = {torch.float32: _lib.CTR_DTYPE_F32, torch.bfloat16: _lib.CTR_DTYPE_BF16,
+               torch.float16: _lib.CTR_DTYPE_F16}
+
+    def __init__(self, ns, nrow, ds, dsd=-1.0, type=0, weighting=None):
+        self.ramp = RampFilterOp(ns, nrow, ds, dsd, type)
+        if weighting is not None and (weighting.ns != ns or weighting.nrow != nrow):
+            raise ValueError("weighting must have the filter's ns and nrow")
+        self.weighting = weighting
+        self.ns, self.nrow = ns, nrow
+        self._plans = {}
+        self._lib = _lib.load()
+
+    def plan(self, device, grad=False, batch=1):
+        dev = device.index if device.index is not None else torch.cuda.current_device()
+        key = (dev, bool(grad))
+        cur = self._plans.get(key)
+        if cur is None or cur[1] < batch:
+            with torch.cuda.device(dev):
+                if cur is not None:
+                    torch.cuda.current_stream().synchronize()
+                    self._lib.ctr_ramp_filter_tc_destroy(cur[0])
+                    del self._plans[key]
+                h = ctypes.c_void_p()
+                w = ctypes.byref(self.weighting.p) if self.weighting is not None else None
+                call("ctr_ramp_filter_tc_create", ctypes.byref(self.ramp.p),
+                     _ptr(self.ramp.taps(torch.device("cuda", dev))), w, int(grad), int(batch),
+                     ctypes.byref(h), _stream())
+                self._plans[key] = (h, batch)
+        return self._plans[key][0]
+
+    def info(self, device):
+        ws, fl = ctypes.c_ulonglong(), ctypes.c_ulonglong()
+        call("ctr_ramp_filter_tc_info", self.plan(device), ctypes.byref(ws), ctypes.byref(fl))
+        return {"workspace_bytes": ws.value, "mma_flops_per_row": fl.value}
+
+    def _run(self, x, grad):
+        if x.dtype not in self._DTYPES:
+            raise TypeError(f"ramp_filter_tc takes float32, bfloat16 or float16, got {x.dtype}")
+        xb, restore = _as_batch(x, self.nrow, self.ns, "ramp_filter_tc")
+        out = torch.empty(xb.shape, dtype=torch.float32, device=xb.device)
+        h = self.plan(xb.device, grad, xb.shape[0])
+        call("ctr_ramp_filter_tc_run", h, self._DTYPES[xb.dtype], _ptr(xb), _ptr(out), xb.shape[0],
+             _stream())
+        return restore(out)
+
+    def forward(self, x):
+        return self._run(x, False)
+
+    def adjoint(self, y):
+        if self.weighting is not None:
+            raise ValueError("the adjoint of the fused weighting + filter is not provided; "
+                             "use RampFilterTCOp without weighting and FanWeightingOp.adjoint")
+        return self._run(y, True)
+
+    def close(self):
+        for h, _ in self._plans.values():
+            self._lib.ctr_ramp_filter_tc_destroy(h)
+        self._plans.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class FanBackprojection2DOp:
     """FanBackprojection2DPixDriven{Prep,,GradPrep,Grad} (reference
     include/bp_fan_2d.h:151-225)."""

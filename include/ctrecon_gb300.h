@@ -129,6 +129,31 @@ int ctr_ramp_filter_grad_f64(const ctr_filter_param* p, const double* in,
                              const double* filter, double* out, int batch,
                              cudaStream_t stream);
 
+/* ---- ramp filter on the BF16 tensor cores (no reference counterpart: the
+ *      reduced-precision form of RampFilter<T> / RampFilterGrad<T>) ----
+ * The filter as a dense Toeplitz GEMM, OUT = X * T^T with T[i][j] = ds*h[i-j]
+ * (grad != 0: ds*h[j-i]).  X and T are split into BF16 hi/lo pairs and the
+ * products hi*hi + hi*lo + lo*hi accumulate in FP32 (relative error near
+ * 2^-16).  The input is stored as FP32, BF16 or FP16 (in_dtype); the optional
+ * fan weighting (FanWeighting<T>, same ns) is applied to it first, in FP32.
+ * The output is FP32 [batch*nrow][ns].  A plan owns the split T (built from
+ * the device taps of ctr_ramp_filter_prep, on `stream`) and the split-X
+ * workspace for max_batch sinograms; it serves one stream at a time. */
+#define CTR_DTYPE_F32 0
+#define CTR_DTYPE_BF16 1
+#define CTR_DTYPE_F16 2
+typedef struct ctr_ramp_tc_plan ctr_ramp_tc_plan;
+int ctr_ramp_filter_tc_create(const ctr_filter_param* p, const double* filter,
+                              const ctr_fan_weighting_param* weighting, int grad, int max_batch,
+                              ctr_ramp_tc_plan** plan, cudaStream_t stream);
+int ctr_ramp_filter_tc_run(ctr_ramp_tc_plan* plan, int in_dtype, const void* in, float* out,
+                           int batch, cudaStream_t stream);
+/* Device bytes the plan holds, and tensor-core FLOPs per input row (the three
+ * products over the padded 128 x 64 tiles). */
+int ctr_ramp_filter_tc_info(const ctr_ramp_tc_plan* plan, unsigned long long* workspace_bytes,
+                            unsigned long long* mma_flops_per_row);
+int ctr_ramp_filter_tc_destroy(ctr_ramp_tc_plan* plan);
+
 /* ---- fan-beam pixel-driven backprojection, uniform orbit
  *      (reference include/bp_fan_2d.h:151-225) ----
  * Tables (FanBackprojection2DPixDrivenPrep / ...GradPrep): xpos double[nx],
