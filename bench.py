@@ -283,6 +283,42 @@ class FanPipeline:
                                           ctypes.c_void_p(out.data_ptr()), *self.bpt, 1, s)
 
 
+class LowpFanPipeline:
+    """Sinogram stored in BF16 or FP16: fan weighting + ramp(fan) as one
+    tensor-core Toeplitz GEMM call (split kernel + tcgen05 GEMM over `splits`
+    BF16 terms per operand, FP32 accumulate), then bp_fan_2d in FP32."""
+
+    def __init__(self, g, device, dtype, splits=3):
+        import torch
+        from ct_recon_extensions_gb300 import _lib
+        from ct_recon_extensions_gb300 import torch_ctrecon as tc
+        self.lib = _lib.load()
+        self.g = g
+        w = tc.FanWeightingOp(g["ns"], g["na"], g["ds"], g["offset_s"], g["dso"], g["dsd"], 1)
+        self.tcop = tc.RampFilterTCOp(g["ns"], g["na"], g["ds"], g["dsd"], 1, weighting=w, splits=splits)
+        self.plan = self.tcop.plan(device, False, 1)
+        self.dt = tc.RampFilterTCOp._DTYPES[dtype]
+        self.bp = tc.FanBackprojection2DOp(g["ns"], g["na"], g["ds"], g["orbit"], g["offset_s"],
+                                           g["orbit_start"], g["nx"], g["ny"], g["dx"], g["dy"],
+                                           g["offset_x"], g["offset_y"], g["dso"], g["dsd"], g["fov"])
+        self.bpt = [ctypes.c_void_p(t.data_ptr()) for t in self.bp.tables(device)]
+        self.filt = torch.empty((g["na"], g["ns"]), dtype=torch.float32, device=device)
+        self.names = ["ramp_filter_tc", "bp_fan_2d"]
+        self.kernels = {"ramp_filter_tc": 2, "bp_fan_2d": 1}
+        info = self.tcop.info(device)
+        self.flops = {"ramp_filter_tc": float(info["mma_flops_per_row"]) * g["na"],
+                      "bp_fan_2d": 32.0 * g["nx"] * g["ny"] * g["na"]}
+        self.updates = float(g["nx"] * g["ny"] * g["na"])
+
+    def launches(self, sino, out, stream):
+        L = self.lib
+        s = ctypes.c_void_p(stream)
+        yield lambda: L.ctr_ramp_filter_tc_run(self.plan, self.dt, ctypes.c_void_p(sino.data_ptr()),
+                                               ctypes.c_void_p(self.filt.data_ptr()), 1, s)
+        yield lambda: L.ctr_bp_fan_2d_f32(ctypes.byref(self.bp.p), ctypes.c_void_p(self.filt.data_ptr()),
+                                          ctypes.c_void_p(out.data_ptr()), *self.bpt, 1, s)
+
+
 def run_device(pipe, pool_dev, outs, steps, warmup, dist, per_kernel=True):
     """Time `steps` pipeline steps on device-resident inputs; returns (seconds,
     per-kernel mean ms, launches)."""
@@ -460,6 +496,132 @@ def run_gd(device, steps, warmup, dist):
         "loss_first": l0, "loss_last": float(loss), "steps": k,
         "gpu_launches": k * (3 + 1),
     }
+
+
+def rel_l2(a, b) -> float:
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    den = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (den if den > 0 else 1.0))
+
+
+LOWP_STRIPS = ((256, 16), (900, 16), (1400, 16), (1800, 16))  # (first row, rows) of the check
+
+
+def lowp_check(g, stored, imgs):
+    """FP64 oracle of the large fan FBP (fan weighting -> ramp(fan) ->
+    bp_fan_2d, the port on all host cores) on 4 strips of 16 image rows,
+    against each path's image: the oracle of the stored sinogram (the kernels'
+    error) and of the exact FP64 sinogram (storage included).  The strips are
+    sub-images whose pixel centres are the full image's rows."""
+    from oracle import Geom, Oracle
+    orc = Oracle("port", threads=os.cpu_count() or 1)
+
+    def strips(sino64):
+        w = orc.fan_weighting(sino64, g["ds"], g["offset_s"], g["dso"], g["dsd"], 1)
+        f = orc.ramp_filter(w, g["ds"], g["dsd"], 1)
+        out = []
+        for r0, k in LOWP_STRIPS:
+            off_y = (g["ny"] - 1) / 2 + g["offset_y"] - r0 - (k - 1) / 2
+            gs = Geom.make(g["ns"], g["na"], g["ds"], g["orbit"], g["nx"], k, g["dx"], g["dy"],
+                           g["offset_s"], g["orbit_start"], g["offset_x"], off_y, g["dso"], g["dsd"],
+                           g["fov"])
+            out.append(orc.bp_fan_2d(f, gs))
+        return np.concatenate(out)
+
+    def rows(img):
+        return np.concatenate([img[r0:r0 + k] for r0, k in LOWP_STRIPS]).astype(np.float64)
+
+    t0 = time.perf_counter()
+    exact = strips(stored["exact"])
+    res = {}
+    for name, img in imgs.items():
+        same = strips(stored[name])
+        got = rows(img)
+        res[name] = {"rel_l2_vs_fp64": rel_l2(got, same),
+                     "max_abs_vs_fp64": float(np.abs(got - same).max()),
+                     "rel_l2_vs_fp64_exact_sinogram": rel_l2(got, exact),
+                     "max_abs_vs_fp64_exact_sinogram": float(np.abs(got - exact).max())}
+    res["image_max_abs"] = float(np.abs(exact).max())
+    res["oracle"] = (f"FP64 port on {os.cpu_count()} threads, rows "
+                     + ", ".join(f"{r0}-{r0 + k - 1}" for r0, k in LOWP_STRIPS)
+                     + f" of {g['ny']} ({sum(k for _, k in LOWP_STRIPS) * g['nx']} pixels), "
+                     f"{time.perf_counter() - t0:.1f} s")
+    return res
+
+
+def run_lowp(device, steps, warmup, dist, check):
+    """The large reduced-precision slice: 2048^2 at 0.25 mm from 2304 fan views
+    over 2pi x 1472 channels.  The sinogram is stored in FP32 (plain path:
+    fan_weighting -> ramp_filter on the FP32 pipe -> bp_fan_2d) and in BF16
+    and FP16 (weighting + filter as the tensor-core Toeplitz GEMM with
+    hi/mid/lo operands, then bp_fan_2d in FP32); bf16_hilo is the BF16 path
+    with the 2-term (hi/lo, 3-product) split.  Each path runs on 4 distinct sinograms; with `check`
+    its error against the FP64 oracle is measured on image strips."""
+    import torch
+    from ct_recon_extensions_gb300 import synthetic as syn
+    g = syn.large_config_5()
+    k = max(3, min(steps, 20))
+    base = syn.fan_sinogram(syn.random_ellipses(5000), g["na"], g["ns"], g["ds"], g["orbit"], g["dso"],
+                            g["dsd"], dtype=np.float64)
+    outs = [torch.empty((g["ny"], g["nx"]), dtype=torch.float32, device=device) for _ in range(2)]
+    paths = {"f32": (lambda: FanPipeline(g, device), torch.float32),
+             "bf16": (lambda: LowpFanPipeline(g, device, torch.bfloat16, 3), torch.bfloat16),
+             "f16": (lambda: LowpFanPipeline(g, device, torch.float16, 3), torch.float16),
+             "bf16_hilo": (lambda: LowpFanPipeline(g, device, torch.bfloat16, 2), torch.bfloat16)}
+    res, imgs, stored = {}, {}, {"exact": base}
+    peak_tc = bf16_peak_tflops()
+    for name, (make, dt) in paths.items():
+        pipe = make()
+        pool = [torch.from_numpy(base * (1.0 + 1e-3 * i)).to(device=device, dtype=dt) for i in range(4)]
+        secs, kern, launches = run_device(pipe, pool, outs, k, warmup, dist)
+        secs = dist.max(secs)
+        r = {"slices_per_s": dist.ws * k / secs, "ms_per_slice": 1e3 * secs / k, "kernel_ms": kern,
+             "gpu_launches": launches, "storage": str(dt).replace("torch.", "")}
+        if name == "f32":
+            r["filter"] = "fan_weighting + ramp_filter, FP32 pipe (direct convolution)"
+        else:
+            fl = pipe.flops["ramp_filter_tc"]
+            tfl = fl / (kern["ramp_filter_tc"] / 1e3) / 1e12
+            r["filter"] = ("weighting + ramp as a Toeplitz GEMM on tcgen05, FP32 accumulate (split kernel"
+                           " + GEMM kernel): " + ("BF16 hi/mid/lo, 6 term products" if pipe.tcop.splits == 3
+                                                  else "BF16 hi/lo, 3 term products"))
+            r["filter_tc"] = {"mma_flops": fl, "tflops": tfl, "peak": peak_tc[0], "frac": tfl / peak_tc[0],
+                              "peak_source": peak_tc[1], "unit": "TFLOP/s"}
+        if check:
+            run = list(pipe.launches(pool[0], outs[0], torch.cuda.current_stream().cuda_stream))
+            for fn in run:
+                if fn() != 0:
+                    raise RuntimeError(pipe.lib.ctr_last_error().decode())
+            imgs[name] = outs[0].cpu().numpy()
+            stored[name] = pool[0].to(torch.float64).cpu().numpy()
+        res[name] = r
+        if hasattr(pipe, "tcop"):
+            torch.cuda.synchronize()
+            pipe.tcop.close()
+        del pool
+    out = {"workload": "fan FBP, 2304 views over 2pi x 1472 ch at 0.6429 mm -> 2048x2048 at 0.25 mm; "
+                       "sinogram stored in FP32, BF16, FP16; backprojection accumulates in FP32",
+           "paths": res, "steps": k,
+           "speedup_bf16_vs_f32": res["bf16"]["slices_per_s"] / res["f32"]["slices_per_s"]}
+    if check:
+        acc = lowp_check(g, stored, imgs)
+        for name in imgs:
+            res[name].update(acc[name])
+        out["image_max_abs"] = acc["image_max_abs"]
+        out["check"] = acc["oracle"]
+    return out
+
+
+def bf16_peak_tflops():
+    """The dense BF16 tensor peak measured on this GPU type (cuBLAS 8192^3,
+    burst), from MEASURED_PEAKS.json beside this file, else the fallback."""
+    p = os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured: cuBLAS bf16 8192^3 burst"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback: 1.9 PFLOP/s bf16 burst"
 
 
 def run_e2e(pipe, pool_host, steps, warmup, in_shape, out_shape, device):
@@ -659,6 +821,10 @@ def main():
     # ---- differentiable pair: gradient descent (config 4) ----
     gd = run_gd(device, args.steps, args.warmup, dist)
 
+    # ---- reduced-precision large slice (config 5); its FP64 check is CPU
+    #      oracle work on rank 0, part of the CPU-baseline leg ----
+    lowp = run_lowp(device, args.steps, args.warmup, dist, rank == 0 and not args.no_cpu_baseline)
+
     # ---- roofline of the dominant kernel ----
     peak_meas = fp32_peak_tflops(device)
     clk_max = clocks.get("sm_max_mhz") or 2070.0
@@ -709,6 +875,7 @@ def main():
                 },
                 "batched_fan_config3": batched,
                 "gd_config4": gd,
+                "lowp_config5": lowp,
             },
         }
         print(json.dumps(line))

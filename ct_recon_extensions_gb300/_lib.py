@@ -97,7 +97,7 @@ PROTOTYPES = {
     "ctr_fbp_fan_plan_info": [c_void_p, _S(PlanInfo)],
     "ctr_fbp_fan_plan_destroy": [c_void_p],
     "ctr_fp_par_2d_f32_noalloc": [_S(ParParam), _P, _P, _P, _P, _P, c_int, _P],
-    "ctr_ramp_filter_tc_create": [_S(FilterParam), _P, _S(FanWeightingParam), c_int, c_int,
+    "ctr_ramp_filter_tc_create": [_S(FilterParam), _P, _S(FanWeightingParam), c_int, c_int, c_int,
                                   ctypes.POINTER(c_void_p), _P],
     "ctr_ramp_filter_tc_run": [c_void_p, c_int, _P, _P, c_int, _P],
     "ctr_ramp_filter_tc_info": [c_void_p, ctypes.POINTER(ctypes.c_ulonglong),

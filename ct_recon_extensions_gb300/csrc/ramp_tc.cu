@@ -5,25 +5,32 @@
 // a zero-padded linear convolution; the grad, src/filter.cc:96-124, uses
 // h[j-i]) is a product with the Toeplitz matrix T[i][j] = ds*h[i-j]:
 // OUT = X T^T with M = rows (views x batch) and N = K = ns.  Both operands are
-// split into BF16 pairs, x = x_hi + x_lo with x_hi = bf16(x) and
-// x_lo = bf16(x - x_hi) (16 significant bits between them), and
-// OUT = X_hi T_hi^T + X_hi T_lo^T + X_lo T_hi^T accumulates in FP32 in tensor
-// memory.  The dropped X_lo T_lo^T and the rounding of the pair leave a
-// relative error near 2^-16 per product.
+// split into BF16 terms, each the BF16 rounding of what the previous terms
+// leave (the remainders are exact in FP32 for X and in FP64 for T):
+//   2 terms (hi, lo; 16 significant bits):  OUT = X0 T0 + X0 T1 + X1 T0,
+//   3 terms (hi, mid, lo; 24 bits):         OUT = X0 T0 + X0 T1 + X1 T0
+//                                                + X0 T2 + X2 T0 + X1 T1,
+// (products written X_a T_b^T), accumulating in FP32 in tensor memory.  The
+// ramp taps sum to zero, so on a smooth sinogram the filter cancels almost
+// all of its input and amplifies operand error about a hundredfold: with 2
+// terms the filtered sinogram of a smooth 1472-channel fan sinogram is off by
+// ~6e-4 (relative L2), with 3 terms by ~1e-6, below FP32 taps (~4e-6).
 //
 // Operand layout in HBM: each operand is stored already tiled the way the
 // tensor core's shared-memory descriptor reads it.  A tile is 128 rows x 64 K
 // elements, K-major with the 128-byte swizzle: row r of the tile starts at
 // byte (r/8)*1024 + (r%8)*128, and its 16-byte chunk c is stored at chunk
-// c ^ (r%8).  The hi tile is followed by the lo tile (a 32 KiB block); row
-// tiles are outer and K blocks inner.  A pipeline stage of the GEMM is then
-// two contiguous 32 KiB bulk copies, with no tensor map.  split_rows writes
+// c ^ (r%8).  The term tiles of one (row tile, K block) follow each other (a
+// block of 2 or 3 x 16 KiB); row tiles are outer and K blocks inner.  A
+// pipeline stage of the GEMM is then two contiguous bulk copies (the X block
+// and the T block), with no tensor map.  split_rows writes
 // the X blocks and fuses the input conversion with the optional fan weighting
 // (src/fan_weighting.cc:19-38).  split_toeplitz builds the T blocks once per
 // plan from the FP64 taps.
 //
 // GEMM: one CTA per 128 x 128 output tile, 4 warps.  Thread 0 streams the K
-// blocks into a 3-stage ring (full / empty mbarriers).  Thread 32 issues
+// blocks into a ring of 192 KiB (3 stages of 64 KiB with 2 terms, 2 of 96 KiB
+// with 3; full / empty mbarriers).  Thread 32 issues
 // tcgen05.mma (M=128, N=128, K=16, BF16 x BF16 -> FP32) into a 128-column
 // TMEM accumulator and frees each stage with tcgen05.commit.  After the last
 // commit the four warps read their 32 TMEM lanes (tcgen05.ld 32x32b), stage
@@ -43,11 +50,12 @@ struct ctr_ramp_tc_plan {
     int device;
     unsigned ns, nrow;
     int max_batch;
+    int splits;             // BF16 terms per operand: 2 (hi, lo) or 3 (hi, mid, lo)
     unsigned kblocks;       // K blocks of 64 channels
     unsigned ntiles;        // output column tiles of 128 channels
     unsigned max_mtiles;    // row tiles of the X workspace
-    unsigned char* T;       // split Toeplitz blocks, ntiles x kblocks x 32 KiB
-    unsigned char* X;       // split input blocks, max_mtiles x kblocks x 32 KiB
+    unsigned char* T;       // split Toeplitz blocks, ntiles x kblocks x splits x 16 KiB
+    unsigned char* X;       // split input blocks, max_mtiles x kblocks x splits x 16 KiB
     float* weight;          // per-channel fan weight, or null
 };
 
@@ -57,10 +65,16 @@ namespace {
 constexpr int kTcRows = 128;                         // rows of an operand tile (M or N)
 constexpr int kTcK = 64;                             // K elements of a tile: 128 bytes of BF16
 constexpr unsigned kTcTile = kTcRows * kTcK * 2;     // 16 KiB
-constexpr unsigned kTcBlock = 2 * kTcTile;           // hi tile + lo tile
-constexpr int kTcStages = 3;
-constexpr unsigned kTcStage = 2 * kTcBlock;          // X block + T block
-constexpr unsigned kTcSmem = kTcStages * kTcStage + 1024;  // + 1 KiB to align the ring
+constexpr unsigned kTcRing = 192 * 1024;             // pipeline ring
+constexpr unsigned kTcSmem = kTcRing + 1024;         // + 1 KiB to align the ring
+
+template <int kSplits>
+struct TcShape {
+    static constexpr unsigned kBlock = kSplits * kTcTile;   // the term tiles of one K block
+    static constexpr unsigned kStage = 2 * kBlock;          // X block + T block
+    static constexpr int kStages = static_cast<int>(kTcRing / kStage);
+    static_assert(kStages >= 2, "ring too small");
+};
 constexpr unsigned kTcCols = 128;                    // TMEM columns of the FP32 accumulator
 constexpr int kTcThreads = 128;
 constexpr int kSplitThreads = 256;
@@ -75,21 +89,25 @@ __device__ __forceinline__ float to_f32(float v) { return v; }
 __device__ __forceinline__ float to_f32(__nv_bfloat16 v) { return __bfloat162float(v); }
 __device__ __forceinline__ float to_f32(__half v) { return __half2float(v); }
 
-// BF16 pair of two FP32 values: hi = bf16(x), lo = bf16(x - hi); x - hi is
-// exact in FP32.
-__device__ __forceinline__ void split2(float a, float b, unsigned& hi, unsigned& lo)
+// BF16 terms of two FP32 values, packed in pairs: term t is the BF16
+// rounding of what terms 0..t-1 leave; every remainder is exact in FP32.
+template <int kSplits>
+__device__ __forceinline__ void split_pair(float a, float b, unsigned (&t)[kSplits])
 {
-    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-    const float2 hf = __bfloat1622float2(h);
-    const __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
-    hi = *reinterpret_cast<const unsigned*>(&h);
-    lo = *reinterpret_cast<const unsigned*>(&l);
+#pragma unroll
+    for (int i = 0; i < kSplits; ++i) {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+        const float2 hf = __bfloat1622float2(h);
+        t[i] = *reinterpret_cast<const unsigned*>(&h);
+        a -= hf.x;
+        b -= hf.y;
+    }
 }
 
 // One thread per 16-byte chunk (8 channels of one row) of the X blocks:
-// converts, weights and splits, writing the chunk of the hi and the lo tile.
+// converts, weights and splits, writing the chunk of every term tile.
 // Rows past `rows` and channels past ns are zero.
-template <typename Tin>
+template <typename Tin, int kSplits>
 __global__ void __launch_bounds__(kSplitThreads)
     split_rows(const Tin* __restrict__ in, const float* __restrict__ weight,
                unsigned char* __restrict__ X, unsigned ns, unsigned long long rows,
@@ -114,18 +132,18 @@ __global__ void __launch_bounds__(kSplitThreads)
         }
         v[e] = x;
     }
-    uint4 hi, lo;
-    split2(v[0], v[1], hi.x, lo.x);
-    split2(v[2], v[3], hi.y, lo.y);
-    split2(v[4], v[5], hi.z, lo.z);
-    split2(v[6], v[7], hi.w, lo.w);
-    unsigned char* dst = X + tile * kTcBlock + sw128_offset(r, c);
-    *reinterpret_cast<uint4*>(dst) = hi;
-    *reinterpret_cast<uint4*>(dst + kTcTile) = lo;
+    unsigned w[4][kSplits];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) split_pair<kSplits>(v[2 * q], v[2 * q + 1], w[q]);
+    unsigned char* dst = X + tile * TcShape<kSplits>::kBlock + sw128_offset(r, c);
+#pragma unroll
+    for (int i = 0; i < kSplits; ++i)
+        *reinterpret_cast<uint4*>(dst + i * kTcTile) = make_uint4(w[0][i], w[1][i], w[2][i], w[3][i]);
 }
 
 // The T blocks: T[n][k] = ds*h[n-k] (grad: ds*h[k-n]) for n, k < ns, split in
-// FP64 (lo = bf16(t - hi) with t - hi exact), zero elsewhere.
+// FP64 (every remainder exact), zero elsewhere.
+template <int kSplits>
 __global__ void __launch_bounds__(kSplitThreads)
     split_toeplitz(const double* __restrict__ taps, unsigned char* __restrict__ T, unsigned ns,
                    double ds, int grad, unsigned kblocks, unsigned long long nchunks)
@@ -138,29 +156,27 @@ __global__ void __launch_bounds__(kSplitThreads)
     const unsigned kb = static_cast<unsigned>(tile - nt * kblocks);
     const long long n = static_cast<long long>(nt * kTcRows + r);
     const unsigned k0 = kb * kTcK + c * 8;
-    unsigned short hs[8], ls[8];
+    unsigned short hs[kSplits][8];
 #pragma unroll
     for (int e = 0; e < 8; ++e) {
         const long long k = k0 + e;
         double t = 0.0;
         if (n < ns && k < ns) t = ds * taps[static_cast<long long>(ns) + (grad ? k - n : n - k)];
-        const __nv_bfloat16 h = __double2bfloat16(t);
-        const __nv_bfloat16 l = __double2bfloat16(t - static_cast<double>(__bfloat162float(h)));
-        hs[e] = *reinterpret_cast<const unsigned short*>(&h);
-        ls[e] = *reinterpret_cast<const unsigned short*>(&l);
+#pragma unroll
+        for (int i = 0; i < kSplits; ++i) {
+            const __nv_bfloat16 h = __double2bfloat16(t);
+            hs[i][e] = *reinterpret_cast<const unsigned short*>(&h);
+            t -= static_cast<double>(__bfloat162float(h));
+        }
     }
-    uint4 hi, lo;
-    hi.x = hs[0] | (static_cast<unsigned>(hs[1]) << 16);
-    hi.y = hs[2] | (static_cast<unsigned>(hs[3]) << 16);
-    hi.z = hs[4] | (static_cast<unsigned>(hs[5]) << 16);
-    hi.w = hs[6] | (static_cast<unsigned>(hs[7]) << 16);
-    lo.x = ls[0] | (static_cast<unsigned>(ls[1]) << 16);
-    lo.y = ls[2] | (static_cast<unsigned>(ls[3]) << 16);
-    lo.z = ls[4] | (static_cast<unsigned>(ls[5]) << 16);
-    lo.w = ls[6] | (static_cast<unsigned>(ls[7]) << 16);
-    unsigned char* dst = T + tile * kTcBlock + sw128_offset(r, c);
-    *reinterpret_cast<uint4*>(dst) = hi;
-    *reinterpret_cast<uint4*>(dst + kTcTile) = lo;
+    unsigned char* dst = T + tile * TcShape<kSplits>::kBlock + sw128_offset(r, c);
+#pragma unroll
+    for (int i = 0; i < kSplits; ++i)
+        *reinterpret_cast<uint4*>(dst + i * kTcTile) =
+            make_uint4(hs[i][0] | (static_cast<unsigned>(hs[i][1]) << 16),
+                       hs[i][2] | (static_cast<unsigned>(hs[i][3]) << 16),
+                       hs[i][4] | (static_cast<unsigned>(hs[i][5]) << 16),
+                       hs[i][6] | (static_cast<unsigned>(hs[i][7]) << 16));
 }
 
 // ---- tcgen05 pieces ------------------------------------------------------------
@@ -221,10 +237,13 @@ __device__ __forceinline__ void tmem_ld32(unsigned taddr, float (&v)[32])
 }
 
 // OUT[rows][ns] (FP32) = X T^T over the split blocks; grid (ntiles, mtiles).
+template <int kSplits>
 __global__ void __launch_bounds__(kTcThreads, 1)
     ramp_tc_gemm(const unsigned char* __restrict__ X, const unsigned char* __restrict__ T,
                  float* __restrict__ out, unsigned ns, unsigned long long rows, unsigned kblocks)
 {
+    constexpr int kTcStages = TcShape<kSplits>::kStages;
+    constexpr unsigned kTcBlock = TcShape<kSplits>::kBlock, kTcStage = TcShape<kSplits>::kStage;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned long long s_full[kTcStages], s_empty[kTcStages], s_done;
     __shared__ unsigned s_tmem, s_issued, s_consumed;
@@ -273,7 +292,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         s_issued = kb;
         if (kb < kblocks) s_abort = 1;
     } else if (threadIdx.x == 32) {
-        // MMA issuer: 4 K-slices x 3 products per K block
+        // MMA issuer: 4 K-slices x (3 or 6) term products per K block, the
+        // products of term indices (a, b) with a + b < kSplits, plus (1, 1) for 3 terms
         unsigned kb = 0;
         for (; kb < kblocks; ++kb) {
             const unsigned s = kb % kTcStages, u = kb / kTcStages;
@@ -282,13 +302,20 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             const unsigned a = base + s * kTcStage, b = a + kTcBlock;
 #pragma unroll
             for (int k = 0; k < kTcK / 16; ++k) {
-                const unsigned long long ah = sw128_desc(a + 32u * k);
-                const unsigned long long al = sw128_desc(a + kTcTile + 32u * k);
-                const unsigned long long bh = sw128_desc(b + 32u * k);
-                const unsigned long long bl = sw128_desc(b + kTcTile + 32u * k);
-                tc_mma(tmem, ah, bh, (kb | k) != 0);
-                tc_mma(tmem, ah, bl, 1u);
-                tc_mma(tmem, al, bh, 1u);
+                unsigned long long ad[kSplits], bd[kSplits];
+#pragma unroll
+                for (int i = 0; i < kSplits; ++i) {
+                    ad[i] = sw128_desc(a + i * kTcTile + 32u * k);
+                    bd[i] = sw128_desc(b + i * kTcTile + 32u * k);
+                }
+                tc_mma(tmem, ad[0], bd[0], (kb | k) != 0);
+                tc_mma(tmem, ad[0], bd[1], 1u);
+                tc_mma(tmem, ad[1], bd[0], 1u);
+                if constexpr (kSplits == 3) {
+                    tc_mma(tmem, ad[0], bd[2], 1u);
+                    tc_mma(tmem, ad[2], bd[0], 1u);
+                    tc_mma(tmem, ad[1], bd[1], 1u);
+                }
             }
             tc_commit(smem_u32(&s_empty[s]));
         }
@@ -354,6 +381,46 @@ unsigned long long split_chunks(unsigned tiles, unsigned kblocks)
     return static_cast<unsigned long long>(tiles) * kblocks * 1024ull;
 }
 
+unsigned block_bytes(int splits) { return splits * kTcTile; }
+
+template <int kSplits>
+int set_gemm_smem()
+{
+    cudaError_t e = cudaFuncSetAttribute(ramp_tc_gemm<kSplits>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(kTcSmem));
+    return e == cudaSuccess ? CTR_OK : fail(CTR_ERR_CUDA, "tensor-core filter smem: %s", cudaGetErrorString(e));
+}
+
+template <int kSplits>
+int run_splits(ctr_ramp_tc_plan* P, int in_dtype, const void* in, float* out, unsigned long long rows,
+               cudaStream_t stream)
+{
+    const unsigned mtiles = div_up(rows, kTcRows);
+    const unsigned long long nch = split_chunks(mtiles, P->kblocks);
+    const unsigned sb = div_up(nch, kSplitThreads);
+    switch (in_dtype) {
+    case CTR_DTYPE_F32:
+        split_rows<float, kSplits><<<sb, kSplitThreads, 0, stream>>>(static_cast<const float*>(in), P->weight,
+                                                                     P->X, P->ns, rows, P->kblocks, nch);
+        break;
+    case CTR_DTYPE_BF16:
+        split_rows<__nv_bfloat16, kSplits><<<sb, kSplitThreads, 0, stream>>>(
+            static_cast<const __nv_bfloat16*>(in), P->weight, P->X, P->ns, rows, P->kblocks, nch);
+        break;
+    case CTR_DTYPE_F16:
+        split_rows<__half, kSplits><<<sb, kSplitThreads, 0, stream>>>(static_cast<const __half*>(in), P->weight,
+                                                                      P->X, P->ns, rows, P->kblocks, nch);
+        break;
+    default:
+        return fail(CTR_ERR_INVALID_ARG, "input dtype %d (0 f32, 1 bf16, 2 f16)", in_dtype);
+    }
+    int st = check_launch("split_rows");
+    if (st) return st;
+    ramp_tc_gemm<kSplits><<<dim3(P->ntiles, mtiles), kTcThreads, kTcSmem, stream>>>(P->X, P->T, out, P->ns,
+                                                                                    rows, P->kblocks);
+    return check_launch("ramp_tc_gemm");
+}
+
 }  // namespace
 }  // namespace ctr
 
@@ -362,8 +429,8 @@ using namespace ctr;
 extern "C" {
 
 int ctr_ramp_filter_tc_create(const ctr_filter_param* p, const double* filter,
-                              const ctr_fan_weighting_param* weighting, int grad, int max_batch,
-                              ctr_ramp_tc_plan** plan, cudaStream_t stream)
+                              const ctr_fan_weighting_param* weighting, int grad, int splits,
+                              int max_batch, ctr_ramp_tc_plan** plan, cudaStream_t stream)
 {
     if (!p || bad_ptr(filter) || !plan) return fail(CTR_ERR_INVALID_ARG, "null argument");
     *plan = nullptr;
@@ -371,6 +438,8 @@ int ctr_ramp_filter_tc_create(const ctr_filter_param* p, const double* filter,
     if (st) return st;
     if (p->ns < 1 || p->nrow < 1) return fail(CTR_ERR_INVALID_ARG, "empty sinogram");
     if (p->ns > 16384) return fail(CTR_ERR_UNSUPPORTED, "ns=%u above the tensor-core filter's 16384", p->ns);
+    if (splits != 2 && splits != 3)
+        return fail(CTR_ERR_INVALID_ARG, "splits %d (2: hi/lo, 3: hi/mid/lo)", splits);
     if (weighting) {
         if (weighting->type != 1 && weighting->type != 2)
             return fail(CTR_ERR_INVALID_ARG, "fan weighting type %d (1 fan, 2 flat)", weighting->type);
@@ -379,16 +448,19 @@ int ctr_ramp_filter_tc_create(const ctr_filter_param* p, const double* filter,
     }
     const unsigned long long max_rows = static_cast<unsigned long long>(p->nrow) * max_batch;
     if (div_up(max_rows, kTcRows) > 65535u) return fail(CTR_ERR_UNSUPPORTED, "too many rows for one plan");
+    st = splits == 2 ? set_gemm_smem<2>() : set_gemm_smem<3>();
+    if (st) return st;
     auto* P = new ctr_ramp_tc_plan{};
     cudaGetDevice(&P->device);
     P->ns = p->ns;
     P->nrow = p->nrow;
     P->max_batch = max_batch;
+    P->splits = splits;
     P->kblocks = div_up(p->ns, kTcK);
     P->ntiles = div_up(p->ns, kTcRows);
     P->max_mtiles = div_up(max_rows, kTcRows);
-    const size_t tb = static_cast<size_t>(P->ntiles) * P->kblocks * kTcBlock;
-    const size_t xb = static_cast<size_t>(P->max_mtiles) * P->kblocks * kTcBlock;
+    const size_t tb = static_cast<size_t>(P->ntiles) * P->kblocks * block_bytes(splits);
+    const size_t xb = static_cast<size_t>(P->max_mtiles) * P->kblocks * block_bytes(splits);
     cudaError_t e = cudaMalloc(&P->T, tb);
     if (e == cudaSuccess) e = cudaMalloc(&P->X, xb);
     if (e == cudaSuccess && weighting) {
@@ -402,15 +474,12 @@ int ctr_ramp_filter_tc_create(const ctr_filter_param* p, const double* filter,
         ctr_ramp_filter_tc_destroy(P);
         return fail(CTR_ERR_CUDA, "tensor-core filter plan: %s", cudaGetErrorString(e));
     }
-    e = cudaFuncSetAttribute(ramp_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(kTcSmem));
-    if (e != cudaSuccess) {
-        ctr_ramp_filter_tc_destroy(P);
-        return fail(CTR_ERR_CUDA, "tensor-core filter smem: %s", cudaGetErrorString(e));
-    }
     const unsigned long long nch = split_chunks(P->ntiles, P->kblocks);
-    split_toeplitz<<<div_up(nch, kSplitThreads), kSplitThreads, 0, stream>>>(
-        filter, P->T, p->ns, p->ds, grad != 0, P->kblocks, nch);
+    const unsigned nb = div_up(nch, kSplitThreads);
+    if (splits == 2)
+        split_toeplitz<2><<<nb, kSplitThreads, 0, stream>>>(filter, P->T, p->ns, p->ds, grad != 0, P->kblocks, nch);
+    else
+        split_toeplitz<3><<<nb, kSplitThreads, 0, stream>>>(filter, P->T, p->ns, p->ds, grad != 0, P->kblocks, nch);
     st = check_launch("split_toeplitz");
     if (st) {
         ctr_ramp_filter_tc_destroy(P);
@@ -432,30 +501,8 @@ int ctr_ramp_filter_tc_run(ctr_ramp_tc_plan* P, int in_dtype, const void* in, fl
     if (batch > P->max_batch) return fail(CTR_ERR_INVALID_ARG, "batch %d above the plan's %d", batch, P->max_batch);
     if (static_cast<const void*>(out) == in) return fail(CTR_ERR_INVALID_ARG, "ramp filter cannot run in place");
     const unsigned long long rows = static_cast<unsigned long long>(P->nrow) * batch;
-    const unsigned mtiles = div_up(rows, kTcRows);
-    const unsigned long long nch = split_chunks(mtiles, P->kblocks);
-    const unsigned sb = div_up(nch, kSplitThreads);
-    switch (in_dtype) {
-    case CTR_DTYPE_F32:
-        split_rows<float><<<sb, kSplitThreads, 0, stream>>>(static_cast<const float*>(in), P->weight, P->X,
-                                                            P->ns, rows, P->kblocks, nch);
-        break;
-    case CTR_DTYPE_BF16:
-        split_rows<__nv_bfloat16><<<sb, kSplitThreads, 0, stream>>>(
-            static_cast<const __nv_bfloat16*>(in), P->weight, P->X, P->ns, rows, P->kblocks, nch);
-        break;
-    case CTR_DTYPE_F16:
-        split_rows<__half><<<sb, kSplitThreads, 0, stream>>>(static_cast<const __half*>(in), P->weight, P->X,
-                                                             P->ns, rows, P->kblocks, nch);
-        break;
-    default:
-        return fail(CTR_ERR_INVALID_ARG, "input dtype %d (0 f32, 1 bf16, 2 f16)", in_dtype);
-    }
-    st = check_launch("split_rows");
-    if (st) return st;
-    ramp_tc_gemm<<<dim3(P->ntiles, mtiles), kTcThreads, kTcSmem, stream>>>(P->X, P->T, out, P->ns, rows,
-                                                                          P->kblocks);
-    return check_launch("ramp_tc_gemm");
+    return P->splits == 2 ? run_splits<2>(P, in_dtype, in, out, rows, stream)
+                          : run_splits<3>(P, in_dtype, in, out, rows, stream);
 }
 
 int ctr_ramp_filter_tc_info(const ctr_ramp_tc_plan* P, unsigned long long* workspace_bytes,
@@ -463,9 +510,10 @@ int ctr_ramp_filter_tc_info(const ctr_ramp_tc_plan* P, unsigned long long* works
 {
     if (!P) return fail(CTR_ERR_INVALID_ARG, "null plan");
     if (workspace_bytes)
-        *workspace_bytes = (static_cast<unsigned long long>(P->ntiles) + P->max_mtiles) * P->kblocks * kTcBlock;
-    if (mma_flops_per_row)  // 3 products of 2 * (N tiles x 128) x (K blocks x 64) per row
-        *mma_flops_per_row = 6ull * P->ntiles * kTcRows * P->kblocks * kTcK;
+        *workspace_bytes = (static_cast<unsigned long long>(P->ntiles) + P->max_mtiles) * P->kblocks *
+                           block_bytes(P->splits);
+    if (mma_flops_per_row)  // term products of 2 * (N tiles x 128) x (K blocks x 64) per row
+        *mma_flops_per_row = (P->splits == 2 ? 3ull : 6ull) * 2ull * P->ntiles * kTcRows * P->kblocks * kTcK;
     return CTR_OK;
 }
 

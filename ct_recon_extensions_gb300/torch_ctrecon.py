@@ -146,7 +146,9 @@ class RampFilterOp:
 
 class RampFilterTCOp:
     """The ramp filter, optionally after fan weighting, as a Toeplitz GEMM on
-    the BF16 tensor cores with hi/lo split operands and FP32 accumulation.
+    the BF16 tensor cores with split operands and FP32 accumulation:
+    splits=3 (hi/mid/lo, six term products; FP32-grade) or splits=2 (hi/lo,
+    three products; ~16 bits per operand).
 
     Input: float32, bfloat16 or float16 sinograms [B,nrow,ns]; output float32.
     No reference counterpart: it is the reduced-precision form of RampFilter
@@ -157,7 +159,10 @@ class RampFilterTCOp:
     _DTYPES = {torch.float32: _lib.CTR_DTYPE_F32, torch.bfloat16: _lib.CTR_DTYPE_BF16,
                torch.float16: _lib.CTR_DTYPE_F16}
 
-    def __init__(self, ns, nrow, ds, dsd=-1.0, type=0, weighting=None):
+    def __init__(self, ns, nrow, ds, dsd=-1.0, type=0, weighting=None, splits=3):
+        if splits not in (2, 3):
+            raise ValueError("splits must be 2 (hi/lo) or 3 (hi/mid/lo)")
+        self.splits = splits
         self.ramp = RampFilterOp(ns, nrow, ds, dsd, type)
         if weighting is not None and (weighting.ns != ns or weighting.nrow != nrow):
             raise ValueError("weighting must have the filter's ns and nrow")
@@ -179,8 +184,8 @@ class RampFilterTCOp:
                 h = ctypes.c_void_p()
                 w = ctypes.byref(self.weighting.p) if self.weighting is not None else None
                 call("ctr_ramp_filter_tc_create", ctypes.byref(self.ramp.p),
-                     _ptr(self.ramp.taps(torch.device("cuda", dev))), w, int(grad), int(batch),
-                     ctypes.byref(h), _stream())
+                     _ptr(self.ramp.taps(torch.device("cuda", dev))), w, int(grad), self.splits,
+                     int(batch), ctypes.byref(h), _stream())
                 self._plans[key] = (h, batch)
         return self._plans[key][0]
 

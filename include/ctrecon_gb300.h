@@ -132,9 +132,11 @@ int ctr_ramp_filter_grad_f64(const ctr_filter_param* p, const double* in,
 /* ---- ramp filter on the BF16 tensor cores (no reference counterpart: the
  *      reduced-precision form of RampFilter<T> / RampFilterGrad<T>) ----
  * The filter as a dense Toeplitz GEMM, OUT = X * T^T with T[i][j] = ds*h[i-j]
- * (grad != 0: ds*h[j-i]).  X and T are split into BF16 hi/lo pairs and the
- * products hi*hi + hi*lo + lo*hi accumulate in FP32 (relative error near
- * 2^-16).  The input is stored as FP32, BF16 or FP16 (in_dtype); the optional
+ * (grad != 0: ds*h[j-i]).  X and T are split into `splits` BF16 terms and the
+ * term products accumulate in FP32: splits = 2 (hi, lo; hi*hi + hi*lo +
+ * lo*hi, 16 bits per operand) or 3 (hi, mid, lo; six products, 24 bits, the
+ * accuracy of the FP32 filter on smooth sinograms, whose ramp filtering
+ * cancels ~100x).  The input is stored as FP32, BF16 or FP16 (in_dtype); the optional
  * fan weighting (FanWeighting<T>, same ns) is applied to it first, in FP32.
  * The output is FP32 [batch*nrow][ns].  A plan owns the split T (built from
  * the device taps of ctr_ramp_filter_prep, on `stream`) and the split-X
@@ -144,11 +146,11 @@ int ctr_ramp_filter_grad_f64(const ctr_filter_param* p, const double* in,
 #define CTR_DTYPE_F16 2
 typedef struct ctr_ramp_tc_plan ctr_ramp_tc_plan;
 int ctr_ramp_filter_tc_create(const ctr_filter_param* p, const double* filter,
-                              const ctr_fan_weighting_param* weighting, int grad, int max_batch,
-                              ctr_ramp_tc_plan** plan, cudaStream_t stream);
+                              const ctr_fan_weighting_param* weighting, int grad, int splits,
+                              int max_batch, ctr_ramp_tc_plan** plan, cudaStream_t stream);
 int ctr_ramp_filter_tc_run(ctr_ramp_tc_plan* plan, int in_dtype, const void* in, float* out,
                            int batch, cudaStream_t stream);
-/* Device bytes the plan holds, and tensor-core FLOPs per input row (the three
+/* Device bytes the plan holds, and tensor-core FLOPs per input row (the term
  * products over the padded 128 x 64 tiles). */
 int ctr_ramp_filter_tc_info(const ctr_ramp_tc_plan* plan, unsigned long long* workspace_bytes,
                             unsigned long long* mma_flops_per_row);
