@@ -47,6 +47,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "FBP slices/s and pixel-view updates/s at rel-L2<=1e-4 vs FP64; batched vs plain"
 SM_COUNT = 152
+LEGS = ("fan", "batched", "gd", "lowp")
 FP32_LANES_PER_SM = 128
 
 
@@ -58,7 +59,14 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--pool", type=int, default=160, help="distinct slices cycled through")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args()
+    ap.add_argument("--legs", default=",".join(LEGS),
+                    help="workloads measured after the headline, reported under extra: a comma "
+                         "list of " + ", ".join(LEGS) + " (or 'none')")
+    a = ap.parse_args()
+    a.legs = set() if a.legs == "none" else set(a.legs.split(","))
+    if not a.legs <= set(LEGS):
+        ap.error(f"--legs: unknown {sorted(a.legs - set(LEGS))}")
+    return a
 
 
 # ---------------------------------------------------------------------------
@@ -806,24 +814,40 @@ def main():
     e2e = {"value": ws * args.steps / e_secs, "unit": "slices/s", "h2d_bytes_per_step": hb,
            "d2h_bytes_per_step": db}
 
-    # ---- fan FBP at its headline size (extra) ----
-    gf = fan_geometry()
-    fpipe = FanPipeline(gf, device)
-    fbase = make_pool("fan", gf, 64, 1000 + 100 * rank)
-    fpool = [torch.from_numpy(fbase[i % 16] * (1.0 + 1e-3 * i)).to(device) for i in range(64)]
-    fouts = [torch.empty((gf["ny"], gf["nx"]), dtype=torch.float32, device=device) for _ in range(4)]
-    f_secs, f_kern, f_launches = run_device(fpipe, fpool, fouts, args.steps, args.warmup, dist)
-    f_secs = dist.max(f_secs)
+    extra = {}
+    # ---- fan FBP at its headline size ----
+    if "fan" in args.legs:
+        gf = fan_geometry()
+        fpipe = FanPipeline(gf, device)
+        fbase = make_pool("fan", gf, 64, 1000 + 100 * rank)
+        fpool = [torch.from_numpy(fbase[i % 16] * (1.0 + 1e-3 * i)).to(device) for i in range(64)]
+        fouts = [torch.empty((gf["ny"], gf["nx"]), dtype=torch.float32, device=device) for _ in range(4)]
+        f_secs, f_kern, f_launches = run_device(fpipe, fpool, fouts, args.steps, args.warmup, dist)
+        f_secs = dist.max(f_secs)
+        fdom = max(f_kern, key=f_kern.get)
+        extra["fan_fbp_config1"] = {
+            "workload": "fan_weighting -> ramp(fan) -> bp_fan_2d, 720 views x 736 ch -> 512x512",
+            "slices_per_s": ws * args.steps / f_secs,
+            "updates_per_s": ws * args.steps / f_secs * fpipe.updates,
+            "kernel_ms": f_kern,
+            "dominant": fdom,
+            "dominant_tflops": fpipe.flops[fdom] / (f_kern[fdom] / 1e3) / 1e12,
+            "gpu_launches": f_launches,
+        }
 
     # ---- batched uneven fan FBP (config 3) against the plain drop-in ----
-    batched = run_batched(device, args.steps, args.warmup, dist)
+    if "batched" in args.legs:
+        extra["batched_fan_config3"] = run_batched(device, args.steps, args.warmup, dist)
 
     # ---- differentiable pair: gradient descent (config 4) ----
-    gd = run_gd(device, args.steps, args.warmup, dist)
+    if "gd" in args.legs:
+        extra["gd_config4"] = run_gd(device, args.steps, args.warmup, dist)
 
     # ---- reduced-precision large slice (config 5); its FP64 check is CPU
     #      oracle work on rank 0, part of the CPU-baseline leg ----
-    lowp = run_lowp(device, args.steps, args.warmup, dist, rank == 0 and not args.no_cpu_baseline)
+    if "lowp" in args.legs:
+        extra["lowp_config5"] = run_lowp(device, args.steps, args.warmup, dist,
+                                         rank == 0 and not args.no_cpu_baseline)
 
     # ---- roofline of the dominant kernel ----
     peak_meas = fp32_peak_tflops(device)
@@ -849,7 +873,8 @@ def main():
             v, k, c = cpu_slices_per_s("port", g, 2, os.cpu_count() or 1)
             cpu = {"value": v, "unit": "slices/s", "cores": c, "kind": k,
                    "sample": "2 slices of the same workload (fp_par_2d -> ramp -> bp_par_2d)"}
-        fdom = max(f_kern, key=f_kern.get)
+        if "fan_fbp_config1" in extra:
+            extra["fan_fbp_config1"]["dominant_frac"] = extra["fan_fbp_config1"]["dominant_tflops"] / peak
         line = {
             "metric": METRIC, "value": value, "unit": "slices/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
@@ -862,21 +887,7 @@ def main():
             "updates_per_s": value * pipe.updates,
             "gpu_launches": launches,
             "e2e": e2e, "roofline": roofline, "clocks": clocks, "cpu_baseline": cpu,
-            "extra": {
-                "fan_fbp_config1": {
-                    "workload": "fan_weighting -> ramp(fan) -> bp_fan_2d, 720 views x 736 ch -> 512x512",
-                    "slices_per_s": ws * args.steps / f_secs,
-                    "updates_per_s": ws * args.steps / f_secs * fpipe.updates,
-                    "kernel_ms": f_kern,
-                    "dominant": fdom,
-                    "dominant_tflops": fpipe.flops[fdom] / (f_kern[fdom] / 1e3) / 1e12,
-                    "dominant_frac": fpipe.flops[fdom] / (f_kern[fdom] / 1e3) / 1e12 / peak,
-                    "gpu_launches": f_launches,
-                },
-                "batched_fan_config3": batched,
-                "gd_config4": gd,
-                "lowp_config5": lowp,
-            },
+            "extra": extra,
         }
         print(json.dumps(line))
     dist.close()
