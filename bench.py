@@ -107,6 +107,12 @@ class Dist:
             self.dist.destroy_process_group()
 
 
+def replica_value(world: int, steps: int, slowest_secs: float) -> float:
+    """Whole-job throughput of N independent replicas: every rank processes
+    `steps` units; the job takes as long as its slowest rank."""
+    return world * steps / slowest_secs
+
+
 # ---------------------------------------------------------------------------
 # clocks during the timed region
 # ---------------------------------------------------------------------------
@@ -804,14 +810,14 @@ def main():
     secs, kern, launches = run_device(pipe, pool_dev, outs, args.steps, args.warmup, dist)
     clocks = clk.stop([(t_a, time.perf_counter())])
     secs = dist.max(secs)
-    value = ws * args.steps / secs
+    value = replica_value(ws, args.steps, secs)
 
     # ---- e2e through the C ABI with pinned host buffers ----
     pool_host = [t.cpu().pin_memory() for t in pool_dev[:32]]
     e_secs, hb, db = run_e2e(pipe, pool_host, args.steps, args.warmup, (g["ny"], g["nx"]),
                              (g["ny"], g["nx"]), device)
     e_secs = dist.max(e_secs)
-    e2e = {"value": ws * args.steps / e_secs, "unit": "slices/s", "h2d_bytes_per_step": hb,
+    e2e = {"value": replica_value(ws, args.steps, e_secs), "unit": "slices/s", "h2d_bytes_per_step": hb,
            "d2h_bytes_per_step": db}
 
     extra = {}
