@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(kBpThreads, 2)
         for (int j = 0; j < nv; ++j) {
             const ViewP P = views[v0 + j];
             float* aj = accw + j * c.W;
-            if (P.mode == kModeFast) {
+            if (mode_fast(P.mode)) {
                 float xs, xc;
                 fast_xs<G>(x, P.vp, c, &xs, &xc);
 #pragma unroll
@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(kBpThreads, 2)
                         atomicAdd(aj + k + 1, t * u);
                     }
                 }
-            } else {
+            } else if (P.mode == kModeEdge) {
 #pragma unroll
                 for (int r = 0; r < kRowsPerThread; ++r) {
                     if (val[r] == 0.0f) continue;

@@ -129,12 +129,19 @@ __device__ __forceinline__ bool edge_tap(float s, int ix, int iy, int ia, int lo
     return true;
 }
 
+// Tiles whose channel range lies farther than this outside [0, ns-1] project
+// entirely off the detector (FP32 corner positions are within ~3e-4 channels).
+constexpr float kSkipEps = 1e-2f;
+
 // Detector window [lo, lo+W) that covers every tap of the tile for one view;
 // *interior is set when every pixel of the tile projects at least one channel
-// inside the detector (no inclusion test needed) and the window fits.
+// inside the detector (no inclusion test needed) and the window fits; *off
+// when every pixel projects outside the detector (the view adds nothing).
+// The channel position over a convex tile is extreme at its corners (affine
+// for the parallel beam; for the fan the ray angle is).
 template <Geo G>
 __device__ int window_start(float2 vp, float x0, float x1, float y0, float y1, const TileConst& c,
-                            bool* interior)
+                            bool* interior, bool* off = nullptr)
 {
     float smin = FLT_MAX, smax = -FLT_MAX;
     bool full = false;
@@ -154,7 +161,9 @@ __device__ int window_start(float2 vp, float x0, float x1, float y0, float y1, c
         }
     }
     *interior = false;
+    if (off) *off = false;
     if (full || !(smin == smin) || !(smax == smax)) return -1;
+    if (off) *off = smax < -kSkipEps || smin > c.nsm1 + kSkipEps;
     int lo = static_cast<int>(floorf(smin)) - 2;
     int hi = static_cast<int>(floorf(smax)) + 3;
     const bool fits = hi - lo + 1 <= c.W;
@@ -296,13 +305,16 @@ constexpr unsigned kMagicBits = 0x4B000000u;
 constexpr int kGroups = 2;
 constexpr int kBlockViews = kGroups * kViewBlock;
 constexpr int kTmaThreads = kGroups * kBpThreads;
-constexpr int kModeEdge = 0, kModeFast = 2;
+constexpr int kModeEdge = 0, kModeSkip = 1, kModeFast = 2;
 
 struct ViewP {
     float2 vp;
     int lo;     // first staged channel
-    int mode;   // kModeEdge or kModeFast
+    int mode;   // kModeEdge, kModeSkip, or >= kModeFast: the interior fast path
+                // (the forward tile stores the view's shared slot base there)
 };
+
+__device__ __forceinline__ bool mode_fast(int m) { return static_cast<unsigned>(m) >= kModeFast; }
 
 __device__ __forceinline__ float2 lds_f2(unsigned addr)
 {
@@ -356,8 +368,8 @@ __device__ ViewP view_setup(const double* __restrict__ t2, int ia, float x0, flo
 {
     ViewP P;
     P.vp = view_params<G>(t2, ia, c);
-    bool inner;
-    P.lo = window_start<G>(P.vp, x0, x1, y0, y1, c, &inner);
+    bool inner, off;
+    P.lo = window_start<G>(P.vp, x0, x1, y0, y1, c, &inner, &off);
     bool fast = inner;
     if constexpr (G == Geo::kFan) {
         // polynomial atan needs d > 0 and |r/d| <= kAtanTmax on the whole tile
@@ -372,7 +384,7 @@ __device__ ViewP view_setup(const double* __restrict__ t2, int ia, float x0, flo
                 fast = fast && d > 0.0f && fabsf(r) <= kAtanTmax * d;
             }
     }
-    P.mode = fast ? kModeFast : kModeEdge;
+    P.mode = fast ? kModeFast : (off ? kModeSkip : kModeEdge);
     return P;
 }
 
@@ -454,9 +466,21 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
         }
     };
 
-    // per-view parameters, windows and paths of this tile for the whole scan
-    for (int ia = tid; ia < c.na; ia += kTmaThreads)
-        views[ia] = view_setup<G>(t2, ia, cx0, cx1, cy0, cy1, c);
+    // per-view parameters, windows and paths of this tile for the whole scan;
+    // a fast view keeps, in place of its mode, the shared address of its pair
+    // slot minus 8 * (kMagicBits + lo), so a tap's address is that plus
+    // 8 * bits(s + 2^23 - 1/2) (values below kModeFast fall back to the edge path)
+    const unsigned pairs_base = smem_u32(pairs);
+    for (int ia = tid; ia < c.na; ia += kTmaThreads) {
+        ViewP P = view_setup<G>(t2, ia, cx0, cx1, cy0, cy1, c);
+        if (mode_fast(P.mode)) {
+            const int slot = ((ia / kBV) & 1) * kBV + ia % kBV;
+            const unsigned base = pairs_base + 8u * static_cast<unsigned>(slot * c.W) -
+                                  8u * (kMagicBits + static_cast<unsigned>(P.lo));
+            P.mode = base >= static_cast<unsigned>(kModeFast) ? static_cast<int>(base) : kModeEdge;
+        }
+        views[ia] = P;
+    }
     if (tid == 0) {
         // every copy destination must be 128-byte aligned; check before issuing any
         const bool aligned = (smem_u32(raw) & 127u) == 0 && (c.WS * sizeof(float)) % 128 == 0;
@@ -481,7 +505,6 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
         y[r] = py(min(ty0 + warp * R + r, c.ny - 1));
         acc[r] = 0.0f;
     }
-    const unsigned pairs_u32 = smem_u32(pairs);
 
     const int wid = tid >> 5;  // warp of the CTA (0..15)
     for (int b = 0; b < nblocks; ++b) {
@@ -526,10 +549,9 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
         for (int j = jb; j < je; ++j) {
             const int ia = b * kBV + j;
             const ViewP P = views[ia];
-            if (P.mode == kModeFast) {
+            if (mode_fast(P.mode)) {
                 // index of s = bits(v) - kMagicBits, v = fl(s + 2^23 - 1/2)
-                const unsigned base = pairs_u32 + 8u * static_cast<unsigned>(((b & 1) * kBV + j) * c.W) -
-                                      8u * (kMagicBits + static_cast<unsigned>(P.lo));
+                const unsigned base = static_cast<unsigned>(P.mode);
                 float xs, xc;
                 fast_xs<G>(x, P.vp, c, &xs, &xc);
 #pragma unroll
@@ -542,7 +564,7 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
                     if constexpr (G == Geo::kFan) part[r] = fmaf(fmaf(u, pv.y, pv.x), w, part[r]);
                     else part[r] = fmaf(u, pv.y, part[r] + pv.x);
                 }
-            } else {
+            } else if (P.mode == kModeEdge) {
                 const float2* wj = pb + j * c.W;
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
