@@ -316,29 +316,42 @@ int launch_tile(K kern, int W, dim3 grid, cudaStream_t stream, const char* what,
 }
 
 
-// Forward dispatch: the bulk-copy kernel when its window fits 256 elements and
-// the sinogram is 16-byte aligned, the cooperative kernel otherwise.
+// Rows per thread of the bulk-copy forward kernel (tile 32 x 8*kFwdRows) and
+// its resident CTAs per SM (sets the register budget).
+constexpr int kFwdRows = 8;
+constexpr int kFwdMinBlocks = 1;
+constexpr int kFwdTileY = (kBpThreads / 32) * kFwdRows;
+
+// Forward dispatch: the bulk-copy kernel (tile 32 x kFwdTileY, window w_tall)
+// when its window fits 256 elements and the sinogram is 16-byte aligned, the
+// cooperative kernel (tile 32 x kTileY, window c.W) otherwise.
 template <Geo G>
 int launch_forward(const float* proj, float* img, const double* t0, const double* t1,
-                   const double* t2, TileConst c, int batch, cudaStream_t stream, const char* what)
+                   const double* t2, TileConst c, int w_tall, int batch, cudaStream_t stream,
+                   const char* what)
 {
-    dim3 grid(div_up(c.nx, kTileX), div_up(c.ny, kTileY), batch);
-    c.W = std::max(c.W, 16);
-    c.WB = (c.W + 4 + 3) / 4 * 4;
-    c.WS = (c.WB + 31) / 32 * 32;
+    TileConst ct = c;
+    // the final group reduction reuses one half of the pair buffer (kBlockViews x W
+    // float2) for kFwdRows x kBpThreads floats: W >= 4 * kFwdRows
+    ct.W = std::max({w_tall, 16, kFwdRows * kBpThreads / (2 * kBlockViews)});
+    ct.WB = (ct.W + 4 + 3) / 4 * 4;
+    ct.WS = (ct.WB + 31) / 32 * 32;
     const unsigned long long total = static_cast<unsigned long long>(c.proj_stride) * batch;
-    c.total4 = static_cast<long long>(total & ~3ull);
-    if (c.WB <= 256 && reinterpret_cast<uintptr_t>(proj) % 16 == 0 && total < (1ull << 31) &&
+    ct.total4 = static_cast<long long>(total & ~3ull);
+    if (ct.WB <= 256 && reinterpret_cast<uintptr_t>(proj) % 16 == 0 && total < (1ull << 31) &&
         c.na <= 4096) {
-        const size_t smem = 128 + 2 * kBlockViews * c.WS * sizeof(float) +
-                            2 * kBlockViews * c.W * sizeof(float2) + c.na * sizeof(ViewP);
-        cudaError_t e = cudaFuncSetAttribute(bp_tile_tma_f32<G>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+        const size_t smem = 128 + 2 * kBlockViews * ct.WS * sizeof(float) +
+                            2 * kBlockViews * ct.W * sizeof(float2) + c.na * sizeof(ViewP);
+        auto kern = bp_tile_tma_f32<G, kFwdRows, kFwdMinBlocks>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              static_cast<int>(smem));
         if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
-        bp_tile_tma_f32<G><<<grid, kTmaThreads, smem, stream>>>(proj, img, t0, t1, t2, c);
+        dim3 grid(div_up(c.nx, kTileX), div_up(c.ny, kFwdTileY), batch);
+        kern<<<grid, kTmaThreads, smem, stream>>>(proj, img, t0, t1, t2, ct);
         return check_launch(what);
     }
+    c.W = std::max(c.W, 16);
+    dim3 grid(div_up(c.nx, kTileX), div_up(c.ny, kTileY), batch);
     return launch_tile(bp_tile_f32_coop<G>, c.W, grid, stream, what, proj, img, t0, t1, t2, c, false);
 }
 
@@ -388,7 +401,9 @@ int fan_forward(const FanArgs& a, const T* proj, T* img, const double* xpos, con
     if (st) return st;
     if constexpr (sizeof(T) == 4) {
         TileConst c = fan_const(a, scaled ? a.scale : 1.0);
-        return launch_forward<Geo::kFan>(proj, img, xpos, ypos, sc, c, batch, stream, "bp_fan_2d");
+        const int w_tall = fan_window(a.ns, a.ds, a.dso, a.dsd, a.nx, a.ny, a.dx, a.dy, a.offset_x,
+                                      a.offset_y, kFwdTileY);
+        return launch_forward<Geo::kFan>(proj, img, xpos, ypos, sc, c, w_tall, batch, stream, "bp_fan_2d");
     } else {
         const double cents = (a.ns - 1) / 2.0 + a.offset_s;
         dim3 grid(div_up(static_cast<size_t>(a.nx) * a.ny, 128), batch);
@@ -494,7 +509,9 @@ int par_forward(const ctr_par_param* p, const T* proj, T* img, const double* xco
     if (st) return st;
     if constexpr (sizeof(T) == 4) {
         TileConst c = par_const(p);
-        return launch_forward<Geo::kPar>(proj, img, xcos, ysin, nullptr, c, batch, stream, "bp_par_2d");
+        const int w_tall = par_window(p->ns, p->ds, p->dx, p->dy, kFwdTileY);
+        return launch_forward<Geo::kPar>(proj, img, xcos, ysin, nullptr, c, w_tall, batch, stream,
+                                         "bp_par_2d");
     } else {
         const double cents = (p->ns - 1) / 2.0 + p->offset_s;
         dim3 grid(div_up(static_cast<size_t>(p->nx) * p->ny, 128), batch);

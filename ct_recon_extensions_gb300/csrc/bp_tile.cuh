@@ -484,8 +484,12 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
     if (tid == 0) {
         // every copy destination must be 128-byte aligned; check before issuing any
         const bool aligned = (smem_u32(raw) & 127u) == 0 && (c.WS * sizeof(float)) % 128 == 0;
-        s_ok = aligned;
+        // the group reduction at the end writes R x kBpThreads floats into one
+        // half of the pair buffer (kBV x W float2)
+        const bool fits = R * kBpThreads <= 2 * kBV * c.W;
+        s_ok = aligned && fits;
         if (!aligned) raise_flag(kFlagMisaligned);
+        if (!fits) raise_flag(kFlagWindowOverflow);
         mbar_init(smem_u32(&s_bar[0]), 1);
         mbar_init(smem_u32(&s_bar[1]), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -606,13 +610,13 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
     return true;
 }
 
-template <Geo G>
-__global__ void __launch_bounds__(kTmaThreads, 2)
+template <Geo G, int R, int MinBlocks>
+__global__ void __launch_bounds__(kTmaThreads, MinBlocks)
     bp_tile_tma_f32(const float* __restrict__ proj, float* __restrict__ img,
                     const double* __restrict__ t0, const double* __restrict__ t1,
                     const double* __restrict__ t2, const TileConst c)
 {
-    tile_forward<G>(proj, img, t0, t1, t2, c, blockIdx.x, blockIdx.y, blockIdx.z);
+    tile_forward<G, R>(proj, img, t0, t1, t2, c, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // ---- host: window bounds --------------------------------------------------
