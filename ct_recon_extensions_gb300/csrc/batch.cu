@@ -10,7 +10,7 @@
 // atomic counter, so items of very different sizes balance across the SMs.
 // The tile body is the single-geometry FP32 backprojector's (bp_tile.cuh).
 //
-// Autotuning (CTR_PLAN_AUTOTUNE): the tile shape (32 x 32 or 32 x 16 pixels)
+// Autotuning (CTR_PLAN_AUTOTUNE): the tile shape (32 x 64, 32 x 32 or 32 x 16 pixels)
 // and the view-block depth (8 or 16 views per group) are chosen by timing each
 // candidate on the plan's own batch once, at plan creation.
 #include <algorithm>
@@ -34,8 +34,9 @@ struct ItemDev {
     int tiles_x;
 };
 
+// 8 rows per thread take one CTA per SM (up to 128 registers), fewer rows two.
 template <int R, int VB>
-__global__ void __launch_bounds__(kTmaThreads, 2)
+__global__ void __launch_bounds__(kTmaThreads, R >= 8 ? 1 : 2)
     bp_fan_batch_f32(const ItemDev* __restrict__ items, const int2* __restrict__ work, int n_work,
                      int* __restrict__ counter)
 {
@@ -64,7 +65,7 @@ __global__ void __launch_bounds__(kTmaThreads, 2)
 struct Config {
     int R, VB;
 };
-constexpr Config kConfigs[] = {{4, 16}, {2, 16}, {4, 8}, {2, 8}};
+constexpr Config kConfigs[] = {{4, 16}, {2, 16}, {4, 8}, {2, 8}, {8, 16}, {8, 8}};
 constexpr int kNumConfigs = sizeof(kConfigs) / sizeof(kConfigs[0]);
 
 template <int R, int VB>
@@ -79,7 +80,9 @@ void* kernel_of(int ci)
     case 0: return batch_kernel<4, 16>();
     case 1: return batch_kernel<2, 16>();
     case 2: return batch_kernel<4, 8>();
-    default: return batch_kernel<2, 8>();
+    case 3: return batch_kernel<2, 8>();
+    case 4: return batch_kernel<8, 16>();
+    default: return batch_kernel<8, 8>();
     }
 }
 
@@ -135,7 +138,7 @@ struct ctr_fbp_plan {
     int n_fblocks = 0;
     unsigned max_ns = 0;
     ctr::ConfigData cfg[ctr::kNumConfigs];
-    int chosen = 0;
+    int chosen = 4;  // without autotuning: 32 x 64 tiles, 16 views per group
     double tuned_ms = 0.0;
     bool autotuned = false;
     ctr::DevArray<int> counter;
