@@ -15,9 +15,15 @@ workload through the C ABI with the slice copied from pinned host memory and
 the reconstruction read back every step; ``roofline`` is the dominant
 kernel's algorithmic FP32 FLOP/s (per-launch CUDA-event durations inside the
 timed region) against the FP32 peak; ``cpu_baseline`` times the oracle port
-(the reference's CPU algorithm restated in C) on this host's cores.  The fan
-FBP at its headline size (fan weighting -> ramp(fan) -> bp_fan_2d, 720 x 736
--> 512x512) is measured the same way and reported under ``extra``.
+(the reference's CPU algorithm restated in C) on this host's cores.
+
+``extra`` (``--legs`` selects): ``fan_fbp_config1`` the fan FBP at its
+headline size (fan weighting -> ramp(fan) -> bp_fan_2d, 720 x 736 -> 512x512);
+``batched_fan_config3`` 64 uneven fan sinograms through one batched plan
+against 64 plain calls; ``gd_config4`` gradient descent through the
+differentiable forward projector (batch 16); ``lowp_config5`` the 2048^2
+fan slice from FP32, BF16 and FP16 sinograms (tensor-core filter), with its
+error against the FP64 oracle on image strips when the CPU-baseline leg runs.
 
 ``--impl reference`` times the reference's CPU implementation of the same
 workload on this host (the compiled reference when its build is present,
