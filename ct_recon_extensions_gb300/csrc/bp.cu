@@ -342,11 +342,46 @@ int launch_forward(const float* proj, float* img, const double* t0, const double
         c.na <= 4096) {
         const size_t smem = 128 + 2 * kBlockViews * ct.WS * sizeof(float) +
                             2 * kBlockViews * ct.W * sizeof(float2) + c.na * sizeof(ViewP);
+        const int tiles_x = static_cast<int>(div_up(c.nx, kTileX));
+        const int tiles_y = static_cast<int>(div_up(c.ny, kFwdTileY));
+        const long long tiles = static_cast<long long>(tiles_x) * tiles_y * batch;
+        const int nb = static_cast<int>(div_up(c.na, kBlockViews));
+        int dev = 0, sms = kSmCount;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (tiles < 4ll * sms && nb > 1) {
+            // fewer than 4 waves of whole tiles: stream-K over (tile, view block) units
+            SkConst k{};
+            k.units = tiles * nb;
+            k.nb = nb;
+            k.tiles_x = tiles_x;
+            k.tiles_per_item = tiles_x * tiles_y;
+            const int ctas = static_cast<int>(std::min<long long>(k.units, sms));
+            k.maxseg = sk_max_segments(tiles, nb, ctas);
+            const size_t part_bytes = static_cast<size_t>(tiles) * k.maxseg * kTileX * kFwdTileY * sizeof(float);
+            void* scratch = nullptr;
+            if (cudaMallocAsync(&scratch, part_bytes + sizeof(int) * tiles, stream) == cudaSuccess) {
+                k.partial = static_cast<float*>(scratch);
+                k.counter = reinterpret_cast<int*>(static_cast<char*>(scratch) + part_bytes);
+                auto kern = bp_tile_tma_sk<G, kFwdRows>;
+                cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     static_cast<int>(smem));
+                if (e == cudaSuccess) e = cudaMemsetAsync(k.counter, 0, sizeof(int) * tiles, stream);
+                if (e == cudaSuccess) {
+                    kern<<<ctas, kTmaThreads, smem, stream>>>(proj, img, t0, t1, t2, ct, k);
+                    e = cudaGetLastError();
+                }
+                cudaFreeAsync(scratch, stream);
+                if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+                return CTR_OK;
+            }
+            cudaGetLastError();  // no scratch: whole tiles per CTA below
+        }
         auto kern = bp_tile_tma_f32<G, kFwdRows, kFwdMinBlocks>;
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              static_cast<int>(smem));
         if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
-        dim3 grid(div_up(c.nx, kTileX), div_up(c.ny, kFwdTileY), batch);
+        dim3 grid(tiles_x, tiles_y, batch);
         kern<<<grid, kTmaThreads, smem, stream>>>(proj, img, t0, t1, t2, ct);
         return check_launch(what);
     }

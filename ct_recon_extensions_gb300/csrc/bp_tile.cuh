@@ -10,6 +10,7 @@
 
 #include "ctr_async.cuh"
 #include "ctr_common.cuh"
+#include "sk_split.h"
 
 namespace ctr {
 namespace {
@@ -388,7 +389,10 @@ __device__ ViewP view_setup(const double* __restrict__ t2, int ia, float x0, flo
     return P;
 }
 
-// One tile (tile_x, tile_y) of item `item`; all 512 threads of the CTA call it.
+// One tile (tile_x, tile_y) of item `item`, over its view blocks
+// [b_begin, b_end) (b_end < 0: all); all 512 threads of the CTA call it.
+// With `partial` null the scaled sums are stored to the image; otherwise the
+// unscaled sums of this range go to partial[row * kTileX + column] of the tile.
 // Re-entrant across calls of a persistent CTA: the mbarriers are
 // (re)initialised here and every copy issued is waited on before returning.
 // Returns false (uniformly) when a check or a bounded wait failed.
@@ -397,7 +401,8 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
                                              const double* __restrict__ t0,
                                              const double* __restrict__ t1,
                                              const double* __restrict__ t2, const TileConst& c,
-                                             int tile_x, int tile_y, int item)
+                                             int tile_x, int tile_y, int item, int b_begin = 0,
+                                             int b_end = -1, float* __restrict__ partial = nullptr)
 {
     constexpr int kTY = (kBpThreads / 32) * R;  // tile height
     constexpr int kBV = kGroups * VB;           // views per staged block
@@ -417,7 +422,8 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
     const int lt = tid - group * kBpThreads;
     const int lane = lt & 31, warp = lt >> 5;
     const int tx0 = tile_x * kTileX, ty0 = tile_y * kTY;
-    const int nblocks = (c.na + kBV - 1) / kBV;
+    const int nblocks = b_end < 0 ? (c.na + kBV - 1) / kBV : b_end;
+    // double-buffer slots and barrier phases count from b_begin
 
     auto px = [&](int ix) -> float {
         if constexpr (G == Geo::kFan) return static_cast<float>(t0[ix]);
@@ -444,8 +450,9 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
         if (b >= nblocks) return;
         const int v0 = b * kBV;
         const int nv = min(kBV, c.na - v0);
-        const unsigned bar = smem_u32(&s_bar[b & 1]);
-        float* slot = raw + (b & 1) * kBV * c.WS;
+        const int lb = b - b_begin;
+        const unsigned bar = smem_u32(&s_bar[lb & 1]);
+        float* slot = raw + (lb & 1) * kBV * c.WS;
         unsigned bytes = 0;
         for (int j = lane; j < nv; j += 32) {
             const long long gx = slot_start(v0 + j) & ~3ll;
@@ -471,10 +478,11 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
     // slot minus 8 * (kMagicBits + lo), so a tap's address is that plus
     // 8 * bits(s + 2^23 - 1/2) (values below kModeFast fall back to the edge path)
     const unsigned pairs_base = smem_u32(pairs);
-    for (int ia = tid; ia < c.na; ia += kTmaThreads) {
+    const int ia_end = min(nblocks * kBV, c.na);
+    for (int ia = b_begin * kBV + tid; ia < ia_end; ia += kTmaThreads) {
         ViewP P = view_setup<G>(t2, ia, cx0, cx1, cy0, cy1, c);
         if (mode_fast(P.mode)) {
-            const int slot = ((ia / kBV) & 1) * kBV + ia % kBV;
+            const int slot = ((ia / kBV - b_begin) & 1) * kBV + ia % kBV;
             const unsigned base = pairs_base + 8u * static_cast<unsigned>(slot * c.W) -
                                   8u * (kMagicBits + static_cast<unsigned>(P.lo));
             P.mode = base >= static_cast<unsigned>(kModeFast) ? static_cast<int>(base) : kModeEdge;
@@ -497,8 +505,8 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
     __syncthreads();
     if (!s_ok) return false;
     if (tid < 32) {
-        issue_block(0);
-        issue_block(1);
+        issue_block(b_begin);
+        issue_block(b_begin + 1);
     }
 
     const int ixc = min(tx0 + lane, c.nx - 1);
@@ -511,14 +519,15 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
     }
 
     const int wid = tid >> 5;  // warp of the CTA (0..15)
-    for (int b = 0; b < nblocks; ++b) {
+    for (int b = b_begin; b < nblocks; ++b) {
+        const int lb = b - b_begin;
         // every thread waits for block b's copies (bounded); a timeout is
         // reported and the block proceeds, so no thread is left at a barrier
-        if (!mbar_wait_bounded(smem_u32(&s_bar[b & 1]), (b >> 1) & 1) && tid == 0)
+        if (!mbar_wait_bounded(smem_u32(&s_bar[lb & 1]), (lb >> 1) & 1) && tid == 0)
             raise_flag(kFlagWaitTimeout);
         const int nv = min(kBV, c.na - b * kBV);
-        const float* slot = raw + (b & 1) * kBV * c.WS;
-        float2* pb = pairs + (b & 1) * kBV * c.W;
+        const float* slot = raw + (lb & 1) * kBV * c.WS;
+        float2* pb = pairs + (lb & 1) * kBV * c.W;
         // one warp per view: rewrite the raw window as (p[i], p[i+1] - p[i]) pairs
         for (int j = wid; j < nv; j += kTmaThreads / 32) {
             const long long st = slot_start(b * kBV + j);
@@ -589,22 +598,28 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
         for (int r = 0; r < R; ++r) acc[r] += part[r];
     }
     // add the second group's sums to the first's, in that order; the reduction
-    // uses the pairs buffer of block nblocks-2, which every thread has finished
-    // reading before the last block's barrier
-    float* red = reinterpret_cast<float*>(pairs + (nblocks & 1) * kBV * c.W);
+    // uses the pairs buffer of the next-to-last block, which every thread has
+    // finished reading before the last block's barrier (or one never used)
+    float* red = reinterpret_cast<float*>(pairs + ((nblocks - b_begin) & 1) * kBV * c.W);
     if (group == 1) {
 #pragma unroll
         for (int r = 0; r < R; ++r) red[r * kBpThreads + lt] = acc[r];
     }
     __syncthreads();
     if (group == 0) {
-        float* I = img + static_cast<size_t>(item) * c.img_stride;
-        const int ix = tx0 + lane;
+        if (partial) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const int iy = ty0 + warp * R + r;
-            if (ix < c.nx && iy < c.ny)
-                I[static_cast<size_t>(iy) * c.nx + ix] = (acc[r] + red[r * kBpThreads + lt]) * c.scale;
+            for (int r = 0; r < R; ++r)
+                partial[(warp * R + r) * kTileX + lane] = acc[r] + red[r * kBpThreads + lt];
+        } else {
+            float* I = img + static_cast<size_t>(item) * c.img_stride;
+            const int ix = tx0 + lane;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int iy = ty0 + warp * R + r;
+                if (ix < c.nx && iy < c.ny)
+                    I[static_cast<size_t>(iy) * c.nx + ix] = (acc[r] + red[r * kBpThreads + lt]) * c.scale;
+            }
         }
     }
     return true;
@@ -617,6 +632,70 @@ __global__ void __launch_bounds__(kTmaThreads, MinBlocks)
                     const double* __restrict__ t2, const TileConst c)
 {
     tile_forward<G, R>(proj, img, t0, t1, t2, c, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// ---- stream-K split of small launches ----------------------------------------
+//
+// A launch with few tiles (a 512^2 image is 128 tiles of 32 x 64) leaves SMs
+// idle when each CTA owns whole tiles.  Here the work is cut into units of
+// (tile, block of kBlockViews views), tiles outer, and CTA c of G takes the
+// contiguous units [c*U/G, (c+1)*U/G): every SM gets the same number of view
+// blocks.  A tile whose units span several CTAs gets one unscaled partial sum
+// per CTA (segment) in `partial`; each CTA counts its segment in on the
+// tile's counter, and the CTA that completes the count adds the segments in
+// segment order, scales and stores the tile (deterministic).
+struct SkConst {
+    long long units;       // tiles x nb
+    int nb;                // view blocks per tile
+    int tiles_x, tiles_per_item;
+    int maxseg;            // segments per tile, at most
+    float* partial;        // [tiles][maxseg][kTileX x tile height]
+    int* counter;          // [tiles], zero at launch
+};
+
+template <Geo G, int R>
+__global__ void __launch_bounds__(kTmaThreads, 1)
+    bp_tile_tma_sk(const float* __restrict__ proj, float* __restrict__ img,
+                   const double* __restrict__ t0, const double* __restrict__ t1,
+                   const double* __restrict__ t2, const TileConst c, const SkConst k)
+{
+    constexpr int kTY = (kBpThreads / 32) * R;
+    constexpr int kTilePix = kTileX * kTY;
+    __shared__ int s_last;
+    const int ctas = static_cast<int>(gridDim.x);
+    const long long U = k.units;
+    const long long u0 = sk_unit_begin(blockIdx.x, ctas, U);
+    const long long u1 = sk_unit_begin(blockIdx.x + 1, ctas, U);
+    for (long long t = u0 / k.nb; t * k.nb < u1; ++t) {
+        const long long tu = t * k.nb;
+        const int b0 = static_cast<int>((u0 > tu ? u0 : tu) - tu);
+        const int b1 = static_cast<int>((u1 < tu + k.nb ? u1 : tu + k.nb) - tu);
+        const int item = static_cast<int>(t / k.tiles_per_item);
+        const int tl = static_cast<int>(t % k.tiles_per_item);
+        const int tx = tl % k.tiles_x, ty = tl / k.tiles_x;
+        const int first = sk_cta_of(tu, ctas, U), last = sk_cta_of(tu + k.nb - 1, ctas, U);
+        if (first == last) {  // the whole tile is this CTA's
+            if (!tile_forward<G, R>(proj, img, t0, t1, t2, c, tx, ty, item)) return;
+            continue;
+        }
+        float* seg = k.partial + (static_cast<size_t>(t) * k.maxseg + (blockIdx.x - first)) * kTilePix;
+        if (!tile_forward<G, R>(proj, img, t0, t1, t2, c, tx, ty, item, b0, b1, seg)) return;
+        __threadfence();  // this segment is visible before it is counted
+        __syncthreads();
+        if (threadIdx.x == 0) s_last = atomicAdd(k.counter + t, 1) == last - first;
+        __syncthreads();
+        if (s_last) {
+            __threadfence();
+            const float* base = k.partial + static_cast<size_t>(t) * k.maxseg * kTilePix;
+            float* I = img + static_cast<size_t>(item) * c.img_stride;
+            for (int idx = threadIdx.x; idx < kTilePix; idx += kTmaThreads) {
+                const int ix = tx * kTileX + idx % kTileX, iy = ty * kTY + idx / kTileX;
+                float v = __ldcg(base + idx);
+                for (int sg = 1; sg <= last - first; ++sg) v += __ldcg(base + sg * kTilePix + idx);
+                if (ix < c.nx && iy < c.ny) I[static_cast<size_t>(iy) * c.nx + ix] = v * c.scale;
+            }
+        }
+    }
 }
 
 // ---- host: window bounds --------------------------------------------------
