@@ -339,9 +339,15 @@ class LowpFanPipeline:
                                           ctypes.c_void_p(out.data_ptr()), *self.bpt, 1, s)
 
 
+# per-kernel CUDA events are recorded on every KERNEL_EVERY-th timed step only,
+# so that their own cost stays out of the step time
+KERNEL_EVERY = 8
+
+
 def run_device(pipe, pool_dev, outs, steps, warmup, dist, per_kernel=True):
     """Time `steps` pipeline steps on device-resident inputs; returns (seconds,
-    per-kernel mean ms, launches)."""
+    per-kernel mean ms, launches).  Per-kernel times come from CUDA events
+    around each launch of every KERNEL_EVERY-th step of the timed region."""
     import torch
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
@@ -360,15 +366,16 @@ def run_device(pipe, pool_dev, outs, steps, warmup, dist, per_kernel=True):
     for k in range(warmup):
         step(k, None)
     torch.cuda.synchronize()
-    ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in pipe.names] for _ in range(steps)] if per_kernel else None
+    sampled = [k for k in range(steps) if k % KERNEL_EVERY == 0] if per_kernel else []
+    ev = {k: [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in pipe.names] for k in sampled}
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     dist.barrier()
     torch.cuda.synchronize()
     t0.record(stream)
     for k in range(steps):
-        step(warmup + k, ev[k] if per_kernel else None)
+        step(warmup + k, ev.get(k))
     t1.record(stream)
     torch.cuda.synchronize()
     dist.barrier()
@@ -376,7 +383,7 @@ def run_device(pipe, pool_dev, outs, steps, warmup, dist, per_kernel=True):
     kern = {}
     if per_kernel:
         for i, n in enumerate(pipe.names):
-            kern[n] = statistics.fmean(ev[k][i][0].elapsed_time(ev[k][i][1]) for k in range(steps))
+            kern[n] = statistics.fmean(ev[k][i][0].elapsed_time(ev[k][i][1]) for k in sampled)
     return secs, kern, sum(pipe.kernels.values()) * steps
 
 
@@ -645,31 +652,31 @@ def bf16_peak_tflops():
 
 
 def run_e2e(pipe, pool_host, steps, warmup, in_shape, out_shape, device):
-    """Through the C ABI with host buffers: per step H2D of the input from
-    pinned memory, the three operators, D2H of the result, stream sync."""
+    """Through the C ABI with host buffers: every step copies its input slice
+    from pinned host memory to the device, runs the pipeline's operators and
+    copies the result back to pinned host memory.  The library's HostStreamer
+    overlaps the copies of neighbouring steps with the compute (2 device
+    buffer pairs, separate copy-in / compute / copy-out streams).  Timed on
+    the host from the first step's copy to the last result on the host."""
     import torch
-    stream = torch.cuda.current_stream()
-    din = torch.empty(in_shape, dtype=torch.float32, device=device)
-    dout = torch.empty(out_shape, dtype=torch.float32, device=device)
-    hout = torch.empty(out_shape, dtype=torch.float32, pin_memory=True)
-    P = len(pool_host)
+    from ct_recon_extensions_gb300.host_stream import HostStreamer
 
-    def step(k):
-        din.copy_(pool_host[k % P], non_blocking=True)
-        for fn in pipe.launches(din, dout, stream.cuda_stream):
+    def step(din, dout, s):
+        for fn in pipe.launches(din, dout, s):
             if fn() != 0:
                 raise RuntimeError(pipe.lib.ctr_last_error().decode())
-        hout.copy_(dout, non_blocking=True)
-        stream.synchronize()
 
-    for k in range(warmup):
-        step(k)
+    hs = HostStreamer(step, in_shape, out_shape, device, depth=2)
+    P = len(pool_host)
+    hout = [torch.empty(out_shape, dtype=torch.float32, pin_memory=True) for _ in range(4)]
+    hs.run([pool_host[k % P] for k in range(warmup)], [hout[k % 4] for k in range(warmup)])
     torch.cuda.synchronize()
+    ins = [pool_host[(warmup + k) % P] for k in range(steps)]
+    outs = [hout[k % 4] for k in range(steps)]
     t = time.perf_counter()
-    for k in range(steps):
-        step(warmup + k)
+    hs.run(ins, outs)
     secs = time.perf_counter() - t
-    return secs, din.numel() * 4, dout.numel() * 4
+    return secs, hs.din[0].numel() * 4, hs.dout[0].numel() * 4
 
 
 def fp32_peak_tflops(device):
