@@ -573,15 +573,22 @@ __global__ void __launch_bounds__(kFpxThreads, 2)
 // caller's grad-prep table (one conversion per tile line and view); the
 // footprint and triangle weights are those of src/fp_par_2d.cc:339-383:
 // channels within |offset| of the pixel's position mid, weight 1 - |mid - is| /
-// |offset|.  Where |offset| <= 1 (every view when dx, dy <= ds) a pixel-view
-// touches at most the channels floor(mid) and floor(mid) + 1, whose weights
-// follow from the fraction with two FMAs, so the gather is two loads and four
-// FMAs.  A border pixel's footprint is one-sided; its end channel is decided
-// from the fixed-point fraction, or, when mid lies within kFaTie units of a
-// channel, in FP64 exactly as the reference does (the general loop, which
-// also takes the wider footprints).
+// |offset|.
+//
+// Interior pixels of views with |offset| <= 1 (every view when dx, dy <= ds)
+// touch at most channels floor(mid) and floor(mid) + 1, whose weights follow
+// from the fraction with two FMAs (saturated: both are at most 1, and the
+// clamp at 0 is the footprint's edge).  fp_adj_f32 stages, per block of views, the
+// channel window of its 32 x 32 tile as zero-padded (p[i], p[i+1]) pairs in
+// shared memory, so such a pixel-view is one 8-byte shared load and a few
+// FMAs; positions advance by 64-bit adds.  It computes every pixel that way.
+// Pixels on the image border have one-sided footprints (channels on the
+// neighbour's side only); fp_adj_border_f32 then recomputes those 4n - 4
+// pixels exactly (one warp each) and overwrites them.  Views with |offset| > 1 or a window
+// wider than the staged one take the exact per-pixel path in both kernels.
 constexpr int kFaViews = 16;
 constexpr int kFaRows = 4;  // pixels per thread (one column), 32x32 tile
+constexpr int kFaWin = 96;  // staged channel pairs per view
 // Units of 2^-32 channel within which a border pixel's position counts as on a
 // channel: the fixed-point position is within 0.5 + 0.5*along units of the
 // reference's FP64 one (along < 8192).
@@ -593,6 +600,72 @@ __device__ __forceinline__ long long fix32_any(double v)
     return ((double_bits(v) >> 52) & 0x7FF) < 1043 ? fix32(v) : llrint(v * kTwo32);
 }
 
+// The reference grad's tap sum for one pixel-view: MID = the pixel's position
+// (fixed point), O1 = the view's offset, `along` = the pixel's index along its
+// line, pp = the caller's (begin, offset) of the pixel's line.  A border pixel's
+// footprint is one-sided (toward the neighbour pixel); its end channel is
+// decided from the fixed-point fraction or, when mid lies within kFaTie units
+// of a channel, in FP64 exactly as the reference does.
+__device__ __forceinline__ float adj_tap_exact(const float* __restrict__ row, long long MID, long long O1,
+                                               float inv, bool two, int along, int n, int ns,
+                                               const double* __restrict__ pp)
+{
+    const int mi = static_cast<int>(MID >> 32);
+    const float mf = frac_of(MID);
+    const bool border = along == 0 || along == n - 1;
+    const unsigned frac_bits = static_cast<unsigned>(MID);
+    const bool tie = border && (n == 1 || frac_bits < kFaTie || frac_bits > 0u - kFaTie);
+    if (two && !tie) {
+        float w0 = fmaxf(fmaf(-mf, inv, 1.0f), 0.0f);
+        float w1 = fmaxf(fmaf(mf, inv, 1.0f - inv), 0.0f);
+        if (border) {
+            const bool ge = (along == 0) != (O1 < 0);  // footprint [mid, mid + |o|]
+            if (ge) w0 = 0.0f;
+            else w1 = 0.0f;
+        }
+        const float p0 = static_cast<unsigned>(mi) < static_cast<unsigned>(ns) ? __ldg(row + mi) : 0.0f;
+        const float p1 = static_cast<unsigned>(mi + 1) < static_cast<unsigned>(ns) ? __ldg(row + mi + 1) : 0.0f;
+        return fmaf(w0, p0, w1 * p1);
+    }
+    long long L = along == 0 ? MID : MID - O1;
+    long long R = along == n - 1 ? MID : MID + O1;
+    if (L > R) {
+        const long long t = L;
+        L = R;
+        R = t;
+    }
+    int lo = max(static_cast<int>((L + 0xFFFFFFFFll) >> 32), 0);
+    int hi = min(static_cast<int>(R >> 32), ns - 1);
+    if (border) {
+        // the end channel sits at the pixel itself with weight ~1: the range
+        // is decided in FP64 as the reference does (mid = begin + offset*along)
+        const double off = pp[1];
+        const double mid = __dadd_rn(pp[0], __dmul_rn(off, static_cast<double>(along)));
+        double left = along == 0 ? mid : __dsub_rn(mid, off);
+        double right = along == n - 1 ? mid : __dadd_rn(mid, off);
+        if (left > right) {
+            const double t = left;
+            left = right;
+            right = t;
+        }
+        lo = static_cast<int>(fmax(ceil(left), 0.0));
+        hi = static_cast<int>(fmin(floor(right), static_cast<double>(ns - 1)));
+    }
+    float part = 0.0f;
+    for (int is = lo; is <= hi; ++is) {
+        const float d = fabsf(mf - static_cast<float>(is - mi));
+        part = fmaf(fmaf(-d, inv, 1.0f), __ldg(row + is), part);
+    }
+    return part;
+}
+
+__device__ __forceinline__ float2 lds_pair(unsigned addr)
+{
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
+    return v;
+}
+
 __global__ void __launch_bounds__(256)
     fp_adj_f32(const float* __restrict__ proj, float* __restrict__ img,
                const double* __restrict__ weights, const double* __restrict__ pos,
@@ -601,7 +674,8 @@ __global__ void __launch_bounds__(256)
     __shared__ long long s_base[kFaViews][32];
     __shared__ long long s_o1[kFaViews];
     __shared__ float s_w[kFaViews], s_inv[kFaViews];
-    __shared__ int s_ux[kFaViews], s_two[kFaViews];
+    __shared__ int s_ux[kFaViews], s_two[kFaViews], s_lo[kFaViews], s_staged[kFaViews];
+    __shared__ __align__(16) float2 s_pair[kFaViews][kFaWin];
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tx0 = blockIdx.x * 32, ty0 = blockIdx.y * 32;
@@ -611,25 +685,54 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int r = 0; r < kFaRows; ++r) acc[r] = 0.0f;
     const int n = c.nx;  // == ny
-    const unsigned ns = static_cast<unsigned>(c.ns);
+    const int ns = c.ns;
 
     for (int v0 = 0; v0 < c.na; v0 += kFaViews) {
         const int nv = min(kFaViews, c.na - v0);
+        // per view: line positions, offset, weight; warp j/2 lanes = lines
         for (int idx = threadIdx.x; idx < nv * 32; idx += 256) {
             const int j = idx >> 5, l = idx & 31;
             const int ia = v0 + j;
             const int ux = usex[ia] != 0;
             const int lin = min((ux ? ty0 : tx0) + l, n - 1);
             const double* pp = pos + (static_cast<size_t>(ia) * n + lin) * 2;
-            s_base[j][l] = fix32_any(pp[0]);
+            const long long B = fix32_any(pp[0]);
+            const long long O1 = fix32_any(pp[1]);
+            s_base[j][l] = B;
+            // the tile's channel range: for a fixed line the position is linear
+            // in `along`, extreme at the tile's first and last along index
+            const int a0 = ux ? tx0 : ty0;
+            const long long m0 = B + static_cast<long long>(a0) * O1;
+            const long long m1 = m0 + 31ll * O1;
+            int lo = static_cast<int>((m0 < m1 ? m0 : m1) >> 32);
+            int hi = static_cast<int>((m0 < m1 ? m1 : m0) >> 32);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+                hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+            }
             if (l == 0) {
                 const float o1 = fabsf(dbl2flt(pp[1]));
-                s_o1[j] = fix32_any(pp[1]);
+                s_o1[j] = O1;
                 s_w[j] = dbl2flt(weights[ia]);
                 s_inv[j] = 1.0f / o1;
                 s_ux[j] = ux;
                 s_two[j] = o1 <= 1.0f;
+                // pairs k = 0..hi-lo+1 hold channels lo+k, lo+k+1
+                s_lo[j] = lo;
+                s_staged[j] = o1 <= 1.0f && hi - lo + 2 <= kFaWin;
             }
+        }
+        __syncthreads();
+        // staged windows: (p[lo+k], p[lo+k+1]), zero off the detector
+        for (int idx = threadIdx.x; idx < nv * kFaWin; idx += 256) {
+            const int j = idx / kFaWin, k = idx - j * kFaWin;
+            if (!s_staged[j]) continue;
+            const float* row = P + static_cast<size_t>(v0 + j) * ns;
+            const int g = s_lo[j] + k;
+            const float p0 = static_cast<unsigned>(g) < static_cast<unsigned>(ns) ? __ldg(row + g) : 0.0f;
+            const float p1 = static_cast<unsigned>(g + 1) < static_cast<unsigned>(ns) ? __ldg(row + g + 1) : 0.0f;
+            s_pair[j][k] = make_float2(p0, p1);
         }
         __syncthreads();
         float blk[kFaRows];  // this view block's partial sums (blocked summation)
@@ -639,69 +742,45 @@ __global__ void __launch_bounds__(256)
             const int ux = s_ux[j];
             const long long O1 = s_o1[j];
             const float inv = s_inv[j], w = s_w[j];
-            const bool two = s_two[j] != 0;
-            const float* row = P + static_cast<size_t>(v0 + j) * c.ns;
+            if (s_staged[j]) {
+                const float inv1 = 1.0f - inv;
+                const unsigned pb = smem_u32(&s_pair[j][0]) - 8u * static_cast<unsigned>(s_lo[j]);
+                if (ux) {  // along = ix, line = row
+                    const long long A = static_cast<long long>(ix) * O1;
 #pragma unroll
-            for (int r = 0; r < kFaRows; ++r) {
-                const int iy = ty0 + warp * kFaRows + r;
-                const int along = ux ? ix : iy;
-                const long long MID = s_base[j][ux ? warp * kFaRows + r : lane] +
-                                      static_cast<long long>(along) * O1;
-                const int mi = static_cast<int>(MID >> 32);
-                const float mf = frac_of(MID);
-                const bool border = along == 0 || along == n - 1;
-                // a border pixel's footprint is one-sided (toward the neighbour
-                // pixel): channels >= mid or <= mid; settled in fixed point unless
-                // mid is within kFaTie units of a channel (then FP64, as the reference)
-                const unsigned frac_bits = static_cast<unsigned>(MID);
-                const bool tie = border && (n == 1 || frac_bits < kFaTie || frac_bits > 0u - kFaTie);
-                float part;
-                if (two && !tie) {
-                    float w0 = fmaxf(fmaf(-mf, inv, 1.0f), 0.0f);
-                    float w1 = fmaxf(fmaf(mf, inv, 1.0f - inv), 0.0f);
-                    if (border) {
-                        const bool ge = (along == 0) != (O1 < 0);  // footprint [mid, mid + |o|]
-                        if (ge) w0 = 0.0f;
-                        else w1 = 0.0f;
+                    for (int r = 0; r < kFaRows; ++r) {
+                        const long long MID = s_base[j][warp * kFaRows + r] + A;
+                        const float mf = frac_of(MID);
+                        const float2 pv = lds_pair(pb + 8u * static_cast<unsigned>(MID >> 32));
+                        const float w0 = __saturatef(fmaf(-mf, inv, 1.0f));
+                        const float w1 = __saturatef(fmaf(mf, inv, inv1));
+                        blk[r] = fmaf(fmaf(w0, pv.x, w1 * pv.y), w, blk[r]);
                     }
-                    const float p0 = static_cast<unsigned>(mi) < ns ? __ldg(row + mi) : 0.0f;
-                    const float p1 = static_cast<unsigned>(mi + 1) < ns ? __ldg(row + mi + 1) : 0.0f;
-                    part = fmaf(w0, p0, w1 * p1);
-                } else {
-                    long long L = along == 0 ? MID : MID - O1;
-                    long long R = along == n - 1 ? MID : MID + O1;
-                    if (L > R) {
-                        const long long t = L;
-                        L = R;
-                        R = t;
-                    }
-                    int lo = max(static_cast<int>((L + 0xFFFFFFFFll) >> 32), 0);
-                    int hi = min(static_cast<int>(R >> 32), c.ns - 1);
-                    if (border) {
-                        // One-sided footprint of a border pixel: its end channel sits at
-                        // the pixel itself with weight ~1, so the range is decided in
-                        // FP64 exactly as the reference does (mid = begin + offset*along).
-                        const int lin = ux ? iy : ix;
-                        const double* pp = pos + (static_cast<size_t>(v0 + j) * n + min(lin, n - 1)) * 2;
-                        const double off = pp[1];
-                        const double mid = __dadd_rn(pp[0], __dmul_rn(off, static_cast<double>(along)));
-                        double left = along == 0 ? mid : __dsub_rn(mid, off);
-                        double right = along == n - 1 ? mid : __dadd_rn(mid, off);
-                        if (left > right) {
-                            const double t = left;
-                            left = right;
-                            right = t;
-                        }
-                        lo = static_cast<int>(fmax(ceil(left), 0.0));
-                        hi = static_cast<int>(fmin(floor(right), static_cast<double>(c.ns - 1)));
-                    }
-                    part = 0.0f;
-                    for (int is = lo; is <= hi; ++is) {
-                        const float d = fabsf(mf - static_cast<float>(is - mi));
-                        part = fmaf(fmaf(-d, inv, 1.0f), __ldg(row + is), part);
+                } else {   // along = row, line = ix
+                    long long MID = s_base[j][lane] + static_cast<long long>(ty0 + warp * kFaRows) * O1;
+#pragma unroll
+                    for (int r = 0; r < kFaRows; ++r) {
+                        const float mf = frac_of(MID);
+                        const float2 pv = lds_pair(pb + 8u * static_cast<unsigned>(MID >> 32));
+                        const float w0 = __saturatef(fmaf(-mf, inv, 1.0f));
+                        const float w1 = __saturatef(fmaf(mf, inv, inv1));
+                        blk[r] = fmaf(fmaf(w0, pv.x, w1 * pv.y), w, blk[r]);
+                        MID += O1;
                     }
                 }
-                blk[r] = fmaf(part, w, blk[r]);
+            } else {
+                const float* row = P + static_cast<size_t>(v0 + j) * ns;
+                const bool two = s_two[j] != 0;
+#pragma unroll
+                for (int r = 0; r < kFaRows; ++r) {
+                    const int iy = ty0 + warp * kFaRows + r;
+                    const int along = ux ? ix : iy;
+                    const int lin = ux ? iy : ix;
+                    const long long MID = s_base[j][ux ? warp * kFaRows + r : lane] +
+                                          static_cast<long long>(along) * O1;
+                    const double* pp = pos + (static_cast<size_t>(v0 + j) * n + min(lin, n - 1)) * 2;
+                    blk[r] = fmaf(adj_tap_exact(row, MID, O1, inv, two, along, n, ns, pp), w, blk[r]);
+                }
             }
         }
 #pragma unroll
@@ -714,6 +793,50 @@ __global__ void __launch_bounds__(256)
         const int iy = ty0 + warp * kFaRows + r;
         if (ix < c.nx && iy < c.ny) O[static_cast<size_t>(iy) * c.nx + ix] = acc[r];
     }
+}
+
+// The 4n - 4 border pixels, exactly, overwriting fp_adj_f32's values: one
+// warp per pixel, lane l summing views l, l+32, ..., then a fixed shuffle tree.
+__global__ void __launch_bounds__(128)
+    fp_adj_border_f32(const float* __restrict__ proj, float* __restrict__ img,
+                      const double* __restrict__ weights, const double* __restrict__ pos,
+                      const int* __restrict__ usex, const FpConst c)
+{
+    const int n = c.nx, ns = c.ns;
+    const int nb = n == 1 ? 1 : 4 * n - 4;
+    const int lane = threadIdx.x & 31;
+    const int b = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (b >= nb) return;  // warp-uniform
+    int ix, iy;
+    if (b < n) {
+        ix = b;
+        iy = 0;
+    } else if (b < 2 * n) {
+        ix = b - n;
+        iy = n - 1;
+    } else if (b < 3 * n - 2) {
+        ix = 0;
+        iy = b - 2 * n + 1;
+    } else {
+        ix = n - 1;
+        iy = b - 3 * n + 3;
+    }
+    const float* P = proj + blockIdx.y * c.proj_stride;
+    float acc = 0.0f;
+    for (int ia = lane; ia < c.na; ia += 32) {
+        const int ux = usex[ia] != 0;
+        const int along = ux ? ix : iy, lin = ux ? iy : ix;
+        const double* pp = pos + (static_cast<size_t>(ia) * n + lin) * 2;
+        const long long O1 = fix32_any(pp[1]);
+        const long long MID = fix32_any(pp[0]) + static_cast<long long>(along) * O1;
+        const float o1 = fabsf(dbl2flt(pp[1]));
+        const float part = adj_tap_exact(P + static_cast<size_t>(ia) * ns, MID, O1, 1.0f / o1,
+                                         o1 <= 1.0f, along, n, ns, pp);
+        acc = fmaf(part, dbl2flt(weights[ia]), acc);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) img[blockIdx.y * c.img_stride + static_cast<size_t>(iy) * n + ix] = acc;
 }
 
 constexpr int kFp64Threads = 128;
@@ -960,6 +1083,8 @@ int fp_adjoint(const ctr_par_param* p, const T* proj, T* img, const double* w,
         FpConst c = fp_const(p);
         dim3 grid(div_up(p->nx, 32), div_up(p->ny, 32), batch);
         fp_adj_f32<<<grid, 256, 0, stream>>>(proj, img, w, pos, usex, c);
+        const unsigned nborder = p->nx == 1 ? 1u : 4u * p->nx - 4u;
+        fp_adj_border_f32<<<dim3(div_up(nborder, 4), batch), 128, 0, stream>>>(proj, img, w, pos, usex, c);
     } else {
         dim3 grid(div_up(p->nx, 32), div_up(p->ny, 8), batch);
         fp_adj_kernel<T><<<grid, dim3(32, 8), 0, stream>>>(proj, img, w, pos, usex, p->ns, p->na,
