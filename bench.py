@@ -756,6 +756,78 @@ def cpu_slices_per_s(kind, g, n_slices, threads):
     return n_slices / secs, "port", threads
 
 
+def cpu_configs(threads):
+    """The oracle port (the reference's CPU algorithm restated in C, T=float)
+    on a bounded sample of each configuration, with all host threads (rows
+    split across threads) and, for configs 1 and 2, one thread.  Config 3
+    times its first items and is scaled by pixel-view updates; config 5 runs
+    weighting and filter in full and backprojects one 16-row strip, scaled to
+    the 2048 rows."""
+    from oracle import Geom, Oracle
+    from ct_recon_extensions_gb300 import synthetic as syn
+
+    def geom(g, ny=None, off_y=None):
+        return Geom.make(g["ns"], g["na"], g["ds"], g["orbit"], g["nx"], g["ny"] if ny is None else ny,
+                         g["dx"], g["dy"], g["offset_s"], g["orbit_start"], g["offset_x"],
+                         g["offset_y"] if off_y is None else off_y, g.get("dso", -1.0), g.get("dsd", -1.0),
+                         g["fov"])
+
+    def timed(fn):
+        t = time.perf_counter()
+        fn()
+        return time.perf_counter() - t
+
+    res = {}
+    g1 = syn.fan_config_1()
+    s1 = syn.fan_sinogram(syn.random_ellipses(1000), g1["na"], g1["ns"], g1["ds"], g1["orbit"], g1["dso"],
+                          g1["dsd"])
+    c1 = {}
+    for nt in (threads, 1):
+        orc = Oracle("port", threads=nt)
+        c1[f"slices_per_s_{nt}t"] = 1.0 / timed(lambda: orc.fbp_fan(s1, geom(g1)))
+    res["fan_fbp_config1"] = dict(c1, sample="1 slice")
+    g2 = par_geometry()
+    c2 = {}
+    for nt in (threads, 1):
+        v, _, _ = cpu_slices_per_s("port", g2, 1, nt)
+        c2[f"slices_per_s_{nt}t"] = v
+    res["parallel_config2"] = dict(c2, sample="1 slice")
+    items = syn.batched_config_3()
+    upd_all = sum(it["nx"] * it["ny"] * it["na"] for it in items) / len(items)
+    orc = Oracle("port", threads=threads)
+    done, upd, secs = 0, 0.0, 0.0
+    while upd < 4e8 and done < len(items):
+        it = items[done]
+        sino = syn.fan_sinogram(syn.random_ellipses(it["seed"]), it["na"], it["ns"], it["ds"], it["orbit"],
+                                it["dso"], it["dsd"])
+        secs += timed(lambda: orc.fbp_fan(sino, geom(it)))
+        upd += it["nx"] * it["ny"] * it["na"]
+        done += 1
+    res["batched_fan_config3"] = {f"slices_per_s_{threads}t": upd / secs / upd_all,
+                                  "sample": f"first {done} of {len(items)} items, scaled by updates"}
+    img = syn.rasterize(syn.random_ellipses(4000), g2["nx"], g2["ny"], g2["dx"], g2["dy"])
+    G2 = geom(g2)
+    sec4 = timed(lambda: orc.fp_par_2d_grad(orc.fp_par_2d(img, G2), G2))
+    res["gd_config4"] = {f"images_per_s_{threads}t": 1.0 / sec4,
+                         "sample": "1 image: fp_par_2d and its adjoint"}
+    g5 = syn.large_config_5()
+    s5 = syn.fan_sinogram(syn.random_ellipses(5000), g5["na"], g5["ns"], g5["ds"], g5["orbit"], g5["dso"],
+                          g5["dsd"])
+    out = {}
+
+    def filt():
+        w = orc.fan_weighting(s5, g5["ds"], g5["offset_s"], g5["dso"], g5["dsd"], 1)
+        out["f"] = orc.ramp_filter(w, g5["ds"], g5["dsd"], 1)
+    secf = timed(filt)
+    k, r0 = 16, 1000
+    gs = geom(g5, ny=k, off_y=(g5["ny"] - 1) / 2 + g5["offset_y"] - r0 - (k - 1) / 2)
+    secb = timed(lambda: orc.bp_fan_2d(out["f"], gs)) * g5["ny"] / k
+    res["lowp_config5"] = {f"slices_per_s_{threads}t": 1.0 / (secf + secb),
+                           "sample": "weighting + filter in full, one 16-row strip of the backprojection "
+                                     "scaled to 2048 rows (FP32 storage)"}
+    return res
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -894,6 +966,21 @@ def main():
                    "sample": "2 slices of the same workload (fp_par_2d -> ramp -> bp_par_2d)"}
         if "fan_fbp_config1" in extra:
             extra["fan_fbp_config1"]["dominant_frac"] = extra["fan_fbp_config1"]["dominant_tflops"] / peak
+        if not args.no_cpu_baseline:
+            # the reference's CPU algorithm beside each configuration
+            nt = os.cpu_count() or 1
+            cc = cpu_configs(nt)
+            gpu = {"fan_fbp_config1": ("slices_per_s", f"slices_per_s_{nt}t"),
+                   "batched_fan_config3": ("slices_per_s", f"slices_per_s_{nt}t"),
+                   "gd_config4": ("images_per_s", f"images_per_s_{nt}t")}
+            for leg, (gk, ck) in gpu.items():
+                if leg in extra:
+                    cc[leg]["gpu_over_cpu"] = extra[leg][gk] / cc[leg][ck]
+            if "lowp_config5" in extra:
+                cc["lowp_config5"]["gpu_over_cpu"] = (extra["lowp_config5"]["paths"]["bf16"]["slices_per_s"] /
+                                                      cc["lowp_config5"][f"slices_per_s_{nt}t"])
+            cc["parallel_config2"]["gpu_over_cpu"] = value / cc["parallel_config2"][f"slices_per_s_{nt}t"]
+            extra["cpu_oracle_port"] = dict(cc, threads=nt, kind="port")
         line = {
             "metric": METRIC, "value": value, "unit": "slices/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
