@@ -578,8 +578,9 @@ __global__ void __launch_bounds__(kFpxThreads, 2)
 // Interior pixels of views with |offset| <= 1 (every view when dx, dy <= ds)
 // touch at most channels floor(mid) and floor(mid) + 1, whose weights follow
 // from the fraction with two FMAs (saturated: both are at most 1, and the
-// clamp at 0 is the footprint's edge).  fp_adj_f32 stages, per block of views, the
-// channel window of its 32 x 32 tile as zero-padded (p[i], p[i+1]) pairs in
+// clamp at 0 is the footprint's edge).  fp_adj_prep converts the caller's
+// positions to 32.32 fixed point once per call; fp_adj_f32 stages, per block
+// of views, the channel window of its 32 x 64 tile as zero-padded (p[i], p[i+1]) pairs in
 // shared memory, so such a pixel-view is one 8-byte shared load and a few
 // FMAs; positions advance by 64-bit adds.  It computes every pixel that way.
 // Pixels on the image border have one-sided footprints (channels on the
@@ -587,8 +588,10 @@ __global__ void __launch_bounds__(kFpxThreads, 2)
 // pixels exactly (one warp each) and overwrites them.  Views with |offset| > 1 or a window
 // wider than the staged one take the exact per-pixel path in both kernels.
 constexpr int kFaViews = 16;
-constexpr int kFaRows = 4;  // pixels per thread (one column), 32x32 tile
-constexpr int kFaWin = 96;  // staged channel pairs per view
+constexpr int kFaRows = 8;                 // pixels per thread (one column)
+constexpr int kFaTileX = 32, kFaTileY = 8 * kFaRows;  // 32 x 64 tile, 256 threads
+constexpr int kFaLines = kFaTileY;         // lines of a tile: rows (64) or columns (32)
+constexpr int kFaWin = 128;                // staged channel pairs per view
 // Units of 2^-32 channel within which a border pixel's position counts as on a
 // channel: the fixed-point position is within 0.5 + 0.5*along units of the
 // reference's FP64 one (along < 8192).
@@ -666,19 +669,51 @@ __device__ __forceinline__ float2 lds_pair(unsigned addr)
     return v;
 }
 
+// Per-view constants of the adjoint, from the caller's grad-prep tables.
+struct AdjView {
+    long long O1;  // offset, 32.32 fixed point
+    float inv;     // 1 / |offset|
+    float w;       // view weight
+    int ux;        // lines are rows
+    int two;       // |offset| <= 1
+};
+
+// One pass over the grad-prep tables per call: the 32.32 fixed-point begin of
+// every (view, line) and the per-view constants, so the gather's CTAs (and
+// batch items) load them instead of converting the FP64 values themselves.
 __global__ void __launch_bounds__(256)
-    fp_adj_f32(const float* __restrict__ proj, float* __restrict__ img,
-               const double* __restrict__ weights, const double* __restrict__ pos,
-               const int* __restrict__ usex, const FpConst c)
+    fp_adj_prep(const double* __restrict__ weights, const double* __restrict__ pos,
+                const int* __restrict__ usex, long long* __restrict__ B, AdjView* __restrict__ V,
+                int na, int n)
 {
-    __shared__ long long s_base[kFaViews][32];
-    __shared__ long long s_o1[kFaViews];
-    __shared__ float s_w[kFaViews], s_inv[kFaViews];
-    __shared__ int s_ux[kFaViews], s_two[kFaViews], s_lo[kFaViews], s_staged[kFaViews];
+    const long long i = static_cast<long long>(blockIdx.x) * 256 + threadIdx.x;
+    if (i >= static_cast<long long>(na) * n) return;
+    const double* pp = pos + i * 2;
+    B[i] = fix32_any(pp[0]);
+    if (i % n == 0) {
+        const int ia = static_cast<int>(i / n);
+        const float o1 = fabsf(dbl2flt(pp[1]));
+        AdjView v;
+        v.O1 = fix32_any(pp[1]);
+        v.inv = 1.0f / o1;
+        v.w = dbl2flt(weights[ia]);
+        v.ux = usex[ia] != 0;
+        v.two = o1 <= 1.0f;
+        V[ia] = v;
+    }
+}
+
+__global__ void __launch_bounds__(256)
+    fp_adj_f32(const float* __restrict__ proj, float* __restrict__ img, const long long* __restrict__ B,
+               const AdjView* __restrict__ V, const double* __restrict__ pos, const FpConst c)
+{
+    __shared__ long long s_base[kFaViews][kFaLines];
+    __shared__ AdjView s_v[kFaViews];
+    __shared__ int s_lo[kFaViews], s_hi[kFaViews];
     __shared__ __align__(16) float2 s_pair[kFaViews][kFaWin];
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int tx0 = blockIdx.x * 32, ty0 = blockIdx.y * 32;
+    const int tx0 = blockIdx.x * kFaTileX, ty0 = blockIdx.y * kFaTileY;
     const int ix = tx0 + lane;
     const float* P = proj + blockIdx.z * c.proj_stride;
     float acc[kFaRows];
@@ -689,97 +724,99 @@ __global__ void __launch_bounds__(256)
 
     for (int v0 = 0; v0 < c.na; v0 += kFaViews) {
         const int nv = min(kFaViews, c.na - v0);
-        // per view: line positions, offset, weight; warp j/2 lanes = lines
-        for (int idx = threadIdx.x; idx < nv * 32; idx += 256) {
-            const int j = idx >> 5, l = idx & 31;
-            const int ia = v0 + j;
-            const int ux = usex[ia] != 0;
-            const int lin = min((ux ? ty0 : tx0) + l, n - 1);
-            const double* pp = pos + (static_cast<size_t>(ia) * n + lin) * 2;
-            const long long B = fix32_any(pp[0]);
-            const long long O1 = fix32_any(pp[1]);
-            s_base[j][l] = B;
-            // the tile's channel range: for a fixed line the position is linear
-            // in `along`, extreme at the tile's first and last along index
-            const int a0 = ux ? tx0 : ty0;
-            const long long m0 = B + static_cast<long long>(a0) * O1;
-            const long long m1 = m0 + 31ll * O1;
-            int lo = static_cast<int>((m0 < m1 ? m0 : m1) >> 32);
-            int hi = static_cast<int>((m0 < m1 ? m1 : m0) >> 32);
+        if (threadIdx.x < nv) {
+            s_v[threadIdx.x] = V[v0 + threadIdx.x];
+            s_lo[threadIdx.x] = INT_MAX;
+            s_hi[threadIdx.x] = INT_MIN;
+        }
+        __syncthreads();
+        // line positions of the tile (rows for row-marching views, else
+        // columns) and the tile's channel range: for a fixed line the position
+        // is linear in `along`, extreme at the tile's first and last along index
+        for (int idx = threadIdx.x; idx < nv * kFaLines; idx += 256) {
+            const int j = idx / kFaLines, l = idx - j * kFaLines;
+            const AdjView& v = s_v[j];
+            const int nl = v.ux ? kFaTileY : kFaTileX;
+            int lo = INT_MAX, hi = INT_MIN;
+            if (l < nl) {
+                const int lin = min((v.ux ? ty0 : tx0) + l, n - 1);
+                const long long b = __ldg(B + static_cast<size_t>(v0 + j) * n + lin);
+                s_base[j][l] = b;
+                const long long m0 = b + static_cast<long long>(v.ux ? tx0 : ty0) * v.O1;
+                const long long m1 = m0 + static_cast<long long>((v.ux ? kFaTileX : kFaTileY) - 1) * v.O1;
+                lo = static_cast<int>((m0 < m1 ? m0 : m1) >> 32);
+                hi = static_cast<int>((m0 < m1 ? m1 : m0) >> 32);
+            }
+            // kFaLines is a multiple of 32: a warp's lanes share one view
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
                 hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
             }
-            if (l == 0) {
-                const float o1 = fabsf(dbl2flt(pp[1]));
-                s_o1[j] = O1;
-                s_w[j] = dbl2flt(weights[ia]);
-                s_inv[j] = 1.0f / o1;
-                s_ux[j] = ux;
-                s_two[j] = o1 <= 1.0f;
-                // pairs k = 0..hi-lo+1 hold channels lo+k, lo+k+1
-                s_lo[j] = lo;
-                s_staged[j] = o1 <= 1.0f && hi - lo + 2 <= kFaWin;
+            if ((idx & 31) == 0 && lo <= hi) {
+                atomicMin(&s_lo[j], lo);
+                atomicMax(&s_hi[j], hi);
             }
         }
         __syncthreads();
         // staged windows: (p[lo+k], p[lo+k+1]), zero off the detector
-        for (int idx = threadIdx.x; idx < nv * kFaWin; idx += 256) {
-            const int j = idx / kFaWin, k = idx - j * kFaWin;
-            if (!s_staged[j]) continue;
+        for (int j = 0; j < nv; ++j) {
+            const bool staged = s_v[j].two && s_hi[j] - s_lo[j] + 2 <= kFaWin;
+            if (!staged) continue;  // uniform
             const float* row = P + static_cast<size_t>(v0 + j) * ns;
-            const int g = s_lo[j] + k;
-            const float p0 = static_cast<unsigned>(g) < static_cast<unsigned>(ns) ? __ldg(row + g) : 0.0f;
-            const float p1 = static_cast<unsigned>(g + 1) < static_cast<unsigned>(ns) ? __ldg(row + g + 1) : 0.0f;
-            s_pair[j][k] = make_float2(p0, p1);
+            const int lo = s_lo[j];
+            for (int k = threadIdx.x; k < kFaWin; k += 256) {
+                const int g = lo + k;
+                const float p0 = static_cast<unsigned>(g) < static_cast<unsigned>(ns) ? __ldg(row + g) : 0.0f;
+                const float p1 = static_cast<unsigned>(g + 1) < static_cast<unsigned>(ns) ? __ldg(row + g + 1) : 0.0f;
+                s_pair[j][k] = make_float2(p0, p1);
+            }
         }
         __syncthreads();
         float blk[kFaRows];  // this view block's partial sums (blocked summation)
 #pragma unroll
         for (int r = 0; r < kFaRows; ++r) blk[r] = 0.0f;
         for (int j = 0; j < nv; ++j) {
-            const int ux = s_ux[j];
-            const long long O1 = s_o1[j];
-            const float inv = s_inv[j], w = s_w[j];
-            if (s_staged[j]) {
-                const float inv1 = 1.0f - inv;
-                const unsigned pb = smem_u32(&s_pair[j][0]) - 8u * static_cast<unsigned>(s_lo[j]);
-                if (ux) {  // along = ix, line = row
-                    const long long A = static_cast<long long>(ix) * O1;
+            const AdjView v = s_v[j];
+            const int lo = s_lo[j];
+            if (v.two && s_hi[j] - lo + 2 <= kFaWin) {
+                const float inv1 = 1.0f - v.inv;
+                const unsigned pb = smem_u32(&s_pair[j][0]) - 8u * static_cast<unsigned>(lo);
+                if (v.ux) {  // along = ix, line = row
+                    const long long A = static_cast<long long>(ix) * v.O1;
 #pragma unroll
                     for (int r = 0; r < kFaRows; ++r) {
                         const long long MID = s_base[j][warp * kFaRows + r] + A;
                         const float mf = frac_of(MID);
                         const float2 pv = lds_pair(pb + 8u * static_cast<unsigned>(MID >> 32));
-                        const float w0 = __saturatef(fmaf(-mf, inv, 1.0f));
-                        const float w1 = __saturatef(fmaf(mf, inv, inv1));
-                        blk[r] = fmaf(fmaf(w0, pv.x, w1 * pv.y), w, blk[r]);
+                        const float w0 = __saturatef(fmaf(-mf, v.inv, 1.0f));
+                        const float w1 = __saturatef(fmaf(mf, v.inv, inv1));
+                        blk[r] = fmaf(fmaf(w0, pv.x, w1 * pv.y), v.w, blk[r]);
                     }
                 } else {   // along = row, line = ix
-                    long long MID = s_base[j][lane] + static_cast<long long>(ty0 + warp * kFaRows) * O1;
+                    long long MID = s_base[j][lane] + static_cast<long long>(ty0 + warp * kFaRows) * v.O1;
 #pragma unroll
                     for (int r = 0; r < kFaRows; ++r) {
                         const float mf = frac_of(MID);
                         const float2 pv = lds_pair(pb + 8u * static_cast<unsigned>(MID >> 32));
-                        const float w0 = __saturatef(fmaf(-mf, inv, 1.0f));
-                        const float w1 = __saturatef(fmaf(mf, inv, inv1));
-                        blk[r] = fmaf(fmaf(w0, pv.x, w1 * pv.y), w, blk[r]);
-                        MID += O1;
+                        const float w0 = __saturatef(fmaf(-mf, v.inv, 1.0f));
+                        const float w1 = __saturatef(fmaf(mf, v.inv, inv1));
+                        blk[r] = fmaf(fmaf(w0, pv.x, w1 * pv.y), v.w, blk[r]);
+                        MID += v.O1;
                     }
                 }
             } else {
                 const float* row = P + static_cast<size_t>(v0 + j) * ns;
-                const bool two = s_two[j] != 0;
 #pragma unroll
                 for (int r = 0; r < kFaRows; ++r) {
                     const int iy = ty0 + warp * kFaRows + r;
-                    const int along = ux ? ix : iy;
-                    const int lin = ux ? iy : ix;
-                    const long long MID = s_base[j][ux ? warp * kFaRows + r : lane] +
-                                          static_cast<long long>(along) * O1;
+                    const int along = v.ux ? ix : iy;
+                    const int lin = v.ux ? iy : ix;
+                    const long long MID = s_base[j][v.ux ? warp * kFaRows + r : lane] +
+                                          static_cast<long long>(along) * v.O1;
                     const double* pp = pos + (static_cast<size_t>(v0 + j) * n + min(lin, n - 1)) * 2;
-                    blk[r] = fmaf(adj_tap_exact(row, MID, O1, inv, two, along, n, ns, pp), w, blk[r]);
+                    blk[r] = fmaf(adj_tap_exact(row, MID, v.O1, v.inv, v.two != 0, along, n, ns, pp), v.w,
+                                  blk[r]);
                 }
             }
         }
@@ -1081,8 +1118,18 @@ int fp_adjoint(const ctr_par_param* p, const T* proj, T* img, const double* w,
     if (st) return st;
     if constexpr (sizeof(T) == 4) {
         FpConst c = fp_const(p);
-        dim3 grid(div_up(p->nx, 32), div_up(p->ny, 32), batch);
-        fp_adj_f32<<<grid, 256, 0, stream>>>(proj, img, w, pos, usex, c);
+        // fixed-point tables of the call (int64 per (view, line), AdjView per view)
+        const size_t nb = sizeof(long long) * p->na * static_cast<size_t>(p->nx);
+        void* scratch = nullptr;
+        cudaError_t e = cudaMallocAsync(&scratch, nb + sizeof(AdjView) * p->na, stream);
+        if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp_par_2d_grad scratch: %s", cudaGetErrorString(e));
+        long long* B = static_cast<long long*>(scratch);
+        AdjView* V = reinterpret_cast<AdjView*>(static_cast<char*>(scratch) + nb);
+        fp_adj_prep<<<div_up(static_cast<unsigned long long>(p->na) * p->nx, 256), 256, 0, stream>>>(
+            w, pos, usex, B, V, p->na, p->nx);
+        dim3 grid(div_up(p->nx, kFaTileX), div_up(p->ny, kFaTileY), batch);
+        fp_adj_f32<<<grid, 256, 0, stream>>>(proj, img, B, V, pos, c);
+        cudaFreeAsync(scratch, stream);
         const unsigned nborder = p->nx == 1 ? 1u : 4u * p->nx - 4u;
         fp_adj_border_f32<<<dim3(div_up(nborder, 4), batch), 128, 0, stream>>>(proj, img, w, pos, usex, c);
     } else {
