@@ -703,7 +703,7 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
     fp_adj_f32(const float* __restrict__ proj, float* __restrict__ img, const long long* __restrict__ B,
                const AdjView* __restrict__ V, const double* __restrict__ pos, const FpConst c)
 {
@@ -732,41 +732,44 @@ __global__ void __launch_bounds__(256)
         __syncthreads();
         // line positions of the tile (rows for row-marching views, else
         // columns) and the tile's channel range: for a fixed line the position
-        // is linear in `along`, extreme at the tile's first and last along index
-        for (int idx = threadIdx.x; idx < nv * kFaLines; idx += 256) {
-            const int j = idx / kFaLines, l = idx - j * kFaLines;
-            const AdjView& v = s_v[j];
-            const int nl = v.ux ? kFaTileY : kFaTileX;
+        // is linear in `along`, extreme at the tile's first and last along index.
+        // Fixed trip count: every load of the block is in flight at once.
+#pragma unroll
+        for (int it = 0; it < kFaViews * kFaLines / 256; ++it) {
+            const int idx = it * 256 + threadIdx.x;
+            const int j = idx / kFaLines, l = idx - j * kFaLines;  // a warp's lanes share j
             int lo = INT_MAX, hi = INT_MIN;
-            if (l < nl) {
-                const int lin = min((v.ux ? ty0 : tx0) + l, n - 1);
-                const long long b = __ldg(B + static_cast<size_t>(v0 + j) * n + lin);
-                s_base[j][l] = b;
-                const long long m0 = b + static_cast<long long>(v.ux ? tx0 : ty0) * v.O1;
-                const long long m1 = m0 + static_cast<long long>((v.ux ? kFaTileX : kFaTileY) - 1) * v.O1;
-                lo = static_cast<int>((m0 < m1 ? m0 : m1) >> 32);
-                hi = static_cast<int>((m0 < m1 ? m1 : m0) >> 32);
+            if (j < nv) {
+                const AdjView& v = s_v[j];
+                if (l < (v.ux ? kFaTileY : kFaTileX)) {
+                    const int lin = min((v.ux ? ty0 : tx0) + l, n - 1);
+                    const long long b = __ldg(B + static_cast<size_t>(v0 + j) * n + lin);
+                    s_base[j][l] = b;
+                    const long long m0 = b + static_cast<long long>(v.ux ? tx0 : ty0) * v.O1;
+                    const long long m1 = m0 + static_cast<long long>((v.ux ? kFaTileX : kFaTileY) - 1) * v.O1;
+                    lo = static_cast<int>((m0 < m1 ? m0 : m1) >> 32);
+                    hi = static_cast<int>((m0 < m1 ? m1 : m0) >> 32);
+                }
             }
-            // kFaLines is a multiple of 32: a warp's lanes share one view
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
                 hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
             }
-            if ((idx & 31) == 0 && lo <= hi) {
+            if ((threadIdx.x & 31) == 0 && lo <= hi) {
                 atomicMin(&s_lo[j], lo);
                 atomicMax(&s_hi[j], hi);
             }
         }
         __syncthreads();
         // staged windows: (p[lo+k], p[lo+k+1]), zero off the detector
-        for (int j = 0; j < nv; ++j) {
-            const bool staged = s_v[j].two && s_hi[j] - s_lo[j] + 2 <= kFaWin;
-            if (!staged) continue;  // uniform
-            const float* row = P + static_cast<size_t>(v0 + j) * ns;
-            const int lo = s_lo[j];
-            for (int k = threadIdx.x; k < kFaWin; k += 256) {
-                const int g = lo + k;
+#pragma unroll
+        for (int it = 0; it < kFaViews * kFaWin / 256; ++it) {
+            const int idx = it * 256 + threadIdx.x;
+            const int j = idx / kFaWin, k = idx - j * kFaWin;
+            if (j < nv && s_v[j].two && s_hi[j] - s_lo[j] + 2 <= kFaWin) {
+                const float* row = P + static_cast<size_t>(v0 + j) * ns;
+                const int g = s_lo[j] + k;
                 const float p0 = static_cast<unsigned>(g) < static_cast<unsigned>(ns) ? __ldg(row + g) : 0.0f;
                 const float p1 = static_cast<unsigned>(g + 1) < static_cast<unsigned>(ns) ? __ldg(row + g + 1) : 0.0f;
                 s_pair[j][k] = make_float2(p0, p1);
