@@ -839,8 +839,8 @@ __global__ void __launch_bounds__(256, 3)
 // warp per pixel, lane l summing views l, l+32, ..., then a fixed shuffle tree.
 __global__ void __launch_bounds__(128)
     fp_adj_border_f32(const float* __restrict__ proj, float* __restrict__ img,
-                      const double* __restrict__ weights, const double* __restrict__ pos,
-                      const int* __restrict__ usex, const FpConst c)
+                      const long long* __restrict__ B, const AdjView* __restrict__ V,
+                      const double* __restrict__ pos, const FpConst c)
 {
     const int n = c.nx, ns = c.ns;
     const int nb = n == 1 ? 1 : 4 * n - 4;
@@ -864,15 +864,13 @@ __global__ void __launch_bounds__(128)
     const float* P = proj + blockIdx.y * c.proj_stride;
     float acc = 0.0f;
     for (int ia = lane; ia < c.na; ia += 32) {
-        const int ux = usex[ia] != 0;
-        const int along = ux ? ix : iy, lin = ux ? iy : ix;
-        const double* pp = pos + (static_cast<size_t>(ia) * n + lin) * 2;
-        const long long O1 = fix32_any(pp[1]);
-        const long long MID = fix32_any(pp[0]) + static_cast<long long>(along) * O1;
-        const float o1 = fabsf(dbl2flt(pp[1]));
-        const float part = adj_tap_exact(P + static_cast<size_t>(ia) * ns, MID, O1, 1.0f / o1,
-                                         o1 <= 1.0f, along, n, ns, pp);
-        acc = fmaf(part, dbl2flt(weights[ia]), acc);
+        const AdjView v = V[ia];
+        const int along = v.ux ? ix : iy, lin = v.ux ? iy : ix;
+        const size_t line = static_cast<size_t>(ia) * n + lin;
+        const long long MID = __ldg(B + line) + static_cast<long long>(along) * v.O1;
+        const float part = adj_tap_exact(P + static_cast<size_t>(ia) * ns, MID, v.O1, v.inv, v.two != 0,
+                                         along, n, ns, pos + line * 2);
+        acc = fmaf(part, v.w, acc);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -1132,9 +1130,9 @@ int fp_adjoint(const ctr_par_param* p, const T* proj, T* img, const double* w,
             w, pos, usex, B, V, p->na, p->nx);
         dim3 grid(div_up(p->nx, kFaTileX), div_up(p->ny, kFaTileY), batch);
         fp_adj_f32<<<grid, 256, 0, stream>>>(proj, img, B, V, pos, c);
-        cudaFreeAsync(scratch, stream);
         const unsigned nborder = p->nx == 1 ? 1u : 4u * p->nx - 4u;
-        fp_adj_border_f32<<<dim3(div_up(nborder, 4), batch), 128, 0, stream>>>(proj, img, w, pos, usex, c);
+        fp_adj_border_f32<<<dim3(div_up(nborder, 4), batch), 128, 0, stream>>>(proj, img, B, V, pos, c);
+        cudaFreeAsync(scratch, stream);  // after every kernel that reads the tables
     } else {
         dim3 grid(div_up(p->nx, 32), div_up(p->ny, 8), batch);
         fp_adj_kernel<T><<<grid, dim3(32, 8), 0, stream>>>(proj, img, w, pos, usex, p->ns, p->na,
