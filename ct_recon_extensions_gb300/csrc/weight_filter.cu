@@ -1,8 +1,8 @@
 // Fan weighting and ramp filtering (reference src/fan_weighting.cc:19-59,
 // src/filter.cc:67-124).
 //
-// Fan weighting is an HBM-bound diagonal scaling: one thread per channel
-// computes the FP64 weight once and streams a block of rows, multiplying in
+// Fan weighting is an HBM-bound diagonal scaling: a CTA computes the FP64
+// weights of its channels once and streams a block of rows, multiplying in
 // FP64 exactly as the reference does (results are bit-identical to its CPU
 // code for both T).
 //
@@ -18,24 +18,43 @@
 namespace ctr {
 namespace {
 
-constexpr int kWeightThreads = 128;
-constexpr int kWeightRows = 8;
+constexpr int kWeightChannels = 128;  // channels per CTA
+constexpr int kWeightThreads = 256;
+constexpr int kWeightRows = 32;       // rows per CTA
+constexpr int kWeightPer = kWeightRows * kWeightChannels / kWeightThreads;  // elements per thread
 
+// A CTA weights a block of kWeightRows x kWeightChannels: the FP64 weights of
+// its channels are computed once into shared memory, then every thread loads
+// all of its elements before storing any (correct in place: each element is
+// read and written by one thread), so the loads are in flight together.
 template <typename T>
 __global__ void __launch_bounds__(kWeightThreads)
-    fan_weight_kernel(const T* __restrict__ in, T* __restrict__ out, unsigned ns,
-                      unsigned long long rows, double ds, double cents, double dso, double dsd,
-                      int type)
+    fan_weight_kernel(const T* in, T* out, unsigned ns, unsigned long long rows, double ds,
+                      double cents, double dso, double dsd, int type)
 {
-    const unsigned is = blockIdx.x * kWeightThreads + threadIdx.x;
-    if (is >= ns) return;
-    const double s = ds * (static_cast<double>(is) - cents);
-    const double w = type == 2 ? dso * fabs(cos(atan2(s, dsd))) / dsd : dso * fabs(cos(s / dsd)) / dsd;
+    __shared__ double s_w[kWeightChannels];
+    const unsigned c0 = blockIdx.x * kWeightChannels;
+    if (threadIdx.x < kWeightChannels) {
+        const unsigned is = c0 + threadIdx.x;
+        const double s = ds * (static_cast<double>(is) - cents);
+        s_w[threadIdx.x] = type == 2 ? dso * fabs(cos(atan2(s, dsd))) / dsd : dso * fabs(cos(s / dsd)) / dsd;
+    }
+    __syncthreads();
     const unsigned long long r0 = static_cast<unsigned long long>(blockIdx.y) * kWeightRows;
-    const unsigned long long r1 = r0 + kWeightRows < rows ? r0 + kWeightRows : rows;
-    for (unsigned long long r = r0; r < r1; ++r) {
-        const size_t k = r * ns + is;
-        out[k] = static_cast<T>(w * static_cast<double>(in[k]));
+    T v[kWeightPer];
+#pragma unroll
+    for (int i = 0; i < kWeightPer; ++i) {
+        const int e = threadIdx.x + kWeightThreads * i;
+        const unsigned long long r = r0 + e / kWeightChannels;
+        const unsigned is = c0 + (e % kWeightChannels);
+        v[i] = r < rows && is < ns ? in[r * ns + is] : T(0);
+    }
+#pragma unroll
+    for (int i = 0; i < kWeightPer; ++i) {
+        const int e = threadIdx.x + kWeightThreads * i;
+        const unsigned long long r = r0 + e / kWeightChannels;
+        const unsigned is = c0 + (e % kWeightChannels);
+        if (r < rows && is < ns) out[r * ns + is] = static_cast<T>(s_w[e % kWeightChannels] * static_cast<double>(v[i]));
     }
 }
 
@@ -51,7 +70,7 @@ int launch_fan_weighting(const ctr_fan_weighting_param* p, const T* in, T* out, 
     if (p->ns < 1 || p->nrow < 1) return fail(CTR_ERR_INVALID_ARG, "empty sinogram");
     const unsigned long long rows = static_cast<unsigned long long>(p->nrow) * batch;
     const double cents = static_cast<double>(p->ns - 1) / 2 + p->offset;
-    dim3 grid(div_up(p->ns, kWeightThreads), div_up(rows, kWeightRows));
+    dim3 grid(div_up(p->ns, kWeightChannels), div_up(rows, kWeightRows));
     if (grid.y > 65535u) return fail(CTR_ERR_UNSUPPORTED, "too many rows for one launch");
     fan_weight_kernel<T><<<grid, kWeightThreads, 0, stream>>>(in, out, p->ns, rows, p->ds, cents,
                                                               p->dso, p->dsd, p->type);
