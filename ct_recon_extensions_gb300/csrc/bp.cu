@@ -320,51 +320,59 @@ int launch_tile(K kern, int W, dim3 grid, cudaStream_t stream, const char* what,
 // its resident CTAs per SM (sets the register budget).
 constexpr int kFwdRows = 8;
 constexpr int kFwdMinBlocks = 1;
+// View groups per CTA of the single-geometry forward kernel: 2 (512 threads,
+// one CTA per SM) or 1 (256 threads, two CTAs per SM on different tiles).
+constexpr int kFwdGroups = 1;
 constexpr int kFwdTileY = (kBpThreads / 32) * kFwdRows;
 // Shared memory the forward kernel may take (one CTA per SM).
 constexpr size_t kFwdSmemMax = 200 * 1024;
 
-// Shared bytes of the bulk-copy forward kernel with VB views per group.
-inline size_t fwd_smem(const TileConst& ct, int VB)
+// Shared bytes of the bulk-copy forward kernel with NG groups of VB views.
+inline size_t fwd_smem(const TileConst& ct, int VB, int NG = kGroups)
 {
-    const size_t bv = static_cast<size_t>(kGroups) * VB;
+    const size_t bv = static_cast<size_t>(NG) * VB;
     return 128 + 2 * bv * ct.WS * sizeof(float) + 2 * bv * ct.W * sizeof(float2) + ct.na * sizeof(ViewP);
 }
 
 // The bulk-copy kernel with VB views per group on tiles of 32 x kFwdTileY:
 // stream-K over (tile, view block) units when the launch has fewer than 4
 // waves of tiles, one CTA per tile otherwise.
-template <Geo G, int VB>
+template <Geo G, int VB, int NG>
 int launch_tma(const float* proj, float* img, const double* t0, const double* t1, const double* t2,
                const TileConst& ct, int batch, cudaStream_t stream, const char* what)
 {
-    const size_t smem = fwd_smem(ct, VB);
+    constexpr int kThreads = NG * kBpThreads;
+    constexpr int kMinBlocks = NG == 1 ? 2 : kFwdMinBlocks;  // same register budget per SM
+    const size_t smem = fwd_smem(ct, VB, NG);
     const int tiles_x = static_cast<int>(div_up(ct.nx, kTileX));
     const int tiles_y = static_cast<int>(div_up(ct.ny, kFwdTileY));
     const long long tiles = static_cast<long long>(tiles_x) * tiles_y * batch;
-    const int nb = static_cast<int>(div_up(ct.na, kGroups * VB));
+    const int nb = static_cast<int>(div_up(ct.na, NG * VB));
     int dev = 0, sms = kSmCount;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (tiles < 4ll * sms && nb > 1) {
+    if (tiles < 4ll * sms * kMinBlocks && nb > 1) {
         SkConst k{};
         k.units = tiles * nb;
         k.nb = nb;
         k.tiles_x = tiles_x;
         k.tiles_per_item = tiles_x * tiles_y;
-        const int ctas = static_cast<int>(std::min<long long>(k.units, sms));
+        auto kern = bp_tile_tma_sk<G, kFwdRows, VB, NG, kMinBlocks>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(smem));
+        int per_sm = 1;
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
+        if (e != cudaSuccess || per_sm < 1) return fail(CTR_ERR_CUDA, "%s: occupancy", what);
+        const int ctas = static_cast<int>(std::min<long long>(k.units, static_cast<long long>(sms) * per_sm));
         k.maxseg = sk_max_segments(tiles, nb, ctas);
         const size_t part_bytes = static_cast<size_t>(tiles) * k.maxseg * kTileX * kFwdTileY * sizeof(float);
         void* scratch = nullptr;
         if (cudaMallocAsync(&scratch, part_bytes + sizeof(int) * tiles, stream) == cudaSuccess) {
             k.partial = static_cast<float*>(scratch);
             k.counter = reinterpret_cast<int*>(static_cast<char*>(scratch) + part_bytes);
-            auto kern = bp_tile_tma_sk<G, kFwdRows, VB>;
-            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 static_cast<int>(smem));
-            if (e == cudaSuccess) e = cudaMemsetAsync(k.counter, 0, sizeof(int) * tiles, stream);
+            e = cudaMemsetAsync(k.counter, 0, sizeof(int) * tiles, stream);
             if (e == cudaSuccess) {
-                kern<<<ctas, kTmaThreads, smem, stream>>>(proj, img, t0, t1, t2, ct, k);
+                kern<<<ctas, kThreads, smem, stream>>>(proj, img, t0, t1, t2, ct, k);
                 e = cudaGetLastError();
             }
             cudaFreeAsync(scratch, stream);
@@ -373,12 +381,12 @@ int launch_tma(const float* proj, float* img, const double* t0, const double* t1
         }
         cudaGetLastError();  // no scratch: whole tiles per CTA below
     }
-    auto kern = bp_tile_tma_f32<G, kFwdRows, kFwdMinBlocks, VB>;
+    auto kern = bp_tile_tma_f32<G, kFwdRows, kMinBlocks, VB, NG>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
     dim3 grid(tiles_x, tiles_y, batch);
-    kern<<<grid, kTmaThreads, smem, stream>>>(proj, img, t0, t1, t2, ct);
+    kern<<<grid, kThreads, smem, stream>>>(proj, img, t0, t1, t2, ct);
     return check_launch(what);
 }
 
@@ -404,10 +412,10 @@ int launch_forward(const float* proj, float* img, const double* t0, const double
         // parallel: 32 views per group halve the block barriers of its short
         // per-view work (bp_par_2d 122.9 -> 121.7 us at 512^2); the fan keeps 16
         // (183 vs 190 us with 32)
-        if (G == Geo::kPar && fwd_smem(ct, 32) <= kFwdSmemMax)
-            return launch_tma<G, 32>(proj, img, t0, t1, t2, ct, batch, stream, what);
-        if (fwd_smem(ct, 16) <= kFwdSmemMax)
-            return launch_tma<G, 16>(proj, img, t0, t1, t2, ct, batch, stream, what);
+        if (G == Geo::kPar && fwd_smem(ct, 32, kFwdGroups) <= kFwdSmemMax / (3 - kFwdGroups))
+            return launch_tma<G, 32, kFwdGroups>(proj, img, t0, t1, t2, ct, batch, stream, what);
+        if (fwd_smem(ct, 16, kFwdGroups) <= kFwdSmemMax / (3 - kFwdGroups))
+            return launch_tma<G, 16, kFwdGroups>(proj, img, t0, t1, t2, ct, batch, stream, what);
     }
     c.W = std::max(c.W, 16);
     dim3 grid(div_up(c.nx, kTileX), div_up(c.ny, kTileY), batch);

@@ -396,7 +396,7 @@ __device__ ViewP view_setup(const double* __restrict__ t2, int ia, float x0, flo
 // Re-entrant across calls of a persistent CTA: the mbarriers are
 // (re)initialised here and every copy issued is waited on before returning.
 // Returns false (uniformly) when a check or a bounded wait failed.
-template <Geo G, int R = kRowsPerThread, int VB = kViewBlock>
+template <Geo G, int R = kRowsPerThread, int VB = kViewBlock, int NG = kGroups>
 __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, float* __restrict__ img,
                                              const double* __restrict__ t0,
                                              const double* __restrict__ t1,
@@ -405,7 +405,8 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
                                              int b_end = -1, float* __restrict__ partial = nullptr)
 {
     constexpr int kTY = (kBpThreads / 32) * R;  // tile height
-    constexpr int kBV = kGroups * VB;           // views per staged block
+    constexpr int kBV = NG * VB;                // views per staged block
+    constexpr int kThreads = NG * kBpThreads;   // NG view groups of 256 threads
     // Dynamic shared memory, 128-byte aligned here: raw slots [2][kBV][WS]
     // (every slot stride a 128-byte multiple), pairs [2][kBV][W], then one
     // ViewP per view of the whole scan.
@@ -479,7 +480,7 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
     // 8 * bits(s + 2^23 - 1/2) (values below kModeFast fall back to the edge path)
     const unsigned pairs_base = smem_u32(pairs);
     const int ia_end = min(nblocks * kBV, c.na);
-    for (int ia = b_begin * kBV + tid; ia < ia_end; ia += kTmaThreads) {
+    for (int ia = b_begin * kBV + tid; ia < ia_end; ia += kThreads) {
         ViewP P = view_setup<G>(t2, ia, cx0, cx1, cy0, cy1, c);
         if (mode_fast(P.mode)) {
             const int slot = ((ia / kBV - b_begin) & 1) * kBV + ia % kBV;
@@ -494,7 +495,7 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
         const bool aligned = (smem_u32(raw) & 127u) == 0 && (c.WS * sizeof(float)) % 128 == 0;
         // the group reduction at the end writes R x kBpThreads floats into one
         // half of the pair buffer (kBV x W float2)
-        const bool fits = R * kBpThreads <= 2 * kBV * c.W;
+        const bool fits = NG == 1 || R * kBpThreads <= 2 * kBV * c.W;
         s_ok = aligned && fits;
         if (!aligned) raise_flag(kFlagMisaligned);
         if (!fits) raise_flag(kFlagWindowOverflow);
@@ -529,7 +530,7 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
         const float* slot = raw + (lb & 1) * kBV * c.WS;
         float2* pb = pairs + (lb & 1) * kBV * c.W;
         // one warp per view: rewrite the raw window as (p[i], p[i+1] - p[i]) pairs
-        for (int j = wid; j < nv; j += kTmaThreads / 32) {
+        for (int j = wid; j < nv; j += kThreads / 32) {
             const long long st = slot_start(b * kBV + j);
             const int lo = views[b * kBV + j].lo;
             const float* src = slot + j * c.WS + static_cast<int>(st & 3ll);
@@ -597,48 +598,51 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[r] += part[r];
     }
-    // add the second group's sums to the first's, in that order; the reduction
-    // uses the pairs buffer of the next-to-last block, which every thread has
-    // finished reading before the last block's barrier (or one never used)
+    // with two groups, add the second group's sums to the first's, in that
+    // order; the reduction uses the pairs buffer of the next-to-last block,
+    // which every thread has finished reading before the last block's barrier
+    // (or one never used)
     float* red = reinterpret_cast<float*>(pairs + ((nblocks - b_begin) & 1) * kBV * c.W);
-    if (group == 1) {
+    if constexpr (NG == 2) {
+        if (group == 1) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) red[r * kBpThreads + lt] = acc[r];
+            for (int r = 0; r < R; ++r) red[r * kBpThreads + lt] = acc[r];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < R; ++r) acc[r] += group == 0 ? red[r * kBpThreads + lt] : 0.0f;
     }
-    __syncthreads();
     if (group == 0) {
         if (partial) {
 #pragma unroll
-            for (int r = 0; r < R; ++r)
-                partial[(warp * R + r) * kTileX + lane] = acc[r] + red[r * kBpThreads + lt];
+            for (int r = 0; r < R; ++r) partial[(warp * R + r) * kTileX + lane] = acc[r];
         } else {
             float* I = img + static_cast<size_t>(item) * c.img_stride;
             const int ix = tx0 + lane;
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int iy = ty0 + warp * R + r;
-                if (ix < c.nx && iy < c.ny)
-                    I[static_cast<size_t>(iy) * c.nx + ix] = (acc[r] + red[r * kBpThreads + lt]) * c.scale;
+                if (ix < c.nx && iy < c.ny) I[static_cast<size_t>(iy) * c.nx + ix] = acc[r] * c.scale;
             }
         }
     }
     return true;
 }
 
-template <Geo G, int R, int MinBlocks>
-__global__ void __launch_bounds__(kTmaThreads, MinBlocks)
+template <Geo G, int R, int MinBlocks, int VB, int NG>
+__global__ void __launch_bounds__(NG * kBpThreads, MinBlocks)
     bp_tile_tma_f32(const float* __restrict__ proj, float* __restrict__ img,
                     const double* __restrict__ t0, const double* __restrict__ t1,
                     const double* __restrict__ t2, const TileConst c)
 {
-    tile_forward<G, R>(proj, img, t0, t1, t2, c, blockIdx.x, blockIdx.y, blockIdx.z);
+    tile_forward<G, R, VB, NG>(proj, img, t0, t1, t2, c, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // ---- stream-K split of small launches ----------------------------------------
 //
 // A launch with few tiles (a 512^2 image is 128 tiles of 32 x 64) leaves SMs
 // idle when each CTA owns whole tiles.  Here the work is cut into units of
-// (tile, block of kBlockViews views), tiles outer, and CTA c of G takes the
+// (tile, block of 2*VB views), tiles outer, and CTA c of G takes the
 // contiguous units [c*U/G, (c+1)*U/G): every SM gets the same number of view
 // blocks.  A tile whose units span several CTAs gets one unscaled partial sum
 // per CTA (segment) in `partial`; each CTA counts its segment in on the
@@ -653,8 +657,8 @@ struct SkConst {
     int* counter;          // [tiles], zero at launch
 };
 
-template <Geo G, int R>
-__global__ void __launch_bounds__(kTmaThreads, 1)
+template <Geo G, int R, int VB, int NG, int MinBlocks>
+__global__ void __launch_bounds__(NG * kBpThreads, MinBlocks)
     bp_tile_tma_sk(const float* __restrict__ proj, float* __restrict__ img,
                    const double* __restrict__ t0, const double* __restrict__ t1,
                    const double* __restrict__ t2, const TileConst c, const SkConst k)
@@ -675,11 +679,11 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
         const int tx = tl % k.tiles_x, ty = tl / k.tiles_x;
         const int first = sk_cta_of(tu, ctas, U), last = sk_cta_of(tu + k.nb - 1, ctas, U);
         if (first == last) {  // the whole tile is this CTA's
-            if (!tile_forward<G, R>(proj, img, t0, t1, t2, c, tx, ty, item)) return;
+            if (!tile_forward<G, R, VB, NG>(proj, img, t0, t1, t2, c, tx, ty, item)) return;
             continue;
         }
         float* seg = k.partial + (static_cast<size_t>(t) * k.maxseg + (blockIdx.x - first)) * kTilePix;
-        if (!tile_forward<G, R>(proj, img, t0, t1, t2, c, tx, ty, item, b0, b1, seg)) return;
+        if (!tile_forward<G, R, VB, NG>(proj, img, t0, t1, t2, c, tx, ty, item, b0, b1, seg)) return;
         __threadfence();  // this segment is visible before it is counted
         __syncthreads();
         if (threadIdx.x == 0) s_last = atomicAdd(k.counter + t, 1) == last - first;
@@ -688,7 +692,7 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
             __threadfence();
             const float* base = k.partial + static_cast<size_t>(t) * k.maxseg * kTilePix;
             float* I = img + static_cast<size_t>(item) * c.img_stride;
-            for (int idx = threadIdx.x; idx < kTilePix; idx += kTmaThreads) {
+            for (int idx = threadIdx.x; idx < kTilePix; idx += NG * kBpThreads) {
                 const int ix = tx * kTileX + idx % kTileX, iy = ty * kTY + idx / kTileX;
                 float v = __ldcg(base + idx);
                 for (int sg = 1; sg <= last - first; ++sg) v += __ldcg(base + sg * kTilePix + idx);
