@@ -34,9 +34,10 @@ struct ItemDev {
     int tiles_x;
 };
 
-// 8 rows per thread take one CTA per SM (up to 128 registers), fewer rows two.
-template <int R, int VB>
-__global__ void __launch_bounds__(kTmaThreads, R >= 8 ? 1 : 2)
+// NG view groups of 256 threads per CTA.  8 rows per thread take up to 128
+// registers: one 512-thread or two 256-thread CTAs per SM; fewer rows, twice that.
+template <int R, int VB, int NG>
+__global__ void __launch_bounds__(NG * kBpThreads, (R >= 8 ? 1 : 2) * (3 - NG))
     bp_fan_batch_f32(const ItemDev* __restrict__ items, const int2* __restrict__ work, int n_work,
                      int* __restrict__ counter)
 {
@@ -56,33 +57,36 @@ __global__ void __launch_bounds__(kTmaThreads, R >= 8 ? 1 : 2)
             reinterpret_cast<int*>(&s_c)[threadIdx.x] = reinterpret_cast<const int*>(&it.c)[threadIdx.x];
         __syncthreads();
         const int tx = wi.y % it.tiles_x, ty = wi.y / it.tiles_x;
-        if (!tile_forward<Geo::kFan, R, VB>(it.proj, it.img, it.xpos, it.ypos, it.sincos, s_c, tx,
-                                            ty, 0))
+        if (!tile_forward<Geo::kFan, R, VB, NG>(it.proj, it.img, it.xpos, it.ypos, it.sincos, s_c, tx,
+                                                ty, 0))
             return;
     }
 }
 
 struct Config {
-    int R, VB;
+    int R, VB, NG;
 };
-constexpr Config kConfigs[] = {{4, 16}, {2, 16}, {4, 8}, {2, 8}, {8, 16}, {8, 8}};
+constexpr Config kConfigs[] = {{4, 16, 2}, {2, 16, 2}, {4, 8, 2}, {2, 8, 2}, {8, 16, 2},
+                               {8, 8, 2},  {8, 16, 1}, {8, 32, 1}};
 constexpr int kNumConfigs = sizeof(kConfigs) / sizeof(kConfigs[0]);
 
-template <int R, int VB>
+template <int R, int VB, int NG>
 void* batch_kernel()
 {
-    return reinterpret_cast<void*>(bp_fan_batch_f32<R, VB>);
+    return reinterpret_cast<void*>(bp_fan_batch_f32<R, VB, NG>);
 }
 
 void* kernel_of(int ci)
 {
     switch (ci) {
-    case 0: return batch_kernel<4, 16>();
-    case 1: return batch_kernel<2, 16>();
-    case 2: return batch_kernel<4, 8>();
-    case 3: return batch_kernel<2, 8>();
-    case 4: return batch_kernel<8, 16>();
-    default: return batch_kernel<8, 8>();
+    case 0: return batch_kernel<4, 16, 2>();
+    case 1: return batch_kernel<2, 16, 2>();
+    case 2: return batch_kernel<4, 8, 2>();
+    case 3: return batch_kernel<2, 8, 2>();
+    case 4: return batch_kernel<8, 16, 2>();
+    case 5: return batch_kernel<8, 8, 2>();
+    case 6: return batch_kernel<8, 16, 1>();
+    default: return batch_kernel<8, 32, 1>();
     }
 }
 
@@ -138,7 +142,7 @@ struct ctr_fbp_plan {
     int n_fblocks = 0;
     unsigned max_ns = 0;
     ctr::ConfigData cfg[ctr::kNumConfigs];
-    int chosen = 4;  // without autotuning: 32 x 64 tiles, 16 views per group
+    int chosen = 6;  // without autotuning: 32 x 64 tiles, one group of 16 views, 2 CTAs per SM
     double tuned_ms = 0.0;
     bool autotuned = false;
     ctr::DevArray<int> counter;
@@ -187,8 +191,8 @@ TileConst item_const(const ctr_fan_bp_param& g, int tile_y, int R, int VB)
 
 int build_config(ctr_fbp_plan* P, int ci, int sm_count)
 {
-    const int R = kConfigs[ci].R, VB = kConfigs[ci].VB;
-    const int ty = (kBpThreads / 32) * R, bv = kGroups * VB;
+    const int R = kConfigs[ci].R, VB = kConfigs[ci].VB, NG = kConfigs[ci].NG;
+    const int ty = (kBpThreads / 32) * R, bv = NG * VB;
     ConfigData& D = P->cfg[ci];
     D.h_items.resize(P->n);
     std::vector<std::pair<double, int2>> work;
@@ -224,7 +228,7 @@ int build_config(ctr_fbp_plan* P, int ci, int sm_count)
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "batch smem: %s", cudaGetErrorString(e));
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTmaThreads, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NG * kBpThreads, smem);
     if (e != cudaSuccess || per_sm < 1) return fail(CTR_ERR_UNSUPPORTED, "batch kernel does not fit an SM");
     D.smem = smem;
     D.n_work = static_cast<int>(wl.size());
@@ -243,7 +247,7 @@ int enqueue(ctr_fbp_plan* P, int ci, cudaStream_t s)
     cudaError_t e = cudaMemsetAsync(P->counter.p, 0, sizeof(int), s);
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "counter reset: %s", cudaGetErrorString(e));
     void* args[] = {&D.items.p, &D.work.p, &D.n_work, &P->counter.p};
-    e = cudaLaunchKernel(kernel_of(ci), dim3(D.grid), dim3(kTmaThreads), args, D.smem, s);
+    e = cudaLaunchKernel(kernel_of(ci), dim3(D.grid), dim3(kConfigs[ci].NG * kBpThreads), args, D.smem, s);
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "batch launch: %s", cudaGetErrorString(e));
     return CTR_OK;
 }
