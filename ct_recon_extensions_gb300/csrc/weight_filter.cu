@@ -91,18 +91,25 @@ constexpr int kFilterMaxThreads = 1024;
 constexpr int kFilterPad = 16;   // zero taps beyond the ends of H
 constexpr int kFilterRowsPlain = 2;
 
+// Thread tasks of a row: (8-output block, parity).  When twice that fits one
+// CTA, each task's inputs are split in two halves run by two threads, whose
+// partial sums are added in a fixed order (halves the serial loop per thread).
+__host__ __device__ inline int filter_tasks(unsigned ns) { return static_cast<int>((ns + 7) / 8) * 2; }
+__host__ __device__ inline bool filter_split(unsigned ns) { return 2 * filter_tasks(ns) <= kFilterMaxThreads; }
+
 __host__ __device__ inline int filter_threads(unsigned ns)
 {
-    const int t = static_cast<int>((ns + 7) / 8) * 2;
+    const int t = filter_tasks(ns) * (filter_split(ns) ? 2 : 1);
     return t < 32 ? 32 : (t > kFilterMaxThreads ? kFilterMaxThreads : (t + 31) / 32 * 32);
 }
 
 // Shared layout: H[-(ns-1) - kFilterPad .. ns - 1 + kFilterPad] (taps * ds),
-// then xs[kRows][ns].
+// then xs[kRows][ns], then the second halves' sums [kRows][tasks][4].
 template <typename T>
 __host__ __device__ inline size_t filter_smem(unsigned ns, int rows)
 {
-    return sizeof(T) * ((2 * static_cast<size_t>(ns) + 2 * kFilterPad) + static_cast<size_t>(rows) * ns);
+    return sizeof(T) * ((2 * static_cast<size_t>(ns) + 2 * kFilterPad) + static_cast<size_t>(rows) * ns +
+                        static_cast<size_t>(rows) * filter_tasks(ns) * 4);
 }
 
 template <typename T, int kRows, bool kGrad>
@@ -139,8 +146,61 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
         xs[idx] = v;
     }
     __syncthreads();
-    const int groups = (n + 7) / 8 * 2;  // thread tasks: (8-output block, parity)
-    if (!s_even) {
+    const int groups = filter_tasks(ns);  // thread tasks: (8-output block, parity)
+    T* red = xs + kRows * n;              // [kRows][groups][4]
+    if (!s_even && filter_split(ns)) {
+        // two threads per task (blockDim.x >= 2 * groups): inputs [jb, jm) and [jm, n)
+        const int task = threadIdx.x;
+        const bool active = task < 2 * groups;
+        const int half = task >= groups ? 1 : 0;
+        const int g = task - half * groups;
+        const int i0 = (g >> 1) * 8 + (g & 1);
+        T acc[kRows][4];
+#pragma unroll
+        for (int r = 0; r < kRows; ++r)
+#pragma unroll
+            for (int m = 0; m < 4; ++m) acc[r][m] = 0;
+        if (active) {
+            const int jb = (i0 + 1) & 1;  // inputs of the other parity
+            const int jm = jb + 2 * ((n - jb + 1) / 4);
+            const int j0 = half ? jm : jb, j1 = half ? n : jm;
+            T w0 = H[i0 - j0], w1 = H[i0 + 2 - j0], w2 = H[i0 + 4 - j0], w3 = H[i0 + 6 - j0];
+#pragma unroll 4
+            for (int j = j0; j < j1; j += 2) {
+#pragma unroll
+                for (int r = 0; r < kRows; ++r) {
+                    const T xv = xs[r * n + j];
+                    acc[r][0] += w0 * xv;
+                    acc[r][1] += w1 * xv;
+                    acc[r][2] += w2 * xv;
+                    acc[r][3] += w3 * xv;
+                }
+                w3 = w2;
+                w2 = w1;
+                w1 = w0;
+                w0 = H[i0 - j - 2];
+            }
+            if (half) {
+#pragma unroll
+                for (int r = 0; r < kRows; ++r)
+#pragma unroll
+                    for (int m = 0; m < 4; ++m) red[(r * groups + g) * 4 + m] = acc[r][m];
+            }
+        }
+        __syncthreads();
+        if (active && !half) {
+            const T t0 = H[0];
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                const int o = i0 + 2 * m;
+                if (o >= n) continue;
+#pragma unroll
+                for (int r = 0; r < kRows; ++r)
+                    if (r < nr)
+                        out[(r0 + r) * ns + o] = t0 * xs[r * n + o] + (acc[r][m] + red[(r * groups + g) * 4 + m]);
+            }
+        }
+    } else if (!s_even) {
         for (int task = threadIdx.x; task < groups; task += blockDim.x) {
             const int i0 = (task >> 1) * 8 + (task & 1);
             T acc[kRows][4];
