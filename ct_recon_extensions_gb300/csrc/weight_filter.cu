@@ -103,39 +103,63 @@ __host__ __device__ inline int filter_threads(unsigned ns)
     return t < 32 ? 32 : (t > kFilterMaxThreads ? kFilterMaxThreads : (t + 31) / 32 * 32);
 }
 
-// Shared layout: H[-(ns-1) - kFilterPad .. ns - 1 + kFilterPad] (taps * ds),
-// then xs[kRows][ns], then the second halves' sums [kRows][tasks][4].
-template <typename T>
-__host__ __device__ inline size_t filter_smem(unsigned ns, int rows)
+// Tap storage: tap idx (offset d + ns - 1 + kFilterPad) lives at word
+// tg*(idx/8) + idx%8.  With tg = 34 (skewed) a warp's lanes, which read taps
+// i0 - j - 2 with i0 = 8q + p (q < 16, p < 2), fall in 32 distinct banks for
+// every j; packed (tg = 8) the 16 groups of 8 fall in 8 banks (4-way
+// conflicts).  The skewed layout is used where it fits the shared memory.
+constexpr int kTapSkewed = 34, kTapPacked = 8;
+__host__ __device__ inline int tap_slot(int idx, int tg) { return tg * (idx >> 3) + (idx & 7); }
+__host__ __device__ inline int tap_words(unsigned ns, int tg)
 {
-    return sizeof(T) * ((2 * static_cast<size_t>(ns) + 2 * kFilterPad) + static_cast<size_t>(rows) * ns +
+    return tap_slot(2 * static_cast<int>(ns) + 2 * kFilterPad, tg);
+}
+
+// Shared layout: the taps H[-(ns-1) - kFilterPad .. ns - 1 + kFilterPad] (taps *
+// ds), then xs[kRows][ns], then the second halves' sums [kRows][tasks][4].
+template <typename T>
+__host__ __device__ inline size_t filter_smem(unsigned ns, int rows, int tg)
+{
+    return sizeof(T) * (static_cast<size_t>(tap_words(ns, tg)) + static_cast<size_t>(rows) * ns +
                         static_cast<size_t>(rows) * filter_tasks(ns) * 4);
+}
+
+// The tap layout for a launch: skewed when it fits kFilterSmemMax.
+constexpr size_t kFilterSmemMax = 200 * 1024;
+template <typename T>
+inline int filter_layout(unsigned ns, int rows)
+{
+    return filter_smem<T>(ns, rows, kTapSkewed) <= kFilterSmemMax ? kTapSkewed : kTapPacked;
 }
 
 template <typename T, int kRows, bool kGrad>
 __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const double* __restrict__ filter,
                                             T* __restrict__ out, const float* __restrict__ weight,
                                             unsigned ns, unsigned long long r0, int nr, double ds,
-                                            unsigned char* smem_raw)
+                                            int tg, unsigned char* smem_raw)
 {
     const int n = static_cast<int>(ns);
     T* H0 = reinterpret_cast<T*>(smem_raw);
-    T* H = H0 + (n - 1) + kFilterPad;  // H[d], d in [-(n-1) - pad, n - 1 + pad]
-    T* xs = H0 + 2 * n + 2 * kFilterPad;
+    const int d0 = (n - 1) + kFilterPad;  // tap d sits at H0[tap_slot(d + d0, tg)]
+    auto H = [&](int d) -> T { return H0[tap_slot(d + d0, tg)]; };
+    T* xs = H0 + tap_words(ns, tg);
     __shared__ int s_even;
 
     const double* h = filter + ns;  // h[k], k in [-ns, ns]
     if (threadIdx.x == 0) s_even = 0;
     __syncthreads();
     bool even = false;
+    // staging loops unrolled so that a thread's global loads are in flight together
+#pragma unroll 4
     for (int idx = threadIdx.x; idx < 2 * n + 2 * kFilterPad; idx += blockDim.x) {
         const int d = idx - (n - 1) - kFilterPad;
         double v = 0.0;
         if (d > -n && d < n) v = kGrad ? h[-d] : h[d];
-        H0[idx] = static_cast<T>(v * ds);
+        H0[tap_slot(idx, tg)] = static_cast<T>(v * ds);
         if (d != 0 && (d & 1) == 0 && v != 0.0) even = true;
     }
     if (even) s_even = 1;
+#pragma unroll 4
     for (int idx = threadIdx.x; idx < kRows * n; idx += blockDim.x) {
         const int r = idx / n, j = idx - r * n;
         T v = 0;
@@ -164,7 +188,7 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
             const int jb = (i0 + 1) & 1;  // inputs of the other parity
             const int jm = jb + 2 * ((n - jb + 1) / 4);
             const int j0 = half ? jm : jb, j1 = half ? n : jm;
-            T w0 = H[i0 - j0], w1 = H[i0 + 2 - j0], w2 = H[i0 + 4 - j0], w3 = H[i0 + 6 - j0];
+            T w0 = H(i0 - j0), w1 = H(i0 + 2 - j0), w2 = H(i0 + 4 - j0), w3 = H(i0 + 6 - j0);
 #pragma unroll 4
             for (int j = j0; j < j1; j += 2) {
 #pragma unroll
@@ -178,7 +202,7 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
                 w3 = w2;
                 w2 = w1;
                 w1 = w0;
-                w0 = H[i0 - j - 2];
+                w0 = H(i0 - j - 2);
             }
             if (half) {
 #pragma unroll
@@ -189,7 +213,7 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
         }
         __syncthreads();
         if (active && !half) {
-            const T t0 = H[0];
+            const T t0 = H(0);
 #pragma unroll
             for (int m = 0; m < 4; ++m) {
                 const int o = i0 + 2 * m;
@@ -209,7 +233,7 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
 #pragma unroll
                 for (int m = 0; m < 4; ++m) acc[r][m] = 0;
             const int jb = (i0 + 1) & 1;  // inputs of the other parity
-            T w0 = H[i0 - jb], w1 = H[i0 + 2 - jb], w2 = H[i0 + 4 - jb], w3 = H[i0 + 6 - jb];
+            T w0 = H(i0 - jb), w1 = H(i0 + 2 - jb), w2 = H(i0 + 4 - jb), w3 = H(i0 + 6 - jb);
 #pragma unroll 4
             for (int j = jb; j < n; j += 2) {
 #pragma unroll
@@ -223,9 +247,9 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
                 w3 = w2;
                 w2 = w1;
                 w1 = w0;
-                w0 = H[i0 - j - 2];
+                w0 = H(i0 - j - 2);
             }
-            const T t0 = H[0];
+            const T t0 = H(0);
 #pragma unroll
             for (int m = 0; m < 4; ++m) {
                 const int o = i0 + 2 * m;
@@ -242,7 +266,7 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
 #pragma unroll
             for (int r = 0; r < kRows; ++r) acc[r] = 0;
             for (int j = 0; j < n; ++j) {
-                const T t = H[o - j];
+                const T t = H(o - j);
 #pragma unroll
                 for (int r = 0; r < kRows; ++r) acc[r] += t * xs[r * n + j];
             }
@@ -258,24 +282,24 @@ template <typename T, bool kGrad>
 __global__ void __launch_bounds__(kFilterMaxThreads)
     ramp_filter_kernel(const T* __restrict__ in, const double* __restrict__ filter,
                        T* __restrict__ out, const float* __restrict__ weight, unsigned ns,
-                       unsigned long long rows, double ds)
+                       unsigned long long rows, double ds, int tg)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const unsigned long long r0 = static_cast<unsigned long long>(blockIdx.x) * kFilterRowsPlain;
     const int nr = static_cast<int>(rows - r0 < kFilterRowsPlain ? rows - r0 : kFilterRowsPlain);
-    filter_rows<T, kFilterRowsPlain, kGrad>(in, filter, out, weight, ns, r0, nr, ds, smem_raw);
+    filter_rows<T, kFilterRowsPlain, kGrad>(in, filter, out, weight, ns, r0, nr, ds, tg, smem_raw);
 }
 
 // Batched FP32 filtering with pre-weighting: one CTA per (job, row block).
 __global__ void __launch_bounds__(kFilterMaxThreads)
-    ramp_filter_batch_kernel(const FilterJob* __restrict__ jobs, const int2* __restrict__ blocks)
+    ramp_filter_batch_kernel(const FilterJob* __restrict__ jobs, const int2* __restrict__ blocks, int tg)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int2 b = blocks[blockIdx.x];  // (job, first row)
     const FilterJob J = jobs[b.x];
     const int nr = min(kFilterRowsPerBlock, static_cast<int>(J.nrow) - b.y);
     filter_rows<float, kFilterRowsPerBlock, false>(J.in, J.taps, J.out, J.weight, J.ns, b.y, nr,
-                                                   J.ds, smem_raw);
+                                                   J.ds, tg, smem_raw);
 }
 
 template <typename T, bool kGrad>
@@ -289,15 +313,16 @@ int launch_ramp_filter(const ctr_filter_param* p, const T* in, const double* fil
     if (p->ns < 1 || p->nrow < 1) return fail(CTR_ERR_INVALID_ARG, "empty sinogram");
     if (in == out) return fail(CTR_ERR_INVALID_ARG, "ramp filter cannot run in place");
     const unsigned long long rows = static_cast<unsigned long long>(p->nrow) * batch;
-    const size_t smem = filter_smem<T>(p->ns, kFilterRowsPlain);
-    if (smem > 200 * 1024)
+    const int tg = filter_layout<T>(p->ns, kFilterRowsPlain);
+    const size_t smem = filter_smem<T>(p->ns, kFilterRowsPlain, tg);
+    if (smem > kFilterSmemMax)
         return fail(CTR_ERR_UNSUPPORTED, "ns=%u exceeds the filter's shared-memory tile", p->ns);
     auto kern = ramp_filter_kernel<T, kGrad>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "filter smem: %s", cudaGetErrorString(e));
     const unsigned blocks = div_up(rows, kFilterRowsPlain);
-    kern<<<blocks, filter_threads(p->ns), smem, stream>>>(in, filter, out, weight, p->ns, rows, p->ds);
+    kern<<<blocks, filter_threads(p->ns), smem, stream>>>(in, filter, out, weight, p->ns, rows, p->ds, tg);
     return check_launch("ramp_filter");
 }
 
@@ -314,13 +339,14 @@ int ramp_filter_weighted_f32(const ctr_filter_param* p, const float* in, const d
 int ramp_filter_batch_f32(const FilterJob* jobs, const int2* blocks, int n_blocks, unsigned max_ns,
                           cudaStream_t stream)
 {
-    const size_t smem = filter_smem<float>(max_ns, kFilterRowsPerBlock);
-    if (smem > 200 * 1024) return fail(CTR_ERR_UNSUPPORTED, "ns=%u too wide for the filter tile", max_ns);
+    const int tg = filter_layout<float>(max_ns, kFilterRowsPerBlock);
+    const size_t smem = filter_smem<float>(max_ns, kFilterRowsPerBlock, tg);
+    if (smem > kFilterSmemMax) return fail(CTR_ERR_UNSUPPORTED, "ns=%u too wide for the filter tile", max_ns);
     cudaError_t e = cudaFuncSetAttribute(ramp_filter_batch_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "filter smem: %s", cudaGetErrorString(e));
     if (n_blocks > 0)
-        ramp_filter_batch_kernel<<<n_blocks, filter_threads(max_ns), smem, stream>>>(jobs, blocks);
+        ramp_filter_batch_kernel<<<n_blocks, filter_threads(max_ns), smem, stream>>>(jobs, blocks, tg);
     return check_launch("ramp_filter_batch");
 }
 
