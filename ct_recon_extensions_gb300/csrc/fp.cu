@@ -245,30 +245,36 @@ __device__ __forceinline__ void slot_ray(unsigned q, int lane, const FpxConst& c
     *is = slot_octet(q - quad * static_cast<unsigned>(c.octets), c) * 8 + (lane & 7);
 }
 
-// imgT[b][x][y] = img[b][y][x] for n x n images (32x32 tiles through shared memory).
-__global__ void __launch_bounds__(256) transpose_f32(const float* __restrict__ in, float* __restrict__ out, int n)
-{
-    __shared__ float t[32][33];
-    const size_t off = static_cast<size_t>(blockIdx.z) * n * n;
-    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
-    for (int r = threadIdx.y; r < 32; r += 8) {
-        const int y = y0 + r, x = x0 + threadIdx.x;
-        if (x < n && y < n) t[r][threadIdx.x] = in[off + static_cast<size_t>(y) * n + x];
-    }
-    __syncthreads();
-    for (int r = threadIdx.y; r < 32; r += 8) {
-        const int x = x0 + r, y = y0 + threadIdx.x;
-        if (x < n && y < n) out[off + static_cast<size_t>(x) * n + y] = t[threadIdx.x][r];
-    }
-}
-
 // ---- set-up kernel: every ray once; block 0 the class lists and CTA cut ------
+// Blocks from `setup_blocks` on transpose the images instead (32 x 32 tiles):
+// the two jobs are independent, and the transpose blocks fill the SMs left idle
+// while the few tie rays of the set-up walk the reference's accumulation.
 __global__ void __launch_bounds__(kFpxSetupThreads)
     fpx_setup(const double* __restrict__ bo, const int* __restrict__ usex, const FpxConst c,
-              const FpxRays r)
+              const FpxRays r, int setup_blocks, const float* __restrict__ img, float* __restrict__ imgT)
 {
     __shared__ int s_chunk[2049];  // block 0: row-marching views before each chunk of 32
     const int tid = threadIdx.x;
+    if (static_cast<int>(blockIdx.x) >= setup_blocks) {
+        // imgT[b][x][y] = img[b][y][x]
+        float (*t)[33] = reinterpret_cast<float (*)[33]>(s_chunk);  // 32 x 33 floats
+        const int n = c.n, tiles = (n + 31) / 32;
+        const int tb = static_cast<int>(blockIdx.x) - setup_blocks;
+        const int item = tb / (tiles * tiles), tt = tb - item * tiles * tiles;
+        const int x0 = (tt % tiles) * 32, y0 = (tt / tiles) * 32;
+        const int tx = tid & 31, ty = tid >> 5;
+        const size_t off = static_cast<size_t>(item) * n * n;
+        for (int rr = ty; rr < 32; rr += kFpxSetupThreads / 32) {
+            const int y = y0 + rr, x = x0 + tx;
+            if (x < n && y < n) t[rr][tx] = img[off + static_cast<size_t>(y) * n + x];
+        }
+        __syncthreads();
+        for (int rr = ty; rr < 32; rr += kFpxSetupThreads / 32) {
+            const int x = x0 + rr, y = y0 + tx;
+            if (x < n && y < n) imgT[off + static_cast<size_t>(x) * n + y] = t[tx][rr];
+        }
+        return;
+    }
     if (blockIdx.x == 0) {
         // class lists with warp ballots over chunks of 32 views: row-marching
         // views (usex) first, then column-marching ones, each padded to quads
@@ -324,7 +330,7 @@ __global__ void __launch_bounds__(kFpxSetupThreads)
         if (tid == 0) r.cuts[c.ctas + 1] = G0;
     }
     const int rays = c.na * c.ns;
-    for (int ray = blockIdx.x * kFpxSetupThreads + tid; ray < rays; ray += gridDim.x * kFpxSetupThreads) {
+    for (int ray = blockIdx.x * kFpxSetupThreads + tid; ray < rays; ray += setup_blocks * kFpxSetupThreads) {
         const int ia = ray / c.ns;
         const double begin = bo[2 * static_cast<size_t>(ray)], step = bo[2 * static_cast<size_t>(ray) + 1];
         long long X0 = 0, S = 0;
@@ -1050,16 +1056,17 @@ int launch_fpx(const FpxConst& c, size_t smem, void* scratch, const float* img, 
     float* imgT = nullptr;
     const FpxRays r = fpx_rays(scratch, c, &imgT);
     const int n = c.n;
-    transpose_f32<<<dim3(div_up(n, 32), div_up(n, 32), batch), dim3(32, 8), 0, stream>>>(img, imgT, n);
-    int st = check_launch("fp_par_2d transpose");
-    if (st) return st;
     cudaError_t e = cudaMemsetAsync(r.nties, 0, sizeof(int), stream);
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp_par_2d: %s", cudaGetErrorString(e));
     const long long rays = static_cast<long long>(c.na) * c.ns;
     const unsigned blocks = static_cast<unsigned>(
         std::min<long long>(div_up(rays, kFpxSetupThreads), 8 * kSmCount));
-    fpx_setup<<<blocks, kFpxSetupThreads, 0, stream>>>(bo, usex, c, r);
-    st = check_launch("fp_par_2d set-up");
+    const unsigned long long tblocks = static_cast<unsigned long long>(div_up(n, 32)) * div_up(n, 32) * batch;
+    if (blocks + tblocks > 0x7FFFFFFFull) return fail(CTR_ERR_UNSUPPORTED, "fp_par_2d: batch too large");
+    // ray set-up and the transposed copy in one launch (set-up blocks first)
+    fpx_setup<<<static_cast<unsigned>(blocks + tblocks), kFpxSetupThreads, 0, stream>>>(
+        bo, usex, c, r, static_cast<int>(blocks), img, imgT);
+    int st = check_launch("fp_par_2d set-up");
     if (st) return st;
     e = cudaFuncSetAttribute(fp_proj_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(smem));

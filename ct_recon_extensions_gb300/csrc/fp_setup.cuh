@@ -290,7 +290,13 @@ CTR_HD void acc_advance(AccWalk* w, double step, int target)
                 // increments for the exact sum before rounding
                 const long long room = D > 0 ? (1ll << 53) - 1 - M1 : M1 - (1ll << 52);
                 const long long ad = D > 0 ? D : -D;
-                long long m = room / ad - 2;
+                // a lower bound of room / ad - 2 in FP32 (conversions and the
+                // quotient are within 3 * 2^-24 relative; the factor 1 - 2^-20
+                // keeps it below the exact quotient): a shorter jump only costs
+                // another iteration, while a 64-bit integer division costs
+                // hundreds of dependent instructions on the device
+                long long m = static_cast<long long>(static_cast<float>(room) / static_cast<float>(ad) *
+                                                     0.99999904632568359375f) - 2;
                 if (m > static_cast<long long>(target - k)) m = target - k;
                 if (m > 0) {
                     const unsigned long long bm =
