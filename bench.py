@@ -995,6 +995,13 @@ def main():
             "e2e": e2e, "roofline": roofline, "clocks": clocks, "cpu_baseline": cpu,
             "extra": extra,
         }
+        # kernel self-checks (bit 0 window, 1 queue, 2 bounded wait, 3 alignment): a set
+        # bit means some launch skipped work, so its numbers would not stand
+        flags = ctypes.c_uint()
+        lib.ctr_kernel_flags(ctypes.byref(flags), 1)
+        line["kernel_flags"] = flags.value
+        if flags.value:
+            print(f"bench: kernel self-check flags 0x{flags.value:x}", file=sys.stderr)
         print(json.dumps(line))
     dist.close()
 
