@@ -83,4 +83,18 @@ __device__ __forceinline__ void bulk_load(unsigned dst, const void* src, unsigne
         : "memory");
 }
 
+// 8-byte asynchronous global -> shared copy (cp.async; both addresses 8-byte
+// aligned); cp_async_wait_all waits for every such copy of the thread.
+__device__ __forceinline__ void cp_async8(unsigned dst, const void* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;"
+                 ::"r"(dst), "l"(reinterpret_cast<unsigned long long>(src))
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 }  // namespace ctr

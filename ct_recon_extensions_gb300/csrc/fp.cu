@@ -23,6 +23,7 @@
 //
 // FP64 kernels follow the reference's arithmetic (one thread per ray / pixel).
 #include <algorithm>
+#include <climits>
 #include <mutex>
 #include <numeric>
 
@@ -584,20 +585,29 @@ __global__ void __launch_bounds__(kFpxThreads, 2)
 // Interior pixels of views with |offset| <= 1 (every view when dx, dy <= ds)
 // touch at most channels floor(mid) and floor(mid) + 1, whose weights follow
 // from the fraction with two FMAs (saturated: both are at most 1, and the
-// clamp at 0 is the footprint's edge).  fp_adj_prep converts the caller's
-// positions to 32.32 fixed point once per call; fp_adj_f32 stages, per block
-// of views, the channel window of its 32 x 64 tile as zero-padded (p[i], p[i+1]) pairs in
-// shared memory, so such a pixel-view is one 8-byte shared load and a few
-// FMAs; positions advance by 64-bit adds.  It computes every pixel that way.
-// Pixels on the image border have one-sided footprints (channels on the
-// neighbour's side only); fp_adj_border_f32 then recomputes those 4n - 4
-// pixels exactly (one warp each) and overwrites them.  Views with |offset| > 1 or a window
-// wider than the staged one take the exact per-pixel path in both kernels.
+// clamp at 0 is the footprint's edge).  Once per call, fp_adj_prep converts
+// the caller's positions to 32.32 fixed point and fp_adj_windows finds, per
+// (view, tile), the channel window the tile's pixels fall in.  fp_adj_f32
+// stages, per block of views, each window as zero-padded pairs (w p[i],
+// w p[i+1]) of IMG images side by side (w = the view weight), so a pixel-view
+// of IMG images is one shared load, a fraction and two weights shared by the
+// images, and two FMAs per image; positions advance by 64-bit adds.  It
+// computes every pixel that way.  Pixels on the image border have one-sided
+// footprints (channels on the neighbour's side only); fp_adj_border_f32 then
+// recomputes those 4n - 4 pixels exactly and overwrites them.  When one image's
+// tiles would not fill the GPU, each tile's views are split into segments whose
+// partial images fp_adj_reduce sums in segment order.
+// Views with |offset| > 1 or a window wider than the staged one take the exact
+// per-pixel path in both kernels.
 constexpr int kFaViews = 16;
-constexpr int kFaRows = 8;                 // pixels per thread (one column)
-constexpr int kFaTileX = 32, kFaTileY = 8 * kFaRows;  // 32 x 64 tile, 256 threads
-constexpr int kFaLines = kFaTileY;         // lines of a tile: rows (64) or columns (32)
-constexpr int kFaWin = 128;                // staged channel pairs per view
+constexpr int kFaTileX = 32;
+// Tile of ROWS pixels of one column per thread: 32 x 8*ROWS pixels, 256 threads.
+template <int ROWS>
+struct FaShape {
+    static constexpr int TY = 8 * ROWS;
+    static constexpr int LINES = TY > kFaTileX ? TY : kFaTileX;  // rows or columns of a tile
+    static constexpr int WIN = 2 * LINES;                        // staged channel pairs per view
+};
 // Units of 2^-32 channel within which a border pixel's position counts as on a
 // channel: the fixed-point position is within 0.5 + 0.5*along units of the
 // reference's FP64 one (along < 8192).
@@ -609,42 +619,50 @@ __device__ __forceinline__ long long fix32_any(double v)
     return ((double_bits(v) >> 52) & 0x7FF) < 1043 ? fix32(v) : llrint(v * kTwo32);
 }
 
-// The reference grad's tap sum for one pixel-view: MID = the pixel's position
+// The reference grad's taps for one pixel-view: MID = the pixel's position
 // (fixed point), O1 = the view's offset, `along` = the pixel's index along its
 // line, pp = the caller's (begin, offset) of the pixel's line.  A border pixel's
 // footprint is one-sided (toward the neighbour pixel); its end channel is
 // decided from the fixed-point fraction or, when mid lies within kFaTie units
-// of a channel, in FP64 exactly as the reference does.
-__device__ __forceinline__ float adj_tap_exact(const float* __restrict__ row, long long MID, long long O1,
-                                               float inv, bool two, int along, int n, int ns,
-                                               const double* __restrict__ pp)
+// of a channel, in FP64 exactly as the reference does.  Either two taps at mi,
+// mi + 1 with weights w0, w1, or channels lo..hi with weight 1 - |mid - is| / |o|.
+struct AdjTap {
+    int mi, lo, hi;
+    float mf, w0, w1;
+    bool two;
+};
+
+__device__ __forceinline__ AdjTap adj_tap_plan(long long MID, long long O1, float inv, bool two, int along,
+                                               int n, int ns, const double* __restrict__ pp)
 {
-    const int mi = static_cast<int>(MID >> 32);
-    const float mf = frac_of(MID);
+    AdjTap t;
+    t.mi = static_cast<int>(MID >> 32);
+    t.mf = frac_of(MID);
     const bool border = along == 0 || along == n - 1;
     const unsigned frac_bits = static_cast<unsigned>(MID);
     const bool tie = border && (n == 1 || frac_bits < kFaTie || frac_bits > 0u - kFaTie);
-    if (two && !tie) {
-        float w0 = fmaxf(fmaf(-mf, inv, 1.0f), 0.0f);
-        float w1 = fmaxf(fmaf(mf, inv, 1.0f - inv), 0.0f);
+    t.two = two && !tie;
+    if (t.two) {
+        t.w0 = fmaxf(fmaf(-t.mf, inv, 1.0f), 0.0f);
+        t.w1 = fmaxf(fmaf(t.mf, inv, 1.0f - inv), 0.0f);
         if (border) {
             const bool ge = (along == 0) != (O1 < 0);  // footprint [mid, mid + |o|]
-            if (ge) w0 = 0.0f;
-            else w1 = 0.0f;
+            if (ge) t.w0 = 0.0f;
+            else t.w1 = 0.0f;
         }
-        const float p0 = static_cast<unsigned>(mi) < static_cast<unsigned>(ns) ? __ldg(row + mi) : 0.0f;
-        const float p1 = static_cast<unsigned>(mi + 1) < static_cast<unsigned>(ns) ? __ldg(row + mi + 1) : 0.0f;
-        return fmaf(w0, p0, w1 * p1);
+        t.lo = t.hi = 0;
+        return t;
     }
+    t.w0 = t.w1 = 0.0f;
     long long L = along == 0 ? MID : MID - O1;
     long long R = along == n - 1 ? MID : MID + O1;
     if (L > R) {
-        const long long t = L;
+        const long long x = L;
         L = R;
-        R = t;
+        R = x;
     }
-    int lo = max(static_cast<int>((L + 0xFFFFFFFFll) >> 32), 0);
-    int hi = min(static_cast<int>(R >> 32), ns - 1);
+    t.lo = max(static_cast<int>((L + 0xFFFFFFFFll) >> 32), 0);
+    t.hi = min(static_cast<int>(R >> 32), ns - 1);
     if (border) {
         // the end channel sits at the pixel itself with weight ~1: the range
         // is decided in FP64 as the reference does (mid = begin + offset*along)
@@ -653,26 +671,30 @@ __device__ __forceinline__ float adj_tap_exact(const float* __restrict__ row, lo
         double left = along == 0 ? mid : __dsub_rn(mid, off);
         double right = along == n - 1 ? mid : __dadd_rn(mid, off);
         if (left > right) {
-            const double t = left;
+            const double x = left;
             left = right;
-            right = t;
+            right = x;
         }
-        lo = static_cast<int>(fmax(ceil(left), 0.0));
-        hi = static_cast<int>(fmin(floor(right), static_cast<double>(ns - 1)));
+        t.lo = static_cast<int>(fmax(ceil(left), 0.0));
+        t.hi = static_cast<int>(fmin(floor(right), static_cast<double>(ns - 1)));
+    }
+    return t;
+}
+
+// The tap sum of one detector row.
+__device__ __forceinline__ float adj_tap_apply(const float* __restrict__ row, const AdjTap& t, float inv, int ns)
+{
+    if (t.two) {
+        const float p0 = static_cast<unsigned>(t.mi) < static_cast<unsigned>(ns) ? __ldg(row + t.mi) : 0.0f;
+        const float p1 = static_cast<unsigned>(t.mi + 1) < static_cast<unsigned>(ns) ? __ldg(row + t.mi + 1) : 0.0f;
+        return fmaf(t.w0, p0, t.w1 * p1);
     }
     float part = 0.0f;
-    for (int is = lo; is <= hi; ++is) {
-        const float d = fabsf(mf - static_cast<float>(is - mi));
+    for (int is = t.lo; is <= t.hi; ++is) {
+        const float d = fabsf(t.mf - static_cast<float>(is - t.mi));
         part = fmaf(fmaf(-d, inv, 1.0f), __ldg(row + is), part);
     }
     return part;
-}
-
-__device__ __forceinline__ float2 lds_pair(unsigned addr)
-{
-    float2 v;
-    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
-    return v;
 }
 
 // Per-view constants of the adjoint, from the caller's grad-prep tables.
@@ -682,6 +704,13 @@ struct AdjView {
     float w;       // view weight
     int ux;        // lines are rows
     int two;       // |offset| <= 1
+};
+
+// Channel window of one (view, tile): pairs lo .. lo + width - 1 are staged;
+// width 0 = the view takes the exact path on this tile.
+struct AdjWin {
+    int lo;
+    int width;
 };
 
 // One pass over the grad-prep tables per call: the 32.32 fixed-point begin of
@@ -709,150 +738,284 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-__global__ void __launch_bounds__(256, 3)
-    fp_adj_f32(const float* __restrict__ proj, float* __restrict__ img, const long long* __restrict__ B,
-               const AdjView* __restrict__ V, const double* __restrict__ pos, const FpConst c)
+// The channel window of every (view, tile).  For a fixed line the position is
+// linear in `along`, so over a tile it spans [B_l + min(a0, a1), B_l + max(a0,
+// a1)], a0 and a1 the offsets of the tile's first and last along index; over
+// the tile's lines that is [Bmin + min(a0, a1), Bmax + max(a0, a1)], Bmin and
+// Bmax the extremes of the line positions of the tile's band (a row band of
+// row-marching views, else a column band; lines past the image repeat the last
+// one, as the gather's line positions do).  One warp per (view, band): the
+// band's extremes, then the window of each tile of the band.  Windows are
+// shared by every image of the batch.
+__global__ void __launch_bounds__(256)
+    fp_adj_windows(const long long* __restrict__ B, const AdjView* __restrict__ V,
+                   AdjWin* __restrict__ W, int na, int n, int tiles_x, int tiles_y, int ty, int win)
 {
-    __shared__ long long s_base[kFaViews][kFaLines];
-    __shared__ AdjView s_v[kFaViews];
-    __shared__ int s_lo[kFaViews], s_hi[kFaViews];
-    __shared__ __align__(16) float2 s_pair[kFaViews][kFaWin];
-
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int tx0 = blockIdx.x * kFaTileX, ty0 = blockIdx.y * kFaTileY;
-    const int ix = tx0 + lane;
-    const float* P = proj + blockIdx.z * c.proj_stride;
-    float acc[kFaRows];
+    const int nbmax = max(tiles_x, tiles_y);
+    const long long wid = (static_cast<long long>(blockIdx.x) * 256 + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (wid >= static_cast<long long>(na) * nbmax) return;  // warp-uniform
+    const int ia = static_cast<int>(wid / nbmax), band = static_cast<int>(wid - static_cast<long long>(ia) * nbmax);
+    const AdjView v = V[ia];
+    if (band >= (v.ux ? tiles_y : tiles_x)) return;  // warp-uniform
+    const int lines = v.ux ? ty : kFaTileX;
+    long long bmin = LLONG_MAX, bmax = LLONG_MIN;
+    for (int l = lane; l < lines; l += 32) {
+        const long long b = __ldg(B + static_cast<size_t>(ia) * n + min(band * lines + l, n - 1));
+        bmin = b < bmin ? b : bmin;
+        bmax = b > bmax ? b : bmax;
+    }
 #pragma unroll
-    for (int r = 0; r < kFaRows; ++r) acc[r] = 0.0f;
+    for (int o = 16; o > 0; o >>= 1) {
+        const long long x = __shfl_xor_sync(0xffffffffu, bmin, o);
+        const long long y = __shfl_xor_sync(0xffffffffu, bmax, o);
+        bmin = x < bmin ? x : bmin;
+        bmax = y > bmax ? y : bmax;
+    }
+    const int ntiles = tiles_x * tiles_y;
+    const int alen = v.ux ? kFaTileX : ty;
+    const int count = v.ux ? tiles_x : tiles_y;
+    for (int k = lane; k < count; k += 32) {
+        const long long a0 = static_cast<long long>(k * alen) * v.O1;
+        const long long a1 = a0 + static_cast<long long>(alen - 1) * v.O1;
+        const int lo = static_cast<int>((bmin + (a0 < a1 ? a0 : a1)) >> 32);
+        const int hi = static_cast<int>((bmax + (a0 < a1 ? a1 : a0)) >> 32);
+        const int t = v.ux ? band * tiles_x + k : k * tiles_x + band;
+        const long long width = static_cast<long long>(hi) - lo + 1;
+        W[static_cast<size_t>(ia) * ntiles + t] = AdjWin{lo, v.two && width <= win ? static_cast<int>(width) : 0};
+    }
+}
+
+// One staged pixel-view of IMG images: pair entry at `a` holds (w p[m], w p[m+1])
+// of each image, m = floor(MID).
+template <int IMG, int ROWS>
+__device__ __forceinline__ void adj_tap_staged(float (&blk)[IMG][ROWS], int r, long long MID, unsigned pb,
+                                               float inv, float inv1)
+{
+    const float mf = frac_of(MID);
+    const float w0 = __saturatef(fmaf(-mf, inv, 1.0f));
+    const float w1 = __saturatef(fmaf(mf, inv, inv1));
+    const unsigned a = pb + 8u * IMG * static_cast<unsigned>(MID >> 32);
+    if constexpr (IMG == 1) {
+        float2 p;
+        asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(p.x), "=f"(p.y) : "r"(a));
+        blk[0][r] = fmaf(w0, p.x, fmaf(w1, p.y, blk[0][r]));
+    } else {
+#pragma unroll
+        for (int h = 0; h < IMG / 2; ++h) {
+            float4 p;
+            asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                         : "=f"(p.x), "=f"(p.y), "=f"(p.z), "=f"(p.w)
+                         : "r"(a + 16u * h));
+            blk[2 * h][r] = fmaf(w0, p.x, fmaf(w1, p.y, blk[2 * h][r]));
+            blk[2 * h + 1][r] = fmaf(w0, p.z, fmaf(w1, p.w, blk[2 * h + 1][r]));
+        }
+    }
+}
+
+// The gather: CTA = one 32 x 8*ROWS tile of IMG images and one segment of
+// seg_len views: blockIdx.z = group * segs + segment, images img0 + group*IMG ...
+// With one segment it writes the images; with several, segment s writes its
+// partial sums to part[s][image] for fp_adj_reduce.  Per block of kFaViews views: one phase loads the tile's line positions and
+// the windows' pairs (all loads in flight), one barrier, compute, one barrier;
+// the next block's view constants and windows are copied (cp.async) during
+// the compute into the other half of s_v / s_w.
+template <int ROWS, int IMG>
+__global__ void __launch_bounds__(256, ROWS * IMG >= 32 ? 2 : 3)
+    fp_adj_f32(const float* __restrict__ proj, float* __restrict__ img, const long long* __restrict__ B,
+               const AdjView* __restrict__ V, const AdjWin* __restrict__ W, const double* __restrict__ pos,
+               const FpConst c, int img0, int segs, int seg_len, float* __restrict__ part, int batch)
+{
+    using S = FaShape<ROWS>;
+    constexpr int TY = S::TY, LINES = S::LINES, WIN = S::WIN;
+    static_assert(IMG == 1 || IMG == 2 || IMG == 4, "images per CTA");
+    __shared__ long long s_base[kFaViews][LINES];
+    __shared__ AdjView s_v[2][kFaViews];
+    __shared__ AdjWin s_w[2][kFaViews];
+    extern __shared__ __align__(16) float s_pair_dyn[];  // [kFaViews][WIN][2 * IMG]
+    float(*s_pair)[WIN][2 * IMG] = reinterpret_cast<float(*)[WIN][2 * IMG]>(s_pair_dyn);
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tx0 = blockIdx.x * kFaTileX, ty0 = blockIdx.y * TY;
+    const int ix = tx0 + lane;
+    const int ntiles = gridDim.x * gridDim.y, tile = blockIdx.y * gridDim.x + blockIdx.x;
+    const int seg = blockIdx.z % segs, im = img0 + (blockIdx.z / segs) * IMG;
+    const int vb = seg * seg_len, ve = min(c.na, vb + seg_len);
+    const float* P = proj + static_cast<size_t>(im) * c.proj_stride;
     const int n = c.nx;  // == ny
     const int ns = c.ns;
-
-    for (int v0 = 0; v0 < c.na; v0 += kFaViews) {
-        const int nv = min(kFaViews, c.na - v0);
-        if (threadIdx.x < nv) {
-            s_v[threadIdx.x] = V[v0 + threadIdx.x];
-            s_lo[threadIdx.x] = INT_MAX;
-            s_hi[threadIdx.x] = INT_MIN;
-        }
-        __syncthreads();
-        // line positions of the tile (rows for row-marching views, else
-        // columns) and the tile's channel range: for a fixed line the position
-        // is linear in `along`, extreme at the tile's first and last along index.
-        // Fixed trip count: every load of the block is in flight at once.
+    float acc[IMG][ROWS];
 #pragma unroll
-        for (int it = 0; it < kFaViews * kFaLines / 256; ++it) {
-            const int idx = it * 256 + threadIdx.x;
-            const int j = idx / kFaLines, l = idx - j * kFaLines;  // a warp's lanes share j
-            int lo = INT_MAX, hi = INT_MIN;
+    for (int i = 0; i < IMG; ++i)
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) acc[i][r] = 0.0f;
+
+    if (tid < min(kFaViews, ve - vb)) {
+        s_v[0][tid] = V[vb + tid];
+        s_w[0][tid] = W[static_cast<size_t>(vb + tid) * ntiles + tile];
+    }
+    __syncthreads();
+    int buf = 0;
+    for (int v0 = vb; v0 < ve; v0 += kFaViews, buf ^= 1) {
+        const int nv = min(kFaViews, ve - v0);
+        // the next block's view constants and windows, copied during this
+        // block into the other half of s_v / s_w (last read before this
+        // block's first barrier)
+        const int vn = v0 + kFaViews + tid;
+        if (tid < kFaViews && vn < ve) {
+            static_assert(sizeof(AdjView) == 24 && sizeof(AdjWin) == 8, "8-byte copies");
+            const unsigned dv = smem_u32(&s_v[buf ^ 1][tid]);
+            const char* sv = reinterpret_cast<const char*>(V + vn);
+            cp_async8(dv, sv);
+            cp_async8(dv + 8, sv + 8);
+            cp_async8(dv + 16, sv + 16);
+            cp_async8(smem_u32(&s_w[buf ^ 1][tid]), W + static_cast<size_t>(vn) * ntiles + tile);
+        }
+        // line positions of the tile: rows for row-marching views, else columns
+#pragma unroll
+        for (int it = 0; it < kFaViews * LINES / 256; ++it) {
+            const int idx = it * 256 + tid;
+            const int j = idx / LINES, l = idx - j * LINES;
             if (j < nv) {
-                const AdjView& v = s_v[j];
-                if (l < (v.ux ? kFaTileY : kFaTileX)) {
-                    const int lin = min((v.ux ? ty0 : tx0) + l, n - 1);
-                    const long long b = __ldg(B + static_cast<size_t>(v0 + j) * n + lin);
-                    s_base[j][l] = b;
-                    const long long m0 = b + static_cast<long long>(v.ux ? tx0 : ty0) * v.O1;
-                    const long long m1 = m0 + static_cast<long long>((v.ux ? kFaTileX : kFaTileY) - 1) * v.O1;
-                    lo = static_cast<int>((m0 < m1 ? m0 : m1) >> 32);
-                    hi = static_cast<int>((m0 < m1 ? m1 : m0) >> 32);
+                const int ux = s_v[buf][j].ux;
+                if (l < (ux ? TY : kFaTileX))
+                    s_base[j][l] = __ldg(B + static_cast<size_t>(v0 + j) * n + min((ux ? ty0 : tx0) + l, n - 1));
+            }
+        }
+        // staged windows: (w p[lo+k], w p[lo+k+1]) per image, zero off the detector
+#pragma unroll
+        for (int it = 0; it < kFaViews * WIN / 256; ++it) {
+            const int idx = it * 256 + tid;
+            const int j = idx / WIN, k = idx - j * WIN;
+            if (j < nv && k < s_w[buf][j].width) {
+                const float w = s_v[buf][j].w;
+                const int g = s_w[buf][j].lo + k;
+                const bool in0 = static_cast<unsigned>(g) < static_cast<unsigned>(ns);
+                const bool in1 = static_cast<unsigned>(g + 1) < static_cast<unsigned>(ns);
+                const float* row = P + static_cast<size_t>(v0 + j) * ns;
+                float e[2 * IMG];
+#pragma unroll
+                for (int i = 0; i < IMG; ++i) {
+                    e[2 * i] = in0 ? __ldg(row + i * c.proj_stride + g) * w : 0.0f;
+                    e[2 * i + 1] = in1 ? __ldg(row + i * c.proj_stride + g + 1) * w : 0.0f;
+                }
+                if constexpr (IMG == 1) {
+                    *reinterpret_cast<float2*>(&s_pair[j][k][0]) = make_float2(e[0], e[1]);
+                } else {
+#pragma unroll
+                    for (int h = 0; h < IMG / 2; ++h)
+                        *reinterpret_cast<float4*>(&s_pair[j][k][4 * h]) =
+                            make_float4(e[4 * h], e[4 * h + 1], e[4 * h + 2], e[4 * h + 3]);
                 }
             }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-                hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-            }
-            if ((threadIdx.x & 31) == 0 && lo <= hi) {
-                atomicMin(&s_lo[j], lo);
-                atomicMax(&s_hi[j], hi);
-            }
         }
         __syncthreads();
-        // staged windows: (p[lo+k], p[lo+k+1]), zero off the detector
+        float blk[IMG][ROWS];  // this view block's partial sums (blocked summation)
 #pragma unroll
-        for (int it = 0; it < kFaViews * kFaWin / 256; ++it) {
-            const int idx = it * 256 + threadIdx.x;
-            const int j = idx / kFaWin, k = idx - j * kFaWin;
-            if (j < nv && s_v[j].two && s_hi[j] - s_lo[j] + 2 <= kFaWin) {
-                const float* row = P + static_cast<size_t>(v0 + j) * ns;
-                const int g = s_lo[j] + k;
-                const float p0 = static_cast<unsigned>(g) < static_cast<unsigned>(ns) ? __ldg(row + g) : 0.0f;
-                const float p1 = static_cast<unsigned>(g + 1) < static_cast<unsigned>(ns) ? __ldg(row + g + 1) : 0.0f;
-                s_pair[j][k] = make_float2(p0, p1);
-            }
-        }
-        __syncthreads();
-        float blk[kFaRows];  // this view block's partial sums (blocked summation)
+        for (int i = 0; i < IMG; ++i)
 #pragma unroll
-        for (int r = 0; r < kFaRows; ++r) blk[r] = 0.0f;
+            for (int r = 0; r < ROWS; ++r) blk[i][r] = 0.0f;
         for (int j = 0; j < nv; ++j) {
-            const AdjView v = s_v[j];
-            const int lo = s_lo[j];
-            if (v.two && s_hi[j] - lo + 2 <= kFaWin) {
+            const AdjView v = s_v[buf][j];
+            const AdjWin wn = s_w[buf][j];
+            if (wn.width > 0) {
                 const float inv1 = 1.0f - v.inv;
-                const unsigned pb = smem_u32(&s_pair[j][0]) - 8u * static_cast<unsigned>(lo);
+                const unsigned pb = smem_u32(&s_pair[j][0][0]) - 8u * IMG * static_cast<unsigned>(wn.lo);
                 if (v.ux) {  // along = ix, line = row
                     const long long A = static_cast<long long>(ix) * v.O1;
 #pragma unroll
-                    for (int r = 0; r < kFaRows; ++r) {
-                        const long long MID = s_base[j][warp * kFaRows + r] + A;
-                        const float mf = frac_of(MID);
-                        const float2 pv = lds_pair(pb + 8u * static_cast<unsigned>(MID >> 32));
-                        const float w0 = __saturatef(fmaf(-mf, v.inv, 1.0f));
-                        const float w1 = __saturatef(fmaf(mf, v.inv, inv1));
-                        blk[r] = fmaf(fmaf(w0, pv.x, w1 * pv.y), v.w, blk[r]);
-                    }
-                } else {   // along = row, line = ix
-                    long long MID = s_base[j][lane] + static_cast<long long>(ty0 + warp * kFaRows) * v.O1;
+                    for (int r = 0; r < ROWS; ++r)
+                        adj_tap_staged<IMG, ROWS>(blk, r, s_base[j][warp * ROWS + r] + A, pb, v.inv, inv1);
+                } else {     // along = row, line = ix
+                    long long MID = s_base[j][lane] + static_cast<long long>(ty0 + warp * ROWS) * v.O1;
 #pragma unroll
-                    for (int r = 0; r < kFaRows; ++r) {
-                        const float mf = frac_of(MID);
-                        const float2 pv = lds_pair(pb + 8u * static_cast<unsigned>(MID >> 32));
-                        const float w0 = __saturatef(fmaf(-mf, v.inv, 1.0f));
-                        const float w1 = __saturatef(fmaf(mf, v.inv, inv1));
-                        blk[r] = fmaf(fmaf(w0, pv.x, w1 * pv.y), v.w, blk[r]);
+                    for (int r = 0; r < ROWS; ++r) {
+                        adj_tap_staged<IMG, ROWS>(blk, r, MID, pb, v.inv, inv1);
                         MID += v.O1;
                     }
                 }
             } else {
-                const float* row = P + static_cast<size_t>(v0 + j) * ns;
 #pragma unroll
-                for (int r = 0; r < kFaRows; ++r) {
-                    const int iy = ty0 + warp * kFaRows + r;
+                for (int r = 0; r < ROWS; ++r) {
+                    const int iy = ty0 + warp * ROWS + r;
                     const int along = v.ux ? ix : iy;
                     const int lin = v.ux ? iy : ix;
-                    const long long MID = s_base[j][v.ux ? warp * kFaRows + r : lane] +
+                    const long long MID = s_base[j][v.ux ? warp * ROWS + r : lane] +
                                           static_cast<long long>(along) * v.O1;
                     const double* pp = pos + (static_cast<size_t>(v0 + j) * n + min(lin, n - 1)) * 2;
-                    blk[r] = fmaf(adj_tap_exact(row, MID, v.O1, v.inv, v.two != 0, along, n, ns, pp), v.w,
-                                  blk[r]);
+                    const AdjTap t = adj_tap_plan(MID, v.O1, v.inv, v.two != 0, along, n, ns, pp);
+#pragma unroll
+                    for (int i = 0; i < IMG; ++i) {
+                        const float* row = P + i * c.proj_stride + static_cast<size_t>(v0 + j) * ns;
+                        blk[i][r] = fmaf(adj_tap_apply(row, t, v.inv, ns), v.w, blk[i][r]);
+                    }
                 }
             }
         }
 #pragma unroll
-        for (int r = 0; r < kFaRows; ++r) acc[r] += blk[r];
+        for (int i = 0; i < IMG; ++i)
+#pragma unroll
+            for (int r = 0; r < ROWS; ++r) acc[i][r] += blk[i][r];
+        cp_async_wait_all();
         __syncthreads();
     }
-    float* O = img + blockIdx.z * c.img_stride;
 #pragma unroll
-    for (int r = 0; r < kFaRows; ++r) {
-        const int iy = ty0 + warp * kFaRows + r;
-        if (ix < c.nx && iy < c.ny) O[static_cast<size_t>(iy) * c.nx + ix] = acc[r];
+    for (int i = 0; i < IMG; ++i) {
+        float* O = segs == 1 ? img + static_cast<size_t>(im + i) * c.img_stride
+                             : part + (static_cast<size_t>(seg) * batch + im + i) * c.img_stride;
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) {
+            const int iy = ty0 + warp * ROWS + r;
+            if (ix < c.nx && iy < c.ny) O[static_cast<size_t>(iy) * c.nx + ix] = acc[i][r];
+        }
+    }
+}
+
+// Sum of the segments' partial images in segment order: img[e] = part[0][e] +
+// part[1][e] + ..., `count` = floats of the batch, as float4 when `vec`.
+__global__ void __launch_bounds__(256)
+    fp_adj_reduce(const float* __restrict__ part, float* __restrict__ img, size_t count, int segs, bool vec)
+{
+    const size_t stride = static_cast<size_t>(gridDim.x) * 256;
+    if (vec) {
+        const float4* P4 = reinterpret_cast<const float4*>(part);
+        float4* O4 = reinterpret_cast<float4*>(img);
+        const size_t n4 = count / 4;
+        for (size_t e = blockIdx.x * 256ull + threadIdx.x; e < n4; e += stride) {
+            float4 a = P4[e];
+            for (int s = 1; s < segs; ++s) {
+                const float4 b = P4[s * n4 + e];
+                a.x += b.x;
+                a.y += b.y;
+                a.z += b.z;
+                a.w += b.w;
+            }
+            O4[e] = a;
+        }
+    } else {
+        for (size_t e = blockIdx.x * 256ull + threadIdx.x; e < count; e += stride) {
+            float a = part[e];
+            for (int s = 1; s < segs; ++s) a += part[s * count + e];
+            img[e] = a;
+        }
     }
 }
 
 // The 4n - 4 border pixels, exactly, overwriting fp_adj_f32's values: one
-// warp per pixel, lane l summing views l, l+32, ..., then a fixed shuffle tree.
+// 128-thread block per pixel and up to kFbImg images (blockIdx.y*kFbImg ..).
+// Thread t sums views t, t+128, ... of each image (the taps of a view are
+// planned once for all images), then a fixed tree: a shuffle tree per warp,
+// the four warps in order.
+constexpr int kFbImg = 8;
 __global__ void __launch_bounds__(128)
     fp_adj_border_f32(const float* __restrict__ proj, float* __restrict__ img,
                       const long long* __restrict__ B, const AdjView* __restrict__ V,
-                      const double* __restrict__ pos, const FpConst c)
+                      const double* __restrict__ pos, const FpConst c, int batch)
 {
+    __shared__ float s_part[4][kFbImg];
     const int n = c.nx, ns = c.ns;
-    const int nb = n == 1 ? 1 : 4 * n - 4;
-    const int lane = threadIdx.x & 31;
-    const int b = blockIdx.x * 4 + (threadIdx.x >> 5);
-    if (b >= nb) return;  // warp-uniform
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int b = blockIdx.x;
     int ix, iy;
     if (b < n) {
         ix = b;
@@ -867,20 +1030,49 @@ __global__ void __launch_bounds__(128)
         ix = n - 1;
         iy = b - 3 * n + 3;
     }
-    const float* P = proj + blockIdx.y * c.proj_stride;
-    float acc = 0.0f;
-    for (int ia = lane; ia < c.na; ia += 32) {
+    const int im0 = blockIdx.y * kFbImg;
+    const int cnt = min(kFbImg, batch - im0);
+    const float* P = proj + static_cast<size_t>(im0) * c.proj_stride;
+    float acc[kFbImg];
+#pragma unroll
+    for (int i = 0; i < kFbImg; ++i) acc[i] = 0.0f;
+    for (int ia = threadIdx.x; ia < c.na; ia += 128) {
         const AdjView v = V[ia];
         const int along = v.ux ? ix : iy, lin = v.ux ? iy : ix;
         const size_t line = static_cast<size_t>(ia) * n + lin;
         const long long MID = __ldg(B + line) + static_cast<long long>(along) * v.O1;
-        const float part = adj_tap_exact(P + static_cast<size_t>(ia) * ns, MID, v.O1, v.inv, v.two != 0,
-                                         along, n, ns, pos + line * 2);
-        acc = fmaf(part, v.w, acc);
+        const AdjTap t = adj_tap_plan(MID, v.O1, v.inv, v.two != 0, along, n, ns, pos + line * 2);
+        const float* row = P + static_cast<size_t>(ia) * ns;
+        if (t.two) {  // every image's two loads issued before the first FMA
+            const bool in0 = static_cast<unsigned>(t.mi) < static_cast<unsigned>(ns);
+            const bool in1 = static_cast<unsigned>(t.mi + 1) < static_cast<unsigned>(ns);
+            float p0[kFbImg], p1[kFbImg];
+#pragma unroll
+            for (int i = 0; i < kFbImg; ++i) {
+                const float* r = row + i * c.proj_stride;
+                p0[i] = i < cnt && in0 ? __ldg(r + t.mi) : 0.0f;
+                p1[i] = i < cnt && in1 ? __ldg(r + t.mi + 1) : 0.0f;
+            }
+#pragma unroll
+            for (int i = 0; i < kFbImg; ++i) acc[i] = fmaf(fmaf(t.w0, p0[i], t.w1 * p1[i]), v.w, acc[i]);
+        } else {
+#pragma unroll
+            for (int i = 0; i < kFbImg; ++i)
+                if (i < cnt) acc[i] = fmaf(adj_tap_apply(row + i * c.proj_stride, t, v.inv, ns), v.w, acc[i]);
+        }
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) img[blockIdx.y * c.img_stride + static_cast<size_t>(iy) * n + ix] = acc;
+    for (int i = 0; i < kFbImg; ++i) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], o);
+        if (lane == 0) s_part[warp][i] = acc[i];
+    }
+    __syncthreads();
+    if (threadIdx.x < cnt) {
+        const int i = threadIdx.x;
+        const float sum = ((s_part[0][i] + s_part[1][i]) + s_part[2][i]) + s_part[3][i];
+        img[static_cast<size_t>(im0 + i) * c.img_stride + static_cast<size_t>(iy) * n + ix] = sum;
+    }
 }
 
 constexpr int kFp64Threads = 128;
@@ -1118,6 +1310,29 @@ int fp_forward(const ctr_par_param* p, const T* img, T* proj, const double* sc,
     return check_launch("fp_par_2d");
 }
 
+// The gather over a batch: CTAs of IMG images, the batch's remainder one image per CTA.
+template <int ROWS, int IMG>
+void fp_adj_launch(const float* proj, float* img, const long long* B, const AdjView* V, const AdjWin* W,
+                   const double* pos, const FpConst& c, int tiles_x, int tiles_y, int batch, int segs,
+                   int seg_len, float* part, cudaStream_t stream)
+{
+    constexpr size_t smem = sizeof(float) * kFaViews * FaShape<ROWS>::WIN * 2 * IMG;
+    constexpr size_t smem1 = sizeof(float) * kFaViews * FaShape<ROWS>::WIN * 2;
+    if (smem > 48 * 1024)  // above the default limit (set per call: the current device's)
+        cudaFuncSetAttribute(fp_adj_f32<ROWS, IMG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(smem));
+    const int groups = batch / IMG, zmax = 65535 / segs;  // grid z = groups x segments
+    for (int g0 = 0; g0 < groups; g0 += zmax)
+        fp_adj_f32<ROWS, IMG><<<dim3(tiles_x, tiles_y, std::min(zmax, groups - g0) * segs), 256, smem, stream>>>(
+            proj, img, B, V, W, pos, c, g0 * IMG, segs, seg_len, part, batch);
+    if constexpr (IMG > 1) {
+        const int rest = batch - groups * IMG;
+        if (rest > 0)
+            fp_adj_f32<ROWS, 1><<<dim3(tiles_x, tiles_y, rest * segs), 256, smem1, stream>>>(
+                proj, img, B, V, W, pos, c, groups * IMG, segs, seg_len, part, batch);
+    }
+}
+
 template <typename T>
 int fp_adjoint(const ctr_par_param* p, const T* proj, T* img, const double* w,
                const double* pos, const int* usex, int batch, cudaStream_t stream)
@@ -1126,19 +1341,51 @@ int fp_adjoint(const ctr_par_param* p, const T* proj, T* img, const double* w,
     if (st) return st;
     if constexpr (sizeof(T) == 4) {
         FpConst c = fp_const(p);
-        // fixed-point tables of the call (int64 per (view, line), AdjView per view)
+        // 32 x 64 tiles, two images per CTA (measured against 32 x 32 tiles
+        // and one or four images per CTA at 512^2 x 720 views, batch 1 and 16)
+        constexpr int kRows = 8, kImg = 2;
+        const int ty = FaShape<kRows>::TY, win = FaShape<kRows>::WIN;
+        const int tiles_x = div_up(p->nx, kFaTileX), tiles_y = div_up(p->ny, ty);
+        const size_t ntiles = static_cast<size_t>(tiles_x) * tiles_y;
+        // View segments per tile: enough CTAs for one image to fill the GPU
+        // (3 per SM).  A function of the geometry and device only, so an image's
+        // sums are the same in any batch.
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        int segs = static_cast<int>(std::max<size_t>(1, std::min<size_t>(8, 3ull * sms / ntiles)));
+        const int seg_len = div_up(div_up(static_cast<int>(p->na), segs), kFaViews) * kFaViews;
+        segs = div_up(static_cast<int>(p->na), seg_len);
+        // tables of the call: fixed-point begin per (view, line), AdjView per
+        // view, AdjWin per (view, tile); the segments' partial images
         const size_t nb = sizeof(long long) * p->na * static_cast<size_t>(p->nx);
+        const size_t nv = sizeof(AdjView) * p->na;
+        const size_t nw = sizeof(AdjWin) * p->na * ntiles;
+        const size_t part_at = (nb + nv + nw + 255) / 256 * 256;
+        const size_t npart = segs > 1 ? sizeof(float) * segs * batch * c.img_stride : 0;
         void* scratch = nullptr;
-        cudaError_t e = cudaMallocAsync(&scratch, nb + sizeof(AdjView) * p->na, stream);
+        cudaError_t e = cudaMallocAsync(&scratch, part_at + npart, stream);
         if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp_par_2d_grad scratch: %s", cudaGetErrorString(e));
         long long* B = static_cast<long long*>(scratch);
         AdjView* V = reinterpret_cast<AdjView*>(static_cast<char*>(scratch) + nb);
+        AdjWin* W = reinterpret_cast<AdjWin*>(static_cast<char*>(scratch) + nb + nv);
+        float* part = segs > 1 ? reinterpret_cast<float*>(static_cast<char*>(scratch) + part_at) : nullptr;
         fp_adj_prep<<<div_up(static_cast<unsigned long long>(p->na) * p->nx, 256), 256, 0, stream>>>(
             w, pos, usex, B, V, p->na, p->nx);
-        dim3 grid(div_up(p->nx, kFaTileX), div_up(p->ny, kFaTileY), batch);
-        fp_adj_f32<<<grid, 256, 0, stream>>>(proj, img, B, V, pos, c);
+        fp_adj_windows<<<div_up(static_cast<unsigned long long>(p->na) * std::max(tiles_x, tiles_y) * 32, 256),
+                         256, 0, stream>>>(B, V, W, p->na, p->nx, tiles_x, tiles_y, ty, win);
+        fp_adj_launch<kRows, kImg>(proj, img, B, V, W, pos, c, tiles_x, tiles_y, batch, segs, seg_len, part,
+                                   stream);
+        if (segs > 1) {
+            const size_t count = static_cast<size_t>(batch) * c.img_stride;
+            const bool vec = count % 4 == 0 && reinterpret_cast<uintptr_t>(img) % 16 == 0;
+            const unsigned blocks = static_cast<unsigned>(
+                std::min<size_t>(div_up(vec ? count / 4 : count, 256), 8ull * sms));
+            fp_adj_reduce<<<blocks, 256, 0, stream>>>(part, img, count, segs, vec);
+        }
         const unsigned nborder = p->nx == 1 ? 1u : 4u * p->nx - 4u;
-        fp_adj_border_f32<<<dim3(div_up(nborder, 4), batch), 128, 0, stream>>>(proj, img, B, V, pos, c);
+        fp_adj_border_f32<<<dim3(nborder, div_up(batch, kFbImg)), 128, 0, stream>>>(proj, img, B, V, pos, c,
+                                                                                  batch);
         cudaFreeAsync(scratch, stream);  // after every kernel that reads the tables
     } else {
         dim3 grid(div_up(p->nx, 32), div_up(p->ny, 8), batch);

@@ -179,6 +179,25 @@ def test_parallel_config2(oracle_port):
     assert rel_l2(rec, rec64) <= 1e-4
 
 
+def test_fp_adjoint_config2_batch(oracle_port):
+    """The FP adjoint at 512^2 x 720 views x 729 bins: against the oracle, and a
+    batch of 7 (image groups of the gather plus a remainder) equal to its items."""
+    from oracle import Geom
+    from ct_recon_extensions_gb300 import synthetic as syn
+    d = syn.parallel_config_2()
+    g = Geom.make(**d)
+    rng = np.random.default_rng(11)
+    sino = fp_op(d).forward(cuda(syn.rasterize(syn.random_ellipses(2100), 512, 512, 0.5, 0.5)))
+    stack = np.concatenate([host(sino)[None],
+                            rng.standard_normal((6, d["na"], d["ns"])).astype(np.float32)])
+    op = fp_op(d)
+    out = host(op.adjoint(cuda(stack)))
+    assert rel_l2(out[0], oracle_port.fp_par_2d_grad(stack[0], g)) <= 1e-5
+    assert rel_l2(out[3], oracle_port.fp_par_2d_grad(stack[3], g)) <= 1e-5
+    for i in range(7):
+        assert np.array_equal(out[i], host(op.adjoint(cuda(stack[i]))))
+
+
 def test_fp_adjoint_config2_dot():
     from ct_recon_extensions_gb300 import synthetic as syn
     d = syn.parallel_config_2()
