@@ -8,8 +8,10 @@
 // detector channels the tile can project into (for a fan the angular extent
 // of a convex tile seen from the source is reached at its corners; for a
 // parallel beam the projection is affine), and stages that window into
-// shared memory as (p[i], p[i+1]-p[i]) pairs, zero outside the detector.  A
-// pixel-view update is then: channel position, floor/fraction, one 8-byte
+// shared memory as pairs, zero outside the detector: (p[k] - k d[k], d[k]),
+// d[k] = p[k+1] - p[k], k the channel less the window start, in the TMA-fed
+// kernels, (p[k], d[k]) in the plain one.  A pixel-view update is then:
+// channel position (relative to the window start), its floor, one 8-byte
 // shared load and one FMA for the interpolation.  The window length W is a
 // host-side bound over all tiles and views; a kernel that meets a wider
 // window raises kFlagWindowOverflow and clamps (never reads out of bounds).
@@ -85,15 +87,16 @@ __global__ void __launch_bounds__(kBpThreads, 2)
             const ViewP P = views[v0 + j];
             float* aj = accw + j * c.W;
             if (mode_fast(P.mode)) {
+                const float cen = c.cents - static_cast<float>(P.lo);
                 float xs, xc;
-                fast_xs<G>(x, P.vp, c, &xs, &xc);
+                fast_xs<G>(x, P.vp, cen, c, &xs, &xc);
 #pragma unroll
                 for (int r = 0; r < kRowsPerThread; ++r) {
                     float w;
-                    const float s = fast_s<G>(xs, xc, y[r], P.vp, c, &w);
+                    const float s = fast_s<G>(xs, xc, y[r], P.vp, cen, c, &w);  // s - lo
                     const float v = s + kMagicHalf;
                     const float u = s - (v - kMagic);
-                    const int k = static_cast<int>(__float_as_uint(v) - kMagicBits) - P.lo;
+                    const int k = static_cast<int>(__float_as_uint(v) - kMagicBits);
                     const float t = val[r] * w;
                     if (t != 0.0f) {
                         atomicAdd(aj + k, t - t * u);

