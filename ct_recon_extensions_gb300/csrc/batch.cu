@@ -213,7 +213,7 @@ int build_config(ctr_fbp_plan* P, int ci, int sm_count)
         for (int t = 0; t < it.tiles_x * tiles_y; ++t) work.push_back({cost, make_int2(i, t)});
         smem = std::max(smem, 128 + 2 * static_cast<size_t>(bv) * it.c.WS * sizeof(float) +
                                   2 * static_cast<size_t>(bv) * it.c.W * sizeof(float2) +
-                                  static_cast<size_t>(g.na) * sizeof(ViewP));
+                                  static_cast<size_t>(g.na) * sizeof(ViewT<Geo::kFan>));
     }
     // longest first; ties keep item order (tiles of one item stay together)
     std::stable_sort(work.begin(), work.end(),

@@ -48,8 +48,8 @@ __global__ void __launch_bounds__(kBpThreads, 2)
                     const double* __restrict__ t0, const double* __restrict__ t1,
                     const double* __restrict__ t2, const TileConst c)
 {
-    extern __shared__ __align__(16) float accw[];  // [kViewBlock][W], then ViewP[na]
-    ViewP* views = reinterpret_cast<ViewP*>(accw + (kViewBlock * c.W + 3) / 4 * 4);
+    extern __shared__ __align__(16) float accw[];  // [kViewBlock][W], then ViewT<G>[na]
+    ViewT<G>* views = reinterpret_cast<ViewT<G>*>(accw + (kViewBlock * c.W + 3) / 4 * 4);
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tx0 = blockIdx.x * kTileX, ty0 = blockIdx.y * kTileY;
@@ -84,16 +84,16 @@ __global__ void __launch_bounds__(kBpThreads, 2)
         for (int idx = threadIdx.x; idx < nv * c.W; idx += kBpThreads) accw[idx] = 0.0f;
         __syncthreads();
         for (int j = 0; j < nv; ++j) {
-            const ViewP P = views[v0 + j];
+            const ViewT<G> P = views[v0 + j];
             float* aj = accw + j * c.W;
             if (mode_fast(P.mode)) {
-                const float cen = c.cents - static_cast<float>(P.lo);
+                const float cen = view_cen<G>(P, c);
                 float xs, xc;
-                fast_xs<G>(x, P.vp, cen, c, &xs, &xc);
+                fast_xs<G>(fast_coord<G>(x, cx0), P.vp, cen, c, &xs, &xc);
 #pragma unroll
                 for (int r = 0; r < kRowsPerThread; ++r) {
                     float w;
-                    const float s = fast_s<G>(xs, xc, y[r], P.vp, cen, c, &w);  // s - lo
+                    const float s = fast_s<G>(xs, xc, fast_coord<G>(y[r], cy0), P.vp, cen, c, &w);  // s - lo
                     const float v = s + kMagicHalf;
                     const float u = s - (v - kMagic);
                     const int k = static_cast<int>(__float_as_uint(v) - kMagicBits);
@@ -308,7 +308,7 @@ int launch_tile(K kern, int W, dim3 grid, cudaStream_t stream, const char* what,
                 const double* sincos, const TileConst& c, bool adjoint)
 {
     size_t smem = static_cast<size_t>(kViewBlock) * W * (adjoint ? sizeof(float) : sizeof(float2));
-    if (adjoint) smem = (static_cast<size_t>(kViewBlock) * W + 3) / 4 * 4 * sizeof(float) + c.na * sizeof(ViewP);
+    if (adjoint) smem = (static_cast<size_t>(kViewBlock) * W + 3) / 4 * 4 * sizeof(float) + c.na * kViewBytesMax;
     if (smem > 160 * 1024) return fail(CTR_ERR_UNSUPPORTED, "%s: window of %d channels too wide", what, W);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
@@ -331,10 +331,11 @@ constexpr int kFwdTileY = (kBpThreads / 32) * kFwdRows;
 constexpr size_t kFwdSmemMax = 200 * 1024;
 
 // Shared bytes of the bulk-copy forward kernel with NG groups of VB views.
+template <Geo G>
 inline size_t fwd_smem(const TileConst& ct, int VB, int NG = kGroups)
 {
     const size_t bv = static_cast<size_t>(NG) * VB;
-    return 128 + 2 * bv * ct.WS * sizeof(float) + 2 * bv * ct.W * sizeof(float2) + ct.na * sizeof(ViewP);
+    return 128 + 2 * bv * ct.WS * sizeof(float) + 2 * bv * ct.W * sizeof(float2) + ct.na * sizeof(ViewT<G>);
 }
 
 // The bulk-copy kernel with VB views per group on tiles of 32 x kFwdTileY:
@@ -346,7 +347,7 @@ int launch_tma(const float* proj, float* img, const double* t0, const double* t1
 {
     constexpr int kThreads = NG * kBpThreads;
     constexpr int kMinBlocks = NG == 1 ? 2 : kFwdMinBlocks;  // same register budget per SM
-    const size_t smem = fwd_smem(ct, VB, NG);
+    const size_t smem = fwd_smem<G>(ct, VB, NG);
     const int tiles_x = static_cast<int>(div_up(ct.nx, kTileX));
     const int tiles_y = static_cast<int>(div_up(ct.ny, kFwdTileY));
     const long long tiles = static_cast<long long>(tiles_x) * tiles_y * batch;
@@ -415,9 +416,9 @@ int launch_forward(const float* proj, float* img, const double* t0, const double
         // parallel: 32 views per group halve the block barriers of its short
         // per-view work (bp_par_2d 122.9 -> 121.7 us at 512^2); the fan keeps 16
         // (183 vs 190 us with 32)
-        if (G == Geo::kPar && fwd_smem(ct, 32, kFwdGroups) <= kFwdSmemMax / (3 - kFwdGroups))
+        if (G == Geo::kPar && fwd_smem<G>(ct, 32, kFwdGroups) <= kFwdSmemMax / (3 - kFwdGroups))
             return launch_tma<G, 32, kFwdGroups>(proj, img, t0, t1, t2, ct, batch, stream, what);
-        if (fwd_smem(ct, 16, kFwdGroups) <= kFwdSmemMax / (3 - kFwdGroups))
+        if (fwd_smem<G>(ct, 16, kFwdGroups) <= kFwdSmemMax / (3 - kFwdGroups))
             return launch_tma<G, 16, kFwdGroups>(proj, img, t0, t1, t2, ct, batch, stream, what);
     }
     c.W = std::max(c.W, 16);

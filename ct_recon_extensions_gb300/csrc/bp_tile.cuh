@@ -317,6 +317,25 @@ struct ViewP {
     int mode;   // kModeEdge, kModeSkip, or >= kModeFast: the interior fast path
                 // (the forward tile stores the view's shared slot base there)
 };
+// Parallel beam: also the channel position of the tile's first pixel less lo,
+// from FP64, so that fast-path positions add only in-tile offsets in FP32.
+struct ViewPar : ViewP {
+    float cen;
+    int pad;
+};
+template <Geo G> struct ViewSel { using type = ViewP; };
+template <> struct ViewSel<Geo::kPar> { using type = ViewPar; };
+template <Geo G> using ViewT = typename ViewSel<G>::type;
+constexpr size_t kViewBytesMax = sizeof(ViewPar);
+
+// Fast-path origin of positions less the window start: the detector centre
+// (fan) or the tile's first pixel (parallel).
+template <Geo G>
+__device__ __forceinline__ float view_cen(const ViewT<G>& P, const TileConst& c)
+{
+    if constexpr (G == Geo::kFan) return c.cents - static_cast<float>(P.lo);
+    else return P.cen;
+}
 
 __device__ __forceinline__ bool mode_fast(int m) { return static_cast<unsigned>(m) >= kModeFast; }
 
@@ -328,10 +347,11 @@ __device__ __forceinline__ float2 lds_f2(unsigned addr)
 }
 
 // Channel position on the interior fast path (shared by the forward and the
-// adjoint), relative to the tile's window: cen = cents - lo.  Fan: xs = dso +
-// x sin b, xc = x cos b; parallel: xs = x cos t / ds + cen.  Returns s - lo
-// (rounded once, to a value below the window length); *w is the fan distance
-// weight 1/(d^2+r^2).
+// adjoint), relative to the tile's window start lo, from ViewP.cen.  Fan (x, y
+// absolute): xs = dso + x sin b, xc = x cos b, s - lo = K atan(r/d) + cen;
+// parallel (x, y offsets from the tile's first pixel): xs = x cos t / ds + cen,
+// s - lo = xs + y sin t / ds.  Returns s - lo (below the window length); *w is
+// the fan distance weight 1/(d^2+r^2).
 template <Geo G>
 __device__ __forceinline__ float fast_s(float xs, float xc, float y, float2 vp, float cen,
                                         const TileConst& c, float* w)
@@ -369,11 +389,17 @@ __device__ __forceinline__ void fast_xs(float x, float2 vp, float cen, const Til
 
 // Per-view parameters, window and path for one tile (thread-local).
 template <Geo G>
-__device__ ViewP view_setup(const double* __restrict__ t2, int ia, float x0, float x1,
-                            float y0, float y1, const TileConst& c)
+__device__ ViewT<G> view_setup(const double* __restrict__ t2, int ia, float x0, float x1,
+                               float y0, float y1, const TileConst& c)
 {
-    ViewP P;
-    P.vp = view_params<G>(t2, ia, c);
+    ViewT<G> P;
+    double sa = 0.0, ca = 0.0;
+    if constexpr (G == Geo::kFan) {
+        P.vp = view_params<G>(t2, ia, c);
+    } else {  // view_params, keeping the FP64 values for cen below
+        ::sincos(c.orbit_start + ia * c.orbit, &sa, &ca);
+        P.vp = make_float2(static_cast<float>(ca * c.inv_ds), static_cast<float>(sa * c.inv_ds));
+    }
     bool inner, off;
     P.lo = window_start<G>(P.vp, x0, x1, y0, y1, c, &inner, &off);
     bool fast = inner;
@@ -391,7 +417,24 @@ __device__ ViewP view_setup(const double* __restrict__ t2, int ia, float x0, flo
             }
     }
     P.mode = fast ? kModeFast : (off ? kModeSkip : kModeEdge);
+    if constexpr (G == Geo::kPar) {
+        // s(x0, y0) - lo in FP64: the fast path adds only offsets within the
+        // tile in FP32 (at most a tile's extent in channels)
+        P.cen = static_cast<float>((static_cast<double>(x0) * ca + static_cast<double>(y0) * sa) * c.inv_ds +
+                                   c.cents_d - P.lo);
+        P.pad = 0;
+    }
     return P;
+}
+
+// Pixel coordinates on the fast path: absolute for the fan, offsets from the
+// tile's first pixel (x0, y0) for the parallel beam (exact: both are on the
+// pixel grid).
+template <Geo G>
+__device__ __forceinline__ float fast_coord(float v, float v0)
+{
+    if constexpr (G == Geo::kFan) return v;
+    else return v - v0;
 }
 
 // One tile (tile_x, tile_y) of item `item`, over its view blocks
@@ -414,12 +457,12 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
     constexpr int kThreads = NG * kBpThreads;   // NG view groups of 256 threads
     // Dynamic shared memory, 128-byte aligned here: raw slots [2][kBV][WS]
     // (every slot stride a 128-byte multiple), pairs [2][kBV][W], then one
-    // ViewP per view of the whole scan.
+    // view record (ViewT<G>) per view of the whole scan.
     extern __shared__ __align__(128) unsigned char smem_dyn[];
     unsigned char* smem = smem_dyn + ((128u - (smem_u32(smem_dyn) & 127u)) & 127u);
     float* raw = reinterpret_cast<float*>(smem);
     float2* pairs = reinterpret_cast<float2*>(smem + 2 * kBV * c.WS * sizeof(float));
-    ViewP* views = reinterpret_cast<ViewP*>(pairs + 2 * kBV * c.W);
+    ViewT<G>* views = reinterpret_cast<ViewT<G>*>(pairs + 2 * kBV * c.W);
     __shared__ __align__(8) unsigned long long s_bar[2];
     __shared__ int s_ok;
 
@@ -487,7 +530,7 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
     const unsigned pairs_base = smem_u32(pairs);
     const int ia_end = min(nblocks * kBV, c.na);
     for (int ia = b_begin * kBV + tid; ia < ia_end; ia += kThreads) {
-        ViewP P = view_setup<G>(t2, ia, cx0, cx1, cy0, cy1, c);
+        ViewT<G> P = view_setup<G>(t2, ia, cx0, cx1, cy0, cy1, c);
         if (mode_fast(P.mode)) {
             const int slot = ((ia / kBV - b_begin) & 1) * kBV + ia % kBV;
             const unsigned base = pairs_base + 8u * static_cast<unsigned>(slot * c.W) - 8u * kMagicBits;
@@ -517,10 +560,12 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
 
     const int ixc = min(tx0 + lane, c.nx - 1);
     const float x = px(ixc);
-    float y[R], acc[R];
+    const float xf = fast_coord<G>(x, cx0);
+    float y[R], yf[R], acc[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         y[r] = py(min(ty0 + warp * R + r, c.ny - 1));
+        yf[r] = fast_coord<G>(y[r], cy0);
         acc[r] = 0.0f;
     }
 
@@ -569,17 +614,17 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
         for (int r = 0; r < R; ++r) part[r] = 0.0f;
         for (int j = jb; j < je; ++j) {
             const int ia = b * kBV + j;
-            const ViewP P = views[ia];
+            const ViewT<G> P = views[ia];
             if (mode_fast(P.mode)) {
                 // floor of s' = bits(fl(s' + 2^23 - 1/2)) - kMagicBits
                 const unsigned base = static_cast<unsigned>(P.mode);
-                const float cen = c.cents - static_cast<float>(P.lo);
+                const float cen = view_cen<G>(P, c);
                 float xs, xc;
-                fast_xs<G>(x, P.vp, cen, c, &xs, &xc);
+                fast_xs<G>(xf, P.vp, cen, c, &xs, &xc);
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
                     float w;
-                    const float s = fast_s<G>(xs, xc, y[r], P.vp, cen, c, &w);
+                    const float s = fast_s<G>(xs, xc, yf[r], P.vp, cen, c, &w);
                     const float2 pv = lds_f2(base + 8u * __float_as_uint(s + kMagicHalf));
                     if constexpr (G == Geo::kFan) part[r] = fmaf(fmaf(s, pv.y, pv.x), w, part[r]);
                     else part[r] += fmaf(s, pv.y, pv.x);

@@ -179,6 +179,20 @@ def test_parallel_config2(oracle_port):
     assert rel_l2(rec, rec64) <= 1e-4
 
 
+def test_parallel_config2_white_noise(oracle_port):
+    """Ramp + bp_par_2d at 512^2 x 720 views x 729 bins on a white-noise sinogram
+    (detector differences as large as the values: the worst case for the FP32
+    channel positions) against the reference's CPU algorithm."""
+    from oracle import Geom
+    from ct_recon_extensions_gb300 import synthetic as syn
+    d = syn.parallel_config_2()
+    g = Geom.make(**d)
+    sino = np.random.default_rng(7).standard_normal((d["na"], d["ns"])).astype(np.float32)
+    rec = host(par_op(d).forward(ramp_op(d, d["na"], 0, dsd=-1.0).forward(cuda(sino))))
+    ref = oracle_port.bp_par_2d(oracle_port.ramp_filter(sino, g.ds, -1.0, 0), g)
+    assert rel_l2(rec, ref) <= 1e-5  # measured 6.8e-6
+
+
 def test_fp_adjoint_config2_batch(oracle_port):
     """The FP adjoint at 512^2 x 720 views x 729 bins: against the oracle, and a
     batch of 7 (image groups of the gather plus a remainder) equal to its items."""
