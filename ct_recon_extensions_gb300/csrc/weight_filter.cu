@@ -132,6 +132,36 @@ inline int filter_layout(unsigned ns, int rows)
     return filter_smem<T>(ns, rows, kTapSkewed) <= kFilterSmemMax ? kTapSkewed : kTapPacked;
 }
 
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
+
+// Inputs j = j0, j0 + 2, ... < j1 (one parity) into the four outputs i0, i0 + 2,
+// i0 + 4, i0 + 6 of kRows rows; w0..w3 are the taps of input j0.  (Blocked
+// partial sums cut the FP32 rounding of the long sums by ~1.3x on phantom
+// sinograms and cost 11 % of the filter's time; not kept.)
+template <typename T, int kRows>
+__device__ __forceinline__ void filter_span(const T* __restrict__ xs, int n, int j0, int j1, int i0, int tg,
+                                            const T* __restrict__ H0, T w0, T w1, T w2, T w3,
+                                            T (&acc)[kRows][4])
+{
+    const int d0 = (n - 1) + kFilterPad;  // tap d sits at H0[tap_slot(d + d0, tg)]
+#pragma unroll 4
+    for (int j = j0; j < j1; j += 2) {
+#pragma unroll
+        for (int r = 0; r < kRows; ++r) {
+            const T xv = xs[r * n + j];
+            acc[r][0] += w0 * xv;
+            acc[r][1] += w1 * xv;
+            acc[r][2] += w2 * xv;
+            acc[r][3] += w3 * xv;
+        }
+        w3 = w2;
+        w2 = w1;
+        w1 = w0;
+        w0 = H0[tap_slot(i0 - j - 2 + d0, tg)];
+    }
+}
+
 template <typename T, int kRows, bool kGrad>
 __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const double* __restrict__ filter,
                                             T* __restrict__ out, const float* __restrict__ weight,
@@ -189,21 +219,7 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
             const int jm = jb + 2 * ((n - jb + 1) / 4);
             const int j0 = half ? jm : jb, j1 = half ? n : jm;
             T w0 = H(i0 - j0), w1 = H(i0 + 2 - j0), w2 = H(i0 + 4 - j0), w3 = H(i0 + 6 - j0);
-#pragma unroll 4
-            for (int j = j0; j < j1; j += 2) {
-#pragma unroll
-                for (int r = 0; r < kRows; ++r) {
-                    const T xv = xs[r * n + j];
-                    acc[r][0] += w0 * xv;
-                    acc[r][1] += w1 * xv;
-                    acc[r][2] += w2 * xv;
-                    acc[r][3] += w3 * xv;
-                }
-                w3 = w2;
-                w2 = w1;
-                w1 = w0;
-                w0 = H(i0 - j - 2);
-            }
+            filter_span<T, kRows>(xs, n, j0, j1, i0, tg, H0, w0, w1, w2, w3, acc);
             if (half) {
 #pragma unroll
                 for (int r = 0; r < kRows; ++r)
@@ -221,7 +237,7 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
 #pragma unroll
                 for (int r = 0; r < kRows; ++r)
                     if (r < nr)
-                        out[(r0 + r) * ns + o] = t0 * xs[r * n + o] + (acc[r][m] + red[(r * groups + g) * 4 + m]);
+                        out[(r0 + r) * ns + o] = fma_t(t0, xs[r * n + o], acc[r][m] + red[(r * groups + g) * 4 + m]);
             }
         }
     } else if (!s_even) {
@@ -234,21 +250,7 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
                 for (int m = 0; m < 4; ++m) acc[r][m] = 0;
             const int jb = (i0 + 1) & 1;  // inputs of the other parity
             T w0 = H(i0 - jb), w1 = H(i0 + 2 - jb), w2 = H(i0 + 4 - jb), w3 = H(i0 + 6 - jb);
-#pragma unroll 4
-            for (int j = jb; j < n; j += 2) {
-#pragma unroll
-                for (int r = 0; r < kRows; ++r) {
-                    const T xv = xs[r * n + j];
-                    acc[r][0] += w0 * xv;
-                    acc[r][1] += w1 * xv;
-                    acc[r][2] += w2 * xv;
-                    acc[r][3] += w3 * xv;
-                }
-                w3 = w2;
-                w2 = w1;
-                w1 = w0;
-                w0 = H(i0 - j - 2);
-            }
+            filter_span<T, kRows>(xs, n, jb, n, i0, tg, H0, w0, w1, w2, w3, acc);
             const T t0 = H(0);
 #pragma unroll
             for (int m = 0; m < 4; ++m) {
@@ -256,7 +258,7 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
                 if (o >= n) continue;
 #pragma unroll
                 for (int r = 0; r < kRows; ++r)
-                    if (r < nr) out[(r0 + r) * ns + o] = t0 * xs[r * n + o] + acc[r][m];
+                    if (r < nr) out[(r0 + r) * ns + o] = fma_t(t0, xs[r * n + o], acc[r][m]);
             }
         }
     } else {
