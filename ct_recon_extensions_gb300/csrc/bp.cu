@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(kBpThreads, 2)
     float* G_ = grad + blockIdx.z * c.proj_stride;
     // per-view parameters, windows and paths of this tile for the whole scan
     for (int ia = threadIdx.x; ia < c.na; ia += kBpThreads)
-        views[ia] = view_setup<G>(t2, ia, cx0, cx1, cy0, cy1, c);
+        views[ia] = view_setup<G>(t0, t1, t2, ia, tx0, ty0, cx0, cx1, cy0, cy1, c);
 
     for (int v0 = 0; v0 < c.na; v0 += kViewBlock) {
         const int nv = min(kViewBlock, c.na - v0);

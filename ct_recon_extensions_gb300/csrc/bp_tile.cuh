@@ -389,16 +389,20 @@ __device__ __forceinline__ void fast_xs(float x, float2 vp, float cen, const Til
 
 // Per-view parameters, window and path for one tile (thread-local).
 template <Geo G>
-__device__ ViewT<G> view_setup(const double* __restrict__ t2, int ia, float x0, float x1,
-                               float y0, float y1, const TileConst& c)
+__device__ ViewT<G> view_setup(const double* __restrict__ t0, const double* __restrict__ t1,
+                               const double* __restrict__ t2, int ia, int ix0, int iy0, float x0,
+                               float x1, float y0, float y1, const TileConst& c)
 {
     ViewT<G> P;
-    double sa = 0.0, ca = 0.0;
     if constexpr (G == Geo::kFan) {
         P.vp = view_params<G>(t2, ia, c);
-    } else {  // view_params, keeping the FP64 values for cen below
-        ::sincos(c.orbit_start + ia * c.orbit, &sa, &ca);
-        P.vp = make_float2(static_cast<float>(ca * c.inv_ds), static_cast<float>(sa * c.inv_ds));
+    } else {
+        // FP32 slopes: on the fast path they multiply offsets within the tile
+        // only (the tile's origin comes from the FP64 tables below)
+        float sf, cf;
+        sincosf(static_cast<float>(c.orbit_start + ia * c.orbit), &sf, &cf);
+        const float ids = static_cast<float>(c.inv_ds);
+        P.vp = make_float2(cf * ids, sf * ids);
     }
     bool inner, off;
     P.lo = window_start<G>(P.vp, x0, x1, y0, y1, c, &inner, &off);
@@ -418,9 +422,12 @@ __device__ ViewT<G> view_setup(const double* __restrict__ t2, int ia, float x0, 
     }
     P.mode = fast ? kModeFast : (off ? kModeSkip : kModeEdge);
     if constexpr (G == Geo::kPar) {
-        // s(x0, y0) - lo in FP64: the fast path adds only offsets within the
-        // tile in FP32 (at most a tile's extent in channels)
-        P.cen = static_cast<float>((static_cast<double>(x0) * ca + static_cast<double>(y0) * sa) * c.inv_ds +
+        // s(x0, y0) - lo in FP64 from the caller's x cos t / y sin t tables
+        // (src/bp_par_2d.cc:70), (ix0, iy0) the tile's first pixel: the fast
+        // path adds only offsets within the tile in FP32 (at most a tile's
+        // extent in channels)
+        P.cen = static_cast<float>((t0[static_cast<size_t>(ix0) * c.na + ia] +
+                                    t1[static_cast<size_t>(iy0) * c.na + ia]) * c.inv_ds +
                                    c.cents_d - P.lo);
         P.pad = 0;
     }
@@ -530,7 +537,7 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
     const unsigned pairs_base = smem_u32(pairs);
     const int ia_end = min(nblocks * kBV, c.na);
     for (int ia = b_begin * kBV + tid; ia < ia_end; ia += kThreads) {
-        ViewT<G> P = view_setup<G>(t2, ia, cx0, cx1, cy0, cy1, c);
+        ViewT<G> P = view_setup<G>(t0, t1, t2, ia, tx0, ty0, cx0, cx1, cy0, cy1, c);
         if (mode_fast(P.mode)) {
             const int slot = ((ia / kBV - b_begin) & 1) * kBV + ia % kBV;
             const unsigned base = pairs_base + 8u * static_cast<unsigned>(slot * c.W) - 8u * kMagicBits;

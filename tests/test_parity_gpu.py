@@ -190,7 +190,7 @@ def test_parallel_config2_white_noise(oracle_port):
     sino = np.random.default_rng(7).standard_normal((d["na"], d["ns"])).astype(np.float32)
     rec = host(par_op(d).forward(ramp_op(d, d["na"], 0, dsd=-1.0).forward(cuda(sino))))
     ref = oracle_port.bp_par_2d(oracle_port.ramp_filter(sino, g.ds, -1.0, 0), g)
-    assert rel_l2(rec, ref) <= 1e-5  # measured 6.8e-6
+    assert rel_l2(rec, ref) <= 1e-5  # measured 7.6e-6
 
 
 def test_fp_adjoint_config2_batch(oracle_port):
