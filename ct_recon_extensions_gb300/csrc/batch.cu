@@ -182,7 +182,8 @@ TileConst item_const(const ctr_fan_bp_param& g, int tile_y, int R, int VB)
     c.cents_d = (g.ns - 1) / 2.0 + g.offset_s;
     c.dso_d = g.dso;
     c.dsd_d = g.dsd;
-    for (int k = 0; k < 6; ++k) c.poly[k] = static_cast<float>(kAtanPoly[k] * g.dsd / g.ds);
+    for (int v = 0; v < kAtanVariants; ++v)
+        for (int k = 0; k < 6; ++k) c.poly[v][k] = static_cast<float>(kAtanPoly[v][k] * g.dsd / g.ds);
     c.proj_stride = static_cast<size_t>(g.ns) * g.na;
     c.img_stride = static_cast<size_t>(g.nx) * g.ny;
     c.total4 = static_cast<long long>(c.proj_stride & ~static_cast<size_t>(3));

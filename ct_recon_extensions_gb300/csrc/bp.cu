@@ -32,6 +32,7 @@
 // runs at the FP32 rounding level.  The FP64 adjoint uses global atomics per
 // tap.
 #include <cfloat>
+#include <type_traits>
 
 #include "bp_tile.cuh"
 
@@ -90,18 +91,27 @@ __global__ void __launch_bounds__(kBpThreads, 2)
                 const float cen = view_cen<G>(P, c);
                 float xs, xc;
                 fast_xs<G>(fast_coord<G>(x, cx0), P.vp, cen, c, &xs, &xc);
+                auto taps = [&](auto variant) {
+                    constexpr int V = decltype(variant)::value;
 #pragma unroll
-                for (int r = 0; r < kRowsPerThread; ++r) {
-                    float w;
-                    const float s = fast_s<G>(xs, xc, fast_coord<G>(y[r], cy0), P.vp, cen, c, &w);  // s - lo
-                    const float v = s + kMagicHalf;
-                    const float u = s - (v - kMagic);
-                    const int k = static_cast<int>(__float_as_uint(v) - kMagicBits);
-                    const float t = val[r] * w;
-                    if (t != 0.0f) {
-                        atomicAdd(aj + k, t - t * u);
-                        atomicAdd(aj + k + 1, t * u);
+                    for (int r = 0; r < kRowsPerThread; ++r) {
+                        float w;
+                        const float s = fast_s<G, V>(xs, xc, fast_coord<G>(y[r], cy0), P.vp, cen, c, &w);  // s - lo
+                        const float v = s + kMagicHalf;
+                        const float u = s - (v - kMagic);
+                        const int k = static_cast<int>(__float_as_uint(v) - kMagicBits);
+                        const float t = val[r] * w;
+                        if (t != 0.0f) {
+                            atomicAdd(aj + k, t - t * u);
+                            atomicAdd(aj + k + 1, t * u);
+                        }
                     }
+                };
+                switch (G == Geo::kFan ? P.mode & 3 : 0) {
+                    case 0: taps(std::integral_constant<int, 0>{}); break;
+                    case 1: taps(std::integral_constant<int, 1>{}); break;
+                    case 2: taps(std::integral_constant<int, 2>{}); break;
+                    default: taps(std::integral_constant<int, 3>{}); break;
                 }
             } else if (P.mode == kModeEdge) {
 #pragma unroll
@@ -458,7 +468,8 @@ TileConst fan_const(const FanArgs& a, double extra_scale)
     c.cents_d = (a.ns - 1) / 2.0 + a.offset_s;
     c.dso_d = a.dso;
     c.dsd_d = a.dsd;
-    for (int k = 0; k < 6; ++k) c.poly[k] = static_cast<float>(kAtanPoly[k] * a.dsd / a.ds);
+    for (int v = 0; v < kAtanVariants; ++v)
+        for (int k = 0; k < 6; ++k) c.poly[v][k] = static_cast<float>(kAtanPoly[v][k] * a.dsd / a.ds);
     c.proj_stride = static_cast<size_t>(a.ns) * a.na;
     c.img_stride = static_cast<size_t>(a.nx) * a.ny;
     return c;

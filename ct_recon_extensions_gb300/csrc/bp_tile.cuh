@@ -35,7 +35,7 @@ struct TileConst {
     double inv_ds;         // parallel: 1/ds
     double centx, centy, dx, dy;  // parallel pixel grid
     double ds_d, cents_d, dso_d, dsd_d;  // FP64 geometry for the exact edge test
-    float poly[6];         // fan: atan polynomial scaled by dsd/ds
+    float poly[4][6];      // fan: the atan polynomial variants, scaled by dsd/ds
     int WB;                // TMA box (elements) per view: >= W + 4, multiple of 4
     int WS;                // shared slot stride per view: WB rounded up to 128 bytes
     long long total4;      // sinogram elements of the launch, rounded down to 4
@@ -294,15 +294,28 @@ __global__ void __launch_bounds__(kBpThreads, 2)
 // the position's last FMA with cents - lo in place of cents, its floor from
 // adding 2^23 - 0.5 (round-to-nearest of s' - 1/2 lands the integer part in
 // the low mantissa bits; s' in [1, 2^22)), and for the fan
-// atan(r/d) is the minimax polynomial below when |r/d| <= kAtanTmax on the
-// whole tile, with an approximate reciprocal of d.
+// atan(r/d) is one of the minimax polynomials below (the lowest degree whose
+// range covers |r/d| on the whole tile, up to 0.6), with an approximate
+// reciprocal of d.
 
-// atan(t) ~= t*P(t^2), |t| <= 0.6, max relative error 3.28e-08 (Remez, degree 5
-// in t^2; coefficients from gen_atan_poly.py).
-constexpr double kAtanPoly[6] = {9.99999967214467378e-01, -3.33326573611355148e-01,
-                                 1.99772013637297047e-01, -1.39992597733896912e-01,
-                                 9.42086263445095634e-02, -4.04465160162714304e-02};
-constexpr float kAtanTmax = 0.6f;
+// atan(t) ~= t*P(t^2), minimax for relative error (Remez; gen_atan_poly.py),
+// four variants of about the same error: a tile takes the lowest degree whose
+// range covers all its pixels.  |t| <= 0.6: degree 5 in t^2, max relative error
+// 3.28e-08; |t| <= 0.45: degree 4, 3.87e-08; |t| <= 0.3: degree 3, 4.84e-08;
+// |t| <= 0.15: degree 2, 4.93e-08.
+constexpr int kAtanVariants = 4;
+__host__ __device__ constexpr float atan_tmax(int v)
+{
+    return v == 0 ? 0.6f : v == 1 ? 0.45f : v == 2 ? 0.3f : 0.15f;
+}
+constexpr double kAtanPoly[kAtanVariants][6] = {
+    {9.99999967214467378e-01, -3.33326573611355148e-01, 1.99772013637297047e-01, -1.39992597733896912e-01,
+     9.42086263445095634e-02, -4.04465160162714304e-02},
+    {9.99999961331696996e-01, -3.33323584754777580e-01, 1.99603534902473234e-01, -1.37111734158844867e-01,
+     7.55531535813081662e-02, 0.0},
+    {9.99999951640157425e-01, -3.33315939607756684e-01, 1.99016376594526256e-01, -1.24757817537760357e-01,
+     0.0, 0.0},
+    {9.99999950700421469e-01, -3.33293746601247498e-01, 1.95275580886984462e-01, 0.0, 0.0, 0.0}};
 constexpr float kMagic = 8388608.0f;       // 2^23
 constexpr float kMagicHalf = 8388607.5f;   // 2^23 - 1/2
 constexpr unsigned kMagicBits = 0x4B000000u;
@@ -310,6 +323,9 @@ constexpr int kGroups = 2;
 constexpr int kBlockViews = kGroups * kViewBlock;
 constexpr int kTmaThreads = kGroups * kBpThreads;
 constexpr int kModeEdge = 0, kModeSkip = 1, kModeFast = 2;
+// A fast view's mode: a multiple of 8 (kModeFastBase, or the forward tile's
+// shared slot base) plus the atan variant in the low two bits.
+constexpr int kModeFastBase = 8;
 
 struct ViewP {
     float2 vp;
@@ -352,20 +368,20 @@ __device__ __forceinline__ float2 lds_f2(unsigned addr)
 // parallel (x, y offsets from the tile's first pixel): xs = x cos t / ds + cen,
 // s - lo = xs + y sin t / ds.  Returns s - lo (below the window length); *w is
 // the fan distance weight 1/(d^2+r^2).
-template <Geo G>
+// V = the atan variant (fan; 0 for the parallel beam).
+template <Geo G, int V = 0>
 __device__ __forceinline__ float fast_s(float xs, float xc, float y, float2 vp, float cen,
                                         const TileConst& c, float* w)
 {
     if constexpr (G == Geo::kFan) {
+        constexpr int deg = 5 - V;
         const float d = fmaf(-y, vp.y, xs);
         const float rr = fmaf(y, vp.x, xc);
         const float t = rr * rcp_approx(d);
         const float z = t * t;
-        float p = fmaf(z, c.poly[5], c.poly[4]);
-        p = fmaf(z, p, c.poly[3]);
-        p = fmaf(z, p, c.poly[2]);
-        p = fmaf(z, p, c.poly[1]);
-        p = fmaf(z, p, c.poly[0]);
+        float p = c.poly[V][deg];
+#pragma unroll
+        for (int k = deg - 1; k >= 0; --k) p = fmaf(z, p, c.poly[V][k]);
         *w = rcp_approx(fmaf(d, d, rr * rr));
         return fmaf(t, p, cen);
     } else {
@@ -408,19 +424,28 @@ __device__ ViewT<G> view_setup(const double* __restrict__ t0, const double* __re
     P.lo = window_start<G>(P.vp, x0, x1, y0, y1, c, &inner, &off);
     bool fast = inner;
     if constexpr (G == Geo::kFan) {
-        // polynomial atan needs d > 0 and |r/d| <= kAtanTmax on the whole tile
-        // (r/d is a linear-fractional function: extremes at the corners)
+        // polynomial atan needs d > 0 and |r/d| <= atan_tmax(0) on the whole
+        // tile (r/d is a linear-fractional function: extremes at the corners);
+        // the tile takes the lowest-degree variant that covers it
         const float xs[2] = {x0, x1}, ys[2] = {y0, y1};
+        float tmax = 0.0f;
 #pragma unroll
         for (int i = 0; i < 2; ++i)
 #pragma unroll
             for (int j = 0; j < 2; ++j) {
                 const float d = fmaf(-ys[j], P.vp.y, fmaf(xs[i], P.vp.x, c.dso));
                 const float r = fmaf(xs[i], P.vp.y, ys[j] * P.vp.x);
-                fast = fast && d > 0.0f && fabsf(r) <= kAtanTmax * d;
+                fast = fast && d > 0.0f && fabsf(r) <= atan_tmax(0) * d;
+                tmax = fmaxf(tmax, fabsf(r) / d);
             }
+        int v = 0;
+#pragma unroll
+        for (int k = 1; k < kAtanVariants; ++k)
+            if (tmax <= atan_tmax(k)) v = k;
+        P.mode = fast ? kModeFastBase + v : (off ? kModeSkip : kModeEdge);
+    } else {
+        P.mode = fast ? kModeFastBase : (off ? kModeSkip : kModeEdge);
     }
-    P.mode = fast ? kModeFast : (off ? kModeSkip : kModeEdge);
     if constexpr (G == Geo::kPar) {
         // s(x0, y0) - lo in FP64 from the caller's x cos t / y sin t tables
         // (src/bp_par_2d.cc:70), (ix0, iy0) the tile's first pixel: the fast
@@ -442,6 +467,21 @@ __device__ __forceinline__ float fast_coord(float v, float v0)
 {
     if constexpr (G == Geo::kFan) return v;
     else return v - v0;
+}
+
+// The fast-path taps of one view for a thread's R pixels (atan variant V).
+template <Geo G, int V, int R>
+__device__ __forceinline__ void fast_rows(float xs, float xc, const float (&yf)[R], float2 vp, float cen,
+                                          const TileConst& c, unsigned base, float (&part)[R])
+{
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        float w;
+        const float s = fast_s<G, V>(xs, xc, yf[r], vp, cen, c, &w);
+        const float2 pv = lds_f2(base + 8u * __float_as_uint(s + kMagicHalf));
+        if constexpr (G == Geo::kFan) part[r] = fmaf(fmaf(s, pv.y, pv.x), w, part[r]);
+        else part[r] += fmaf(s, pv.y, pv.x);
+    }
 }
 
 // One tile (tile_x, tile_y) of item `item`, over its view blocks
@@ -531,9 +571,9 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
 
     // per-view parameters, windows and paths of this tile for the whole scan;
     // a fast view keeps, in place of its mode, the shared address of its pair
-    // slot minus 8 * kMagicBits, so a tap's address is that plus
-    // 8 * bits(s' + 2^23 - 1/2), s' = s - lo (values below kModeFast fall back
-    // to the edge path)
+    // slot minus 8 * kMagicBits (a multiple of 8), so a tap's address is that
+    // plus 8 * bits(s' + 2^23 - 1/2), s' = s - lo; the low two bits keep the
+    // atan variant (values below kModeFastBase fall back to the edge path)
     const unsigned pairs_base = smem_u32(pairs);
     const int ia_end = min(nblocks * kBV, c.na);
     for (int ia = b_begin * kBV + tid; ia < ia_end; ia += kThreads) {
@@ -541,7 +581,8 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
         if (mode_fast(P.mode)) {
             const int slot = ((ia / kBV - b_begin) & 1) * kBV + ia % kBV;
             const unsigned base = pairs_base + 8u * static_cast<unsigned>(slot * c.W) - 8u * kMagicBits;
-            P.mode = base >= static_cast<unsigned>(kModeFast) ? static_cast<int>(base) : kModeEdge;
+            P.mode = base >= static_cast<unsigned>(kModeFastBase) ? static_cast<int>(base | (P.mode & 3))
+                                                                 : kModeEdge;
         }
         views[ia] = P;
     }
@@ -624,17 +665,19 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
             const ViewT<G> P = views[ia];
             if (mode_fast(P.mode)) {
                 // floor of s' = bits(fl(s' + 2^23 - 1/2)) - kMagicBits
-                const unsigned base = static_cast<unsigned>(P.mode);
+                const unsigned base = static_cast<unsigned>(P.mode) & ~3u;
                 const float cen = view_cen<G>(P, c);
                 float xs, xc;
                 fast_xs<G>(xf, P.vp, cen, c, &xs, &xc);
-#pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    float w;
-                    const float s = fast_s<G>(xs, xc, yf[r], P.vp, cen, c, &w);
-                    const float2 pv = lds_f2(base + 8u * __float_as_uint(s + kMagicHalf));
-                    if constexpr (G == Geo::kFan) part[r] = fmaf(fmaf(s, pv.y, pv.x), w, part[r]);
-                    else part[r] += fmaf(s, pv.y, pv.x);
+                if constexpr (G == Geo::kFan) {
+                    switch (P.mode & 3) {
+                        case 0: fast_rows<G, 0, R>(xs, xc, yf, P.vp, cen, c, base, part); break;
+                        case 1: fast_rows<G, 1, R>(xs, xc, yf, P.vp, cen, c, base, part); break;
+                        case 2: fast_rows<G, 2, R>(xs, xc, yf, P.vp, cen, c, base, part); break;
+                        default: fast_rows<G, 3, R>(xs, xc, yf, P.vp, cen, c, base, part); break;
+                    }
+                } else {
+                    fast_rows<G, 0, R>(xs, xc, yf, P.vp, cen, c, base, part);
                 }
             } else if (P.mode == kModeEdge) {
                 const float2* wj = pb + j * c.W;

@@ -7,12 +7,16 @@ mathematical function itself.  The kernel only uses it where every pixel of a
 tile satisfies |r/d| <= TMAX (d > 0), i.e. fan angles up to ~31 degrees; other
 tiles use atan2f.
 
-    python gen_atan_poly.py  -> prints the C++ table pasted into bp.cu
+    python gen_atan_poly.py  -> prints the C++ tables pasted into bp_tile.cuh
+
+A tile takes the lowest degree whose range covers every pixel of the tile
+(VARIANTS: (TMAX, DEG) pairs of about the same relative error, ~4e-8).
 """
 import numpy as np
 
 TMAX = 0.6
 DEG = 5
+VARIANTS = ((0.6, 5), (0.45, 4), (0.3, 3), (0.15, 2))
 
 
 def remez(tmax=TMAX, deg=DEG, iters=80):
@@ -42,6 +46,11 @@ def remez(tmax=TMAX, deg=DEG, iters=80):
 
 
 if __name__ == "__main__":
-    c, err = remez()
-    print(f"// atan(t) ~= t*P(t^2), |t| <= {TMAX}, max relative error {err:.2e} (Remez, degree {DEG} in t^2)")
-    print("constexpr double kAtanPoly[%d] = {%s};" % (len(c), ", ".join(f"{v:.17e}" for v in c)))
+    rows, errs = [], []
+    for tmax, deg in VARIANTS:
+        c, err = remez(tmax, deg)
+        rows.append("{" + ", ".join(f"{v:.17e}" for v in list(c) + [0.0] * (5 - deg)) + "}")
+        errs.append(f"|t| <= {tmax}: degree {deg}, max relative error {err:.2e}")
+    print("// atan(t) ~= t*P(t^2) (Remez, degree in t^2): " + "; ".join(errs))
+    print("ranges (atan_tmax):", ", ".join(f"{t}" for t, _ in VARIANTS))
+    print("constexpr double kAtanPoly[%d][6] = {%s};" % (len(VARIANTS), ",\n    ".join(rows)))
