@@ -1,6 +1,9 @@
 // Per-ray set-up of the FP32 ray-driven forward projector: the ray's sample
 // range and its 32.32 fixed-point line, from the caller's FP64 table entry
-// (begin, step) of the reference's prep (src/fp_par_2d.cc:180-199).
+// (begin, step) of the reference's prep (src/fp_par_2d.cc:180-199).  The _n
+// forms take the number of samples n and the extent ext of the axis (samples
+// valid iff 0 <= x(k) <= ext-1) separately: the ray-casting projector walks one
+// axis of a 2-D ray with n != ext; the plain forms are n == ext.
 //
 // A sample k of the ray sits at x(k) = begin + k*step (pixel units along the
 // marched row); it is used iff 0 <= x(k) <= n-1 (src/fp_par_2d.cc:237,259).
@@ -105,15 +108,15 @@ CTR_HD long long tie_units(int n) { return static_cast<long long>(n) + 1024; }
 // the ray must take the FP64 path (tie, magnitude, or an estimate that did
 // not verify).  On success the valid samples are [*k0, *k1] (empty when
 // *k1 < *k0) and every valid sample has tie_units(n) <= X(k) <= L - tie_units(n).
-CTR_HD bool ray_fixed(double begin, double step, int n, long long* X0, long long* Sout, int* k0o,
-                      int* k1o)
+CTR_HD bool ray_fixed_n(double begin, double step, int n, int ext, long long* X0, long long* Sout,
+                        int* k0o, int* k1o)
 {
     // exact-range guard (also rejects NaN / Inf): |begin| < 2^20, |step| < 4
     const int eb = static_cast<int>((double_bits(begin) >> 52) & 0x7FF);
     const int es = static_cast<int>((double_bits(step) >> 52) & 0x7FF);
     if (eb >= 1043 || es >= 1025) return false;
     const long long B = fix32(begin), S = fix32(step);
-    const long long L = static_cast<long long>(n - 1) << 32;
+    const long long L = static_cast<long long>(ext - 1) << 32;
     const long long T = tie_units(n);
     auto X = [&](int k) { return B + static_cast<long long>(k) * S; };
     auto inside = [&](int k) {
@@ -132,7 +135,7 @@ CTR_HD bool ray_fixed(double begin, double step, int n, long long* X0, long long
     } else {
         // real-valued crossing points, estimated in FP32, then settled exactly
         const float fb = dbl2flt(begin), fs = dbl2flt(step);
-        float ta = -fb / fs, tb = (static_cast<float>(n - 1) - fb) / fs;
+        float ta = -fb / fs, tb = (static_cast<float>(ext - 1) - fb) / fs;
         if (ta > tb) {
             const float t = ta;
             ta = tb;
@@ -176,6 +179,12 @@ CTR_HD bool ray_fixed(double begin, double step, int n, long long* X0, long long
     return true;
 }
 
+CTR_HD bool ray_fixed(double begin, double step, int n, long long* X0, long long* Sout, int* k0o,
+                      int* k1o)
+{
+    return ray_fixed_n(begin, step, n, n, X0, Sout, k0o, k1o);
+}
+
 // For a ray that ray_fixed could not settle: the samples certainly inside
 // (T <= X(k) <= L - T, decided in fixed point) as [*c0, *c1], and the
 // ambiguous samples next to them (|X| < T or |X - L| < T), at most two at each
@@ -183,14 +192,14 @@ CTR_HD bool ray_fixed(double begin, double step, int n, long long* X0, long long
 // rule (acc_inside), which the caller evaluates separately.  Returns false when
 // the ray needs ray_fp64 instead: magnitudes out of range, no certain sample,
 // or a longer ambiguous run (a ray almost parallel to an image edge).
-CTR_HD bool ray_split(double begin, double step, int n, long long* X0, long long* Sout, int* c0o,
-                      int* c1o, int* amb, int* namb)
+CTR_HD bool ray_split_n(double begin, double step, int n, int ext, long long* X0, long long* Sout,
+                        int* c0o, int* c1o, int* amb, int* namb)
 {
     const int eb = static_cast<int>((double_bits(begin) >> 52) & 0x7FF);
     const int es = static_cast<int>((double_bits(step) >> 52) & 0x7FF);
     if (eb >= 1043 || es >= 1025 || n < 4) return false;
     const long long B = fix32(begin), S = fix32(step);
-    const long long L = static_cast<long long>(n - 1) << 32;
+    const long long L = static_cast<long long>(ext - 1) << 32;
     const long long T = tie_units(n);
     auto X = [&](int k) { return B + static_cast<long long>(k) * S; };
     auto in = [&](int k) {
@@ -205,7 +214,7 @@ CTR_HD bool ray_split(double begin, double step, int n, long long* X0, long long
     if (S == 0) return false;  // all samples alike: left to ray_fp64
     const float fb = dbl2flt(begin), fs = dbl2flt(step);
     const float tl = static_cast<float>(T) / 4294967296.0f;
-    const float hi_x = static_cast<float>(n - 1) - tl;
+    const float hi_x = static_cast<float>(ext - 1) - tl;
     float ta = (tl - fb) / fs, tb = (hi_x - fb) / fs;
     if (ta > tb) {
         const float t = ta;
@@ -236,6 +245,12 @@ CTR_HD bool ray_split(double begin, double step, int n, long long* X0, long long
     *c1o = c1;
     *namb = m;
     return true;
+}
+
+CTR_HD bool ray_split(double begin, double step, int n, long long* X0, long long* Sout, int* c0o,
+                      int* c1o, int* amb, int* namb)
+{
+    return ray_split_n(begin, step, n, n, X0, Sout, c0o, c1o, amb, namb);
 }
 
 // Bits -> double (host and device).
@@ -376,10 +391,10 @@ CTR_HD void col_range(long long X0, long long S, int b0, int b1, int lo, int hi,
 // sample k used iff 0 <= x <= n-1.  The 32.32 line is anchored at the
 // smallest-x valid sample, so X >= 0 on every valid sample.  Rare (ties at the
 // image border), so its n FP64 additions cost nothing overall.
-CTR_HD void ray_fp64(double begin, double step, int n, long long* X0, long long* Sout, int* k0o,
-                     int* k1o)
+CTR_HD void ray_fp64_n(double begin, double step, int n, int ext, long long* X0, long long* Sout,
+                       int* k0o, int* k1o)
 {
-    const double lim = static_cast<double>(n - 1);
+    const double lim = static_cast<double>(ext - 1);
     int k0 = n, k1 = -1;
     double x = begin;
     for (int k = 0; k < n; ++k) {
@@ -403,6 +418,12 @@ CTR_HD void ray_fp64(double begin, double step, int n, long long* X0, long long*
     *Sout = S;
     *k0o = k0;
     *k1o = k1;
+}
+
+CTR_HD void ray_fp64(double begin, double step, int n, long long* X0, long long* Sout, int* k0o,
+                     int* k1o)
+{
+    ray_fp64_n(begin, step, n, n, X0, Sout, k0o, k1o);
 }
 
 }  // namespace ctr

@@ -298,6 +298,30 @@ class Oracle:
                                                   _p(proj), _p(img), _p(w), _p(pos), _p(usex)))
         return img
 
+    # -- parallel ray-casting FP (src/fp_par_2d.cc:18-145) -----------------
+    def fp_par_2d_cast_tables(self, g: Geom, step_size: float = 0.125):
+        sc = np.empty((g.na, 2)); begins = np.empty((g.na, g.ns, 2))
+        nsteps = np.empty((g.na, g.ns), np.int32)
+        self._fn("fp_par_2d_cast_prep")(ctypes.byref(g), ctypes.c_double(step_size), _p(sc),
+                                        _p(begins), _p(nsteps))
+        return sc, begins, nsteps
+
+    def fp_par_2d_cast(self, img, g: Geom, step_size: float = 0.125):
+        img = self._c(img)
+        assert img.shape == (g.ny, g.nx)
+        sc, begins, nsteps = self.fp_par_2d_cast_tables(g, step_size)
+        proj = np.empty((g.na, g.ns), dtype=img.dtype)
+        st = ctypes.c_double(step_size)
+        if self.kind == "reference":
+            self._fn(f"fp_par_2d_cast_{_sfx(img.dtype)}")(ctypes.byref(g), st, _p(img), _p(proj),
+                                                          _p(sc), _p(begins), _p(nsteps))
+        else:
+            f = self._fn(f"fp_par_2d_cast_views_{_sfx(img.dtype)}")
+            self._run_ranges(g.na, lambda a, b: f(ctypes.byref(g), _c_uint(a), _c_uint(b), st,
+                                                  _p(img), _p(proj), _p(sc), _p(begins),
+                                                  _p(nsteps)))
+        return proj
+
     # -- composed FBP -------------------------------------------------------
     def fbp_fan(self, proj, g: Geom, weighting_type=1):
         """fan_weighting -> ramp(fan) -> bp_fan_2d, as the reference's CPU

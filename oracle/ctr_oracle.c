@@ -161,6 +161,50 @@ int orc_fp_par_2d_prep(const orc_geom* g, double* sincostbl, double* beginoffset
     return 1;
 }
 
+/* src/fp_par_2d.cc:18-80: ray casting.  The view angle and the channel's
+ * detector coordinate are running sums (angle += orbit, s += ds), the angle
+ * is not wrapped, and a ray takes (int)(chord / step) samples of step
+ * step_size (pixels) from its entry point on the FoV circle of radius fov;
+ * a ray that misses the circle has none. */
+int orc_fp_par_2d_cast_prep(const orc_geom* g, double step_size, double* sincostbl, double* begins,
+                            int* nsteps)
+{
+    const double xc = (double)(g->nx - 1) / 2.0 + g->offset_x;
+    const double yc = (double)(g->ny - 1) / 2.0 + g->offset_y;
+    const double fov2 = g->fov * g->fov;
+    const double s0 = -((double)(g->ns - 1) / 2.0 + g->offset_s) * g->ds;
+    double angle = g->orbit_start;
+    for (unsigned ia = 0; ia < g->na; ++ia) {
+        const double sa = sin(angle), ca = cos(angle);
+        sincostbl[2 * ia] = sa;
+        sincostbl[2 * ia + 1] = ca;
+        const double sx = step_size * sa, sy = step_size * ca;
+        const int along_x = sa > (1.0 / 1.414);
+        double s = s0;
+        for (unsigned is = 0; is < g->ns; ++is) {
+            const size_t r = (size_t)ia * g->ns + is;
+            const double h2 = fov2 - s * s;
+            if (h2 > 0) {
+                const double h = sqrt(h2);
+                const double x1 = (s * ca - h * sa) / g->dx + xc;
+                const double y1 = -(s * sa + h * ca) / g->dy + yc;
+                const double x2 = (s * ca + h * sa) / g->dx + xc;
+                const double y2 = -(s * sa - h * ca) / g->dy + yc;
+                nsteps[r] = along_x ? (int)((x2 - x1) / sx) : (int)((y2 - y1) / sy);
+                begins[2 * r] = x1;
+                begins[2 * r + 1] = y1;
+            } else {
+                nsteps[r] = 0;
+                begins[2 * r] = 0;
+                begins[2 * r + 1] = 0;
+            }
+            s += g->ds;
+        }
+        angle += g->orbit;
+    }
+    return 1;
+}
+
 /* src/fp_par_2d.cc:285-321: the angle is NOT wrapped here (as in the
  * reference); pos holds, per view, n = nx = ny (channel start, channel step)
  * pairs. */

@@ -137,6 +137,16 @@ int orc_fp_par_2d_grad_rows_f64(const orc_geom* g, unsigned y0, unsigned y1,
                                 const double* proj, double* img, const double* weights,
                                 const double* pos, const int* usex);
 
+/* ---- parallel ray-casting FP: src/fp_par_2d.cc:18-145 ---- */
+int orc_fp_par_2d_cast_prep(const orc_geom* g, double step_size, double* sincostbl, double* begins,
+                            int* nsteps);
+int orc_fp_par_2d_cast_views_f32(const orc_geom* g, unsigned a0, unsigned a1, double step_size,
+                                 const float* img, float* proj, const double* sincostbl,
+                                 const double* begins, const int* nsteps);
+int orc_fp_par_2d_cast_views_f64(const orc_geom* g, unsigned a0, unsigned a1, double step_size,
+                                 const double* img, double* proj, const double* sincostbl,
+                                 const double* begins, const int* nsteps);
+
 #ifdef __cplusplus
 }
 #endif

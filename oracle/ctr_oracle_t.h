@@ -338,6 +338,44 @@ int ORC_FN(orc_fp_par_2d_views)(const orc_geom* g, unsigned a0, unsigned a1, con
     return 1;
 }
 
+/* src/fp_par_2d.cc:82-145: ray casting of views [a0, a1).  Positions run as
+ * FP64 sums from the entry point; a sample inside [0, nx-1] x [0, ny-1] adds
+ * the bilinear interpolation (floor / ceil corners) to a double sum, scaled by
+ * step_size * dx at the end. */
+int ORC_FN(orc_fp_par_2d_cast_views)(const orc_geom* g, unsigned a0, unsigned a1, double step_size,
+                                     const T* img, T* proj, const double* sincostbl,
+                                     const double* begins, const int* nsteps)
+{
+    const double xmax = (double)g->nx - 1, ymax = (double)g->ny - 1;
+    for (unsigned ia = a0; ia < a1; ++ia) {
+        const double sx = step_size * sincostbl[2 * ia], sy = step_size * sincostbl[2 * ia + 1];
+        for (unsigned is = 0; is < g->ns; ++is) {
+            const size_t r = (size_t)ia * g->ns + is;
+            const int nstep = nsteps[r];
+            if (nstep <= 0) {
+                proj[r] = 0;
+                continue;
+            }
+            double x = begins[2 * r], y = begins[2 * r + 1], sum = 0;
+            for (int k = 0; k < nstep; ++k) {
+                if (x >= 0 && x <= xmax && y >= 0 && y <= ymax) {
+                    const int ix1 = (int)floor(x), ix2 = (int)ceil(x);
+                    const int iy1 = (int)floor(y), iy2 = (int)ceil(y);
+                    const double u = x - ix1, v = y - iy1;
+                    const T* r1 = img + (size_t)iy1 * g->nx;
+                    const T* r2 = img + (size_t)iy2 * g->nx;
+                    sum += (1 - v) * ((1 - u) * r1[ix1] + u * r1[ix2]) +
+                           v * ((1 - u) * r2[ix1] + u * r2[ix2]);
+                }
+                x += sx;
+                y += sy;
+            }
+            proj[r] = (T)(sum * step_size * g->dx);
+        }
+    }
+    return 1;
+}
+
 /* src/fp_par_2d.cc:323-391: per-pixel gather over each view's channel
  * footprint (triangle weights), rows [y0, y1) of the image. */
 int ORC_FN(orc_fp_par_2d_grad_rows)(const orc_geom* g, unsigned y0, unsigned y1, const T* proj,

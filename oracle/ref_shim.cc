@@ -132,8 +132,26 @@ ParallelProjection2DParam fp_param(const orc_geom* g)
             .calculate_on_cpu(proj, img, weights, pos, usex);                                  \
     }
 
+#define REF_CAST(T, SFX)                                                                       \
+    extern "C" int ref_fp_par_2d_cast_##SFX(const orc_geom* g, double step_size, const T* img,  \
+                                            T* proj, const double* sc, const double* begins,    \
+                                            const int* nsteps)                                  \
+    {                                                                                          \
+        return ParallelProjection2DRayCasting<T>(fp_param(g), step_size)                       \
+            .calculate_on_cpu(img, proj, sc, begins, nsteps);                                  \
+    }
+
 REF_T(float, f32)
 REF_T(double, f64)
+REF_CAST(float, f32)
+REF_CAST(double, f64)
+
+extern "C" int ref_fp_par_2d_cast_prep(const orc_geom* g, double step_size, double* sc,
+                                       double* begins, int* nsteps)
+{
+    return ParallelProjection2DRayCastingPrepare(fp_param(g), step_size)
+        .calculate_on_cpu(sc, begins, nsteps);
+}
 
 extern "C" int ref_ramp_filter_prep(unsigned ns, double ds, double dsd, int type,
                                     double* filter)

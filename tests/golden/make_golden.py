@@ -7,7 +7,7 @@ fixtures pin the oracle port (tests/test_oracle_golden.py) and the CUDA path
 (tests/test_parity_gpu.py).  Needs the reference checkout, so it runs only
 where that exists:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 
 Operators whose reference code is not well defined (the parallel-BP grad and
 the fan-angle grad) have no reference fixture; their oracle is pinned by the
@@ -62,6 +62,14 @@ CASES = {
     "fp_full_wrap": dict(kind="fp", g=dict(ns=67, na=72, ds=7.0, orbit=2 * math.pi / 72,
                                            orbit_start=-0.2, nx=48, ny=48, dx=6.0, dy=6.0,
                                            offset_x=0.3, offset_y=0.1)),
+    # ray casting (src/fp_par_2d.cc:18-145): the FoV radius bounds the rays
+    "cast_half": dict(kind="cast", step=0.125,
+                      g=dict(ns=91, na=60, ds=4.5, orbit=math.pi / 60, nx=64, ny=64, dx=4.0,
+                             dy=4.0, offset_s=0.25, fov=120.0)),
+    "cast_full_rect": dict(kind="cast", step=0.25,
+                           g=dict(ns=67, na=72, ds=7.0, orbit=-2 * math.pi / 72, orbit_start=0.3,
+                                  nx=48, ny=40, dx=6.0, dy=6.0, offset_x=0.3, offset_y=-0.2,
+                                  fov=150.0)),
 }
 
 
@@ -136,18 +144,27 @@ def make_case(name, spec, ref: Oracle):
             out[f"fp_{sfx}"] = ref.fp_par_2d(img.astype(dt), g)
             out[f"proj_in_{sfx}"] = proj_in.astype(dt)
             out[f"fp_grad_{sfx}"] = ref.fp_par_2d_grad(proj_in.astype(dt), g)
+    elif kind == "cast":
+        img = syn.rasterize(ph, g.nx, g.ny, g.dx, g.dy, g.offset_x, g.offset_y, dtype=np.float64)
+        img += 0.001 * rng.standard_normal(img.shape)
+        out["step"] = np.float64(spec["step"])
+        for sfx, dt in (("f32", np.float32), ("f64", np.float64)):
+            out[f"img_{sfx}"] = img.astype(dt)
+            out[f"cast_{sfx}"] = ref.fp_par_2d_cast(img.astype(dt), g, spec["step"])
     else:
         raise ValueError(kind)
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
 
 
-def main():
+def main(names=None):
     build(ref=True)
     ref = Oracle("reference")
     for name, spec in CASES.items():
+        if names and name not in names:
+            continue
         make_case(name, spec, ref)
         print("wrote", name)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])
