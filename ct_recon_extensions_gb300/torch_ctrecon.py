@@ -341,15 +341,20 @@ class ParallelBackprojection2DOp:
 
 
 class ParallelProjection2DOp:
-    """ParallelProjection2DRayDriven{Prepare,,GradPrep,Grad} (reference
-    include/fp_par_2d.h:209-278)."""
+    """Parallel-beam forward projection, `method` as the reference op's attr:
+    "raydriven" (ParallelProjection2DRayDriven{Prepare,,GradPrep,Grad},
+    reference include/fp_par_2d.h:209-278) or "raycasting"
+    (ParallelProjection2DRayCasting{Prepare,}, include/fp_par_2d.h:155-203,
+    step_size pixels per sample, rays bounded by the FoV circle of radius fov;
+    no gradient, as in the reference)."""
 
     def __init__(self, ns, na, ds, orbit, offset_s, orbit_start, nx, ny, dx, dy, offset_x,
-                 offset_y, fov=-1.0, method="raydriven"):
-        if method != "raydriven":
-            raise ValueError(f"projection method {method!r}: only 'raydriven' is implemented")
-        if nx != ny:
+                 offset_y, fov=-1.0, method="raydriven", step_size=0.125):
+        if method not in ("raydriven", "raycasting"):
+            raise ValueError(f"projection method {method!r}: 'raydriven' or 'raycasting'")
+        if method == "raydriven" and nx != ny:
             raise ValueError("Image should have same width and height for raydriven projection.")
+        self.method, self.step_size = method, float(step_size)
         self.p = ParParam(ns, na, ds, orbit, offset_s, orbit_start, nx, ny, dx, dy, offset_x,
                           offset_y, fov)
         self.ns, self.na, self.nx, self.ny = ns, na, nx, ny
@@ -357,6 +362,16 @@ class ParallelProjection2DOp:
         self._adj_tables = _Tables()
 
     def tables(self, device):
+        if self.method == "raycasting":
+            def build_cast(dev):
+                sc = torch.empty((self.na, 2), dtype=torch.float64, device=dev)
+                bg = torch.empty((self.na, self.ns, 2), dtype=torch.float64, device=dev)
+                nst = torch.empty((self.na, self.ns), dtype=torch.int32, device=dev)
+                call("ctr_fp_par_2d_cast_prep", ctypes.byref(self.p), self.step_size, _ptr(sc),
+                     _ptr(bg), _ptr(nst), _stream())
+                return sc, bg, nst
+            return self._fwd_tables.get(device, build_cast)
+
         def build(dev):
             sc = torch.empty((self.na, 2), dtype=torch.float64, device=dev)
             bo = torch.empty((self.na, self.ns, 2), dtype=torch.float64, device=dev)
@@ -379,11 +394,18 @@ class ParallelProjection2DOp:
     def forward(self, img):
         xb, restore = _as_batch(img, self.ny, self.nx, "fp_par_2d")
         proj = torch.empty((xb.shape[0], self.na, self.ns), dtype=xb.dtype, device=xb.device)
-        call(f"ctr_fp_par_2d_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(proj),
-             *map(_ptr, self.tables(xb.device)), xb.shape[0], _stream())
+        if self.method == "raycasting":
+            call(f"ctr_fp_par_2d_cast_{_sfx(xb)}", ctypes.byref(self.p), self.step_size, _ptr(xb),
+                 _ptr(proj), *map(_ptr, self.tables(xb.device)), xb.shape[0], _stream())
+        else:
+            call(f"ctr_fp_par_2d_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(proj),
+                 *map(_ptr, self.tables(xb.device)), xb.shape[0], _stream())
         return restore(proj)
 
     def adjoint(self, proj):
+        if self.method == "raycasting":
+            raise NotImplementedError("Gradient is not yet implemented for raycasting forward "
+                                      "projector.")
         xb, restore = _as_batch(proj, self.na, self.ns, "fp_par_2d_grad")
         img = torch.empty((xb.shape[0], self.ny, self.nx), dtype=xb.dtype, device=xb.device)
         call(f"ctr_fp_par_2d_grad_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(img),

@@ -253,6 +253,22 @@ int ctr_fp_par_2d_grad_f64(const ctr_par_param* p, const double* proj, double* i
                            const double* weights, const double* pos, const int* usex,
                            int batch, cudaStream_t stream);
 
+/* ---- parallel-beam ray-casting forward projection
+ *      (reference include/fp_par_2d.h:155-203, src/fp_par_2d.cc:18-145) ----
+ * Prep (ParallelProjection2DRayCastingPrepare, its step_size argument):
+ * sincostbl double[na][2], begins double[na][ns][2] (the ray's entry point on
+ * the FoV circle of radius fov, in pixel indices), nsteps int[na][ns].
+ * Forward (ParallelProjection2DRayCasting): samples every step_size pixels;
+ * the reference has no gradient for this method. */
+int ctr_fp_par_2d_cast_prep(const ctr_par_param* p, double step_size, double* sincostbl,
+                            double* begins, int* nsteps, cudaStream_t stream);
+int ctr_fp_par_2d_cast_f32(const ctr_par_param* p, double step_size, const float* img,
+                           float* proj, const double* sincostbl, const double* begins,
+                           const int* nsteps, int batch, cudaStream_t stream);
+int ctr_fp_par_2d_cast_f64(const ctr_par_param* p, double step_size, const double* img,
+                           double* proj, const double* sincostbl, const double* begins,
+                           const int* nsteps, int batch, cudaStream_t stream);
+
 /* ---- allocation-free FP32 forward projection (no counterpart in the
  *      reference; same arguments and results as ctr_fp_par_2d_f32) ----
  * For callers that cannot allocate device memory inside a call: a host that

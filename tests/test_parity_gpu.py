@@ -91,6 +91,25 @@ def test_fp_ray_driven(name, sfx, dt):
     assert rel_l2(host(op.adjoint(cuda(c[f"proj_in_{sfx}"]))), c[f"fp_grad_{sfx}"]) <= tol(dt)
 
 
+def _cast_op(g, step):
+    from ct_recon_extensions_gb300 import torch_ctrecon as tc
+    return tc.ParallelProjection2DOp(g["ns"], g["na"], g["ds"], g["orbit"], g["offset_s"],
+                                     g["orbit_start"], g["nx"], g["ny"], g["dx"], g["dy"],
+                                     g["offset_x"], g["offset_y"], g["fov"], method="raycasting",
+                                     step_size=step)
+
+
+@pytest.mark.parametrize("name", gc.names("cast"))
+@pytest.mark.parametrize("sfx,dt", DT)
+def test_fp_ray_casting(name, sfx, dt):
+    c = gc.load(name)
+    g = c["geom"]
+    op = _cast_op(g, float(c["step"]))
+    assert rel_l2(host(op.forward(cuda(c[f"img_{sfx}"]))), c[f"cast_{sfx}"]) <= tol(dt)
+    with pytest.raises(NotImplementedError):
+        op.adjoint(cuda(np.zeros((g["na"], g["ns"]), dt)))
+
+
 # ---- adjoint dot tests --------------------------------------------------------
 
 def _dot(op, x_shape, y_shape, dt, seed=0):
@@ -191,6 +210,26 @@ def test_parallel_config2_white_noise(oracle_port):
     rec = host(par_op(d).forward(ramp_op(d, d["na"], 0, dsd=-1.0).forward(cuda(sino))))
     ref = oracle_port.bp_par_2d(oracle_port.ramp_filter(sino, g.ds, -1.0, 0), g)
     assert rel_l2(rec, ref) <= 1e-5  # measured 7.6e-6
+
+
+def test_fp_ray_casting_config2(oracle_port):
+    """Ray casting at 512^2 (0.5 mm) -> 720 views x 729 bins over pi, FoV radius
+    128 mm, step 0.125 pixel, against the oracle (~1.7e9 samples), and a batch
+    of 3 equal to its items."""
+    from oracle import Geom
+    from ct_recon_extensions_gb300 import synthetic as syn
+    d = dict(syn.parallel_config_2(), fov=128.0)
+    g = Geom.make(**d)
+    img0 = syn.rasterize(syn.random_ellipses(2200), 512, 512, 0.5, 0.5)
+    op = _cast_op(d, 0.125)
+    out = host(op.forward(cuda(img0)))
+    assert rel_l2(out, oracle_port.fp_par_2d_cast(img0, g, 0.125)) <= 1e-5
+    rng = np.random.default_rng(5)
+    stack = np.stack([img0, rng.random((512, 512)).astype(np.float32), np.zeros((512, 512), np.float32)])
+    outs = host(op.forward(cuda(stack)))
+    assert np.array_equal(outs[0], out)
+    assert np.array_equal(outs[1], host(op.forward(cuda(stack[1]))))
+    assert np.all(outs[2] == 0)
 
 
 def test_fp_adjoint_config2_batch(oracle_port):
