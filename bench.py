@@ -23,7 +23,9 @@ headline size (fan weighting -> ramp(fan) -> bp_fan_2d, 720 x 736 -> 512x512);
 against 64 plain calls; ``gd_config4`` gradient descent through the
 differentiable forward projector (batch 16); ``lowp_config5`` the 2048^2
 fan slice from FP32, BF16 and FP16 sinograms (tensor-core filter), with its
-error against the FP64 oracle on image strips when the CPU-baseline leg runs.
+error against the FP64 oracle on image strips when the CPU-baseline leg runs;
+``fp_methods`` the parallel forward projector's other method, ray casting
+(512^2 -> 720 x 729, FoV radius 128 mm, 0.125-pixel steps), beside ray driven.
 
 ``--impl reference`` times the reference's CPU implementation of the same
 workload on this host (the compiled reference when its build is present,
@@ -53,7 +55,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "FBP slices/s and pixel-view updates/s at rel-L2<=1e-4 vs FP64; batched vs plain"
 SM_COUNT = 152
-LEGS = ("fan", "batched", "gd", "lowp")
+LEGS = ("fan", "batched", "gd", "lowp", "fpmethods")
 FP32_LANES_PER_SM = 128
 
 
@@ -445,6 +447,50 @@ def run_batched(device, steps, warmup, dist):
                                             "tuned_ms", "graph", "launches_per_run")},
         "gpu_launches": int(info["launches_per_run"]) * k, "runs": k,
     }
+
+
+def run_fp_methods(device, steps, warmup, dist):
+    """The parallel forward projector by method on the headline geometry
+    (512^2 at 0.5 mm -> 720 views x 729 bins over pi): ray casting with a 128 mm
+    FoV radius and 0.125-pixel steps (its kept samples counted from the prep's
+    step counts, clipped to the image), and ray driven, one image per call."""
+    import torch
+    from ct_recon_extensions_gb300 import synthetic as syn
+    from ct_recon_extensions_gb300 import torch_ctrecon as tc
+    g = dict(syn.parallel_config_2(), fov=128.0)
+    img = torch.from_numpy(syn.rasterize(syn.random_ellipses(4100), g["nx"], g["ny"], g["dx"],
+                                         g["dy"])).float().to(device)
+    out = {}
+    for method in ("raycasting", "raydriven"):
+        op = tc.ParallelProjection2DOp(g["ns"], g["na"], g["ds"], g["orbit"], g["offset_s"],
+                                       g["orbit_start"], g["nx"], g["ny"], g["dx"], g["dy"],
+                                       g["offset_x"], g["offset_y"], g["fov"], method=method)
+        for _ in range(max(1, warmup)):
+            op.forward(img)
+        k = max(3, min(steps, 50))
+        stream = torch.cuda.current_stream()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        dist.barrier()
+        torch.cuda.synchronize()
+        t0.record(stream)
+        for _ in range(k):
+            op.forward(img)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        dist.barrier()
+        ms = dist.max(t0.elapsed_time(t1)) / k
+        row = {"ms_per_call": ms, "projections_per_s": 1e3 / ms, "calls": k}
+        if method == "raycasting":
+            steps_total = float(op.tables(img.device)[2].to(torch.int64).sum())
+            row.update({"samples_per_call": steps_total, "gsamples_per_s": steps_total / ms / 1e6,
+                        "step_size": op.step_size, "fov_mm": g["fov"], "gpu_launches": k})
+        else:
+            row.update({"gpu_launches": 2 * k})
+        out[method] = row
+    out["workload"] = ("fp_par_2d by method, 512^2 @0.5 mm -> 720 x 729 over pi; ray casting: "
+                       "FoV radius 128 mm, 0.125-pixel steps")
+    return out
 
 
 def run_gd(device, steps, warmup, dist):
@@ -933,6 +979,10 @@ def main():
     # ---- differentiable pair: gradient descent (config 4) ----
     if "gd" in args.legs:
         extra["gd_config4"] = run_gd(device, args.steps, args.warmup, dist)
+
+    # ---- the forward projector's other method (ray casting) ----
+    if "fpmethods" in args.legs:
+        extra["fp_methods"] = run_fp_methods(device, args.steps, args.warmup, dist)
 
     # ---- reduced-precision large slice (config 5); its FP64 check is CPU
     #      oracle work on rank 0, part of the CPU-baseline leg ----
