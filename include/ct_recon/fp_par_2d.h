@@ -1,5 +1,6 @@
 // C++ mirror of the reference's include/fp_par_2d.h (ray-driven parallel
-// projection, its prep, grad prep and grad) over libctrecon_gb300.
+// projection, its prep, grad prep and grad; ray casting and its prep) over
+// libctrecon_gb300.
 #ifndef CT_RECON_GB300_FP_PAR_2D_H_
 #define CT_RECON_GB300_FP_PAR_2D_H_
 
@@ -100,6 +101,60 @@ public:
 
 protected:
     ParallelProjection2DParam param_;
+};
+
+// Ray casting (reference include/fp_par_2d.h:155-203): samples every step_size
+// pixels inside the FoV circle of radius fov; no gradient, as in the reference.
+class ParallelProjection2DRayCastingPrepare {
+public:
+    explicit ParallelProjection2DRayCastingPrepare(const ParallelProjection2DParam& param,
+                                                   const double step_size = 0.125)
+        : param_(param), step_size_(step_size)
+    {}
+    virtual ~ParallelProjection2DRayCastingPrepare() {}
+    bool calculate_on_cpu(double*, double*, int*) const { return false; }
+    // sincostbl double[na][2], begins double[na][ns][2], nsteps int[na][ns] (device)
+    bool calculate_on_gpu(double* sincostbl, double* begins, int* nsteps, cudaStream_t stream) const
+    {
+        const ctr_par_param p = param_.c();
+        return detail::finish(ctr_fp_par_2d_cast_prep(&p, step_size_, sincostbl, begins, nsteps, stream),
+                              stream);
+    }
+
+protected:
+    ParallelProjection2DParam param_;
+    double step_size_;
+};
+
+template <typename T>
+class ParallelProjection2DRayCasting {
+public:
+    explicit ParallelProjection2DRayCasting(const ParallelProjection2DParam& param,
+                                            const double step_size = 0.125)
+        : param_(param), step_size_(step_size)
+    {}
+    virtual ~ParallelProjection2DRayCasting() {}
+    bool calculate_on_cpu(const T*, T*, const double*, const double*, const int*) const
+    {
+        return false;
+    }
+    bool calculate_on_gpu(const T* img, T* proj, const double* sincostbl, const double* begins,
+                          const int* nsteps, cudaStream_t stream) const
+    {
+        const ctr_par_param p = param_.c();
+        const int st = detail::Precision<T>::is_double
+                           ? ctr_fp_par_2d_cast_f64(&p, step_size_, reinterpret_cast<const double*>(img),
+                                                    reinterpret_cast<double*>(proj), sincostbl, begins,
+                                                    nsteps, 1, stream)
+                           : ctr_fp_par_2d_cast_f32(&p, step_size_, reinterpret_cast<const float*>(img),
+                                                    reinterpret_cast<float*>(proj), sincostbl, begins,
+                                                    nsteps, 1, stream);
+        return detail::finish(st, stream);
+    }
+
+protected:
+    ParallelProjection2DParam param_;
+    double step_size_;
 };
 
 }  // namespace ct_recon
