@@ -322,6 +322,47 @@ class Oracle:
                                                   _p(nsteps)))
         return proj
 
+    # -- parallel distance-driven FP and its grad (src/fp_par_2d.cc:396-653) ----
+    def fp_par_2d_dd_tables(self, g: Geom):
+        sc = np.empty((g.na, 2)); bo = np.empty((g.na, g.ns, 3)); usex = np.empty(g.na, np.int32)
+        self._fn("fp_par_2d_dd_prep")(ctypes.byref(g), _p(sc), _p(bo), _p(usex))
+        return sc, bo, usex
+
+    def fp_par_2d_dd_grad_tables(self, g: Geom):
+        if g.nx != g.ny:
+            raise ValueError("distance-driven projection needs nx == ny")
+        w = np.empty(g.na); pos = np.empty((g.na, g.nx, 2)); usex = np.empty(g.na, np.int32)
+        self._fn("fp_par_2d_dd_grad_prep")(ctypes.byref(g), _p(w), _p(pos), _p(usex))
+        return w, pos, usex
+
+    def fp_par_2d_dd(self, img, g: Geom):
+        img = self._c(img)
+        assert img.shape == (g.ny, g.nx)
+        sc, bo, usex = self.fp_par_2d_dd_tables(g)
+        proj = np.empty((g.na, g.ns), dtype=img.dtype)
+        if self.kind == "reference":
+            self._fn(f"fp_par_2d_dd_{_sfx(img.dtype)}")(ctypes.byref(g), _p(img), _p(proj), _p(sc),
+                                                        _p(bo), _p(usex))
+        else:
+            f = self._fn(f"fp_par_2d_dd_views_{_sfx(img.dtype)}")
+            self._run_ranges(g.na, lambda a, b: f(ctypes.byref(g), _c_uint(a), _c_uint(b),
+                                                  _p(img), _p(proj), _p(sc), _p(bo), _p(usex)))
+        return proj
+
+    def fp_par_2d_dd_grad(self, proj, g: Geom):
+        proj = self._c(proj)
+        assert proj.shape == (g.na, g.ns)
+        w, pos, usex = self.fp_par_2d_dd_grad_tables(g)
+        img = np.empty((g.ny, g.nx), dtype=proj.dtype)
+        if self.kind == "reference":
+            self._fn(f"fp_par_2d_dd_grad_{_sfx(proj.dtype)}")(ctypes.byref(g), _p(proj), _p(img),
+                                                              _p(w), _p(pos), _p(usex))
+        else:
+            f = self._fn(f"fp_par_2d_dd_grad_rows_{_sfx(proj.dtype)}")
+            self._run_ranges(g.ny, lambda a, b: f(ctypes.byref(g), _c_uint(a), _c_uint(b),
+                                                  _p(proj), _p(img), _p(w), _p(pos), _p(usex)))
+        return img
+
     # -- composed FBP -------------------------------------------------------
     def fbp_fan(self, proj, g: Geom, weighting_type=1):
         """fan_weighting -> ramp(fan) -> bp_fan_2d, as the reference's CPU

@@ -205,6 +205,82 @@ int orc_fp_par_2d_cast_prep(const orc_geom* g, double step_size, double* sincost
     return 1;
 }
 
+/* src/fp_par_2d.cc:396-452: distance driven.  The running angle is wrapped
+ * into [0, 2pi); per channel (footprint centre, step per line, half width),
+ * the centre a running sum over channels. */
+int orc_fp_par_2d_dd_prep(const orc_geom* g, double* sincostbl, double* beginoffset, int* usex)
+{
+    const double centx = (double)(g->nx - 1) / 2.0 + g->offset_x;
+    const double centy = (double)(g->ny - 1) / 2.0 + g->offset_y;
+    const double cents = (double)(g->ns - 1) / 2.0 + g->offset_s;
+    double angle = g->orbit_start;
+    for (unsigned ia = 0; ia < g->na; ++ia) {
+        while (angle < 0) angle += 2 * M_PI;
+        while (angle >= 2 * M_PI) angle -= 2 * M_PI;
+        const double sa = sin(angle), ca = cos(angle);
+        sincostbl[2 * ia] = sa;
+        sincostbl[2 * ia + 1] = ca;
+        usex[ia] = views_along_x(angle);
+        double step, chan, begin;
+        if (usex[ia]) {
+            step = g->dy * sa / (ca * g->dx);
+            chan = g->ds / (ca * g->dx);
+            begin = centx - centy * step - cents * chan;
+        } else {
+            step = g->dx * ca / (sa * g->dy);
+            chan = -g->ds / (sa * g->dy);
+            begin = centy - centx * step - cents * chan;
+        }
+        double* bo = beginoffset + (size_t)ia * g->ns * 3;
+        for (unsigned is = 0; is < g->ns; ++is) {
+            bo[3 * is] = begin;
+            bo[3 * is + 1] = step;
+            bo[3 * is + 2] = chan / 2;
+            begin += chan;
+        }
+        angle += g->orbit;
+    }
+    return 1;
+}
+
+/* src/fp_par_2d.cc:547-596: the angle is NOT wrapped (as in the reference);
+ * per view n = nx = ny (channel of the line's first pixel, channel step). */
+int orc_fp_par_2d_dd_grad_prep(const orc_geom* g, double* weights, double* pos, int* usex)
+{
+    const double centx = (double)(g->nx - 1) / 2.0 + g->offset_x;
+    const double centy = (double)(g->ny - 1) / 2.0 + g->offset_y;
+    const double cents = (double)(g->ns - 1) / 2.0 + g->offset_s;
+    double angle = g->orbit_start;
+    for (unsigned ia = 0; ia < g->na; ++ia) {
+        const double sa = sin(angle), ca = cos(angle);
+        const int ux = views_along_x(angle);
+        usex[ia] = ux;
+        double begin, o1, o2;
+        unsigned n;
+        if (ux) {
+            weights[ia] = fabs(g->dy / ca);
+            o1 = g->dx * ca / g->ds;
+            o2 = -g->dy * sa / g->ds;
+            begin = cents - centx * o1 - centy * o2;
+            n = g->ny;
+        } else {
+            weights[ia] = fabs(g->dx / sa);
+            o1 = -g->dy * sa / g->ds;
+            o2 = g->dx * ca / g->ds;
+            begin = cents - centy * o1 - centx * o2;
+            n = g->nx;
+        }
+        double* pp = pos + (size_t)ia * g->nx * 2;
+        for (unsigned i = 0; i < n; ++i) {
+            pp[2 * i] = begin;
+            pp[2 * i + 1] = o1;
+            begin += o2;
+        }
+        angle += g->orbit;
+    }
+    return 1;
+}
+
 /* src/fp_par_2d.cc:285-321: the angle is NOT wrapped here (as in the
  * reference); pos holds, per view, n = nx = ny (channel start, channel step)
  * pairs. */

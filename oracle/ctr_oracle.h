@@ -147,6 +147,22 @@ int orc_fp_par_2d_cast_views_f64(const orc_geom* g, unsigned a0, unsigned a1, do
                                  const double* img, double* proj, const double* sincostbl,
                                  const double* begins, const int* nsteps);
 
+/* ---- parallel distance-driven FP and its reference grad: src/fp_par_2d.cc:396-653 ---- */
+int orc_fp_par_2d_dd_prep(const orc_geom* g, double* sincostbl, double* beginoffset, int* usex);
+int orc_fp_par_2d_dd_grad_prep(const orc_geom* g, double* weights, double* pos, int* usex);
+int orc_fp_par_2d_dd_views_f32(const orc_geom* g, unsigned a0, unsigned a1, const float* img,
+                               float* proj, const double* sincostbl, const double* beginoffset,
+                               const int* usex);
+int orc_fp_par_2d_dd_views_f64(const orc_geom* g, unsigned a0, unsigned a1, const double* img,
+                               double* proj, const double* sincostbl, const double* beginoffset,
+                               const int* usex);
+int orc_fp_par_2d_dd_grad_rows_f32(const orc_geom* g, unsigned y0, unsigned y1, const float* proj,
+                                   float* img, const double* weights, const double* pos,
+                                   const int* usex);
+int orc_fp_par_2d_dd_grad_rows_f64(const orc_geom* g, unsigned y0, unsigned y1, const double* proj,
+                                   double* img, const double* weights, const double* pos,
+                                   const int* usex);
+
 #ifdef __cplusplus
 }
 #endif

@@ -376,6 +376,109 @@ int ORC_FN(orc_fp_par_2d_cast_views)(const orc_geom* g, unsigned a0, unsigned a1
     return 1;
 }
 
+/* src/fp_par_2d.cc:455-540: distance-driven projection of views [a0, a1).
+ * Per line of the marched axis, the footprint [left, right] (running FP64
+ * sums) averages the trapezoid of neighbouring pixel pairs over the pixel
+ * intervals it covers, in T.  The reference runs the pixel loop with an
+ * unsigned index from floor(left); a negative floor converts (undefined in
+ * C++) to a huge unsigned on the x86-64 builds the fixtures come from, so such
+ * a line contributes nothing: written out here as that rule. */
+int ORC_FN(orc_fp_par_2d_dd_views)(const orc_geom* g, unsigned a0, unsigned a1, const T* img,
+                                   T* proj, const double* sincostbl, const double* beginoffset,
+                                   const int* usex)
+{
+    for (unsigned ia = a0; ia < a1; ++ia) {
+        const double* bo = beginoffset + (size_t)ia * g->ns * 3;
+        const int ux = usex[ia];
+        const double w = ux ? fabs(g->dy / sincostbl[2 * ia + 1]) : fabs(g->dx / sincostbl[2 * ia]);
+        const unsigned nl = ux ? g->ny : g->nx;     /* lines */
+        const unsigned na_ = ux ? g->nx : g->ny;    /* pixels along a line */
+        for (unsigned is = 0; is < g->ns; ++is) {
+            const double c = bo[3 * is], off = bo[3 * is + 1], hw = bo[3 * is + 2];
+            double left = c - hw, right = c + hw;
+            if (left > right) {
+                const double t = left;
+                left = right;
+                right = t;
+            }
+            T sum = 0;
+            for (unsigned l = 0; l < nl; ++l) {
+                T tsum = 0, lsum = 0;
+                const double fl = floor(left), cr = ceil(right);
+                if (fl >= 0) {
+                    for (unsigned i = (unsigned)fl; (double)i < cr; ++i) {
+                        if (i >= na_ - 1) continue;
+                        const double a = (double)(i + 1) < right ? (double)(i + 1) : right;
+                        const double b = (double)i > left ? (double)i : left;
+                        const double len = a - b;
+                        const T p0 = ux ? img[i + (size_t)l * g->nx] : img[l + (size_t)i * g->nx];
+                        const T p1 = ux ? img[i + 1 + (size_t)l * g->nx] : img[l + (size_t)(i + 1) * g->nx];
+                        tsum += len * (p0 + p1) / 2;
+                        lsum += len;
+                    }
+                }
+                if (lsum > 0) sum += tsum / lsum;
+                left += off;
+                right += off;
+            }
+            proj[(size_t)ia * g->ns + is] = (T)(sum * w);
+        }
+    }
+    return 1;
+}
+
+/* src/fp_par_2d.cc:598-653: the reference's distance-driven "gradient", rows
+ * [y0, y1) of the image (not the adjoint of the forward above: that one
+ * normalises by the covered length).  Per pixel and view the channel footprint
+ * [left, right] around the pixel's channel; the channel loop's unsigned index
+ * from ceil(left - 0.5) skips the view when that is negative (see above), and
+ * channels past ns read on into the following view's row, as the reference's
+ * unchecked index does (0 past the last view). */
+int ORC_FN(orc_fp_par_2d_dd_grad_rows)(const orc_geom* g, unsigned y0, unsigned y1, const T* proj,
+                                       T* img, const double* weights, const double* pos,
+                                       const int* usex)
+{
+    const size_t total = (size_t)g->na * g->ns;
+    for (unsigned iy = y0; iy < y1; ++iy) {
+        for (unsigned ix = 0; ix < g->nx; ++ix) {
+            double sum = 0.0;
+            for (unsigned ia = 0; ia < g->na; ++ia) {
+                const double* pp = pos + (size_t)ia * g->nx * 2;
+                double mid, left, right;
+                if (usex[ia]) {
+                    const double begin = pp[2 * iy], off = pp[2 * iy + 1];
+                    mid = begin + off * ix;
+                    left = ix == 0 ? mid : mid - off;
+                    right = ix == g->nx - 1 ? mid : mid + off;
+                } else {
+                    const double begin = pp[2 * ix], off = pp[2 * ix + 1];
+                    mid = begin + off * iy;
+                    left = iy == 0 ? mid : mid - off;
+                    right = iy == g->ny - 1 ? mid : mid + off;
+                }
+                if (left > right) {
+                    const double t = left;
+                    left = right;
+                    right = t;
+                }
+                double tmp = 0.0;
+                const double c0 = ceil(left - 0.5), c1 = floor(right + 0.5);
+                if (c0 >= 0) {
+                    for (unsigned is = (unsigned)c0; (double)is <= c1; ++is) {
+                        const double a = (double)is + 0.5 < right ? (double)is + 0.5 : right;
+                        const double b = (double)is - 0.5 > left ? (double)is - 0.5 : left;
+                        const size_t k = (size_t)ia * g->ns + is;
+                        tmp += (a - b) * (k < total ? proj[k] : 0) / 2;
+                    }
+                }
+                sum += tmp * weights[ia];
+            }
+            img[(size_t)iy * g->nx + ix] = (T)sum;
+        }
+    }
+    return 1;
+}
+
 /* src/fp_par_2d.cc:323-391: per-pixel gather over each view's channel
  * footprint (triangle weights), rows [y0, y1) of the image. */
 int ORC_FN(orc_fp_par_2d_grad_rows)(const orc_geom* g, unsigned y0, unsigned y1, const T* proj,

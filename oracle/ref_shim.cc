@@ -141,10 +141,37 @@ ParallelProjection2DParam fp_param(const orc_geom* g)
             .calculate_on_cpu(img, proj, sc, begins, nsteps);                                  \
     }
 
+#define REF_DD(T, SFX)                                                                         \
+    extern "C" int ref_fp_par_2d_dd_##SFX(const orc_geom* g, const T* img, T* proj,            \
+                                          const double* sc, const double* bo, const int* usex) \
+    {                                                                                          \
+        return ParallelProjection2DDisDriven<T>(fp_param(g))                                   \
+            .calculate_on_cpu(img, proj, sc, bo, usex);                                        \
+    }                                                                                          \
+    extern "C" int ref_fp_par_2d_dd_grad_##SFX(const orc_geom* g, const T* proj, T* img,       \
+                                               const double* w, const double* pos,             \
+                                               const int* usex)                                \
+    {                                                                                          \
+        return ParallelProjection2DDisDrivenGrad<T>(fp_param(g))                               \
+            .calculate_on_cpu(proj, img, w, pos, usex);                                        \
+    }
+
 REF_T(float, f32)
 REF_T(double, f64)
 REF_CAST(float, f32)
 REF_CAST(double, f64)
+REF_DD(float, f32)
+REF_DD(double, f64)
+
+extern "C" int ref_fp_par_2d_dd_prep(const orc_geom* g, double* sc, double* bo, int* usex)
+{
+    return ParallelProjection2DDisDrivenPrep(fp_param(g)).calculate_on_cpu(sc, bo, usex);
+}
+
+extern "C" int ref_fp_par_2d_dd_grad_prep(const orc_geom* g, double* w, double* pos, int* usex)
+{
+    return ParallelProjection2DDisDrivenGradPrep(fp_param(g)).calculate_on_cpu(w, pos, usex);
+}
 
 extern "C" int ref_fp_par_2d_cast_prep(const orc_geom* g, double step_size, double* sc,
                                        double* begins, int* nsteps)

@@ -62,6 +62,13 @@ CASES = {
     "fp_full_wrap": dict(kind="fp", g=dict(ns=67, na=72, ds=7.0, orbit=2 * math.pi / 72,
                                            orbit_start=-0.2, nx=48, ny=48, dx=6.0, dy=6.0,
                                            offset_x=0.3, offset_y=0.1)),
+    # distance driven (src/fp_par_2d.cc:396-653); detectors cover the image
+    # diagonal plus a channel, like the ray-driven cases (unchecked channels)
+    "dd_half": dict(kind="dd", g=dict(ns=91, na=60, ds=4.5, orbit=math.pi / 60, nx=64, ny=64,
+                                      dx=4.0, dy=4.0, offset_s=0.25)),
+    "dd_full_wrap": dict(kind="dd", g=dict(ns=67, na=72, ds=7.0, orbit=2 * math.pi / 72,
+                                           orbit_start=-0.2, nx=48, ny=48, dx=6.0, dy=6.0,
+                                           offset_x=0.3, offset_y=0.1)),
     # ray casting (src/fp_par_2d.cc:18-145): the FoV radius bounds the rays
     "cast_half": dict(kind="cast", step=0.125,
                       g=dict(ns=91, na=60, ds=4.5, orbit=math.pi / 60, nx=64, ny=64, dx=4.0,
@@ -144,6 +151,15 @@ def make_case(name, spec, ref: Oracle):
             out[f"fp_{sfx}"] = ref.fp_par_2d(img.astype(dt), g)
             out[f"proj_in_{sfx}"] = proj_in.astype(dt)
             out[f"fp_grad_{sfx}"] = ref.fp_par_2d_grad(proj_in.astype(dt), g)
+    elif kind == "dd":
+        img = syn.rasterize(ph, g.nx, g.ny, g.dx, g.dy, g.offset_x, g.offset_y, dtype=np.float64)
+        img += 0.001 * rng.standard_normal(img.shape)
+        proj_in = rng.standard_normal((g.na, g.ns))
+        for sfx, dt in (("f32", np.float32), ("f64", np.float64)):
+            out[f"img_{sfx}"] = img.astype(dt)
+            out[f"dd_{sfx}"] = ref.fp_par_2d_dd(img.astype(dt), g)
+            out[f"proj_in_{sfx}"] = proj_in.astype(dt)
+            out[f"dd_grad_{sfx}"] = ref.fp_par_2d_dd_grad(proj_in.astype(dt), g)
     elif kind == "cast":
         img = syn.rasterize(ph, g.nx, g.ny, g.dx, g.dy, g.offset_x, g.offset_y, dtype=np.float64)
         img += 0.001 * rng.standard_normal(img.shape)

@@ -75,6 +75,15 @@ def test_fp_ray_casting(port, name, sfx, dt):
     assert np.array_equal(port.fp_par_2d_cast(c[f"img_{sfx}"], g, float(c["step"])), c[f"cast_{sfx}"])
 
 
+@pytest.mark.parametrize("name", gc.names("dd"))
+@pytest.mark.parametrize("sfx,dt", SFX)
+def test_fp_distance_driven(port, name, sfx, dt):
+    c = gc.load(name)
+    g = gc.geom(c)
+    assert np.array_equal(port.fp_par_2d_dd(c[f"img_{sfx}"], g), c[f"dd_{sfx}"])
+    assert np.array_equal(port.fp_par_2d_dd_grad(c[f"proj_in_{sfx}"], g), c[f"dd_grad_{sfx}"])
+
+
 def _dot_rel(a_x, y, x, at_y):
     lhs = float(np.vdot(a_x.astype(np.float64), y.astype(np.float64)))
     rhs = float(np.vdot(x.astype(np.float64), at_y.astype(np.float64)))
