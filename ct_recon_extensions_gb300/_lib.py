@@ -98,6 +98,8 @@ PROTOTYPES = {
     "ctr_fbp_fan_plan_destroy": [c_void_p],
     "ctr_fp_par_2d_f32_noalloc": [_S(ParParam), _P, _P, _P, _P, _P, c_int, _P],
     "ctr_fp_par_2d_cast_prep": [_S(ParParam), c_double, _P, _P, _P, _P],
+    "ctr_fp_par_2d_dd_prep": [_S(ParParam), _P, _P, _P, _P],
+    "ctr_fp_par_2d_dd_grad_prep": [_S(ParParam), _P, _P, _P, _P],
     "ctr_ramp_filter_tc_create": [_S(FilterParam), _P, _S(FanWeightingParam), c_int, c_int, c_int,
                                   ctypes.POINTER(c_void_p), _P],
     "ctr_ramp_filter_tc_run": [c_void_p, c_int, _P, _P, c_int, _P],
@@ -124,6 +126,8 @@ for _t in ("f32", "f64"):
         f"ctr_fp_par_2d_{_t}": [_S(ParParam), _P, _P, _P, _P, _P, c_int, _P],
         f"ctr_fp_par_2d_grad_{_t}": [_S(ParParam), _P, _P, _P, _P, _P, c_int, _P],
         f"ctr_fp_par_2d_cast_{_t}": [_S(ParParam), c_double, _P, _P, _P, _P, _P, c_int, _P],
+        f"ctr_fp_par_2d_dd_{_t}": [_S(ParParam), _P, _P, _P, _P, _P, c_int, _P],
+        f"ctr_fp_par_2d_dd_grad_{_t}": [_S(ParParam), _P, _P, _P, _P, _P, c_int, _P],
     })
 _RESTYPES = {"ctr_status_string": c_char_p, "ctr_last_error": c_char_p}
 

@@ -343,17 +343,24 @@ class ParallelBackprojection2DOp:
 class ParallelProjection2DOp:
     """Parallel-beam forward projection, `method` as the reference op's attr:
     "raydriven" (ParallelProjection2DRayDriven{Prepare,,GradPrep,Grad},
-    reference include/fp_par_2d.h:209-278) or "raycasting"
+    reference include/fp_par_2d.h:209-278), "raycasting"
     (ParallelProjection2DRayCasting{Prepare,}, include/fp_par_2d.h:155-203,
     step_size pixels per sample, rays bounded by the FoV circle of radius fov;
-    no gradient, as in the reference)."""
+    no gradient, as in the reference) or "disdriven"
+    (ParallelProjection2DDisDriven{Prep,,GradPrep,Grad},
+    include/fp_par_2d.h:283-352; its adjoint is the reference's distance-driven
+    grad, which the reference op registers as the gradient)."""
 
     def __init__(self, ns, na, ds, orbit, offset_s, orbit_start, nx, ny, dx, dy, offset_x,
                  offset_y, fov=-1.0, method="raydriven", step_size=0.125):
-        if method not in ("raydriven", "raycasting"):
-            raise ValueError(f"projection method {method!r}: 'raydriven' or 'raycasting'")
+        if method not in ("raydriven", "raycasting", "disdriven"):
+            raise ValueError(f"projection method {method!r}: 'raydriven', 'raycasting' or "
+                             "'disdriven'")
         if method == "raydriven" and nx != ny:
             raise ValueError("Image should have same width and height for raydriven projection.")
+        if method == "disdriven" and nx != ny:
+            raise ValueError("Image should have same width and height for distance-driven "
+                             "projection.")
         self.method, self.step_size = method, float(step_size)
         self.p = ParParam(ns, na, ds, orbit, offset_s, orbit_start, nx, ny, dx, dy, offset_x,
                           offset_y, fov)
@@ -371,6 +378,15 @@ class ParallelProjection2DOp:
                      _ptr(bg), _ptr(nst), _stream())
                 return sc, bg, nst
             return self._fwd_tables.get(device, build_cast)
+        if self.method == "disdriven":
+            def build_dd(dev):
+                sc = torch.empty((self.na, 2), dtype=torch.float64, device=dev)
+                bo = torch.empty((self.na, self.ns, 3), dtype=torch.float64, device=dev)
+                ux = torch.empty(self.na, dtype=torch.int32, device=dev)
+                call("ctr_fp_par_2d_dd_prep", ctypes.byref(self.p), _ptr(sc), _ptr(bo), _ptr(ux),
+                     _stream())
+                return sc, bo, ux
+            return self._fwd_tables.get(device, build_dd)
 
         def build(dev):
             sc = torch.empty((self.na, 2), dtype=torch.float64, device=dev)
@@ -382,12 +398,13 @@ class ParallelProjection2DOp:
         return self._fwd_tables.get(device, build)
 
     def grad_tables(self, device):
+        name = "ctr_fp_par_2d_dd_grad_prep" if self.method == "disdriven" else "ctr_fp_par_2d_grad_prep"
+
         def build(dev):
             w = torch.empty(self.na, dtype=torch.float64, device=dev)
             pos = torch.empty((self.na, self.nx, 2), dtype=torch.float64, device=dev)
             ux = torch.empty(self.na, dtype=torch.int32, device=dev)
-            call("ctr_fp_par_2d_grad_prep", ctypes.byref(self.p), _ptr(w), _ptr(pos), _ptr(ux),
-                 _stream())
+            call(name, ctypes.byref(self.p), _ptr(w), _ptr(pos), _ptr(ux), _stream())
             return w, pos, ux
         return self._adj_tables.get(device, build)
 
@@ -397,6 +414,9 @@ class ParallelProjection2DOp:
         if self.method == "raycasting":
             call(f"ctr_fp_par_2d_cast_{_sfx(xb)}", ctypes.byref(self.p), self.step_size, _ptr(xb),
                  _ptr(proj), *map(_ptr, self.tables(xb.device)), xb.shape[0], _stream())
+        elif self.method == "disdriven":
+            call(f"ctr_fp_par_2d_dd_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(proj),
+                 *map(_ptr, self.tables(xb.device)), xb.shape[0], _stream())
         else:
             call(f"ctr_fp_par_2d_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(proj),
                  *map(_ptr, self.tables(xb.device)), xb.shape[0], _stream())
@@ -408,7 +428,8 @@ class ParallelProjection2DOp:
                                       "projector.")
         xb, restore = _as_batch(proj, self.na, self.ns, "fp_par_2d_grad")
         img = torch.empty((xb.shape[0], self.ny, self.nx), dtype=xb.dtype, device=xb.device)
-        call(f"ctr_fp_par_2d_grad_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(img),
+        kind = "dd_grad" if self.method == "disdriven" else "grad"
+        call(f"ctr_fp_par_2d_{kind}_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(img),
              *map(_ptr, self.grad_tables(xb.device)), xb.shape[0], _stream())
         return restore(img)
 

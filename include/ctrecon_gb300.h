@@ -269,6 +269,31 @@ int ctr_fp_par_2d_cast_f64(const ctr_par_param* p, double step_size, const doubl
                            double* proj, const double* sincostbl, const double* begins,
                            const int* nsteps, int batch, cudaStream_t stream);
 
+/* ---- parallel-beam distance-driven forward projection and its gradient
+ *      (reference include/fp_par_2d.h:283-352, src/fp_par_2d.cc:396-653) ----
+ * Prep (ParallelProjection2DDisDrivenPrep): sincostbl double[na][2],
+ * beginoffset double[na][ns][3] (footprint centre, step per line, half width),
+ * usex int[na].  Grad prep (...DisDrivenGradPrep): weights double[na],
+ * pos double[na][nx][2], usex int[na].  The grad is the reference's
+ * (ParallelProjection2DDisDrivenGrad), which is not the adjoint of the
+ * length-normalised forward.  Requires nx == ny, as the reference op does. */
+int ctr_fp_par_2d_dd_prep(const ctr_par_param* p, double* sincostbl, double* beginoffset,
+                          int* usex, cudaStream_t stream);
+int ctr_fp_par_2d_dd_grad_prep(const ctr_par_param* p, double* weights, double* pos, int* usex,
+                               cudaStream_t stream);
+int ctr_fp_par_2d_dd_f32(const ctr_par_param* p, const float* img, float* proj,
+                         const double* sincostbl, const double* beginoffset, const int* usex,
+                         int batch, cudaStream_t stream);
+int ctr_fp_par_2d_dd_f64(const ctr_par_param* p, const double* img, double* proj,
+                         const double* sincostbl, const double* beginoffset, const int* usex,
+                         int batch, cudaStream_t stream);
+int ctr_fp_par_2d_dd_grad_f32(const ctr_par_param* p, const float* proj, float* img,
+                              const double* weights, const double* pos, const int* usex,
+                              int batch, cudaStream_t stream);
+int ctr_fp_par_2d_dd_grad_f64(const ctr_par_param* p, const double* proj, double* img,
+                              const double* weights, const double* pos, const int* usex,
+                              int batch, cudaStream_t stream);
+
 /* ---- allocation-free FP32 forward projection (no counterpart in the
  *      reference; same arguments and results as ctr_fp_par_2d_f32) ----
  * For callers that cannot allocate device memory inside a call: a host that

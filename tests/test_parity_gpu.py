@@ -110,6 +110,23 @@ def test_fp_ray_casting(name, sfx, dt):
         op.adjoint(cuda(np.zeros((g["na"], g["ns"]), dt)))
 
 
+def _dd_op(g):
+    from ct_recon_extensions_gb300 import torch_ctrecon as tc
+    return tc.ParallelProjection2DOp(g["ns"], g["na"], g["ds"], g["orbit"], g["offset_s"],
+                                     g["orbit_start"], g["nx"], g["ny"], g["dx"], g["dy"],
+                                     g["offset_x"], g["offset_y"], g["fov"], method="disdriven")
+
+
+@pytest.mark.parametrize("name", gc.names("dd"))
+@pytest.mark.parametrize("sfx,dt", DT)
+def test_fp_distance_driven(name, sfx, dt):
+    c = gc.load(name)
+    g = c["geom"]
+    op = _dd_op(g)
+    assert rel_l2(host(op.forward(cuda(c[f"img_{sfx}"]))), c[f"dd_{sfx}"]) <= tol(dt)
+    assert rel_l2(host(op.adjoint(cuda(c[f"proj_in_{sfx}"]))), c[f"dd_grad_{sfx}"]) <= tol(dt)
+
+
 # ---- adjoint dot tests --------------------------------------------------------
 
 def _dot(op, x_shape, y_shape, dt, seed=0):
@@ -230,6 +247,27 @@ def test_fp_ray_casting_config2(oracle_port):
     assert np.array_equal(outs[0], out)
     assert np.array_equal(outs[1], host(op.forward(cuda(stack[1]))))
     assert np.all(outs[2] == 0)
+
+
+def test_fp_distance_driven_config2(oracle_port):
+    """Distance driven at 512^2 (0.5 mm) -> 720 views x 729 bins over pi and the
+    reference's distance-driven grad, against the oracle; a batch of 2 equal to
+    its items."""
+    from oracle import Geom
+    from ct_recon_extensions_gb300 import synthetic as syn
+    d = syn.parallel_config_2()
+    g = Geom.make(**d)
+    img0 = syn.rasterize(syn.random_ellipses(2300), 512, 512, 0.5, 0.5)
+    op = _dd_op(d)
+    out = host(op.forward(cuda(img0)))
+    assert rel_l2(out, oracle_port.fp_par_2d_dd(img0, g)) <= 1e-5
+    proj = np.random.default_rng(8).standard_normal((d["na"], d["ns"])).astype(np.float32)
+    gr = host(op.adjoint(cuda(proj)))
+    assert rel_l2(gr, oracle_port.fp_par_2d_dd_grad(proj, g)) <= 1e-5
+    stack = np.stack([img0, np.random.default_rng(9).random((512, 512)).astype(np.float32)])
+    outs = host(op.forward(cuda(stack)))
+    assert np.array_equal(outs[0], out)
+    assert np.array_equal(outs[1], host(op.forward(cuda(stack[1]))))
 
 
 def test_fp_adjoint_config2_batch(oracle_port):
