@@ -24,8 +24,9 @@ against 64 plain calls; ``gd_config4`` gradient descent through the
 differentiable forward projector (batch 16); ``lowp_config5`` the 2048^2
 fan slice from FP32, BF16 and FP16 sinograms (tensor-core filter), with its
 error against the FP64 oracle on image strips when the CPU-baseline leg runs;
-``fp_methods`` the parallel forward projector's other method, ray casting
-(512^2 -> 720 x 729, FoV radius 128 mm, 0.125-pixel steps), beside ray driven.
+``fp_methods`` the parallel forward projector's other methods, ray casting
+(512^2 -> 720 x 729, FoV radius 128 mm, 0.125-pixel steps) and distance
+driven, beside ray driven.
 
 ``--impl reference`` times the reference's CPU implementation of the same
 workload on this host (the compiled reference when its build is present,
@@ -452,8 +453,8 @@ def run_batched(device, steps, warmup, dist):
 def run_fp_methods(device, steps, warmup, dist):
     """The parallel forward projector by method on the headline geometry
     (512^2 at 0.5 mm -> 720 views x 729 bins over pi): ray casting with a 128 mm
-    FoV radius and 0.125-pixel steps (its kept samples counted from the prep's
-    step counts, clipped to the image), and ray driven, one image per call."""
+    FoV radius and 0.125-pixel steps (its samples counted from the prep's step
+    counts), distance driven and ray driven, one image per call."""
     import torch
     from ct_recon_extensions_gb300 import synthetic as syn
     from ct_recon_extensions_gb300 import torch_ctrecon as tc
@@ -461,7 +462,7 @@ def run_fp_methods(device, steps, warmup, dist):
     img = torch.from_numpy(syn.rasterize(syn.random_ellipses(4100), g["nx"], g["ny"], g["dx"],
                                          g["dy"])).float().to(device)
     out = {}
-    for method in ("raycasting", "raydriven"):
+    for method in ("raycasting", "disdriven", "raydriven"):
         op = tc.ParallelProjection2DOp(g["ns"], g["na"], g["ds"], g["orbit"], g["offset_s"],
                                        g["orbit_start"], g["nx"], g["ny"], g["dx"], g["dy"],
                                        g["offset_x"], g["offset_y"], g["fov"], method=method)
@@ -485,11 +486,14 @@ def run_fp_methods(device, steps, warmup, dist):
             steps_total = float(op.tables(img.device)[2].to(torch.int64).sum())
             row.update({"samples_per_call": steps_total, "gsamples_per_s": steps_total / ms / 1e6,
                         "step_size": op.step_size, "fov_mm": g["fov"], "gpu_launches": k})
+        elif method == "disdriven":
+            row.update({"line_footprints_per_s": g["na"] * g["ns"] * g["ny"] / ms * 1e3,
+                        "gpu_launches": k})
         else:
             row.update({"gpu_launches": 2 * k})
         out[method] = row
     out["workload"] = ("fp_par_2d by method, 512^2 @0.5 mm -> 720 x 729 over pi; ray casting: "
-                       "FoV radius 128 mm, 0.125-pixel steps")
+                       "FoV radius 128 mm, 0.125-pixel steps; distance driven; ray driven")
     return out
 
 
