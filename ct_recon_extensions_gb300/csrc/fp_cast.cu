@@ -38,49 +38,6 @@ __device__ __forceinline__ float cast_frac(long long X)
     return __uint_as_float(0x3F800000u | (static_cast<unsigned>(X) >> 9)) - 1.0f;
 }
 
-// Samples [k0, k1] of one axis (empty: k1 < k0) and its 32.32 line.
-__device__ void cast_axis(double begin, double step, int nsamp, int ext, long long* X0, long long* S,
-                          int* k0, int* k1)
-{
-    if (ray_fixed_n(begin, step, nsamp, ext, X0, S, k0, k1)) return;
-    int amb[4], namb = 0, c0, c1;
-    if (ray_split_n(begin, step, nsamp, ext, X0, S, &c0, &c1, amb, &namb)) {
-        // the certain range [c0, c1] and up to two ambiguous samples at each
-        // end, decided by the reference's accumulation, walked in order
-        for (int a = 1; a < namb; ++a)
-            for (int b = a; b > 0 && amb[b] < amb[b - 1]; --b) {
-                const int t = amb[b];
-                amb[b] = amb[b - 1];
-                amb[b - 1] = t;
-            }
-        bool in[4] = {false, false, false, false};
-        AccWalk w{begin, 0};
-        for (int a = 0; a < namb; ++a) {
-            acc_advance(&w, step, amb[a]);
-            in[a] = w.x >= 0.0 && w.x <= static_cast<double>(ext - 1);
-        }
-        int lo = c0, hi = c1;
-        for (int k = c0 - 1; k >= c0 - 2; --k) {  // contiguous: stop at the first outside
-            bool ok = false;
-            for (int a = 0; a < namb; ++a)
-                if (amb[a] == k) ok = in[a];
-            if (!ok) break;
-            lo = k;
-        }
-        for (int k = c1 + 1; k <= c1 + 2; ++k) {
-            bool ok = false;
-            for (int a = 0; a < namb; ++a)
-                if (amb[a] == k) ok = in[a];
-            if (!ok) break;
-            hi = k;
-        }
-        *k0 = lo;
-        *k1 = hi;
-        return;
-    }
-    ray_fp64_n(begin, step, nsamp, ext, X0, S, k0, k1);
-}
-
 // The FP32 kernel: a warp takes 32 consecutive rays.  Each lane first sets up
 // one of them (sample range and fixed-point lines), then the warp marches the
 // rays one after the other, lane l taking samples k0 + l, k0 + l + 32, ...: a
@@ -106,8 +63,8 @@ __global__ void __launch_bounds__(kCastThreads)
             const int ia = static_cast<int>(ray / ns);
             const double sx = step_size * sincos[2 * ia], sy = step_size * sincos[2 * ia + 1];
             int kx0, kx1, ky0, ky1;
-            cast_axis(begins[2 * ray], sx, nstep, nx, &X0, &SX, &kx0, &kx1);
-            cast_axis(begins[2 * ray + 1], sy, nstep, ny, &Y0, &SY, &ky0, &ky1);
+            axis_range(begins[2 * ray], sx, nstep, nx, &X0, &SX, &kx0, &kx1);
+            axis_range(begins[2 * ray + 1], sy, nstep, ny, &Y0, &SY, &ky0, &ky1);
             k0 = max(kx0, ky0);
             k1 = min(kx1, ky1);
         }

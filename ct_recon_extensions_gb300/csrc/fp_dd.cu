@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "ctr_common.cuh"
+#include "fp_setup.cuh"
 
 namespace ctr {
 namespace {
@@ -33,23 +34,34 @@ namespace {
 constexpr int kDdThreads = 128;
 constexpr double kDdPi = 3.14159265358979323846;
 
-template <typename T>
-__global__ void __launch_bounds__(kDdThreads)
-    fp_dd_kernel(const T* __restrict__ img, T* __restrict__ proj, const double* __restrict__ sincos,
-                 const double* __restrict__ bo, const int* __restrict__ usex, int ns, int na, int nx, int ny,
-                 double dx, double dy, size_t img_stride, size_t proj_stride)
+// Fraction of a 32.32 fixed-point value, from its low word's top 23 bits.
+__device__ __forceinline__ float dd_frac(long long X)
 {
-    const long long ray = static_cast<long long>(blockIdx.x) * kDdThreads + threadIdx.x;
-    if (ray >= static_cast<long long>(na) * ns) return;
-    const int ia = static_cast<int>(ray / ns);
-    const T* I = img + blockIdx.y * img_stride;
-    const int ux = usex[ia];
-    const double w = ux ? fabs(dy / sincos[2 * ia + 1]) : fabs(dx / sincos[2 * ia]);
-    const int nl = ux ? ny : nx;    // lines
-    const int nal = ux ? nx : ny;   // pixels along a line
+    return __uint_as_float(0x3F800000u | (static_cast<unsigned>(X) >> 9)) - 1.0f;
+}
+
+// imgT[b][x][y] = img[b][y][x] (32 x 32 tiles)
+__global__ void __launch_bounds__(256) dd_transpose(const float* __restrict__ img, float* __restrict__ imgT, int n)
+{
+    __shared__ float t[32][33];
+    const size_t off = static_cast<size_t>(blockIdx.z) * n * n;
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int r = ty; r < 32; r += 8)
+        if (x0 + tx < n && y0 + r < n) t[r][tx] = img[off + static_cast<size_t>(y0 + r) * n + x0 + tx];
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8)
+        if (y0 + tx < n && x0 + r < n) imgT[off + static_cast<size_t>(x0 + r) * n + y0 + tx] = t[tx][r];
+}
+
+// One ray of the forward with the reference's own arithmetic: FP64 edges,
+// interval range and lengths; sums in T (FP32 for T = float).
+template <typename T>
+__device__ T dd_ray_exact(const T* __restrict__ I, const double* __restrict__ b, int ux, int nl, int nal,
+                          int nx)
+{
     const size_t step_line = ux ? static_cast<size_t>(nx) : 1;   // next line
     const size_t step_pix = ux ? 1 : static_cast<size_t>(nx);    // next pixel along the line
-    const double* b = bo + 3 * ray;
     const double off = b[1];
     double left = __dsub_rn(b[0], b[2]), right = __dadd_rn(b[0], b[2]);
     if (left > right) {
@@ -62,7 +74,7 @@ __global__ void __launch_bounds__(kDdThreads)
         const double fl = floor(left), cr = ceil(right);
         T tsum = 0, lsum = 0;
         if (fl >= 0.0) {
-            // intervals i0 .. i1 (i < cr), all but those from nal - 1 on
+            // intervals i0 .. (i < cr), all but those from nal - 1 on
             const int i0 = static_cast<int>(fl);
             const int iend = cr < static_cast<double>(nal - 1) ? static_cast<int>(cr) : nal - 1;
             const T* line = I + static_cast<size_t>(l) * step_line;
@@ -86,7 +98,111 @@ __global__ void __launch_bounds__(kDdThreads)
         left += off;
         right += off;
     }
-    proj[blockIdx.y * proj_stride + ray] = static_cast<T>(sum * w);
+    return sum;
+}
+
+// FP64 forward: the reference's loop, one thread per ray.
+__global__ void __launch_bounds__(kDdThreads)
+    fp_dd_f64(const double* __restrict__ img, double* __restrict__ proj, const double* __restrict__ sincos,
+              const double* __restrict__ bo, const int* __restrict__ usex, int ns, int na, int nx, int ny,
+              double dx, double dy, size_t img_stride, size_t proj_stride)
+{
+    const long long ray = static_cast<long long>(blockIdx.x) * kDdThreads + threadIdx.x;
+    if (ray >= static_cast<long long>(na) * ns) return;
+    const int ia = static_cast<int>(ray / ns);
+    const int ux = usex[ia];
+    const double w = ux ? fabs(dy / sincos[2 * ia + 1]) : fabs(dx / sincos[2 * ia]);
+    const double sum = dd_ray_exact<double>(img + blockIdx.y * img_stride, bo + 3 * ray, ux, ux ? ny : nx,
+                                            ux ? nx : ny, nx);
+    proj[blockIdx.y * proj_stride + ray] = sum * w;
+}
+
+// FP32 forward.  The reference's discontinuous decisions come down to which
+// lines count: a line adds tsum / lsum iff its footprint start satisfies
+// 0 <= left < n-1 (a negative start skips it; from n-1 on no interval is
+// left), a contiguous range of lines since left is a running sum.  That range
+// is decided as the reference decides it (axis_range, and a line exactly at
+// n-1 dropped after an exact check).  Inside it both edges march in 32.32
+// fixed point, and the covered lengths are FP32 relative to the first
+// interval; everything else varies continuously with the edges.  Lines of
+// column-marching views read the transposed copy, so a warp's loads stay
+// within a few rows.  Rays outside the fixed-point range take dd_ray_exact.
+__global__ void __launch_bounds__(kDdThreads)
+    fp_dd_f32(const float* __restrict__ img, const float* __restrict__ imgT, float* __restrict__ proj,
+              const double* __restrict__ sincos, const double* __restrict__ bo, const int* __restrict__ usex,
+              int ns, int na, int n, double dx, double dy, size_t img_stride, size_t proj_stride)
+{
+    const long long ray = static_cast<long long>(blockIdx.x) * kDdThreads + threadIdx.x;
+    if (ray >= static_cast<long long>(na) * ns) return;
+    const int ia = static_cast<int>(ray / ns);
+    const int ux = usex[ia];
+    const float w = static_cast<float>(ux ? fabs(dy / sincos[2 * ia + 1]) : fabs(dx / sincos[2 * ia]));
+    const double* b = bo + 3 * ray;
+    float* out = proj + blockIdx.y * proj_stride + ray;
+    const double off = b[1];
+    double left0 = __dsub_rn(b[0], b[2]), right0 = __dadd_rn(b[0], b[2]);
+    if (left0 > right0) {
+        const double t = left0;
+        left0 = right0;
+        right0 = t;
+    }
+    const int er = static_cast<int>((double_bits(right0) >> 52) & 0x7FF);
+    const int el = static_cast<int>((double_bits(left0) >> 52) & 0x7FF);
+    const int eo = static_cast<int>((double_bits(off) >> 52) & 0x7FF);
+    if (er >= 1043 || el >= 1043 || eo >= 1025 || n < 2) {  // beyond the fixed-point range
+        *out = dd_ray_exact<float>(img + blockIdx.y * img_stride, b, ux, n, n, n) * w;
+        return;
+    }
+    long long XL, S;
+    int k0, k1;
+    axis_range(left0, off, n, n, &XL, &S, &k0, &k1);
+    // a start exactly at n-1 leaves no interval: the range's end there drops
+    if (k0 <= k1) {
+        const double lim = static_cast<double>(n - 1);
+        const long long L = static_cast<long long>(n - 1) << 32, T = tie_units(n);
+        if (off == 0.0) {
+            if (left0 == lim) k1 = k0 - 1;
+        } else {
+            const int ke = off > 0.0 ? k1 : k0;
+            const long long X = XL + static_cast<long long>(ke) * S;
+            if (X > L - T && X < L + T) {
+                AccWalk wk{left0, 0};
+                acc_advance(&wk, off, ke);
+                if (wk.x == lim) {
+                    if (off > 0.0) --k1;
+                    else ++k0;
+                }
+            }
+        }
+    }
+    const float* I = (ux ? img : imgT) + blockIdx.y * img_stride;  // lines are rows of I
+    const long long XR = fix32(right0) + (XL - fix32(left0));        // the same anchor as the left edge
+    long long xl = XL + static_cast<long long>(k0) * S, xr = XR + static_cast<long long>(k0) * S;
+    float sum = 0.0f;
+    for (int l = k0; l <= k1; ++l) {
+        const int h = static_cast<int>(xl >> 32);
+        const int i0 = min(max(h, 0), n - 2);
+        // the start relative to interval i0 (clamped: the fixed-point start may
+        // sit a hair outside [0, n-1) where the exact one is inside)
+        const float lr = h == i0 ? dd_frac(xl) : (h < 0 ? 0.0f : 1.0f);
+        const int hr = static_cast<int>(xr >> 32);
+        const float rr = static_cast<float>(hr - i0) + dd_frac(xr);
+        const int ie = min(hr + (static_cast<unsigned>(xr) != 0u ? 1 : 0), n - 1);
+        const float* line = I + static_cast<size_t>(l) * n;
+        float tsum = 0.0f, lsum = 0.0f;
+        for (int i = i0; i < ie; ++i) {
+            const float j = static_cast<float>(i - i0);
+            const float len = fmaxf(fminf(j + 1.0f, rr) - fmaxf(j, lr), 0.0f);
+            tsum = fmaf(len, (__ldg(line + i) + __ldg(line + i + 1)) * 0.5f, tsum);
+            lsum += len;
+        }
+        // a counted line always covers part of interval i0; where the clamped
+        // fixed-point edges leave no length, that sliver's trapezoid is the mean
+        sum += lsum > 0.0f ? tsum / lsum : (__ldg(line + i0) + __ldg(line + i0 + 1)) * 0.5f;
+        xl += S;
+        xr += S;
+    }
+    *out = sum * w;
 }
 
 template <typename T>
@@ -162,10 +278,25 @@ int dd_forward(const ctr_par_param* p, const T* img, T* proj, const double* sc, 
     int st = check_dd(p, img, proj, sc, bo, usex, batch);
     if (st) return st;
     const unsigned long long rays = static_cast<unsigned long long>(p->na) * p->ns;
-    fp_dd_kernel<T><<<dim3(div_up(rays, kDdThreads), batch), kDdThreads, 0, stream>>>(
-        img, proj, sc, bo, usex, p->ns, p->na, p->nx, p->ny, p->dx, p->dy,
-        static_cast<size_t>(p->nx) * p->ny, static_cast<size_t>(p->na) * p->ns);
-    return check_launch("fp_par_2d distance driven");
+    const size_t is = static_cast<size_t>(p->nx) * p->ny, ps = static_cast<size_t>(p->na) * p->ns;
+    const dim3 grid(div_up(rays, kDdThreads), batch);
+    if constexpr (sizeof(T) == 8) {
+        fp_dd_f64<<<grid, kDdThreads, 0, stream>>>(img, proj, sc, bo, usex, p->ns, p->na, p->nx, p->ny, p->dx,
+                                                   p->dy, is, ps);
+        return check_launch("fp_par_2d distance driven");
+    } else {
+        const int n = static_cast<int>(p->nx);
+        if (batch > 65535) return fail(CTR_ERR_UNSUPPORTED, "batch > 65535");
+        float* imgT = nullptr;
+        cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&imgT), sizeof(float) * is * batch, stream);
+        if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "distance-driven scratch: %s", cudaGetErrorString(e));
+        dd_transpose<<<dim3(div_up(n, 32), div_up(n, 32), batch), 256, 0, stream>>>(img, imgT, n);
+        fp_dd_f32<<<grid, kDdThreads, 0, stream>>>(img, imgT, proj, sc, bo, usex, p->ns, p->na, n, p->dx, p->dy,
+                                                   is, ps);
+        st = check_launch("fp_par_2d distance driven");
+        cudaFreeAsync(imgT, stream);  // after the kernel that reads it
+        return st;
+    }
 }
 
 template <typename T>

@@ -426,4 +426,50 @@ CTR_HD void ray_fp64(double begin, double step, int n, long long* X0, long long*
     ray_fp64_n(begin, step, n, n, X0, Sout, k0o, k1o);
 }
 
+// The exact range [*k0, *k1] (empty: *k1 < *k0) of samples k < n of a line
+// whose FP64 running position (begin + step + ... , k additions) lies in
+// [0, ext-1], with the line's 32.32 fixed-point form: fixed point where that is
+// certain, the accumulation itself (acc_advance) for the up to two ambiguous
+// samples at each end, the plain FP64 walk otherwise.  The position is
+// monotone in k, so the range is contiguous.
+CTR_HD void axis_range(double begin, double step, int n, int ext, long long* X0, long long* S, int* k0,
+                       int* k1)
+{
+    if (ray_fixed_n(begin, step, n, ext, X0, S, k0, k1)) return;
+    int amb[4], namb = 0, c0, c1;
+    if (ray_split_n(begin, step, n, ext, X0, S, &c0, &c1, amb, &namb)) {
+        for (int a = 1; a < namb; ++a)
+            for (int b = a; b > 0 && amb[b] < amb[b - 1]; --b) {
+                const int t = amb[b];
+                amb[b] = amb[b - 1];
+                amb[b - 1] = t;
+            }
+        bool in[4] = {false, false, false, false};
+        AccWalk w{begin, 0};
+        for (int a = 0; a < namb; ++a) {
+            acc_advance(&w, step, amb[a]);
+            in[a] = w.x >= 0.0 && w.x <= static_cast<double>(ext - 1);
+        }
+        int lo = c0, hi = c1;
+        for (int k = c0 - 1; k >= c0 - 2; --k) {  // contiguous: stop at the first outside
+            bool ok = false;
+            for (int a = 0; a < namb; ++a)
+                if (amb[a] == k) ok = in[a];
+            if (!ok) break;
+            lo = k;
+        }
+        for (int k = c1 + 1; k <= c1 + 2; ++k) {
+            bool ok = false;
+            for (int a = 0; a < namb; ++a)
+                if (amb[a] == k) ok = in[a];
+            if (!ok) break;
+            hi = k;
+        }
+        *k0 = lo;
+        *k1 = hi;
+        return;
+    }
+    ray_fp64_n(begin, step, n, ext, X0, S, k0, k1);
+}
+
 }  // namespace ctr
