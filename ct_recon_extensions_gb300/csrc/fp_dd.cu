@@ -242,14 +242,26 @@ __global__ void __launch_bounds__(kDdThreads)
         // channels past the sinogram's end add 0: the loop stops there (finite
         // for any input)
         const double last = fmin(c1, static_cast<double>(total - 1 - static_cast<size_t>(ia) * ns));
+        const int first = static_cast<int>(fmin(c0, last + 1.0));
         Acc tmp = 0;
-        for (int is = static_cast<int>(fmin(c0, last + 1.0)); static_cast<double>(is) <= last; ++is) {
-            const double hi = __dadd_rn(static_cast<double>(is), 0.5), lo = __dsub_rn(static_cast<double>(is), 0.5);
-            const double len = __dsub_rn(hi < right ? hi : right, lo > left ? lo : left);
-            const size_t k = static_cast<size_t>(ia) * ns + is;
-            const T p = k < total ? P[k] : static_cast<T>(0);
-            if constexpr (sizeof(T) == 4) tmp = fmaf(static_cast<float>(len), p * 0.5f, tmp);
-            else tmp += len * p / 2;
+        if constexpr (sizeof(T) == 4) {
+            // the view counts (decided above in FP64); the covered lengths vary
+            // continuously with the edges: FP32, relative to the first channel
+            const float lr = static_cast<float>(__dsub_rn(left, static_cast<double>(first)));
+            const float rr = static_cast<float>(__dsub_rn(right, static_cast<double>(first)));
+            const int cnt = static_cast<int>(last) - first + 1;
+            const float* row = reinterpret_cast<const float*>(P) + static_cast<size_t>(ia) * ns + first;
+            for (int j = 0; j < cnt; ++j) {
+                const float fj = static_cast<float>(j);
+                const float len = fminf(fj + 0.5f, rr) - fmaxf(fj - 0.5f, lr);
+                tmp = fmaf(len, __ldg(row + j) * 0.5f, tmp);
+            }
+        } else {
+            for (int is = first; static_cast<double>(is) <= last; ++is) {
+                const double hi = __dadd_rn(static_cast<double>(is), 0.5), lo = __dsub_rn(static_cast<double>(is), 0.5);
+                const double len = __dsub_rn(hi < right ? hi : right, lo > left ? lo : left);
+                tmp += len * P[static_cast<size_t>(ia) * ns + is] / 2;
+            }
         }
         if constexpr (sizeof(T) == 4) sum = fmaf(tmp, static_cast<float>(weights[ia]), sum);
         else sum += tmp * weights[ia];
