@@ -56,7 +56,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "FBP slices/s and pixel-view updates/s at rel-L2<=1e-4 vs FP64; batched vs plain"
 SM_COUNT = 152
-LEGS = ("fan", "batched", "gd", "lowp", "fpmethods")
+LEGS = ("fan", "batched", "gd", "lowp", "fpmethods", "helical")
 FP32_LANES_PER_SM = 128
 
 
@@ -495,6 +495,122 @@ def run_fp_methods(device, steps, warmup, dist):
     out["workload"] = ("fp_par_2d by method, 512^2 @0.5 mm -> 720 x 729 over pi; ray casting: "
                        "FoV radius 128 mm, 0.125-pixel steps; distance driven; ray driven")
     return out
+
+
+def helical_scan():
+    """A clinical-size helical scan: 736 channels x 64 rows, 1152 views per
+    rotation, pitch 1 (the couch moves nt * dso / dsd per rotation, the row unit
+    of the reference's z -> row mapping), 128 slices of 1 mm over one rotation
+    of couch travel (9 views apart), views enough for 360LI around every slice."""
+    from ct_recon_extensions_gb300._lib import HelicalParam
+    ns, nt, vpr, dso, dsd = 736, 64, 1152, 595.0, 1085.6
+    cm = nt * dso / dsd / vpr
+    nz, step = 128, 9
+    c0 = vpr + 8                      # first slice's nearest view (360LI needs c0 - vpr >= 0)
+    na = c0 + step * (nz - 1) + vpr + 8
+    return HelicalParam(ns=ns, nt=nt, na=na, ds=1.2858, dt=1.0, offset_s=1.25, offset_t=0.0,
+                        orbit_start=0.0, orbit=2 * math.pi / vpr, couch_begin=0.0, couch_mov=cm,
+                        view_per_rot=vpr, nz=nz, dz=step * cm, z0=c0 * cm + 0.1 * cm,
+                        thickness=1.0, dso=dso, dsd=dsd)
+
+
+def helical_bytes(h, method, itemsize):
+    """Algorithmic bytes of one rebinning call: the output plus every input row
+    some sample reads (per view, the union over slices of the thick-slice rows,
+    taken at the extreme fan angles)."""
+    center_s = (h.ns - 1) / 2.0 + h.offset_s
+    gam = (np.array([0.0, h.ns - 1]) - center_s) * h.ds / h.dsd
+    cgs = np.concatenate([np.cos(gam), [1.0]])
+    ct = (h.nt - 1) / 2.0 + h.offset_t
+    lo_v = np.full(h.na, h.nt, np.int64)
+    hi_v = np.zeros(h.na, np.int64)
+    z = h.z0
+    for _ in range(h.nz):
+        c = int(round((z - h.couch_begin) / h.couch_mov))
+        lo, hi = (c - h.view_per_rot, c + h.view_per_rot - 1) if method == "360" else \
+            (c - h.view_per_rot // 2, c - h.view_per_rot // 2 + h.view_per_rot - 1)
+        v = np.arange(max(lo - 1, 0), hi + 1)
+        zd = z - h.couch_begin - v * h.couch_mov
+        for cg in cgs:
+            top = np.clip(ct - (zd + h.thickness / 2) / h.dso * cg * h.dsd, 0, h.nt)
+            bot = np.clip(ct - (zd - h.thickness / 2) / h.dso * cg * h.dsd, 0, h.nt)
+            r0, r1 = np.floor(top).astype(np.int64), np.ceil(bot).astype(np.int64)
+            ok = r1 > r0
+            lo_v[v[ok]] = np.minimum(lo_v[v[ok]], r0[ok])
+            hi_v[v[ok]] = np.maximum(hi_v[v[ok]], r1[ok])
+        z += h.dz
+    rows = np.maximum(hi_v - lo_v, 0).sum()
+    return int(rows) * h.ns * itemsize + h.nz * h.view_per_rot * h.ns * itemsize
+
+
+def run_helical(device, steps, warmup, dist, cpu):
+    """Helical rebinning (360LI and 180LI) of one clinical-size scan per call,
+    T=float (FP64 arithmetic inside, as the reference), input larger than L2;
+    with `cpu`, the oracle port on the host cores over a 2-slice sample."""
+    import torch
+    from ct_recon_extensions_gb300 import torch_ctrecon as tc
+    h = helical_scan()
+    gen = torch.Generator(device=device).manual_seed(11)
+    x = 1 + 0.1 * torch.randn((1, h.na, h.nt, h.ns), generator=gen, device=device)
+    peak = hbm_peak_gbs()
+    out = {"workload": (f"helical scan {h.na} views x {h.nt} rows x {h.ns} ch, "
+                        f"{h.view_per_rot} views/rotation, pitch 1 -> {h.nz} slices x "
+                        f"{h.view_per_rot} x {h.ns}, T=float")}
+    for method in ("360", "180"):
+        op = tc.HelicalInterpolationOp(h.ns, h.nt, h.na, h.ds, h.dt, h.offset_s, h.offset_t,
+                                       h.orbit_start, h.orbit, h.couch_begin, h.couch_mov,
+                                       h.view_per_rot, h.nz, h.dz, h.z0, h.thickness, h.dso,
+                                       h.dsd, method)
+        res = torch.empty((1, h.nz, h.view_per_rot, h.ns), device=device)
+        status = torch.zeros(h.nz, dtype=torch.int32, device=device)
+        for _ in range(max(3, warmup)):
+            op.launch(x, res, status)
+        k = max(3, min(steps, 20))
+        stream = torch.cuda.current_stream()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        dist.barrier()
+        torch.cuda.synchronize()
+        t0.record(stream)
+        for _ in range(k):
+            op.launch(x, res, status)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        dist.barrier()
+        ms = dist.max(t0.elapsed_time(t1)) / k
+        nbytes = helical_bytes(h, method, 4)
+        row = {"ms_per_call": ms, "slices_per_s": h.nz / ms * 1e3,
+               "outputs_per_s": h.nz * h.view_per_rot * h.ns / ms * 1e3,
+               "algorithmic_bytes": nbytes, "achieved_gbs": nbytes / ms / 1e6,
+               "hbm_peak_gbs": peak, "hbm_frac": nbytes / ms / 1e6 / peak,
+               "status_words_nonzero": int((status != 0).sum()), "gpu_launches": k}
+        if cpu:
+            from oracle import Heli, Oracle
+            nthreads = os.cpu_count() or 1
+            sub = Heli(**{f: getattr(h, f) for f, _ in Heli._fields_})
+            sub.nz = 2
+            xs = x[0].cpu().numpy()
+            port = Oracle("port", threads=nthreads)
+            port.helical(xs, sub, method)
+            t = time.perf_counter()
+            port.helical(xs, sub, method)
+            dt = time.perf_counter() - t
+            row["cpu_port"] = {"slices_per_s": 2 / dt, "threads": nthreads,
+                               "sample": "2 slices of the same scan (slices are independent)"}
+            row["gpu_over_cpu"] = row["slices_per_s"] / row["cpu_port"]["slices_per_s"]
+        out[method] = row
+    return out
+
+
+def hbm_peak_gbs():
+    """The HBM copy bandwidth measured on this GPU type, from MEASURED_PEAKS.json
+    beside this file, else the fallback."""
+    p = os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return 6800.0
 
 
 def run_gd(device, steps, warmup, dist):
@@ -987,6 +1103,11 @@ def main():
     # ---- the forward projector's other method (ray casting) ----
     if "fpmethods" in args.legs:
         extra["fp_methods"] = run_fp_methods(device, args.steps, args.warmup, dist)
+
+    # ---- helical rebinning (360LI / 180LI) of a clinical-size scan ----
+    if "helical" in args.legs:
+        extra["helical"] = run_helical(device, args.steps, args.warmup, dist,
+                                       rank == 0 and not args.no_cpu_baseline)
 
     # ---- reduced-precision large slice (config 5); its FP64 check is CPU
     #      oracle work on rank 0, part of the CPU-baseline leg ----

@@ -66,6 +66,18 @@ class ParParam(ctypes.Structure):
                 ("offset_y", c_double), ("fov", c_double)]
 
 
+class HelicalParam(ctypes.Structure):
+    _fields_ = [("ns", c_uint), ("nt", c_uint), ("na", c_uint), ("ds", c_double), ("dt", c_double),
+                ("offset_s", c_double), ("offset_t", c_double), ("orbit_start", c_double),
+                ("orbit", c_double), ("couch_begin", c_double), ("couch_mov", c_double),
+                ("view_per_rot", c_uint), ("nz", c_uint), ("dz", c_double), ("z0", c_double),
+                ("thickness", c_double), ("dso", c_double), ("dsd", c_double)]
+
+
+CTR_HELICAL_360, CTR_HELICAL_180 = 0, 1
+CTR_HELICAL_NO_ROWS, CTR_HELICAL_OUTSIDE, CTR_HELICAL_BAD_TABLE, CTR_HELICAL_NO_VIEWS = 1, 2, 4, 8
+
+
 class PlanInfo(ctypes.Structure):
     _fields_ = [("n_items", c_int), ("work_items", ctypes.c_longlong), ("tile_rows", c_int),
                 ("view_block", c_int), ("ctas", c_int), ("autotuned", c_int),
@@ -106,6 +118,8 @@ PROTOTYPES = {
     "ctr_ramp_filter_tc_info": [c_void_p, ctypes.POINTER(ctypes.c_ulonglong),
                                 ctypes.POINTER(ctypes.c_ulonglong)],
     "ctr_ramp_filter_tc_destroy": [c_void_p],
+    "ctr_helical_interpolation_table_bytes": [_S(HelicalParam)],
+    "ctr_helical_interpolation_prep": [_S(HelicalParam), c_int, _P, _P],
 }
 
 # storage types of ctr_ramp_filter_tc_run's input
@@ -128,8 +142,11 @@ for _t in ("f32", "f64"):
         f"ctr_fp_par_2d_cast_{_t}": [_S(ParParam), c_double, _P, _P, _P, _P, _P, c_int, _P],
         f"ctr_fp_par_2d_dd_{_t}": [_S(ParParam), _P, _P, _P, _P, _P, c_int, _P],
         f"ctr_fp_par_2d_dd_grad_{_t}": [_S(ParParam), _P, _P, _P, _P, _P, c_int, _P],
+        f"ctr_helical_interpolation_360_{_t}": [_S(HelicalParam), _P, _P, _P, _P, c_int, _P],
+        f"ctr_helical_interpolation_180_{_t}": [_S(HelicalParam), _P, _P, _P, _P, c_int, _P],
     })
-_RESTYPES = {"ctr_status_string": c_char_p, "ctr_last_error": c_char_p}
+_RESTYPES = {"ctr_status_string": c_char_p, "ctr_last_error": c_char_p,
+             "ctr_helical_interpolation_table_bytes": ctypes.c_size_t}
 
 _lock = threading.Lock()
 _lib = None

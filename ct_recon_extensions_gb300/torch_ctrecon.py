@@ -23,8 +23,8 @@ from functools import lru_cache
 import torch
 
 from . import _lib
-from ._lib import (FanBpAngleParam, FanBpParam, FanWeightingParam, FilterParam, ParParam,
-                   call)
+from ._lib import (FanBpAngleParam, FanBpParam, FanWeightingParam, FilterParam, HelicalParam,
+                   ParParam, call)
 
 _FILTER_TYPES = {"par": 0, "fan": 1, "flat": 2}
 _WEIGHT_TYPES = {"fan": 1, "flat": 2}
@@ -432,6 +432,92 @@ class ParallelProjection2DOp:
         call(f"ctr_fp_par_2d_{kind}_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(img),
              *map(_ptr, self.grad_tables(xb.device)), xb.shape[0], _stream())
         return restore(img)
+
+
+class HelicalInterpolationOp:
+    """HelicalInterpolation360 / HelicalInterpolation180 (reference
+    include/helical_interpolation.h:17-116, src/helical_interpolation.cc:80-370;
+    CPU-only there): helical sinograms ``[na][nt][ns]`` (view, detector row,
+    channel; optionally with a leading batch dimension) to one fan-beam
+    sinogram per slice, ``[nz][view_per_rot][ns]``.  Bit-identical to the
+    reference.  Raises RuntimeError with the reference's messages where it
+    throws ("View not enough for this slice!", "No row data available!")."""
+
+    _METHODS = {"360": _lib.CTR_HELICAL_360, "180": _lib.CTR_HELICAL_180}
+
+    def __init__(self, ns, nt, na, ds, dt, offset_s, offset_t, orbit_start, orbit, couch_begin,
+                 couch_mov, view_per_rot, nz, dz, z0, thickness, dso, dsd, method="360"):
+        if str(method) not in self._METHODS:
+            raise ValueError("helical interpolation method must be '360' or '180'")
+        self.method = str(method)
+        self.p = HelicalParam(ns, nt, na, ds, dt, offset_s, offset_t, orbit_start, orbit,
+                              couch_begin, couch_mov, view_per_rot, nz, dz, z0, thickness, dso,
+                              dsd)
+        self.shape_in = (na, nt, ns)
+        self.shape_out = (nz, view_per_rot, ns)
+        self._tables = _Tables()
+
+    def table(self, device):
+        def build(dev):
+            n = _lib.load().ctr_helical_interpolation_table_bytes(ctypes.byref(self.p))
+            t = torch.empty(n, dtype=torch.uint8, device=dev)
+            call("ctr_helical_interpolation_prep", ctypes.byref(self.p),
+                 self._METHODS[self.method], _ptr(t), _stream())
+            return t
+        return self._tables.get(device, build)
+
+    def launch(self, proj, out, status):
+        """Stream-ordered launch of ``proj`` [B, na, nt, ns] into ``out``
+        [B, nz, vpr, ns]; ORs the CTR_HELICAL_* bits into the int32 device tensor
+        ``status`` of B*nz words, one per item and slice."""
+        call(f"ctr_helical_interpolation_{self.method}_{_sfx(proj)}", ctypes.byref(self.p),
+             _ptr(proj), _ptr(out), _ptr(self.table(proj.device)), _ptr(status), proj.shape[0],
+             _stream())
+
+    @staticmethod
+    def raise_status(words):
+        """The reference's exception for one item's per-slice status words: it
+        processes slices in order and throws at the first problem."""
+        for w in words:
+            if w & _lib.CTR_HELICAL_BAD_TABLE:
+                raise RuntimeError("helical_interpolation: table prepared for another geometry")
+            if w & _lib.CTR_HELICAL_NO_VIEWS:
+                raise RuntimeError("View not enough for this slice!")
+            if w & _lib.CTR_HELICAL_NO_ROWS:
+                raise RuntimeError("No row data available!")
+
+    def forward(self, proj):
+        if not proj.is_cuda:
+            raise ValueError("helical_interpolation: input must be a CUDA tensor (no CPU implementation)")
+        single = proj.dim() == 3
+        xb = (proj.unsqueeze(0) if single else proj).contiguous()
+        if xb.dim() != 4 or tuple(xb.shape[1:]) != self.shape_in:
+            raise ValueError(f"helical_interpolation: expected [B,] {self.shape_in}, got {tuple(proj.shape)}")
+        nz = self.shape_out[0]
+        out = torch.empty((xb.shape[0],) + self.shape_out, dtype=xb.dtype, device=xb.device)
+        status = torch.zeros(xb.shape[0] * nz, dtype=torch.int32, device=xb.device)
+        self.launch(xb, out, status)
+        words = status.cpu().tolist()
+        for b in range(xb.shape[0]):
+            self.raise_status(words[b * nz:(b + 1) * nz])
+        if any(w & _lib.CTR_HELICAL_OUTSIDE for w in words):
+            import warnings
+            warnings.warn("helical_interpolation: a 180LI complementary sample lies before the "
+                          "first view and was read as 0 (the reference reads out of bounds)")
+        return out[0] if single else out
+
+
+def helical_interpolation(proj, ns, nt, na, ds, dt, view_per_rot, couch_mov, nz, dz, z0,
+                          thickness, dso, dsd, offset_s=0.0, offset_t=0.0, orbit_start=0.0,
+                          orbit=None, couch_begin=0.0, method="360"):
+    """Rebin a helical sinogram into per-slice fan sinograms (360LI or 180LI);
+    ``orbit`` defaults to 2*pi / view_per_rot."""
+    if orbit is None:
+        orbit = 2 * math.pi / view_per_rot
+    op = HelicalInterpolationOp(ns, nt, na, ds, dt, offset_s, offset_t, orbit_start, orbit,
+                                couch_begin, couch_mov, view_per_rot, nz, dz, z0, thickness, dso,
+                                dsd, method)
+    return op.forward(proj)
 
 
 # ---------------------------------------------------------------------------

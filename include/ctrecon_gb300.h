@@ -347,6 +347,61 @@ int ctr_fbp_fan_plan_run(ctr_fbp_plan* plan, const float* const* proj, float* co
 int ctr_fbp_fan_plan_info(const ctr_fbp_plan* plan, ctr_fbp_plan_info* info);
 int ctr_fbp_fan_plan_destroy(ctr_fbp_plan* plan);
 
+/* ---- helical rebinning: HelicalInterpolation360<T> / HelicalInterpolation180<T>
+ *      (reference include/helical_interpolation.h:17-116, src/helical_interpolation.cc:80-370;
+ *      CPU-only there) ----
+ * Input [na][nt][ns] (view, detector row, channel), output
+ * [nz][view_per_rot][ns]: one fan-beam sinogram per slice z0 + iz*dz (dz added
+ * iz times).  The result equals the reference's bit for bit (FP64 arithmetic
+ * in its order for both T).  As in the reference, dt and orbit_start are
+ * unused: slab edges map to detector rows as z * dsd / dso.
+ *
+ * ctr_helical_interpolation_prep fills a caller-owned device table of
+ * ctr_helical_interpolation_table_bytes(p) bytes for one method (per-channel
+ * cos(gamma) and complementary rays, per-slice view ranges).  The run entry
+ * points OR bits into status[b*nz + iz], one device word per item and slice
+ * (zero them first; read them after the stream).  The reference processes
+ * slices in order and throws at the first problem; the first slice (in order)
+ * with a nonzero word names it:
+ *   CTR_HELICAL_NO_VIEWS  the slice needs views outside [0, na): the
+ *                         reference's "View not enough for this slice!" (the
+ *                         slice is not written);
+ *   CTR_HELICAL_NO_ROWS   a sample has no detector row in either ray: "No row
+ *                         data available!" (the sample is written as 0);
+ *   CTR_HELICAL_OUTSIDE   (not an error) a 180LI complementary sample lies in a
+ *                         view before view 0; the reference reads out of
+ *                         bounds there, here it reads 0.  Only possible when a
+ *                         slice's first view is 0;
+ *   CTR_HELICAL_BAD_TABLE the table was prepared for another method or
+ *                         geometry (nothing is written; reported in word 0). */
+typedef struct ctr_helical_param {
+    unsigned int ns, nt, na;
+    double ds, dt, offset_s, offset_t, orbit_start, orbit, couch_begin, couch_mov;
+    unsigned int view_per_rot, nz;
+    double dz, z0, thickness, dso, dsd;
+} ctr_helical_param;
+#define CTR_HELICAL_360 0
+#define CTR_HELICAL_180 1
+#define CTR_HELICAL_NO_ROWS 1u
+#define CTR_HELICAL_OUTSIDE 2u
+#define CTR_HELICAL_BAD_TABLE 4u
+#define CTR_HELICAL_NO_VIEWS 8u
+size_t ctr_helical_interpolation_table_bytes(const ctr_helical_param* p);
+int ctr_helical_interpolation_prep(const ctr_helical_param* p, int method, void* table,
+                                   cudaStream_t stream);
+int ctr_helical_interpolation_360_f32(const ctr_helical_param* p, const float* in, float* out,
+                                      const void* table, unsigned int* status, int batch,
+                                      cudaStream_t stream);
+int ctr_helical_interpolation_360_f64(const ctr_helical_param* p, const double* in, double* out,
+                                      const void* table, unsigned int* status, int batch,
+                                      cudaStream_t stream);
+int ctr_helical_interpolation_180_f32(const ctr_helical_param* p, const float* in, float* out,
+                                      const void* table, unsigned int* status, int batch,
+                                      cudaStream_t stream);
+int ctr_helical_interpolation_180_f64(const ctr_helical_param* p, const double* in, double* out,
+                                      const void* table, unsigned int* status, int batch,
+                                      cudaStream_t stream);
+
 /* ---- numpy extension ABI (reference numpy_ext, the *_npext.cu files and common.cu) ----
  * Same names and signatures as the reference's libnumpy_ctext: handles over
  * HOST double arrays, FP64 kernels, blocking.  set_device(-1) (the reference's

@@ -60,6 +60,39 @@ class Geom(ctypes.Structure):
                    offset_y, dso, dsd, fov)
 
 
+class Heli(ctypes.Structure):
+    """Mirror of ``orc_heli`` (ctr_oracle.h): HelicalInterpolationParam's fields
+    in its order (reference include/helical_interpolation.h:17-64)."""
+
+    _fields_ = [
+        ("ns", _c_uint), ("nt", _c_uint), ("na", _c_uint),
+        ("ds", _c_double), ("dt", _c_double), ("offset_s", _c_double), ("offset_t", _c_double),
+        ("orbit_start", _c_double), ("orbit", _c_double), ("couch_begin", _c_double),
+        ("couch_mov", _c_double),
+        ("view_per_rot", _c_uint), ("nz", _c_uint),
+        ("dz", _c_double), ("z0", _c_double), ("thickness", _c_double), ("dso", _c_double),
+        ("dsd", _c_double),
+    ]
+
+    @classmethod
+    def make(cls, ns, nt, na, ds, dt, view_per_rot, couch_mov, nz, dz, z0, thickness, dso, dsd,
+             offset_s=0.0, offset_t=0.0, orbit_start=0.0, orbit=None, couch_begin=0.0):
+        if orbit is None:
+            orbit = 2 * math.pi / view_per_rot
+        return cls(ns, nt, na, ds, dt, offset_s, offset_t, orbit_start, orbit, couch_begin,
+                   couch_mov, view_per_rot, nz, dz, z0, thickness, dso, dsd)
+
+
+# the reference's std::runtime_error messages (src/helical_interpolation.cc:87-148)
+HELI_ERRORS = {-1: "View not enough for this slice!", -2: "No row data available!"}
+
+
+class HelicalError(RuntimeError):
+    def __init__(self, code: int):
+        super().__init__(HELI_ERRORS.get(code, f"helical status {code}"))
+        self.code = code
+
+
 def build(ref: bool | None = None, quiet: bool = True) -> None:
     """Compile the port (always) and the reference build (when the reference
     checkout exists, or when ``ref`` is True)."""
@@ -362,6 +395,37 @@ class Oracle:
             self._run_ranges(g.ny, lambda a, b: f(ctypes.byref(g), _c_uint(a), _c_uint(b),
                                                   _p(proj), _p(img), _p(w), _p(pos), _p(usex)))
         return img
+
+    # -- helical rebinning (src/helical_interpolation.cc:80-370) -----------
+    def helical(self, proj, h: Heli, method: str = "360"):
+        """HelicalInterpolation360 / 180 ``calculate_on_cpu``: [na][nt][ns] ->
+        [nz][view_per_rot][ns].  Returns (out, outside): ``outside`` is True when a
+        180LI corresponding-view sample fell outside the scan's views (read as 0
+        here, an out-of-bounds read in the reference).  Raises HelicalError where
+        the reference throws."""
+        if method not in ("360", "180"):
+            raise ValueError(method)
+        proj = self._c(proj)
+        assert proj.shape == (h.na, h.nt, h.ns)
+        out = np.zeros((h.nz, h.view_per_rot, h.ns), dtype=proj.dtype)
+        sfx = _sfx(proj.dtype)
+        if self.kind == "reference":
+            st = self._fn(f"helical_{method}_{sfx}")(ctypes.byref(h), _p(proj), _p(out))
+            if st < 0:
+                raise HelicalError(st)
+            return out, False
+        f = self._fn(f"helical_{method}_slices_{sfx}")
+        ranges = _chunks(h.nz, self.threads) if h.nz else []
+        call = lambda r: f(ctypes.byref(h), _c_uint(r[0]), _c_uint(r[1]), _p(proj), _p(out))  # noqa: E731
+        if len(ranges) > 1:
+            with ThreadPoolExecutor(len(ranges)) as ex:
+                res = list(ex.map(call, ranges))
+        else:
+            res = [call(r) for r in ranges]
+        for st in res:  # slice order: the first failing slice is the reference's throw
+            if st < 0:
+                raise HelicalError(st)
+        return out, any(st == 3 for st in res)
 
     # -- composed FBP -------------------------------------------------------
     def fbp_fan(self, proj, g: Geom, weighting_type=1):

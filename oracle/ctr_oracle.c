@@ -322,6 +322,34 @@ int orc_fp_par_2d_grad_prep(const orc_geom* g, double* weights, double* pos, int
     return 1;
 }
 
+/* ---- helical rebinning helpers (src/helical_interpolation.cc:80-334) ---- */
+
+/* Slice z position: z0 plus dz added iz times, as the calculate_on_cpu loops
+ * advance it (src/helical_interpolation.cc:339-347). */
+static double heli_slice_z(const orc_heli* h, unsigned iz)
+{
+    double z = h->z0;
+    for (unsigned i = 0; i < iz; ++i) z += h->dz;
+    return z;
+}
+
+/* Detector rows [*r0, *r1) averaged for one sample whose source sits z_dif
+ * below the slice, with cos(gamma) = cg: the thick-slice edges projected onto
+ * the detector (src/helical_interpolation.cc:105-111), clamped to the
+ * detector.  Returns 0 when the slab misses the detector (bottom edge above
+ * row 0 or top edge past the last row). */
+static int heli_rows(const orc_heli* h, double center_t, double z_dif, double cg, int* r0, int* r1)
+{
+    double top = center_t - (z_dif + h->thickness / 2.0) / h->dso * cg * h->dsd;
+    double bot = center_t - (z_dif - h->thickness / 2.0) / h->dso * cg * h->dsd;
+    if (bot < 0 || top >= (double)h->nt) return 0;
+    if (top < 0) top = 0;
+    if (bot >= (double)h->nt) bot = (double)h->nt;
+    *r0 = (int)floor(top);
+    *r1 = (int)ceil(bot);
+    return 1;
+}
+
 #define T float
 #define SFX f32
 #include "ctr_oracle_t.h"

@@ -163,6 +163,29 @@ int orc_fp_par_2d_dd_grad_rows_f64(const orc_geom* g, unsigned y0, unsigned y1, 
                                    double* img, const double* weights, const double* pos,
                                    const int* usex);
 
+/* ---- helical rebinning: src/helical_interpolation.cc:80-370 ----
+ * Field order of HelicalInterpolationParam (include/helical_interpolation.h:17-64).
+ * Input [na][nt][ns] (view, detector row, channel), output [nz][view_per_rot][ns].
+ * Slices [z0, z1) of the reference's calculate_on_cpu loop (slice iz sits at
+ * z0 + dz added iz times).  Returns 1, or 3 when a 180LI corresponding-view
+ * sample fell outside the scan's views and read as 0 (the reference reads out
+ * of bounds there); ORC_HELI_ERR_VIEWS / ORC_HELI_ERR_ROWS where the
+ * reference throws "View not enough for this slice!" / "No row data
+ * available!" (the output rows before that point are written, as in the
+ * reference). */
+typedef struct orc_heli {
+    unsigned int ns, nt, na;
+    double ds, dt, offset_s, offset_t, orbit_start, orbit, couch_begin, couch_mov;
+    unsigned int view_per_rot, nz;
+    double dz, z0, thickness, dso, dsd;
+} orc_heli;
+#define ORC_HELI_ERR_VIEWS (-1)
+#define ORC_HELI_ERR_ROWS (-2)
+int orc_helical_360_slices_f32(const orc_heli* h, unsigned z0, unsigned z1, const float* in, float* out);
+int orc_helical_360_slices_f64(const orc_heli* h, unsigned z0, unsigned z1, const double* in, double* out);
+int orc_helical_180_slices_f32(const orc_heli* h, unsigned z0, unsigned z1, const float* in, float* out);
+int orc_helical_180_slices_f64(const orc_heli* h, unsigned z0, unsigned z1, const double* in, double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -532,6 +532,146 @@ int ORC_FN(orc_fp_par_2d_grad_rows)(const orc_geom* g, unsigned y0, unsigned y1,
     return 1;
 }
 
+/* Average of input rows [r0, r1) of one view and channel, in double
+ * (src/helical_interpolation.cc:112-117). */
+static double ORC_FN(heli_mean)(const orc_heli* h, const T* in, int view, unsigned is, int r0, int r1)
+{
+    double acc = 0;
+    int n = 0;
+    for (int r = r0; r < r1; ++r, ++n)
+        acc += in[is + ((size_t)r + (size_t)view * h->nt) * h->ns];
+    return acc / n;
+}
+
+/* Input sample (view, row, channel) of a 180LI corresponding ray; a view
+ * outside [0, na) reads as 0 and sets *outside (the reference indexes out of
+ * bounds there). */
+static double ORC_FN(heli_at)(const orc_heli* h, const T* in, int view, int r, int c, int* outside)
+{
+    if (view < 0 || (unsigned)view >= h->na) {
+        *outside = 1;
+        return 0.0;
+    }
+    return in[(size_t)c + ((size_t)r + (size_t)view * h->nt) * h->ns];
+}
+
+/* The two-sample z interpolation of both rebinning methods
+ * (src/helical_interpolation.cc:137-149); 0 when neither sample exists. */
+static int ORC_FN(heli_store)(T* o, int use_cur, int use_cor, double zd, double zd2, double vcur,
+                              double vcor)
+{
+    if (use_cur && use_cor)
+        *o = (T)((zd * vcor - zd2 * vcur) / (zd - zd2));
+    else if (use_cur)
+        *o = (T)vcur;
+    else if (use_cor)
+        *o = (T)vcor;
+    else
+        return 0;
+    return 1;
+}
+
+/* 360LI, src/helical_interpolation.cc:80-153 (helical_interpolation_360_2_,
+ * the variant HelicalInterpolation360::calculate_on_cpu calls).  Views
+ * [center - vpr, center + vpr) around the slice's nearest view; each output
+ * view pairs the measured view with the one a rotation away on the other side
+ * of the slice; each sample is the mean of the detector rows the thick slice
+ * covers. */
+int ORC_FN(orc_helical_360_slices)(const orc_heli* h, unsigned z0, unsigned z1, const T* in, T* out)
+{
+    const int vpr = (int)h->view_per_rot;
+    const double center_t = (double)(h->nt - 1) / 2.0 + h->offset_t;
+    const double center_s = (double)(h->ns - 1) / 2.0 + h->offset_s;
+    for (unsigned iz = z0; iz < z1; ++iz) {
+        const double z = heli_slice_z(h, iz);
+        const int center = (int)round((z - h->couch_begin) / h->couch_mov);
+        const int lo = center - vpr, hi = center + vpr - 1;
+        if (lo < 0 || (unsigned)hi >= h->na) return ORC_HELI_ERR_VIEWS;
+        const int first = (lo / vpr + 1) * vpr;
+        T* o = out + (size_t)iz * h->view_per_rot * h->ns;
+        for (int iv = 0; iv < vpr; ++iv, o += h->ns) {
+            const int cur = first + iv;
+            const int cor = cur >= center ? cur - vpr : cur + vpr;
+            const double zd = z - h->couch_begin - cur * h->couch_mov;
+            const double zd2 = z - h->couch_begin - cor * h->couch_mov;
+            for (unsigned is = 0; is < h->ns; ++is) {
+                const double s = ((double)is - center_s) * h->ds;
+                const double cg = cos(s / h->dsd);
+                int r0, r1;
+                double vcur = 0, vcor = 0;
+                const int ucur = heli_rows(h, center_t, zd, cg, &r0, &r1);
+                if (ucur) vcur = ORC_FN(heli_mean)(h, in, cur, is, r0, r1);
+                const int ucor = heli_rows(h, center_t, zd2, cg, &r0, &r1);
+                if (ucor) vcor = ORC_FN(heli_mean)(h, in, cor, is, r0, r1);
+                if (!ORC_FN(heli_store)(o + is, ucur, ucor, zd, zd2, vcur, vcor)) return ORC_HELI_ERR_ROWS;
+            }
+        }
+    }
+    return 1;
+}
+
+/* 180LI, src/helical_interpolation.cc:155-251 (helical_interpolation_180_2_,
+ * the variant HelicalInterpolation180::calculate_on_cpu calls).  Views
+ * [center - vpr/2, center - vpr/2 + vpr); the second sample of each ray is its
+ * complementary ray (view offset (pi - 2 gamma) / orbit, mirrored channel),
+ * bilinear in view and channel, wrapped into the view range once each way. */
+int ORC_FN(orc_helical_180_slices)(const orc_heli* h, unsigned z0, unsigned z1, const T* in, T* out)
+{
+    const int vpr = (int)h->view_per_rot;
+    const double center_t = (double)(h->nt - 1) / 2.0 + h->offset_t;
+    const double center_s = (double)(h->ns - 1) / 2.0 + h->offset_s;
+    int outside = 0;
+    for (unsigned iz = z0; iz < z1; ++iz) {
+        const double z = heli_slice_z(h, iz);
+        const int center = (int)round((z - h->couch_begin) / h->couch_mov);
+        const int lo = center - (int)(h->view_per_rot / 2), hi = lo + vpr - 1;
+        if (lo < 0 || (unsigned)hi >= h->na) return ORC_HELI_ERR_VIEWS;
+        const int first = (int)(ceil(lo / (double)h->view_per_rot) * h->view_per_rot);
+        T* o = out + (size_t)iz * h->view_per_rot * h->ns;
+        for (int iv = 0; iv < vpr; ++iv, o += h->ns) {
+            int cur = first + iv;
+            if (cur > hi) cur -= vpr;
+            const double zd = z - h->couch_begin - cur * h->couch_mov;
+            for (unsigned is = 0; is < h->ns; ++is) {
+                const double s = ((double)is - center_s) * h->ds;
+                const double gamma = s / h->dsd;
+                const double cg = cos(gamma);
+                int r0, r1;
+                double vcur = 0, vcor = 0;
+                const int ucur = heli_rows(h, center_t, zd, cg, &r0, &r1);
+                if (ucur) vcur = ORC_FN(heli_mean)(h, in, cur, is, r0, r1);
+                double cv = cur - (M_PI - 2 * gamma) / h->orbit;
+                if (cv < lo) cv = cv + h->view_per_rot;
+                if (cv > hi) cv = cv - h->view_per_rot;
+                const double zd2 = z - h->couch_begin - cv * h->couch_mov;
+                const int ucor = heli_rows(h, center_t, zd2, cg, &r0, &r1);
+                if (ucor) {
+                    const int vl = (int)floor(cv), vr = (int)ceil(cv);
+                    const double u = cv - vl;
+                    const double sc = center_s - s / h->ds;
+                    if (sc < 0 || sc > (double)(h->ns - 1)) {
+                        o[is] = (T)vcur;  /* mirrored channel off the detector */
+                        continue;
+                    }
+                    const int cl = (int)floor(sc), cr = (int)ceil(sc);
+                    const double v = sc - cl;
+                    double left = 0, right = 0;
+                    int n = 0;
+                    for (int r = r0; r < r1; ++r, ++n) {
+                        left += (1 - v) * ORC_FN(heli_at)(h, in, vl, r, cl, &outside) +
+                                v * ORC_FN(heli_at)(h, in, vl, r, cr, &outside);
+                        right += (1 - v) * ORC_FN(heli_at)(h, in, vr, r, cl, &outside) +
+                                 v * ORC_FN(heli_at)(h, in, vr, r, cr, &outside);
+                    }
+                    vcor = ((1 - u) * left + u * right) / n;
+                }
+                if (!ORC_FN(heli_store)(o + is, ucur, ucor, zd, zd2, vcur, vcor)) return ORC_HELI_ERR_ROWS;
+            }
+        }
+    }
+    return outside ? 3 : 1;
+}
+
 #undef ORC_FN
 #undef ORC_CAT
 #undef ORC_CAT2

@@ -7,6 +7,8 @@
 // Only methods whose reference code is well defined are exposed: the
 // parallel-BP grad (src/bp_par_2d.cc:145-199, uninitialised pointers) and the
 // fan-angle grad (src/bp_fan_2d_angle.cc:124-169, uninitialised ypos) are not.
+#include <stdexcept>
+#include <string>
 #include <vector>
 
 #include "include/bp_fan_2d.h"
@@ -16,12 +18,27 @@
 #include "include/fan_weighting.h"
 #include "include/filter.h"
 #include "include/fp_par_2d.h"
+#include "include/helical_interpolation.h"
 
 #include "ctr_oracle.h"
 
 using namespace ct_recon;
 
 namespace {
+
+HelicalInterpolationParam heli_param(const orc_heli* h)
+{
+    return HelicalInterpolationParam(h->ns, h->nt, h->na, h->ds, h->dt, h->offset_s, h->offset_t,
+                                     h->orbit_start, h->orbit, h->couch_begin, h->couch_mov,
+                                     h->view_per_rot, h->nz, h->dz, h->z0, h->thickness, h->dso,
+                                     h->dsd);
+}
+
+int heli_error(const std::runtime_error& e)
+{
+    return std::string(e.what()).find("View") != std::string::npos ? ORC_HELI_ERR_VIEWS
+                                                                    : ORC_HELI_ERR_ROWS;
+}
 
 FanBackprojection2DParam fan_param(const orc_geom* g)
 {
@@ -156,8 +173,30 @@ ParallelProjection2DParam fp_param(const orc_geom* g)
             .calculate_on_cpu(proj, img, w, pos, usex);                                        \
     }
 
+// Helical rebinning: the reference throws std::runtime_error; the message
+// maps to the oracle's codes (-1 "View not enough ...", -2 "No row data ...").
+#define REF_HELI(T, SFX)                                                                       \
+    extern "C" int ref_helical_360_##SFX(const orc_heli* h, const T* in, T* out)               \
+    {                                                                                          \
+        try {                                                                                  \
+            return HelicalInterpolation360<T>(heli_param(h)).calculate_on_cpu(in, out);        \
+        } catch (const std::runtime_error& e) {                                                \
+            return heli_error(e);                                                              \
+        }                                                                                      \
+    }                                                                                          \
+    extern "C" int ref_helical_180_##SFX(const orc_heli* h, const T* in, T* out)               \
+    {                                                                                          \
+        try {                                                                                  \
+            return HelicalInterpolation180<T>(heli_param(h)).calculate_on_cpu(in, out);        \
+        } catch (const std::runtime_error& e) {                                                \
+            return heli_error(e);                                                              \
+        }                                                                                      \
+    }
+
 REF_T(float, f32)
 REF_T(double, f64)
+REF_HELI(float, f32)
+REF_HELI(double, f64)
 REF_CAST(float, f32)
 REF_CAST(double, f64)
 REF_DD(float, f32)

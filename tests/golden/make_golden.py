@@ -79,6 +79,62 @@ CASES = {
                                   fov=150.0)),
 }
 
+# Helical rebinning (src/helical_interpolation.cc:80-370).  Rows map to z as
+# z * dsd / dso (the reference's implied 1 mm rows), so a pitch-p scan moves
+# p * nt * dso / dsd per rotation.  Slices keep every needed view >= 1 (the
+# 180LI complementary rays of a slice whose first view is 0 make the reference
+# read before its input).  "expect" is the reference's status: 1, or the
+# oracle codes of its two runtime_errors.
+_P1 = 8 * 500.0 / 1000.0 / 60  # pitch 1: couch step per view for nt=8, dso/dsd=0.5, 60 views/rotation
+HELI_CASES = {
+    "heli_p1": dict(h=dict(ns=48, nt=8, na=170, ds=1.0, dt=1.0, view_per_rot=60, couch_mov=_P1,
+                           nz=6, dz=0.3, z0=5.2, thickness=1.0, dso=500.0, dsd=1000.0,
+                           offset_s=0.25, offset_t=-0.3), expect=1),
+    # clockwise rotation, couch moving towards -z, pitch 1.2, thick slices
+    "heli_cw_back": dict(h=dict(ns=40, nt=12, na=180, ds=1.3, dt=1.0, view_per_rot=50,
+                                couch_mov=-12 * 600.0 / 1100.0 * 1.2 / 50, couch_begin=40.0,
+                                orbit=-2 * math.pi / 50, nz=7, dz=0.35,
+                                z0=40.0 - 12 * 600.0 / 1100.0 * 1.2 / 50 * 120, thickness=1.5,
+                                dso=600.0, dsd=1100.0, offset_s=-0.35, offset_t=0.4), expect=1),
+    # pitch 2.6: samples where both rays miss the detector rows
+    "heli_norows": dict(h=dict(ns=32, nt=6, na=120, ds=1.0, dt=1.0, view_per_rot=40,
+                               couch_mov=6 * 0.5 * 2.6 / 40, nz=3, dz=0.5, z0=7.8 * 2.0,
+                               thickness=0.5, dso=500.0, dsd=1000.0), expect=-2),
+    # the first slice needs views before view 0
+    "heli_views": dict(h=dict(ns=32, nt=6, na=120, ds=1.0, dt=1.0, view_per_rot=40,
+                              couch_mov=6 * 0.5 / 40, nz=3, dz=0.5, z0=1.0, thickness=0.5,
+                              dso=500.0, dsd=1000.0), expect=-1),
+}
+
+
+def heli(d):
+    from oracle import Heli
+    return Heli.make(**d)
+
+
+def make_heli_case(name, spec, ref: Oracle):
+    from oracle import HelicalError
+    h = heli(spec["h"])
+    rng = np.random.default_rng(9000 + sum(map(ord, name)))
+    v, t, s = np.meshgrid(np.arange(h.na), np.arange(h.nt), np.arange(h.ns), indexing="ij")
+    x = (1.5 + np.sin(0.07 * v + 0.5 * t) * np.cos(0.13 * s) + 0.2 * np.cos(0.011 * v * t)
+         + 0.05 * rng.standard_normal(v.shape))
+    x = np.round(x * 4096) / 4096  # 12 fractional bits: compresses, and exact in float32
+    out = dict(params=json.dumps(dict(kind="heli", heli={f: getattr(h, f) for f, _ in h._fields_},
+                                      expect=spec["expect"])))
+    out["in_f64"] = x  # the float input is its exact cast, x.astype(float32)
+    for sfx, dt in (("f32", np.float32), ("f64", np.float64)):
+        for m in ("360", "180"):
+            try:
+                res, _ = ref.helical(x.astype(dt), h, m)
+                st = 1
+            except HelicalError as e:
+                res, st = np.zeros((h.nz, h.view_per_rot, h.ns), dt), e.code
+            assert st == spec["expect"], (name, m, st)
+            out[f"out{m}_{sfx}"] = res
+            out[f"status{m}"] = np.int32(st)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+
 
 def geom(d):
     full = dict(offset_s=0.0, orbit_start=0.0, offset_x=0.0, offset_y=0.0, dso=-1.0, dsd=-1.0,
@@ -179,6 +235,11 @@ def main(names=None):
         if names and name not in names:
             continue
         make_case(name, spec, ref)
+        print("wrote", name)
+    for name, spec in HELI_CASES.items():
+        if names and name not in names:
+            continue
+        make_heli_case(name, spec, ref)
         print("wrote", name)
 
 

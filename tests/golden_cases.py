@@ -22,8 +22,17 @@ def load(name):
     d = {k: z[k] for k in z.files}
     p = json.loads(str(d.pop("params")))
     d["kind"] = p["kind"]
-    d["geom"] = p["geom"]
+    if p["kind"] == "heli":
+        d["heli"] = p["heli"]
+        d["expect"] = p["expect"]
+    else:
+        d["geom"] = p["geom"]
     return d
+
+
+def heli(case):
+    from oracle import Heli
+    return Heli(**case["heli"])
 
 
 def geom(case):

@@ -78,3 +78,20 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     monkeypatch.setattr(L, "LIB_PATH", str(tmp_path / "absent.so"))
     with pytest.raises(L.CtrLibraryError):
         L.load()
+
+
+def test_helical_host_checks_without_gpu(lib):
+    """Helical prep and run: table size and argument checks resolve on the host
+    before any CUDA call."""
+    from ct_recon_extensions_gb300 import _lib as L
+    p = L.HelicalParam(32, 6, 120, 1.0, 1.0, 0.0, 0.0, 0.0, 2 * 3.141592653589793 / 40, 0.0,
+                       6 * 0.5 / 40, 40, 3, 0.5, 1.0, 0.5, 500.0, 1000.0)
+    assert lib.ctr_helical_interpolation_table_bytes(ctypes.byref(p)) == 16 + 32 * 32 + 32 * 3
+    assert lib.ctr_helical_interpolation_table_bytes(None) == 0
+    assert lib.ctr_helical_interpolation_prep(None, 0, None, None) == 1
+    assert lib.ctr_helical_interpolation_prep(ctypes.byref(p), 7, ctypes.c_void_p(16), None) == 1
+    assert lib.ctr_helical_interpolation_prep(ctypes.byref(p), 0, None, None) == 1
+    bad = L.HelicalParam(32, 6, 120, 1.0, 1.0, 0.0, 0.0, 0.0, 0.1, 0.0, 0.0, 40, 3, 0.5, 1.0,
+                         0.5, 500.0, 1000.0)  # couch_mov == 0
+    assert lib.ctr_helical_interpolation_prep(ctypes.byref(bad), 0, ctypes.c_void_p(16), None) == 1
+    assert lib.ctr_helical_interpolation_360_f32(ctypes.byref(p), None, None, None, None, 1, None) == 1

@@ -84,6 +84,45 @@ def test_fp_distance_driven(port, name, sfx, dt):
     assert np.array_equal(port.fp_par_2d_dd_grad(c[f"proj_in_{sfx}"], g), c[f"dd_grad_{sfx}"])
 
 
+@pytest.mark.parametrize("name", gc.names("heli"))
+@pytest.mark.parametrize("sfx,dt", SFX)
+@pytest.mark.parametrize("method", ["360", "180"])
+def test_helical(port, name, sfx, dt, method):
+    """Helical rebinning, bit for bit, including where the reference throws
+    (the status codes of its two runtime_errors)."""
+    from oracle import HelicalError
+    c = gc.load(name)
+    h = gc.heli(c)
+    x = c["in_f64"].astype(dt)
+    want = int(c[f"status{method}"])
+    try:
+        out, outside = port.helical(x, h, method)
+        got = 1
+    except HelicalError as e:
+        got = e.code
+    assert got == want
+    if want == 1:
+        assert not outside
+        assert np.array_equal(out, c[f"out{method}_{sfx}"])
+
+
+def test_helical_first_view_zero_reads_zero():
+    """180LI slice whose first view is 0: the complementary rays just before it
+    read as 0 and are reported (the reference reads out of bounds there, so
+    this case has no reference fixture).  Pitch 0.5, so that the rays half a
+    rotation away still reach the detector rows."""
+    from oracle import Heli, Oracle
+    h = Heli.make(ns=32, nt=6, na=80, ds=1.0, dt=1.0, view_per_rot=40, couch_mov=3 * 0.5 / 40,
+                  nz=1, dz=0.5, z0=20 * 3 * 0.5 / 40, thickness=0.5, dso=500.0, dsd=1000.0)
+    x = np.ones((h.na, h.nt, h.ns))
+    out, outside = Oracle("port").helical(x, h, "180")
+    assert outside and np.isfinite(out).all()
+    out360, outside360 = Oracle("port").helical(np.ones((120, 6, 32)), Heli.make(
+        ns=32, nt=6, na=120, ds=1.0, dt=1.0, view_per_rot=40, couch_mov=6 * 0.5 / 40, nz=1,
+        dz=0.5, z0=40 * 6 * 0.5 / 40, thickness=0.5, dso=500.0, dsd=1000.0), "360")
+    assert not outside360 and np.allclose(out360, 1.0)
+
+
 def _dot_rel(a_x, y, x, at_y):
     lhs = float(np.vdot(a_x.astype(np.float64), y.astype(np.float64)))
     rhs = float(np.vdot(x.astype(np.float64), at_y.astype(np.float64)))
