@@ -86,7 +86,9 @@ def test_helical_host_checks_without_gpu(lib):
     from ct_recon_extensions_gb300 import _lib as L
     p = L.HelicalParam(32, 6, 120, 1.0, 1.0, 0.0, 0.0, 0.0, 2 * 3.141592653589793 / 40, 0.0,
                        6 * 0.5 / 40, 40, 3, 0.5, 1.0, 0.5, 500.0, 1000.0)
-    assert lib.ctr_helical_interpolation_table_bytes(ctypes.byref(p)) == 16 + 32 * 32 + 32 * 3
+    # header, FP64 channel and slice sections, FP32 channel section, one row per (slice, view)
+    assert lib.ctr_helical_interpolation_table_bytes(ctypes.byref(p)) == \
+        16 + 32 * 32 + 32 * 3 + 40 * 32 + 80 * 3 * 40
     assert lib.ctr_helical_interpolation_table_bytes(None) == 0
     assert lib.ctr_helical_interpolation_prep(None, 0, None, None) == 1
     assert lib.ctr_helical_interpolation_prep(ctypes.byref(p), 7, ctypes.c_void_p(16), None) == 1
