@@ -26,7 +26,10 @@ fan slice from FP32, BF16 and FP16 sinograms (tensor-core filter), with its
 error against the FP64 oracle on image strips when the CPU-baseline leg runs;
 ``fp_methods`` the parallel forward projector's other methods, ray casting
 (512^2 -> 720 x 729, FoV radius 128 mm, 0.125-pixel steps) and distance
-driven, beside ray driven.
+driven, beside ray driven; ``helical`` 360LI / 180LI rebinning of a
+clinical-size helical scan (736 channels x 64 rows, 1152 views per rotation,
+pitch 1, 128 slices) with its algorithmic bytes against the measured HBM
+bandwidth and the oracle port beside it.
 
 ``--impl reference`` times the reference's CPU implementation of the same
 workload on this host (the compiled reference when its build is present,
