@@ -205,6 +205,8 @@ __global__ void __launch_bounds__(kDdThreads)
     *out = sum * w;
 }
 
+// The reference's distance-driven grad in FP64 (T = double), one thread per
+// pixel: edges, channel range, lengths and sums with its operations.
 template <typename T>
 __global__ void __launch_bounds__(kDdThreads)
     fp_dd_grad_kernel(const T* __restrict__ proj, T* __restrict__ img, const double* __restrict__ weights,
@@ -216,8 +218,8 @@ __global__ void __launch_bounds__(kDdThreads)
     const int iy = static_cast<int>(pix / nx), ix = static_cast<int>(pix - static_cast<long long>(iy) * nx);
     const T* P = proj + blockIdx.y * proj_stride;
     const size_t total = static_cast<size_t>(na) * ns;
-    using Acc = typename std::conditional<sizeof(T) == 4, float, double>::type;
-    Acc sum = 0;
+    static_assert(sizeof(T) == 8, "the FP32 grad is fp_dd_grad_f32");
+    T sum = 0;
     for (int ia = 0; ia < na; ++ia) {
         const double* pp = pos + static_cast<size_t>(ia) * nx * 2;
         double mid, left, right;
@@ -243,30 +245,145 @@ __global__ void __launch_bounds__(kDdThreads)
         // for any input)
         const double last = fmin(c1, static_cast<double>(total - 1 - static_cast<size_t>(ia) * ns));
         const int first = static_cast<int>(fmin(c0, last + 1.0));
-        Acc tmp = 0;
-        if constexpr (sizeof(T) == 4) {
-            // the view counts (decided above in FP64); the covered lengths vary
-            // continuously with the edges: FP32, relative to the first channel
-            const float lr = static_cast<float>(__dsub_rn(left, static_cast<double>(first)));
-            const float rr = static_cast<float>(__dsub_rn(right, static_cast<double>(first)));
-            const int cnt = static_cast<int>(last) - first + 1;
-            const float* row = reinterpret_cast<const float*>(P) + static_cast<size_t>(ia) * ns + first;
-            for (int j = 0; j < cnt; ++j) {
-                const float fj = static_cast<float>(j);
-                const float len = fminf(fj + 0.5f, rr) - fmaxf(fj - 0.5f, lr);
-                tmp = fmaf(len, __ldg(row + j) * 0.5f, tmp);
-            }
-        } else {
-            for (int is = first; static_cast<double>(is) <= last; ++is) {
-                const double hi = __dadd_rn(static_cast<double>(is), 0.5), lo = __dsub_rn(static_cast<double>(is), 0.5);
-                const double len = __dsub_rn(hi < right ? hi : right, lo > left ? lo : left);
-                tmp += len * P[static_cast<size_t>(ia) * ns + is] / 2;
-            }
+        T tmp = 0;
+        for (int is = first; static_cast<double>(is) <= last; ++is) {
+            const double hi = __dadd_rn(static_cast<double>(is), 0.5), lo = __dsub_rn(static_cast<double>(is), 0.5);
+            const double len = __dsub_rn(hi < right ? hi : right, lo > left ? lo : left);
+            tmp += len * P[static_cast<size_t>(ia) * ns + is] / 2;
         }
-        if constexpr (sizeof(T) == 4) sum = fmaf(tmp, static_cast<float>(weights[ia]), sum);
-        else sum += tmp * weights[ia];
+        sum += tmp * weights[ia];
     }
     img[blockIdx.y * img_stride + pix] = static_cast<T>(sum);
+}
+
+// ---- FP32 grad with fixed-point decisions ---------------------------------------
+// Per (pixel, view) the grad's only discontinuous decisions are
+// c0 = ceil(left - 0.5) (the view counts iff c0 >= 0; its first channel) and
+// c1 = floor(right + 0.5) (its last channel), left/right = begin + off*k -/+ off
+// from the reference's FP64 (view, line) table.  A per-call prologue turns that
+// table into 32.32 fixed point; the edges are then exact integer arithmetic
+// within (1 + (k+1)/2) * 2^-32 of the exact values, and the reference's FP64
+// edges are within 1e-12 of those.  Wherever left - 0.5 or right + 0.5 lies
+// within kDdFxGuard (2^-16) of an integer the pair reruns the FP64 decision
+// code, so every decision is the reference's.  Overlap lengths come from the
+// fixed-point offsets to the first channel, in FP32.
+struct DdGradFx {
+    long long b, o;  // begin and step of one (view, line), 32.32 fixed point; b == kDdFxBad: use FP64
+};
+constexpr long long kDdFxBad = -0x7fffffffffffffffLL - 1;
+constexpr long long kDdHalf = 1LL << 31;
+constexpr unsigned kDdFxGuard = 1u << 16;
+
+__global__ void dd_grad_fx_prep(const double* __restrict__ pos, const double* __restrict__ weights,
+                                DdGradFx* __restrict__ fx, float* __restrict__ wf, int na, int nx)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < na) wf[i] = static_cast<float>(weights[i]);
+    if (i >= static_cast<long long>(na) * nx) return;
+    const double b = pos[2 * i], o = pos[2 * i + 1];
+    DdGradFx e{kDdFxBad, 0};
+    // |begin|, |off| * nx and the edges stay far inside the 64-bit range
+    if (fabs(b) < 1073741824.0 && fabs(o) * (nx + 1) < 1073741824.0)
+        e = DdGradFx{__double2ll_rn(b * 4294967296.0), __double2ll_rn(o * 4294967296.0)};
+    fx[i] = e;
+}
+
+// The reference's FP64 decisions for one (pixel, view): false when the view
+// adds nothing; else the first channel, the channel count and the edges
+// relative to the first channel.
+__device__ __forceinline__ bool dd_grad_decide64(const double* __restrict__ pp, int ux, int ix, int iy, int nx,
+                                                 int ny, long long room, int& first, int& cnt, float& lr,
+                                                 float& rr)
+{
+    double mid, left, right;
+    if (ux) {
+        const double begin = pp[2 * iy], off = pp[2 * iy + 1];
+        mid = __dadd_rn(begin, __dmul_rn(off, static_cast<double>(ix)));
+        left = ix == 0 ? mid : __dsub_rn(mid, off);
+        right = ix == nx - 1 ? mid : __dadd_rn(mid, off);
+    } else {
+        const double begin = pp[2 * ix], off = pp[2 * ix + 1];
+        mid = __dadd_rn(begin, __dmul_rn(off, static_cast<double>(iy)));
+        left = iy == 0 ? mid : __dsub_rn(mid, off);
+        right = iy == ny - 1 ? mid : __dadd_rn(mid, off);
+    }
+    if (left > right) {
+        const double t = left;
+        left = right;
+        right = t;
+    }
+    const double c0 = ceil(__dsub_rn(left, 0.5)), c1 = floor(__dadd_rn(right, 0.5));
+    if (!(c0 >= 0.0)) return false;
+    const double last = fmin(c1, static_cast<double>(room));
+    first = static_cast<int>(fmin(c0, last + 1.0));
+    cnt = static_cast<int>(last) - first + 1;
+    lr = static_cast<float>(__dsub_rn(left, static_cast<double>(first)));
+    rr = static_cast<float>(__dsub_rn(right, static_cast<double>(first)));
+    return true;
+}
+
+__global__ void __launch_bounds__(kDdThreads)
+    fp_dd_grad_f32(const float* __restrict__ proj, float* __restrict__ img, const double* __restrict__ pos,
+                   const DdGradFx* __restrict__ fx, const float* __restrict__ wf, const int* __restrict__ usex,
+                   int ns, int na, int nx, int ny, size_t img_stride, size_t proj_stride)
+{
+    const long long pix = static_cast<long long>(blockIdx.x) * kDdThreads + threadIdx.x;
+    if (pix >= static_cast<long long>(nx) * ny) return;
+    const int iy = static_cast<int>(pix / nx), ix = static_cast<int>(pix - static_cast<long long>(iy) * nx);
+    const float* P = proj + blockIdx.y * proj_stride;
+    const long long total = static_cast<long long>(na) * ns;
+    float sum = 0.0f;
+    for (int ia = 0; ia < na; ++ia) {
+        const int ux = usex[ia];
+        const int line = ux ? iy : ix, k = ux ? ix : iy, kmax = ux ? nx - 1 : ny - 1;
+        // channels past the sinogram's end add 0: the loop stops there
+        const long long room = total - 1 - static_cast<long long>(ia) * ns;
+        const DdGradFx e = fx[static_cast<size_t>(ia) * nx + line];
+        int first = 0, cnt = 0;
+        float lr = 0.0f, rr = 0.0f;
+        bool exact = e.b == kDdFxBad;
+        if (!exact) {
+            const long long mid = e.b + e.o * k;
+            long long left = k == 0 ? mid : mid - e.o, right = k == kmax ? mid : mid + e.o;
+            if (left > right) {
+                const long long t = left;
+                left = right;
+                right = t;
+            }
+            const long long L = left - kDdHalf, R = right + kDdHalf;
+            const unsigned lf = static_cast<unsigned>(L), rf = static_cast<unsigned>(R);
+            if (lf < kDdFxGuard || lf > 0u - kDdFxGuard || rf < kDdFxGuard || rf > 0u - kDdFxGuard) {
+                exact = true;  // an edge within 2^-16 of a decision boundary
+            } else {
+                const long long c0 = (L >> 32) + 1;  // ceil: the fraction is nonzero here
+                const long long c1 = R >> 32;         // floor
+                if (c0 < 0) continue;
+                const long long last = c1 < room ? c1 : room;
+                const long long f = c0 < last + 1 ? c0 : last + 1;
+                const long long dl = left - (f << 32), dr = right - (f << 32);
+                if (dl <= -(1LL << 38) || dl >= (1LL << 38) || dr <= -(1LL << 38) || dr >= (1LL << 38)) {
+                    exact = true;  // a footprint wider than the FP32 offsets' range
+                } else {
+                    first = static_cast<int>(f);
+                    cnt = static_cast<int>(last - f + 1);
+                    lr = static_cast<float>(static_cast<int>(dl >> 8)) * 5.9604644775390625e-8f;  // 2^-24
+                    rr = static_cast<float>(static_cast<int>(dr >> 8)) * 5.9604644775390625e-8f;
+                }
+            }
+        }
+        if (exact && !dd_grad_decide64(pos + static_cast<size_t>(ia) * nx * 2, ux, ix, iy, nx, ny, room, first,
+                                       cnt, lr, rr))
+            continue;
+        const float* row = P + static_cast<size_t>(ia) * ns + first;
+        float tmp = 0.0f;
+        for (int j = 0; j < cnt; ++j) {
+            const float fj = static_cast<float>(j);
+            const float len = fminf(fj + 0.5f, rr) - fmaxf(fj - 0.5f, lr);
+            tmp = fmaf(len, __ldg(row + j) * 0.5f, tmp);
+        }
+        sum = fmaf(tmp, wf[ia], sum);
+    }
+    img[blockIdx.y * img_stride + pix] = sum;
 }
 
 int check_dd(const ctr_par_param* p, const void* a, const void* b, const void* t0, const void* t1,
@@ -318,10 +435,28 @@ int dd_grad(const ctr_par_param* p, const T* proj, T* img, const double* w, cons
     int st = check_dd(p, proj, img, w, pos, usex, batch);
     if (st) return st;
     const unsigned long long pix = static_cast<unsigned long long>(p->nx) * p->ny;
-    fp_dd_grad_kernel<T><<<dim3(div_up(pix, kDdThreads), batch), kDdThreads, 0, stream>>>(
-        proj, img, w, pos, usex, p->ns, p->na, p->nx, p->ny, static_cast<size_t>(p->nx) * p->ny,
-        static_cast<size_t>(p->na) * p->ns);
-    return check_launch("fp_par_2d distance-driven grad");
+    if constexpr (sizeof(T) == 8) {
+        fp_dd_grad_kernel<T><<<dim3(div_up(pix, kDdThreads), batch), kDdThreads, 0, stream>>>(
+            proj, img, w, pos, usex, p->ns, p->na, p->nx, p->ny, static_cast<size_t>(p->nx) * p->ny,
+            static_cast<size_t>(p->na) * p->ns);
+        return check_launch("fp_par_2d distance-driven grad");
+    } else {
+        // the fixed-point table and FP32 weights of this call (stream-ordered scratch)
+        const size_t n_fx = static_cast<size_t>(p->na) * p->nx;
+        char* scratch = nullptr;
+        cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&scratch),
+                                        sizeof(DdGradFx) * n_fx + sizeof(float) * p->na, stream);
+        if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "distance-driven grad scratch: %s", cudaGetErrorString(e));
+        DdGradFx* fx = reinterpret_cast<DdGradFx*>(scratch);
+        float* wf = reinterpret_cast<float*>(fx + n_fx);
+        dd_grad_fx_prep<<<div_up(n_fx > p->na ? n_fx : p->na, 256), 256, 0, stream>>>(pos, w, fx, wf, p->na, p->nx);
+        fp_dd_grad_f32<<<dim3(div_up(pix, kDdThreads), batch), kDdThreads, 0, stream>>>(
+            proj, img, pos, fx, wf, usex, p->ns, p->na, p->nx, p->ny, static_cast<size_t>(p->nx) * p->ny,
+            static_cast<size_t>(p->na) * p->ns);
+        st = check_launch("fp_par_2d distance-driven grad");
+        cudaFreeAsync(scratch, stream);  // after the kernels that read it
+        return st;
+    }
 }
 
 bool dd_views_along_x(double angle)

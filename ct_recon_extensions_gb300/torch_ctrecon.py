@@ -699,6 +699,18 @@ def fan_backprojection_2d_grad(grad_in, img_shape, img_space, proj_shape, channe
     return apply_adjoint(op, grad_in)
 
 
+def fan_projection_2d(img, img_shape, img_space, proj_shape, channel_space, img_offset=(0, 0),
+                      channel_offset=0, orbit_start=0, orbit=math.pi / 180, dso=1000, dsd=1500,
+                      fov=-1):
+    """Matched fan-beam forward projector (the reference has no fan projector):
+    the exact adjoint of the pixel-driven fan_backprojection_2d, so that
+    (fan_projection_2d, fan_backprojection_2d) is an exact A / A^T pair for
+    fan-beam iterative reconstruction.  Differentiable; its backward is the
+    backprojection.  img: [B, ny, nx, 1] -> [B, na, ns, 1]."""
+    return fan_backprojection_2d_grad(img, img_shape, img_space, proj_shape, channel_space,
+                                      img_offset, channel_offset, orbit_start, orbit, dso, dsd, fov)
+
+
 def fan_backprojection_2d_angle(proj, angles, img_shape, img_space, proj_shape, channel_space,
                                 img_offset=(0, 0), channel_offset=0, dso=1000, dsd=1500, fov=-1):
     """Fan BP over an explicit angle list, unscaled (the reference's numpy
