@@ -62,3 +62,38 @@ def test_mirror_fbp_matches_reference(tmp_path):
     grad = np.fromfile(tmp_path / "grad.f32", np.float32).reshape(g["na"], g["ns"])
     assert rel_l2(recon, c["bp_f32"]) <= 1e-5
     assert rel_l2(grad, c["bp_grad_f32"]) <= 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["heli_p1", "heli_norows", "heli_views"])
+def test_mirror_helical_matches_reference(tmp_path, name):
+    """HelicalInterpolation360/180<double> through the C++ mirror: the reference's
+    outputs (FP64, bit-exact up to the hosts' libm cos) and its exceptions."""
+    from ct_recon_extensions_gb300 import build
+    lib = build.build()
+    cuda = _cuda_home()
+    assert cuda, "CUDA toolkit not found"
+    exe = tmp_path / "mirror_helical"
+    r = subprocess.run(["g++", "-std=c++14", "-O2", "-I", os.path.join(ROOT, "include"), "-I",
+                        os.path.join(cuda, "include"), os.path.join(ROOT, "tests", "cpp", "mirror_helical.cc"),
+                        "-o", str(exe), lib, f"-Wl,-rpath,{os.path.dirname(lib)}", "-L",
+                        os.path.join(cuda, "lib64"), "-lcudart"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    c = gc.load(name)
+    h = c["heli"]
+    c["in_f64"].tofile(tmp_path / "in.f64")
+    env = dict(os.environ, LD_LIBRARY_PATH=os.path.join(cuda, "lib64") + ":" + os.environ.get("LD_LIBRARY_PATH", ""))
+    keys = ("ns", "nt", "na", "ds", "dt", "offset_s", "offset_t", "orbit_start", "orbit", "couch_begin",
+            "couch_mov", "view_per_rot", "nz", "dz", "z0", "thickness", "dso", "dsd")
+    for method in ("360", "180"):
+        r = subprocess.run([str(exe), str(tmp_path), method] + [repr(h[k]) for k in keys],
+                           capture_output=True, text=True, env=env)
+        want = int(c[f"status{method}"])
+        if want == 1:
+            assert r.returncode == 0, r.stdout + r.stderr
+            got = np.fromfile(tmp_path / f"out{method}.f64").reshape(h["nz"], h["view_per_rot"], h["ns"])
+            ref = c[f"out{method}_f64"]
+            assert np.allclose(got, ref, rtol=1e-13, atol=1e-13 * np.abs(ref).max())
+        else:
+            msg = "View not enough for this slice!" if want == -1 else "No row data available!"
+            assert r.returncode == 2 and msg in r.stdout, r.stdout + r.stderr
