@@ -323,7 +323,7 @@ __device__ __forceinline__ float mean_f(const float* __restrict__ col, unsigned 
 {
     float acc = 0.0f;
     for (int r = r0; r < r1; ++r) acc += __ldg(col + static_cast<size_t>(r) * ns);
-    return acc / static_cast<float>(r1 - r0);
+    return __fdividef(acc, static_cast<float>(r1 - r0));  // within 2 ulp; 0/0 stays NaN
 }
 
 __device__ __forceinline__ float at_f(const float* __restrict__ in, const HeliGeo& g, int view, int r, int c,
@@ -422,9 +422,9 @@ __device__ __forceinline__ void heli_fast_one(const float* __restrict__ in, floa
                 }
                 if (outside) atomicOr(status, CTR_HELICAL_OUTSIDE);
             }
-            vcor = ((1.0f - cf.u) * left + cf.u * right) / static_cast<float>(r1 - r0);
+            vcor = __fdividef((1.0f - cf.u) * left + cf.u * right, static_cast<float>(r1 - r0));
         }
-        val = ucur && ucor ? (row.zd * vcor - zd2 * vcur) / (row.zd - zd2) : (ucur ? vcur : vcor);
+        val = ucur && ucor ? __fdividef(row.zd * vcor - zd2 * vcur, row.zd - zd2) : (ucur ? vcur : vcor);
     }
     if (!ucur && !ucor) {
         atomicOr(status, CTR_HELICAL_NO_ROWS);  // the reference throws "No row data available!"
