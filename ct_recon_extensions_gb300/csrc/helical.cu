@@ -435,7 +435,7 @@ __device__ __forceinline__ void heli_fast_one(const float* __restrict__ in, floa
 
 // Views per block of the fast kernel: a block covers kHeliThreads channels of
 // kHeliViews consecutive output views of one slice.
-constexpr int kHeliViews = 8;
+constexpr int kHeliViews = 16;
 
 template <int M>
 __global__ void __launch_bounds__(kHeliThreads, M == CTR_HELICAL_360 ? 8 : 6)
