@@ -168,10 +168,9 @@ TileConst item_const(const ctr_fan_bp_param& g, int tile_y, int R, int VB)
 {
     TileConst c{};
     c.ns = g.ns; c.na = g.na; c.nx = g.nx; c.ny = g.ny;
-    c.W = fan_window(g.ns, g.ds, g.dso, g.dsd, g.nx, g.ny, g.dx, g.dy, g.offset_x, g.offset_y, tile_y);
-    c.W = std::max(c.W, 64 * R / VB);
-    c.WB = (c.W + 4 + 3) / 4 * 4;
-    c.WS = (c.WB + 31) / 32 * 32;
+    set_window(c, std::max(fan_window(g.ns, g.ds, g.dso, g.dsd, g.nx, g.ny, g.dx, g.dy, g.offset_x,
+                                      g.offset_y, tile_y),
+                           64 * R / VB));
     c.cents = static_cast<float>((g.ns - 1) / 2.0 + g.offset_s);
     c.nsm1 = static_cast<float>(g.ns - 1);
     c.dso = static_cast<float>(g.dso);
@@ -182,8 +181,9 @@ TileConst item_const(const ctr_fan_bp_param& g, int tile_y, int R, int VB)
     c.cents_d = (g.ns - 1) / 2.0 + g.offset_s;
     c.dso_d = g.dso;
     c.dsd_d = g.dsd;
-    for (int v = 0; v < kAtanVariants; ++v)
-        for (int k = 0; k < 6; ++k) c.poly[v][k] = static_cast<float>(kAtanPoly[v][k] * g.dsd / g.ds);
+    c.dx = g.dx;
+    c.dy = g.dy;
+    fill_fan_tables(c, g.dsd, g.ds);
     c.proj_stride = static_cast<size_t>(g.ns) * g.na;
     c.img_stride = static_cast<size_t>(g.nx) * g.ny;
     c.total4 = static_cast<long long>(c.proj_stride & ~static_cast<size_t>(3));
@@ -214,7 +214,7 @@ int build_config(ctr_fbp_plan* P, int ci, int sm_count)
         for (int t = 0; t < it.tiles_x * tiles_y; ++t) work.push_back({cost, make_int2(i, t)});
         smem = std::max(smem, 128 + 2 * static_cast<size_t>(bv) * it.c.WS * sizeof(float) +
                                   2 * static_cast<size_t>(bv) * it.c.W * sizeof(float2) +
-                                  static_cast<size_t>(g.na) * sizeof(ViewT<Geo::kFan>));
+                                  static_cast<size_t>(g.na) * sizeof(ViewRec));
     }
     // longest first; ties keep item order (tiles of one item stay together)
     std::stable_sort(work.begin(), work.end(),

@@ -3,18 +3,17 @@
 //
 // FP32 path (the fast path).  A CTA owns a kTileX x kTileY pixel tile; each
 // thread owns kRowsPerThread pixels of one column and keeps their sums in
-// registers across all views.  Views are processed in blocks of kViewBlock:
-// for each view the CTA computes, from the tile corners, the window of
-// detector channels the tile can project into (for a fan the angular extent
-// of a convex tile seen from the source is reached at its corners; for a
-// parallel beam the projection is affine), and stages that window into
-// shared memory as pairs, zero outside the detector: (p[k] - k d[k], d[k]),
-// d[k] = p[k+1] - p[k], k the channel less the window start, in the TMA-fed
-// kernels, (p[k], d[k]) in the plain one.  A pixel-view update is then:
-// channel position (relative to the window start), its floor, one 8-byte
-// shared load and one FMA for the interpolation.  The window length W is a
-// host-side bound over all tiles and views; a kernel that meets a wider
-// window raises kFlagWindowOverflow and clamps (never reads out of bounds).
+// registers across all views.  Views are processed in blocks: for each view
+// the CTA computes, from the tile corners, the window of detector channels
+// the tile can project into (for a fan the angular extent of a convex tile
+// seen from the source is reached at its corners; for a parallel beam the
+// projection is affine), and stages that window into shared memory as pairs,
+// zero outside the detector.  A pixel-view update is then: the channel
+// position relative to the window centre (tile-relative arithmetic,
+// bp_tile.cuh), its rounding, one 8-byte shared load and one FMA for the
+// interpolation.  The window length W is a host-side bound over all tiles and
+// views; a kernel that meets a wider window raises kFlagWindowOverflow and
+// clamps (never reads out of bounds).
 //
 // Reference semantics kept exactly: the term of a view is included iff the
 // channel position s satisfies 0 <= s <= ns-1 (src/bp_fan_2d.cc:71); the
@@ -23,14 +22,8 @@
 //
 // FP64 path: one thread per pixel with the reference's own arithmetic order,
 // reading the caller's FP64 tables (src/bp_fan_2d.cc:46-91,
-// src/bp_par_2d.cc:51-90, src/bp_par_2d_sv.cc:55-92).
-//
-// Adjoints: the FP32 adjoint reuses the tile/window structure and scatters
-// each pixel's two taps into a shared-memory window accumulator; windows are
-// then added to the sinogram with one global atomic per channel and view
-// (the sinogram is zeroed first).  Summation order therefore varies between
-// runs at the FP32 rounding level.  The FP64 adjoint uses global atomics per
-// tap.
+// src/bp_par_2d.cc:51-90, src/bp_par_2d_sv.cc:55-92).  The FP64 adjoint uses
+// global atomics per tap.
 #include <cfloat>
 #include <type_traits>
 
@@ -39,105 +32,289 @@
 namespace ctr {
 namespace {
 
-// Adjoint FP32 tile kernel: img [ny][nx] -> grad [na][ns] (grad pre-zeroed).
-// Takes exactly the taps of the forward (same path choice per view and tile,
-// same arithmetic) and scatters them into a shared-memory window per view,
-// which is then added to the sinogram with one atomic per channel.
+// ---- FP32 adjoint ---------------------------------------------------------------
+//
+// img [ny][nx] -> grad [na][ns] (grad pre-zeroed): the exact transpose of the
+// FP32 forward.  It uses the forward's tiles (32 x kTileY), window, view
+// records and position arithmetic (bp_tile.cuh), so every (pixel, view) gets
+// the forward's channel index, fraction and weight.
+//
+// Work is split stream-K over (tile, block of kViewBlock views) units like the
+// forward; no segment needs combining, because every CTA adds into the
+// sinogram.  Per block, the CTA scatters each pixel's two taps into a window
+// of 32-bit fixed-point accumulators per view in shared memory
+// (red.shared.add.u32: integer shared atomics run at load speed without
+// conflicts, float ones measured 3x slower), then adds each nonzero window
+// entry to the sinogram with one global float atomic (so the summation order
+// over tiles varies between runs at the FP32 rounding level).
+//
+// Fixed point: a tile's values are scaled by a power of two so that the
+// largest |value| is below 2^fx_bits (fx_bits <= 20, chosen on the host so a
+// window entry's sum of taps stays below 2^31); a tap t*u is rounded to an
+// integer with one FMA (adding 1.5*2^23), and the two taps of a pixel add up
+// to round(t) exactly.  The quantisation step is 2^-fx_bits of the tile's
+// largest value.  Tiles holding non-finite values add every tap to the
+// sinogram directly in FP32, as do fan tiles on the absolute path.
+//
+// Thread mapping per view: lanes along x (as the forward) where the position
+// changes faster along x, along y otherwise; 32 neighbouring lanes then hit
+// distinct or at most pairwise-equal accumulators.
+struct AdjUnits {
+    long long units;  // tiles x nb
+    int nb;           // view blocks per tile
+    int tiles_x, tiles_per_item;
+};
+
+constexpr int kAdjChunkBlocks = 64;  // view records set up per chunk of blocks
+
+// A fast view's mode in the adjoint: the address of its accumulator slot plus
+// 4 kc, less 4 kMagicBits, with the variant in the low bits.
+__device__ __forceinline__ int adj_fast_mode(unsigned slot_addr, const TileConst& c, int mode)
+{
+    const unsigned base = slot_addr + 4u * static_cast<unsigned>(c.kc) - 4u * kMagicBits;
+    const int v = mode_variant(mode);
+    return base >= static_cast<unsigned>(kModeFastBase) ? static_cast<int>(base | static_cast<unsigned>(v))
+                                                        : kModeEdgeRel + v;
+}
+
+// round(x) for |x| < 2^22 as an integer, by one FP32 add.
+__device__ __forceinline__ int round_int(float x)
+{
+    return static_cast<int>(__float_as_uint(__fadd_rn(x, kMagic)) - kMagicBits);
+}
+
+// The two taps of one pixel with fixed-point value t at window-relative
+// position sig (j = round(sig) + kc, accumulator address addr of j):
+// (round(t) - q1) at j and q1 = round(t u) at j + 1, u = sig - round(sig) + 1/2.
+__device__ __forceinline__ void adj_taps(unsigned addr, float sig, float t)
+{
+    const float r = round_sigma(sig);
+    const float u = __fadd_rn(__fadd_rn(sig, -r), 0.5f);
+    const int q1 = static_cast<int>(__float_as_uint(__fmaf_rn(t, u, kMagic)) - kMagicBits);
+    const int q0 = round_int(t) - q1;
+    red_shared_u32(addr, static_cast<unsigned>(q0));
+    red_shared_u32(addr + 4u, static_cast<unsigned>(q1));
+}
+
 template <Geo G>
 __global__ void __launch_bounds__(kBpThreads, 2)
-    bp_tile_adj_f32(const float* __restrict__ img, float* __restrict__ grad,
-                    const double* __restrict__ t0, const double* __restrict__ t1,
-                    const double* __restrict__ t2, const TileConst c)
+    bp_tile_adj(const float* __restrict__ img, float* __restrict__ grad, const double* __restrict__ t0,
+                const double* __restrict__ t1, const double* __restrict__ t2, const TileConst c,
+                const AdjUnits k)
 {
-    extern __shared__ __align__(16) float accw[];  // [kViewBlock][W], then ViewT<G>[na]
-    ViewT<G>* views = reinterpret_cast<ViewT<G>*>(accw + (kViewBlock * c.W + 3) / 4 * 4);
+    constexpr int R = kRowsPerThread;
+    extern __shared__ __align__(16) unsigned char adj_smem[];
+    unsigned* win = reinterpret_cast<unsigned*>(adj_smem);  // [kViewBlock][W]
+    ViewRec* views = reinterpret_cast<ViewRec*>(adj_smem + (kViewBlock * c.W * 4 + 15) / 16 * 16);
+    __shared__ unsigned s_max[kBpThreads / 32];
 
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int tx0 = blockIdx.x * kTileX, ty0 = blockIdx.y * kTileY;
-    auto px = [&](int ix) -> float {
-        if constexpr (G == Geo::kFan) return static_cast<float>(t0[ix]);
-        else return static_cast<float>((ix - c.centx) * c.dx);
-    };
-    auto py = [&](int iy) -> float {
-        if constexpr (G == Geo::kFan) return static_cast<float>(t1[iy]);
-        else return static_cast<float>((c.centy - iy) * c.dy);
-    };
-    const int ix = tx0 + lane;
-    const int ixc = min(ix, c.nx - 1);
-    const float x = px(ixc);
-    const float* I = img + blockIdx.z * c.img_stride;
-    float y[kRowsPerThread], val[kRowsPerThread];
-#pragma unroll
-    for (int r = 0; r < kRowsPerThread; ++r) {
-        const int iy = ty0 + warp * kRowsPerThread + r;
-        y[r] = py(min(iy, c.ny - 1));
-        val[r] = (ix < c.nx && iy < c.ny) ? I[static_cast<size_t>(iy) * c.nx + ix] * c.scale : 0.0f;
-    }
-    const float cx0 = px(tx0), cx1 = px(min(tx0 + kTileX - 1, c.nx - 1));
-    const float cy0 = py(ty0), cy1 = py(min(ty0 + kTileY - 1, c.ny - 1));
-    float* G_ = grad + blockIdx.z * c.proj_stride;
-    // per-view parameters, windows and paths of this tile for the whole scan
-    for (int ia = threadIdx.x; ia < c.na; ia += kBpThreads)
-        views[ia] = view_setup<G>(t0, t1, t2, ia, tx0, ty0, cx0, cx1, cy0, cy1, c);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int ctas = static_cast<int>(gridDim.x);
+    const long long U = k.units;
+    const long long u0 = sk_unit_begin(blockIdx.x, ctas, U);
+    const long long u1 = sk_unit_begin(blockIdx.x + 1, ctas, U);
+    const unsigned win_base = smem_u32(win);
+    for (int i = tid; i < kViewBlock * c.W; i += kBpThreads) win[i] = 0u;  // the flush re-zeroes
 
-    for (int v0 = 0; v0 < c.na; v0 += kViewBlock) {
-        const int nv = min(kViewBlock, c.na - v0);
-        for (int idx = threadIdx.x; idx < nv * c.W; idx += kBpThreads) accw[idx] = 0.0f;
-        __syncthreads();
-        for (int j = 0; j < nv; ++j) {
-            const ViewT<G> P = views[v0 + j];
-            float* aj = accw + j * c.W;
-            if (mode_fast(P.mode)) {
-                const float cen = view_cen<G>(P, c);
-                float xs, xc;
-                fast_xs<G>(fast_coord<G>(x, cx0), P.vp, cen, c, &xs, &xc);
-                auto taps = [&](auto variant) {
-                    constexpr int V = decltype(variant)::value;
+    for (long long t = u0 / k.nb; t * k.nb < u1; ++t) {
+        const long long tu = t * k.nb;
+        const int b0 = static_cast<int>((u0 > tu ? u0 : tu) - tu);
+        const int b1 = static_cast<int>((u1 < tu + k.nb ? u1 : tu + k.nb) - tu);
+        const int item = static_cast<int>(t / k.tiles_per_item);
+        const int tl = static_cast<int>(t % k.tiles_per_item);
+        const TileBox B = tile_box<G>(t0, t1, tl % k.tiles_x, tl / k.tiles_x, kTileY, c);
+        __syncthreads();  // s_max of the previous tile has been read by every warp
+        const float* I = img + static_cast<size_t>(item) * c.img_stride;
+        float* Gs = grad + static_cast<size_t>(item) * c.proj_stride;
+
+        // pixels of the two mappings: x-major (column lane, rows warp*R + r) and
+        // y-major (column warp*4 + (r & 3), row lane + 32 (r >> 2))
+        float vx[R], vy[R], oyx[R], oxy[4], oyy[R / 4];
+        const int ixx = min(B.tx0 + lane, c.nx - 1);
+        const float oxx = off_x<G>(t0, ixx, B.ixm, c);
+        unsigned m = 0u;
+        bool bad = false;
 #pragma unroll
-                    for (int r = 0; r < kRowsPerThread; ++r) {
-                        float w;
-                        const float s = fast_s<G, V>(xs, xc, fast_coord<G>(y[r], cy0), P.vp, cen, c, &w);  // s - lo
-                        const float v = s + kMagicHalf;
-                        const float u = s - (v - kMagic);
-                        const int k = static_cast<int>(__float_as_uint(v) - kMagicBits);
-                        const float t = val[r] * w;
-                        if (t != 0.0f) {
-                            atomicAdd(aj + k, t - t * u);
-                            atomicAdd(aj + k + 1, t * u);
+        for (int r = 0; r < R; ++r) {
+            const int ix = B.tx0 + lane, iy = B.ty0 + warp * R + r;
+            vx[r] = (ix < c.nx && iy < c.ny) ? I[static_cast<size_t>(iy) * c.nx + ix] : 0.0f;
+            oyx[r] = off_y<G>(t1, min(iy, c.ny - 1), B.iym, c);
+            const int jx = B.tx0 + warp * 4 + (r & 3), jy = B.ty0 + lane + 32 * (r >> 2);
+            vy[r] = (jx < c.nx && jy < c.ny) ? I[static_cast<size_t>(jy) * c.nx + jx] : 0.0f;
+            m = max(m, __float_as_uint(fabsf(vx[r])));
+            bad = bad || !isfinite(vx[r]);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) oxy[q] = off_x<G>(t0, min(B.tx0 + warp * 4 + q, c.nx - 1), B.ixm, c);
+#pragma unroll
+        for (int h = 0; h < R / 4; ++h) oyy[h] = off_y<G>(t1, min(B.ty0 + lane + 32 * h, c.ny - 1), B.iym, c);
+        m = __reduce_max_sync(0xffffffffu, m);
+        if (lane == 0) s_max[warp] = m;
+        const bool any_bad = __syncthreads_or(bad) != 0;
+        m = 0u;
+#pragma unroll
+        for (int w = 0; w < kBpThreads / 32; ++w) m = max(m, s_max[w]);
+        if (m == 0u && !any_bad) continue;  // an all-zero tile adds nothing (uniform)
+        int ex = 0;
+        frexpf(__uint_as_float(m), &ex);
+        const int sh = c.fx_bits - ex;  // values * 2^sh are below 2^fx_bits
+        // per pixel: the scaled value; the parallel beam also keeps round(t)
+        // as an integer (its taps do not depend on the view)
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            vx[r] = any_bad ? vx[r] * c.scale : ldexpf(vx[r], sh);
+            vy[r] = any_bad ? vy[r] * c.scale : ldexpf(vy[r], sh);
+        }
+        const float back = ldexpf(c.scale, -sh);  // fixed point -> sinogram units
+
+        for (int b = b0; b < b1; ++b) {
+            if ((b - b0) % kAdjChunkBlocks == 0) {
+                // view records of the next chunk of blocks (slot j of block b: win + j*W)
+                const int va = b * kViewBlock;
+                const int vb = min(min(b1, b + kAdjChunkBlocks) * kViewBlock, c.na);
+                __syncthreads();
+                for (int ia = va + tid; ia < vb; ia += kBpThreads) {
+                    ViewRec P = view_setup<G>(t0, t1, t2, ia, B, c);
+                    if (mode_fast(P.mode))
+                        P.mode = adj_fast_mode(win_base + 4u * static_cast<unsigned>((ia % kViewBlock) * c.W), c,
+                                               P.mode);
+                    views[ia - va] = P;
+                }
+                __syncthreads();
+            }
+            const int v0 = b * kViewBlock;
+            const int nv = min(kViewBlock, c.na - v0);
+            const ViewRec* vb = views + (b - b0) % kAdjChunkBlocks * kViewBlock;
+            for (int j = 0; j < nv; ++j) {
+                const FastRec F = load_fast(vb + j);
+                if (F.mode == kModeSkip) continue;
+                const int ia = v0 + j;
+                const unsigned slot = win_base + 4u * static_cast<unsigned>(j * c.W);
+                const bool xmaj = fabsf(F.p0) * static_cast<float>(c.dx) >= fabsf(F.p1) * static_cast<float>(c.dy);
+                if (mode_fast(F.mode) && !any_bad) {
+                    const FastRec& P = F;
+                    const unsigned base = static_cast<unsigned>(P.mode) & ~3u;
+                    if constexpr (G == Geo::kPar) {
+                        if (xmaj) {
+                            const float xs = par_xpart(oxx, P);
+#pragma unroll
+                            for (int r = 0; r < R; ++r) {
+                                const float sig = par_sigma(xs, oyx[r], P);
+                                adj_taps(base + 4u * __float_as_uint(__fadd_rn(sig, kMagic)), sig, vx[r]);
+                            }
+                        } else {
+#pragma unroll
+                            for (int r = 0; r < R; ++r) {
+                                const float sig = par_sigma(par_xpart(oxy[r & 3], P), oyy[r >> 2], P);
+                                adj_taps(base + 4u * __float_as_uint(__fadd_rn(sig, kMagic)), sig, vy[r]);
+                            }
+                        }
+                    } else {
+                        auto fan_fast = [&](auto vc) {
+                            constexpr int V = decltype(vc)::value;
+                            if (xmaj) {
+                                const FanX X = fan_xpart(oxx, P);
+#pragma unroll
+                                for (int r = 0; r < R; ++r) {
+                                    float w;
+                                    const float sig = fan_sigma<V>(X, oyx[r], P, c, &w);
+                                    adj_taps(base + 4u * __float_as_uint(__fadd_rn(sig, kMagic)), sig,
+                                             __fmul_rn(vx[r], w));
+                                }
+                            } else {
+#pragma unroll
+                                for (int r = 0; r < R; ++r) {
+                                    float w;
+                                    const float sig = fan_sigma<V>(fan_xpart(oxy[r & 3], P), oyy[r >> 2], P, c, &w);
+                                    adj_taps(base + 4u * __float_as_uint(__fadd_rn(sig, kMagic)), sig,
+                                             __fmul_rn(vy[r], w));
+                                }
+                            }
+                        };
+                        switch (mode_variant(P.mode)) {
+                            case 0: fan_fast(std::integral_constant<int, 0>{}); break;
+                            case 1: fan_fast(std::integral_constant<int, 1>{}); break;
+                            default: fan_fast(std::integral_constant<int, 2>{}); break;
                         }
                     }
-                };
-                switch (G == Geo::kFan ? P.mode & 3 : 0) {
-                    case 0: taps(std::integral_constant<int, 0>{}); break;
-                    case 1: taps(std::integral_constant<int, 1>{}); break;
-                    case 2: taps(std::integral_constant<int, 2>{}); break;
-                    default: taps(std::integral_constant<int, 3>{}); break;
+                    continue;
                 }
-            } else if (P.mode == kModeEdge) {
-#pragma unroll
-                for (int r = 0; r < kRowsPerThread; ++r) {
-                    if (val[r] == 0.0f) continue;
-                    float w, u;
-                    int k;
-                    const float s = channel_of<G>(x, y[r], P.vp, c, &w);
-                    const int iyc = min(ty0 + warp * kRowsPerThread + r, c.ny - 1);
-                    if (edge_tap<G>(s, ixc, iyc, v0 + j, P.lo, t0, t1, t2, c, &k, &u)) {
-                        const float t = val[r] * w;
-                        atomicAdd(aj + k, t - t * u);
-                        atomicAdd(aj + k + 1, t * u);
+                const ViewRec P = vb[j];
+                // edge views (and every view of a tile with non-finite values):
+                // x-major, the forward's inclusion decisions; fixed-point taps into
+                // the window, or FP32 taps straight into the sinogram
+                const bool direct = any_bad || (G == Geo::kFan && P.mode == kModeEdgeAbs);
+                float* Grow = Gs + static_cast<size_t>(ia) * c.ns + P.lo;
+                auto tap = [&](int jj, float sig2, float t) {
+                    const float u = __fadd_rn(sig2, -(static_cast<float>(jj - c.kc) - 0.5f));
+                    if (direct) {
+                        const float a1 = t * u;
+                        const int g = P.lo + jj;  // taps off the detector carry no weight
+                        if (t != 0.0f && g >= 0 && g < c.ns) atomicAdd(Grow + jj, t - a1);
+                        if (t != 0.0f && g + 1 >= 0 && g + 1 < c.ns) atomicAdd(Grow + jj + 1, a1);
+                    } else {
+                        const int q1 = static_cast<int>(__float_as_uint(__fmaf_rn(t, u, kMagic)) - kMagicBits);
+                        const int q0 = round_int(t) - q1;
+                        red_shared_u32(slot + 4u * jj, static_cast<unsigned>(q0));
+                        red_shared_u32(slot + 4u * jj + 4u, static_cast<unsigned>(q1));
+                    }
+                };
+                const int iy0 = B.ty0 + warp * R;
+                if constexpr (G == Geo::kFan) {
+                    if (P.mode == kModeEdgeAbs) {
+                        const float x = static_cast<float>(t0[ixx]);
+                        for (int r = 0; r < R; ++r) {
+                            const int iyc = min(iy0 + r, c.ny - 1);
+                            float w, sig2;
+                            int jj;
+                            const float s = channel_abs<G>(x, static_cast<float>(t1[iyc]), make_float2(P.p0, P.p1), c, &w);
+                            if (edge_tap_abs<G>(s, ixx, iyc, ia, P.lo, t0, t1, t2, c, &jj, &sig2))
+                                tap(jj, sig2, (any_bad ? vx[r] : vx[r] * back) * w);
+                        }
+                        continue;
+                    }
+                    auto fan_edge = [&](auto vc) {
+                        constexpr int V = decltype(vc)::value;
+                        const FanX X = fan_xpart(oxx, P);
+                        for (int r = 0; r < R; ++r) {
+                            float w, sig2;
+                            int jj;
+                            const float sig = fan_sigma<V>(X, oyx[r], P, c, &w);
+                            if (edge_tap<G>(sig, ixx, min(iy0 + r, c.ny - 1), ia, P.lo, t0, t1, t2, c, &jj, &sig2))
+                                tap(jj, sig2, any_bad ? vx[r] * (w * P.e) : __fmul_rn(vx[r], w));
+                        }
+                    };
+                    switch (mode_variant(P.mode)) {
+                        case 0: fan_edge(std::integral_constant<int, 0>{}); break;
+                        case 1: fan_edge(std::integral_constant<int, 1>{}); break;
+                        default: fan_edge(std::integral_constant<int, 2>{}); break;
+                    }
+                } else {
+                    const float xs = par_xpart(oxx, P);
+                    for (int r = 0; r < R; ++r) {
+                        float sig2;
+                        int jj;
+                        const float sig = par_sigma(xs, oyx[r], P);
+                        if (edge_tap<G>(sig, ixx, min(iy0 + r, c.ny - 1), ia, P.lo, t0, t1, t2, c, &jj, &sig2))
+                            tap(jj, sig2, vx[r]);
                     }
                 }
             }
+            __syncthreads();
+            // flush: window entries -> sinogram (and back to zero)
+            for (int idx = tid; idx < nv * c.W; idx += kBpThreads) {
+                const unsigned a = win[idx];
+                if (a == 0u) continue;
+                win[idx] = 0u;
+                const int j = idx / c.W, kk = idx - j * c.W;
+                const ViewRec& P = vb[j];
+                const int g = P.lo + kk;
+                if (g >= 0 && g < c.ns)
+                    atomicAdd(Gs + static_cast<size_t>(v0 + j) * c.ns + g,
+                              static_cast<float>(static_cast<int>(a)) * (back * P.e));
+            }
+            __syncthreads();
         }
-        __syncthreads();
-        for (int idx = threadIdx.x; idx < nv * c.W; idx += kBpThreads) {
-            const int j = idx / c.W, k = idx - j * c.W;
-            const int g = views[v0 + j].lo + k;
-            const float a = accw[idx];
-            if (g >= 0 && g < c.ns && a != 0.0f)
-                atomicAdd(G_ + static_cast<size_t>(v0 + j) * c.ns + g, a);
-        }
-        __syncthreads();
     }
 }
 
@@ -312,81 +489,62 @@ __global__ void __launch_bounds__(kSvThreads)
 
 // ---- host side ---------------------------------------------------------------
 
-template <class K>
-int launch_tile(K kern, int W, dim3 grid, cudaStream_t stream, const char* what,
-                const void* a0, void* a1, const double* xpos, const double* ypos,
-                const double* sincos, const TileConst& c, bool adjoint)
+// Resident CTAs per SM of the tile kernels (two of 256 threads).
+constexpr int kTileCtasPerSm = 2;
+// Shared memory one tile CTA may take (two CTAs per SM).
+constexpr size_t kTileSmemMax = 110 * 1024;
+
+int sm_count()
 {
-    size_t smem = static_cast<size_t>(kViewBlock) * W * (adjoint ? sizeof(float) : sizeof(float2));
-    if (adjoint) smem = (static_cast<size_t>(kViewBlock) * W + 3) / 4 * 4 * sizeof(float) + c.na * kViewBytesMax;
-    if (smem > 160 * 1024) return fail(CTR_ERR_UNSUPPORTED, "%s: window of %d channels too wide", what, W);
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
-    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
-    kern<<<grid, kBpThreads, smem, stream>>>(static_cast<const float*>(a0), static_cast<float*>(a1),
-                                             xpos, ypos, sincos, c);
-    return check_launch(what);
-}
-
-
-// Rows per thread of the bulk-copy forward kernel (tile 32 x 8*kFwdRows) and
-// its resident CTAs per SM (sets the register budget).
-constexpr int kFwdRows = 8;
-constexpr int kFwdMinBlocks = 1;
-// View groups per CTA of the single-geometry forward kernel: 2 (512 threads,
-// one CTA per SM) or 1 (256 threads, two CTAs per SM on different tiles).
-constexpr int kFwdGroups = 1;
-constexpr int kFwdTileY = (kBpThreads / 32) * kFwdRows;
-// Shared memory the forward kernel may take (one CTA per SM).
-constexpr size_t kFwdSmemMax = 200 * 1024;
-
-// Shared bytes of the bulk-copy forward kernel with NG groups of VB views.
-template <Geo G>
-inline size_t fwd_smem(const TileConst& ct, int VB, int NG = kGroups)
-{
-    const size_t bv = static_cast<size_t>(NG) * VB;
-    return 128 + 2 * bv * ct.WS * sizeof(float) + 2 * bv * ct.W * sizeof(float2) + ct.na * sizeof(ViewT<G>);
-}
-
-// The bulk-copy kernel with VB views per group on tiles of 32 x kFwdTileY:
-// stream-K over (tile, view block) units when the launch has fewer than 4
-// waves of tiles, one CTA per tile otherwise.
-template <Geo G, int VB, int NG>
-int launch_tma(const float* proj, float* img, const double* t0, const double* t1, const double* t2,
-               const TileConst& ct, int batch, cudaStream_t stream, const char* what)
-{
-    constexpr int kThreads = NG * kBpThreads;
-    constexpr int kMinBlocks = NG == 1 ? 2 : kFwdMinBlocks;  // same register budget per SM
-    const size_t smem = fwd_smem<G>(ct, VB, NG);
-    const int tiles_x = static_cast<int>(div_up(ct.nx, kTileX));
-    const int tiles_y = static_cast<int>(div_up(ct.ny, kFwdTileY));
-    const long long tiles = static_cast<long long>(tiles_x) * tiles_y * batch;
-    const int nb = static_cast<int>(div_up(ct.na, NG * VB));
     int dev = 0, sms = kSmCount;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (tiles < 4ll * sms * kMinBlocks && nb > 1) {
+    return sms;
+}
+
+// Shared bytes of the bulk-copy forward kernel with NG groups of VB views.
+inline size_t fwd_smem(const TileConst& ct, int VB, int NG = 1)
+{
+    const size_t bv = static_cast<size_t>(NG) * VB;
+    return 128 + 2 * bv * ct.WS * sizeof(float) + 2 * bv * ct.W * sizeof(float2) + ct.na * sizeof(ViewRec);
+}
+
+// The bulk-copy kernel (one group of VB views, tiles of 32 x kTileY): stream-K
+// over (tile, view block) units when the launch has fewer than 4 waves of
+// tiles, one CTA per tile otherwise.
+template <Geo G, int VB>
+int launch_tma(const float* proj, float* img, const double* t0, const double* t1, const double* t2,
+               const TileConst& ct, int batch, cudaStream_t stream, const char* what)
+{
+    constexpr int kR = kRowsPerThread;
+    const size_t smem = fwd_smem(ct, VB);
+    const int tiles_x = static_cast<int>(div_up(ct.nx, kTileX));
+    const int tiles_y = static_cast<int>(div_up(ct.ny, kTileY));
+    const long long tiles = static_cast<long long>(tiles_x) * tiles_y * batch;
+    const int nb = static_cast<int>(div_up(ct.na, VB));
+    const int sms = sm_count();
+    if (tiles < 4ll * sms * kTileCtasPerSm && nb > 1) {
         SkConst k{};
         k.units = tiles * nb;
         k.nb = nb;
         k.tiles_x = tiles_x;
         k.tiles_per_item = tiles_x * tiles_y;
-        auto kern = bp_tile_tma_sk<G, kFwdRows, VB, NG, kMinBlocks>;
+        auto kern = bp_tile_tma_sk<G, kR, VB, 1, kTileCtasPerSm>;
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              static_cast<int>(smem));
         int per_sm = 1;
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBpThreads, smem);
         if (e != cudaSuccess || per_sm < 1) return fail(CTR_ERR_CUDA, "%s: occupancy", what);
         const int ctas = static_cast<int>(std::min<long long>(k.units, static_cast<long long>(sms) * per_sm));
         k.maxseg = sk_max_segments(tiles, nb, ctas);
-        const size_t part_bytes = static_cast<size_t>(tiles) * k.maxseg * kTileX * kFwdTileY * sizeof(float);
+        const size_t part_bytes = static_cast<size_t>(tiles) * k.maxseg * kTileX * kTileY * sizeof(float);
         void* scratch = nullptr;
         if (cudaMallocAsync(&scratch, part_bytes + sizeof(int) * tiles, stream) == cudaSuccess) {
             k.partial = static_cast<float*>(scratch);
             k.counter = reinterpret_cast<int*>(static_cast<char*>(scratch) + part_bytes);
             e = cudaMemsetAsync(k.counter, 0, sizeof(int) * tiles, stream);
             if (e == cudaSuccess) {
-                kern<<<ctas, kThreads, smem, stream>>>(proj, img, t0, t1, t2, ct, k);
+                kern<<<ctas, kBpThreads, smem, stream>>>(proj, img, t0, t1, t2, ct, k);
                 e = cudaGetLastError();
             }
             cudaFreeAsync(scratch, stream);
@@ -395,45 +553,85 @@ int launch_tma(const float* proj, float* img, const double* t0, const double* t1
         }
         cudaGetLastError();  // no scratch: whole tiles per CTA below
     }
-    auto kern = bp_tile_tma_f32<G, kFwdRows, kMinBlocks, VB, NG>;
+    auto kern = bp_tile_tma_f32<G, kR, kTileCtasPerSm, VB, 1>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
     dim3 grid(tiles_x, tiles_y, batch);
-    kern<<<grid, kThreads, smem, stream>>>(proj, img, t0, t1, t2, ct);
+    kern<<<grid, kBpThreads, smem, stream>>>(proj, img, t0, t1, t2, ct);
     return check_launch(what);
 }
 
-// Forward dispatch: the bulk-copy kernel (tile 32 x kFwdTileY, window w_tall;
-// parallel: 32 views per group where that fits the shared memory, else 16) when its
-// window fits 256 elements and the sinogram is 16-byte aligned, the
-// cooperative kernel (tile 32 x kTileY, window c.W) otherwise.
+// Forward dispatch: the bulk-copy kernel when its window fits one 256-element
+// box and the sinogram is 16-byte aligned (parallel: 32 views per block where
+// that fits the shared memory, else 16), the cooperative kernel otherwise.
+// Both use the geometry's one window (c.W), so they compute the same
+// positions as the adjoint.
 template <Geo G>
 int launch_forward(const float* proj, float* img, const double* t0, const double* t1,
-                   const double* t2, TileConst c, int w_tall, int batch, cudaStream_t stream,
-                   const char* what)
+                   const double* t2, TileConst c, int batch, cudaStream_t stream, const char* what)
 {
-    TileConst ct = c;
-    // the final group reduction reuses one half of the pair buffer (2*VB x W
-    // float2) for kFwdRows x kBpThreads floats: W >= 4 * kFwdRows (VB >= 16)
-    ct.W = std::max({w_tall, 16, kFwdRows * kBpThreads / (2 * kBlockViews)});
-    ct.WB = (ct.W + 4 + 3) / 4 * 4;
-    ct.WS = (ct.WB + 31) / 32 * 32;
     const unsigned long long total = static_cast<unsigned long long>(c.proj_stride) * batch;
-    ct.total4 = static_cast<long long>(total & ~3ull);
-    if (ct.WB <= 256 && reinterpret_cast<uintptr_t>(proj) % 16 == 0 && total < (1ull << 31) &&
+    c.total4 = static_cast<long long>(total & ~3ull);
+    if (c.WB <= 256 && reinterpret_cast<uintptr_t>(proj) % 16 == 0 && total < (1ull << 31) &&
         c.na <= 4096) {
-        // parallel: 32 views per group halve the block barriers of its short
-        // per-view work (bp_par_2d 122.9 -> 121.7 us at 512^2); the fan keeps 16
-        // (183 vs 190 us with 32)
-        if (G == Geo::kPar && fwd_smem<G>(ct, 32, kFwdGroups) <= kFwdSmemMax / (3 - kFwdGroups))
-            return launch_tma<G, 32, kFwdGroups>(proj, img, t0, t1, t2, ct, batch, stream, what);
-        if (fwd_smem<G>(ct, 16, kFwdGroups) <= kFwdSmemMax / (3 - kFwdGroups))
-            return launch_tma<G, 16, kFwdGroups>(proj, img, t0, t1, t2, ct, batch, stream, what);
+        // parallel: 32 views per block halve the block barriers of its short
+        // per-view work; the fan keeps 16
+        if (G == Geo::kPar && fwd_smem(c, 32) <= kTileSmemMax)
+            return launch_tma<G, 32>(proj, img, t0, t1, t2, c, batch, stream, what);
+        if (fwd_smem(c, 16) <= kTileSmemMax)
+            return launch_tma<G, 16>(proj, img, t0, t1, t2, c, batch, stream, what);
     }
-    c.W = std::max(c.W, 16);
+    const size_t smem = static_cast<size_t>(kViewBlock) * c.W * sizeof(float2);
+    if (smem > 160 * 1024) return fail(CTR_ERR_UNSUPPORTED, "%s: window of %d channels too wide", what, c.W);
+    auto kern = bp_tile_f32_coop<G>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
     dim3 grid(div_up(c.nx, kTileX), div_up(c.ny, kTileY), batch);
-    return launch_tile(bp_tile_f32_coop<G>, c.W, grid, stream, what, proj, img, t0, t1, t2, c, false);
+    kern<<<grid, kBpThreads, smem, stream>>>(proj, img, t0, t1, t2, c);
+    return check_launch(what);
+}
+
+// Fixed-point bits of the adjoint's largest tap: a window entry sums the taps
+// of the tile's pixels within one channel of it, at most `hits` pixels (a
+// band two channel pitches wide across the tile, on the pixel lattice), each
+// below 2^(fx_bits+1) (the fan's relative weight is at most ~2); the sum must
+// stay below 2^31.
+int adj_fx_bits(double pitch_mm, double dx, double dy)
+{
+    const double pix = std::min(std::fabs(dx), std::fabs(dy));
+    const double diag = std::sqrt(std::pow(kTileX * dx, 2) + std::pow(kTileY * dy, 2)) / pix;
+    double hits = (2.0 * std::fabs(pitch_mm) / pix + 1.5) * (diag + 1.5);
+    if (!(hits < kTileX * kTileY)) hits = kTileX * kTileY;
+    int fx = 20;
+    while (fx > 8 && hits * std::ldexp(2.0, fx) >= 2147483647.0) --fx;
+    return fx;
+}
+
+// The adjoint: stream-K over (tile, view block) units, as many CTAs as are
+// resident.
+template <Geo G>
+int launch_adjoint(const float* img, float* grad, const double* t0, const double* t1, const double* t2,
+                   const TileConst& c, int batch, cudaStream_t stream, const char* what)
+{
+    const size_t smem = (static_cast<size_t>(kViewBlock) * c.W * 4 + 15) / 16 * 16 +
+                        static_cast<size_t>(std::min(c.na, kAdjChunkBlocks * kViewBlock)) * sizeof(ViewRec);
+    if (smem > kTileSmemMax) return fail(CTR_ERR_UNSUPPORTED, "%s: window of %d channels too wide", what, c.W);
+    const int tiles_x = static_cast<int>(div_up(c.nx, kTileX));
+    const int tiles_y = static_cast<int>(div_up(c.ny, kTileY));
+    AdjUnits k{};
+    k.nb = static_cast<int>(div_up(c.na, kViewBlock));
+    k.tiles_x = tiles_x;
+    k.tiles_per_item = tiles_x * tiles_y;
+    k.units = static_cast<long long>(k.tiles_per_item) * batch * k.nb;
+    auto kern = bp_tile_adj<G>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    int per_sm = 1;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBpThreads, smem);
+    if (e != cudaSuccess || per_sm < 1) return fail(CTR_ERR_CUDA, "%s: occupancy", what);
+    const int ctas = static_cast<int>(std::min<long long>(k.units, static_cast<long long>(sm_count()) * per_sm));
+    kern<<<ctas, kBpThreads, smem, stream>>>(img, grad, t0, t1, t2, c, k);
+    return check_launch(what);
 }
 
 struct FanArgs {
@@ -454,22 +652,29 @@ int check_fan(const FanArgs& a, const void* in, const void* out, const double* x
     return CTR_OK;
 }
 
+// The FP32 kernels' constants for a fan geometry (window for 32 x kTileY tiles).
 TileConst fan_const(const FanArgs& a, double extra_scale)
 {
     TileConst c{};
     c.ns = a.ns; c.na = a.na; c.nx = a.nx; c.ny = a.ny;
-    c.W = fan_window(a.ns, a.ds, a.dso, a.dsd, a.nx, a.ny, a.dx, a.dy, a.offset_x, a.offset_y);
+    set_window(c, tile_window(fan_window(a.ns, a.ds, a.dso, a.dsd, a.nx, a.ny, a.dx, a.dy, a.offset_x,
+                                         a.offset_y)));
     c.cents = static_cast<float>((a.ns - 1) / 2.0 + a.offset_s);
     c.nsm1 = static_cast<float>(a.ns - 1);
     c.dso = static_cast<float>(a.dso);
     c.K = static_cast<float>(a.dsd / a.ds);
     c.scale = static_cast<float>(a.dsd * a.dsd * extra_scale);
+    c.dx = a.dx;
+    c.dy = a.dy;
     c.ds_d = a.ds;
     c.cents_d = (a.ns - 1) / 2.0 + a.offset_s;
     c.dso_d = a.dso;
     c.dsd_d = a.dsd;
-    for (int v = 0; v < kAtanVariants; ++v)
-        for (int k = 0; k < 6; ++k) c.poly[v][k] = static_cast<float>(kAtanPoly[v][k] * a.dsd / a.ds);
+    fill_fan_tables(c, a.dsd, a.ds);
+    // channel pitch at the far side of the image (the widest)
+    const double hx = ((a.nx - 1) / 2.0 + std::fabs(a.offset_x)) * a.dx;
+    const double hy = ((a.ny - 1) / 2.0 + std::fabs(a.offset_y)) * a.dy;
+    c.fx_bits = adj_fx_bits(a.ds * (std::fabs(a.dso) + std::sqrt(hx * hx + hy * hy)) / std::fabs(a.dsd), a.dx, a.dy);
     c.proj_stride = static_cast<size_t>(a.ns) * a.na;
     c.img_stride = static_cast<size_t>(a.nx) * a.ny;
     return c;
@@ -482,10 +687,8 @@ int fan_forward(const FanArgs& a, const T* proj, T* img, const double* xpos, con
     int st = check_fan(a, proj, img, xpos, ypos, sc, batch);
     if (st) return st;
     if constexpr (sizeof(T) == 4) {
-        TileConst c = fan_const(a, scaled ? a.scale : 1.0);
-        const int w_tall = fan_window(a.ns, a.ds, a.dso, a.dsd, a.nx, a.ny, a.dx, a.dy, a.offset_x,
-                                      a.offset_y, kFwdTileY);
-        return launch_forward<Geo::kFan>(proj, img, xpos, ypos, sc, c, w_tall, batch, stream, "bp_fan_2d");
+        const TileConst c = fan_const(a, scaled ? a.scale : 1.0);
+        return launch_forward<Geo::kFan>(proj, img, xpos, ypos, sc, c, batch, stream, "bp_fan_2d");
     } else {
         const double cents = (a.ns - 1) / 2.0 + a.offset_s;
         dim3 grid(div_up(static_cast<size_t>(a.nx) * a.ny, 128), batch);
@@ -512,10 +715,8 @@ int fan_adjoint(const FanArgs& a, const T* img, T* grad, const double* xpos, con
     cudaError_t e = cudaMemsetAsync(grad, 0, sizeof(T) * static_cast<size_t>(a.ns) * a.na * batch, stream);
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "zero grad: %s", cudaGetErrorString(e));
     if constexpr (sizeof(T) == 4) {
-        TileConst c = fan_const(a, scaled ? a.scale : 1.0);
-        dim3 grid(div_up(a.nx, kTileX), div_up(a.ny, kTileY), batch);
-        return launch_tile(bp_tile_adj_f32<Geo::kFan>, c.W, grid, stream, "bp_fan_2d_grad", img,
-                           grad, xpos, ypos, sc, c, true);
+        const TileConst c = fan_const(a, scaled ? a.scale : 1.0);
+        return launch_adjoint<Geo::kFan>(img, grad, xpos, ypos, sc, c, batch, stream, "bp_fan_2d_grad");
     } else {
         const double cents = (a.ns - 1) / 2.0 + a.offset_s;
         dim3 grid(div_up(static_cast<size_t>(a.nx) * a.ny, 128), batch);
@@ -561,23 +762,27 @@ int check_par(const ctr_par_param* p, const void* in, const void* out, const dou
     return CTR_OK;
 }
 
+// The FP32 kernels' constants for a parallel geometry (window for 32 x kTileY tiles).
 TileConst par_const(const ctr_par_param* p)
 {
     TileConst c{};
     c.ns = p->ns; c.na = p->na; c.nx = p->nx; c.ny = p->ny;
-    c.W = par_window(p->ns, p->ds, p->dx, p->dy);
+    set_window(c, tile_window(par_window(p->ns, p->ds, p->dx, p->dy)));
     c.cents = static_cast<float>((p->ns - 1) / 2.0 + p->offset_s);
     c.nsm1 = static_cast<float>(p->ns - 1);
     c.scale = static_cast<float>(p->orbit);
     c.orbit_start = p->orbit_start;
     c.orbit = p->orbit;
     c.inv_ds = 1.0 / p->ds;
+    c.inv_dx = 1.0 / p->dx;
+    c.inv_dy = 1.0 / p->dy;
     c.centx = (p->nx - 1) / 2.0 + p->offset_x;
     c.centy = (p->ny - 1) / 2.0 + p->offset_y;
     c.dx = p->dx;
     c.dy = p->dy;
     c.ds_d = p->ds;
     c.cents_d = (p->ns - 1) / 2.0 + p->offset_s;
+    c.fx_bits = adj_fx_bits(p->ds, p->dx, p->dy);
     c.proj_stride = static_cast<size_t>(p->ns) * p->na;
     c.img_stride = static_cast<size_t>(p->nx) * p->ny;
     return c;
@@ -590,9 +795,7 @@ int par_forward(const ctr_par_param* p, const T* proj, T* img, const double* xco
     int st = check_par(p, proj, img, xcos, ysin, batch);
     if (st) return st;
     if constexpr (sizeof(T) == 4) {
-        TileConst c = par_const(p);
-        const int w_tall = par_window(p->ns, p->ds, p->dx, p->dy, kFwdTileY);
-        return launch_forward<Geo::kPar>(proj, img, xcos, ysin, nullptr, c, w_tall, batch, stream,
+        return launch_forward<Geo::kPar>(proj, img, xcos, ysin, nullptr, par_const(p), batch, stream,
                                          "bp_par_2d");
     } else {
         const double cents = (p->ns - 1) / 2.0 + p->offset_s;
@@ -614,10 +817,8 @@ int par_adjoint(const ctr_par_param* p, const T* img, T* grad, const double* xco
     cudaError_t e = cudaMemsetAsync(grad, 0, sizeof(T) * static_cast<size_t>(p->ns) * p->na * batch, stream);
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "zero grad: %s", cudaGetErrorString(e));
     if constexpr (sizeof(T) == 4) {
-        TileConst c = par_const(p);
-        dim3 grid(div_up(p->nx, kTileX), div_up(p->ny, kTileY), batch);
-        return launch_tile(bp_tile_adj_f32<Geo::kPar>, c.W, grid, stream, "bp_par_2d_grad", img,
-                           grad, xcos, ysin, nullptr, c, true);
+        return launch_adjoint<Geo::kPar>(img, grad, xcos, ysin, nullptr, par_const(p), batch, stream,
+                                         "bp_par_2d_grad");
     } else {
         const double cents = (p->ns - 1) / 2.0 + p->offset_s;
         dim3 grid(div_up(static_cast<size_t>(p->nx) * p->ny, 128), batch);

@@ -1,7 +1,25 @@
 // Device side of the FP32 pixel-driven backprojectors, shared by the
 // single-geometry entry points (bp.cu) and the batched plan (batch.cu): view
-// parameters, detector windows, the fast interior and exact edge tap paths,
-// and the tile bodies.  Everything here has internal linkage per file.
+// parameters, detector windows, tile-relative channel positions, the fast
+// interior and exact edge tap paths, and the tile bodies of the forward
+// operator.  Everything here has internal linkage per file.
+//
+// Channel positions are taken relative to each tile's reference pixel (the
+// pixel nearest the tile centre), whose position is computed per (tile, view)
+// in FP64 from the caller's tables.  The FP32 part then only adds offsets
+// within the tile, so its rounding is that of a small quantity:
+//   parallel: s = s(ref) + ox cos t / ds + oy sin t / ds, slopes from the
+//             caller's FP64 x cos t / y sin t tables;
+//   fan:      gamma = gamma(ref) + atan(tau), tau = (ox a + oy b) /
+//             (1 + ox b - oy a), where (a, b) = (A, B) / R^2 and (A, B) is the
+//             source-to-reference-pixel vector in the view's frame (R its
+//             length), and the distance weight 1/(d^2 + r^2) =
+//             (1/R^2) / (dn^2 + n^2) with n = ox a + oy b, dn = 1 + ox b - oy a.
+// (ox, oy) is the pixel's offset from the reference pixel in mm.  Positions
+// are stored as sigma = s - (lo + kc + 1/2): lo is the tile's detector window
+// start and kc its centre, so |sigma| <= W/2 and the staged pairs hold
+// (p[j] - (j - kc - 1/2) d[j], d[j]), d[j] = p[j+1] - p[j]; a tap is one
+// 8-byte shared load at j = round(sigma) + kc and one FMA, q + sigma d.
 #pragma once
 
 #include <algorithm>
@@ -17,51 +35,78 @@ namespace {
 
 constexpr int kBpThreads = 256;
 constexpr int kTileX = 32;
-constexpr int kRowsPerThread = 4;
+// Rows per thread of the single-geometry kernels (tile 32 x 64); the batched
+// plan's autotuner also runs 2 and 4.
+constexpr int kRowsPerThread = 8;
 constexpr int kTileY = (kBpThreads / 32) * kRowsPerThread;
 constexpr int kViewBlock = 16;
 
 enum class Geo { kFan, kPar };
 
+// Fan relative-position variants (gen_atan_poly.py): a tile takes the last
+// (smallest) range that covers |tau| on all its pixels.
+// |t| <= 0.3: atan degree 4 (8.5e-10); |t| <= 0.12: degree 3 (3.6e-11);
+// |t| <= 0.06: degree 2 (2.1e-10)
+constexpr int kRelVariants = 3;
+__host__ __device__ constexpr float rel_tmax(int v) { return v == 0 ? 0.3f : v == 1 ? 0.12f : 0.06f; }
+constexpr int kRelAtanDeg[kRelVariants] = {4, 3, 2};
+constexpr double kRelAtan[3][5] = {{9.99999999147148877e-01, -3.33332854976151782e-01, 1.99956912895000311e-01, -1.41487832354163345e-01, 9.29816211336887688e-02},
+    {9.99999999963666064e-01, -3.33333252438835770e-01, 1.99971830243045878e-01, -1.39709592103805486e-01, 0.00000000000000000e+00},
+    {9.99999999792751670e-01, -3.33332296470573552e-01, 1.99231096240648553e-01, 0.00000000000000000e+00, 0.00000000000000000e+00}};
+// atan(j/16) for j = 0..kAtanTab-1 (filled on the host): the reference ray's
+// angle is atan(j/16) + atan(delta) with |delta| <= 1/32.
+constexpr int kAtanTab = 17;
+
 // Per-launch constants of the FP32 tile kernels.
 struct TileConst {
     int ns, na, nx, ny;
     int W;                 // staged window length (channels)
+    int kc;                // window centre (W / 2)
+    int WB;                // bulk-copy box (elements) per view: >= W + 4, multiple of 4
+    int WS;                // shared slot stride per view: WB rounded up to 128 bytes
     float cents;           // (ns-1)/2 + offset_s
     float nsm1;            // ns - 1
-    float dso, K;          // fan: source distance, dsd/ds
+    float dso, K;          // fan, FP32: source distance, dsd/ds (window corners, absolute path)
     float scale;           // applied once to the final sum
+    int fx_bits;           // adjoint: fixed-point bits of a unit tap (see bp.cu)
     double orbit_start, orbit;  // parallel: view angle = orbit_start + ia*orbit
     double inv_ds;         // parallel: 1/ds
+    double inv_dx, inv_dy; // parallel: 1/dx, 1/dy
     double centx, centy, dx, dy;  // parallel pixel grid
-    double ds_d, cents_d, dso_d, dsd_d;  // FP64 geometry for the exact edge test
-    float poly[4][6];      // fan: the atan polynomial variants, scaled by dsd/ds
-    int WB;                // TMA box (elements) per view: >= W + 4, multiple of 4
-    int WS;                // shared slot stride per view: WB rounded up to 128 bytes
+    double ds_d, cents_d, dso_d, dsd_d, K_d;  // FP64 geometry
+    float apoly[kRelVariants][5];  // fan: (dsd/ds) atan(t)/t in powers of t^2
+    double atab[kAtanTab];
     long long total4;      // sinogram elements of the launch, rounded down to 4
     size_t proj_stride, img_stride;
 };
 
-// FP32 channel positions are within ~3e-4 channels of the reference's FP64
-// value (s up to ~2e3, plus atan2f error).  Within kEdgeEps of a detector end
-// the inclusion decision is recomputed in FP64 from the caller's tables.
+// Sets the window length and everything derived from it.
+inline void set_window(TileConst& c, int W)
+{
+    c.W = W;
+    c.kc = W / 2;
+    c.WB = (W + 4 + 3) / 4 * 4;
+    c.WS = (c.WB + 31) / 32 * 32;
+}
+
+// Host: the fan's relative-position tables (scaled by dsd/ds where noted).
+inline void fill_fan_tables(TileConst& c, double dsd, double ds)
+{
+    c.K_d = dsd / ds;
+    for (int v = 0; v < kRelVariants; ++v)
+        for (int k = 0; k < 5; ++k) c.apoly[v][k] = static_cast<float>(kRelAtan[v][k] * c.K_d);
+    for (int j = 0; j < kAtanTab; ++j) c.atab[j] = std::atan(j / 16.0);
+}
+
+// FP32 channel positions near a detector end are within ~1e-3 channels of the
+// reference's FP64 value on the absolute path (s up to ~2e3, plus atan2f
+// error) and far closer on the relative paths.  Within kEdgeEps of an end the
+// inclusion decision is recomputed in FP64 from the caller's tables.
 constexpr float kEdgeEps = 2e-3f;
 
-// ---- per-view parameters ---------------------------------------------------
-// Fan: (sin b, cos b) from the caller's table.  Parallel: (cos t / ds,
-// sin t / ds) from the geometry, with t = orbit_start + ia*orbit.
-template <Geo G>
-__device__ __forceinline__ float2 view_params(const double* __restrict__ sincos, int ia,
-                                              const TileConst& c)
-{
-    if constexpr (G == Geo::kFan) {
-        return make_float2(static_cast<float>(sincos[2 * ia]), static_cast<float>(sincos[2 * ia + 1]));
-    } else {
-        double sa, ca;
-        ::sincos(c.orbit_start + ia * c.orbit, &sa, &ca);
-        return make_float2(static_cast<float>(ca * c.inv_ds), static_cast<float>(sa * c.inv_ds));
-    }
-}
+// round(x) for |x| < 2^22: bits(x + kMagic) - kMagicBits (round to nearest even).
+constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+constexpr unsigned kMagicBits = 0x4B400000u;
 
 __device__ __forceinline__ float rcp_approx(float x)
 {
@@ -70,11 +115,113 @@ __device__ __forceinline__ float rcp_approx(float x)
     return r;
 }
 
-// Channel position of pixel (x, y) for a view, and the fan distance weight
-// 1/(d^2 + r^2) (dsd^2 is applied with the final scale).
+__device__ __forceinline__ float2 lds_f2(unsigned addr)
+{
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
+    return v;
+}
+
+__device__ __forceinline__ void red_shared_u32(unsigned addr, unsigned v)
+{
+    asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+
+// ---- per-(tile, view) records ---------------------------------------------
+
+// Modes of a (tile, view): below kModeFastBase, kModeSkip, kModeEdgeAbs or
+// kModeEdgeRel + the fan variant; a fast view (every tap on the detector and
+// inside the window, relative position) keeps, in place of its mode, a
+// shared address base (a multiple of 4, at least kModeFastBase) with the
+// fan's variant in the low two bits.
+constexpr int kModeSkip = 1;     // the tile projects entirely off the detector
+constexpr int kModeEdgeAbs = 2;  // fan only: absolute FP32 position (tiles the
+                                 // relative form does not cover)
+constexpr int kModeEdgeRel = 4;  // relative position, per-pixel inclusion test
+constexpr int kModeFastBase = 8;
+
+// The fields the fast path reads, one 16-byte shared load.
+struct __align__(16) FastRec {
+    float p0, p1;  // parallel: cos t/ds, sin t/ds; fan relative: a, b; fan
+                   // absolute: sin b, cos b
+    float cen;     // position of the reference pixel less (lo + kc + 1/2)
+    int mode;      // kModeSkip / kModeEdgeAbs / kModeEdgeRel + variant, or a fast-path base
+};
+struct __align__(16) ViewRec : FastRec {
+    float e;       // fan relative: 1/R^2 (folded into the staged pairs); else 1
+    int lo;        // first staged channel
+};
+
+__device__ __forceinline__ FastRec load_fast(const ViewRec* v)
+{
+    const float4 f = *reinterpret_cast<const float4*>(v);
+    return FastRec{f.x, f.y, f.z, __float_as_int(f.w)};
+}
+
+__device__ __forceinline__ bool mode_fast(int m) { return static_cast<unsigned>(m) >= kModeFastBase; }
+__device__ __forceinline__ bool mode_edge_rel(int m) { return (m & ~3) == kModeEdgeRel; }
+__device__ __forceinline__ int mode_variant(int m) { return m & 3; }
+
+// Tile geometry shared by the forward and the adjoint: origin, reference
+// pixel and the FP32 corners (absolute, for the window) and corner offsets.
+struct TileBox {
+    int tx0, ty0, ixm, iym;
+    float x0, x1, y0, y1;      // absolute corner coordinates (mm)
+    float ox0, ox1, oy0, oy1;  // corner offsets from the reference pixel (mm)
+};
+
 template <Geo G>
-__device__ __forceinline__ float channel_of(float x, float y, float2 vp, const TileConst& c,
-                                            float* w)
+__device__ __forceinline__ double pix_x(const double* __restrict__ t0, int ix, const TileConst& c)
+{
+    if constexpr (G == Geo::kFan) return t0[ix];
+    else return (ix - c.centx) * c.dx;
+}
+template <Geo G>
+__device__ __forceinline__ double pix_y(const double* __restrict__ t1, int iy, const TileConst& c)
+{
+    if constexpr (G == Geo::kFan) return t1[iy];
+    else return (c.centy - iy) * c.dy;
+}
+// Offsets of a pixel from the tile's reference pixel, rounded once to FP32.
+template <Geo G>
+__device__ __forceinline__ float off_x(const double* __restrict__ t0, int ix, int ixm, const TileConst& c)
+{
+    if constexpr (G == Geo::kFan) return static_cast<float>(t0[ix] - t0[ixm]);
+    else return static_cast<float>((ix - ixm) * c.dx);
+}
+template <Geo G>
+__device__ __forceinline__ float off_y(const double* __restrict__ t1, int iy, int iym, const TileConst& c)
+{
+    if constexpr (G == Geo::kFan) return static_cast<float>(t1[iy] - t1[iym]);
+    else return static_cast<float>((iym - iy) * c.dy);
+}
+
+template <Geo G>
+__device__ __forceinline__ TileBox tile_box(const double* __restrict__ t0, const double* __restrict__ t1,
+                                            int tile_x, int tile_y, int tile_h, const TileConst& c)
+{
+    TileBox B;
+    B.tx0 = tile_x * kTileX;
+    B.ty0 = tile_y * tile_h;
+    B.ixm = min(B.tx0 + kTileX / 2, c.nx - 1);
+    B.iym = min(B.ty0 + tile_h / 2, c.ny - 1);
+    const int ix1 = min(B.tx0 + kTileX - 1, c.nx - 1), iy1 = min(B.ty0 + tile_h - 1, c.ny - 1);
+    B.x0 = static_cast<float>(pix_x<G>(t0, B.tx0, c));
+    B.x1 = static_cast<float>(pix_x<G>(t0, ix1, c));
+    B.y0 = static_cast<float>(pix_y<G>(t1, B.ty0, c));
+    B.y1 = static_cast<float>(pix_y<G>(t1, iy1, c));
+    B.ox0 = off_x<G>(t0, B.tx0, B.ixm, c);
+    B.ox1 = off_x<G>(t0, ix1, B.ixm, c);
+    B.oy0 = off_y<G>(t1, B.ty0, B.iym, c);
+    B.oy1 = off_y<G>(t1, iy1, B.iym, c);
+    return B;
+}
+
+// Absolute FP32 channel position of pixel (x, y) and the fan distance weight
+// 1/(d^2 + r^2); vp = (sin b, cos b) (fan) or (cos t/ds, sin t/ds) (parallel).
+// Used for detector windows (tile corners) and the fan's absolute edge path.
+template <Geo G>
+__device__ __forceinline__ float channel_abs(float x, float y, float2 vp, const TileConst& c, float* w)
 {
     if constexpr (G == Geo::kFan) {
         const float d = fmaf(-y, vp.y, fmaf(x, vp.x, c.dso));
@@ -107,29 +254,6 @@ __device__ __noinline__ double channel_exact(int ix, int iy, int ia, const doubl
     }
 }
 
-// One pixel-view tap on an edge view: inclusion decided as the reference does
-// (exactly, in FP64, near the detector ends); returns false when excluded.
-template <Geo G>
-__device__ __forceinline__ bool edge_tap(float s, int ix, int iy, int ia, int lo,
-                                         const double* t0, const double* t1, const double* t2,
-                                         const TileConst& c, int* k, float* u)
-{
-    float fs;
-    if (fabsf(s) < kEdgeEps || fabsf(s - c.nsm1) < kEdgeEps) {
-        const double sd = channel_exact<G>(ix, iy, ia, t0, t1, t2, c);
-        if (!(sd >= 0.0 && sd <= static_cast<double>(c.ns - 1))) return false;
-        const double fd = floor(sd);
-        fs = static_cast<float>(fd);
-        *u = static_cast<float>(sd - fd);
-    } else {
-        if (!(s >= 0.0f && s <= c.nsm1)) return false;
-        fs = floorf(s);
-        *u = s - fs;
-    }
-    *k = min(max(static_cast<int>(fs) - lo, 0), c.W - 2);
-    return true;
-}
-
 // Tiles whose channel range lies farther than this outside [0, ns-1] project
 // entirely off the detector (FP32 corner positions are within ~3e-4 channels).
 constexpr float kSkipEps = 1e-2f;
@@ -141,12 +265,11 @@ constexpr float kSkipEps = 1e-2f;
 // The channel position over a convex tile is extreme at its corners (affine
 // for the parallel beam; for the fan the ray angle is).
 template <Geo G>
-__device__ int window_start(float2 vp, float x0, float x1, float y0, float y1, const TileConst& c,
-                            bool* interior, bool* off = nullptr)
+__device__ int window_start(float2 vp, const TileBox& B, const TileConst& c, bool* interior, bool* off)
 {
     float smin = FLT_MAX, smax = -FLT_MAX;
     bool full = false;
-    const float xs[2] = {x0, x1}, ys[2] = {y0, y1};
+    const float xs[2] = {B.x0, B.x1}, ys[2] = {B.y0, B.y1};
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
 #pragma unroll
@@ -156,15 +279,15 @@ __device__ int window_start(float2 vp, float x0, float x1, float y0, float y1, c
                 if (d <= 0.0f) full = true;
             }
             float w;
-            const float s = channel_of<G>(xs[i], ys[j], vp, c, &w);
+            const float s = channel_abs<G>(xs[i], ys[j], vp, c, &w);
             smin = fminf(smin, s);
             smax = fmaxf(smax, s);
         }
     }
     *interior = false;
-    if (off) *off = false;
+    *off = false;
     if (full || !(smin == smin) || !(smax == smax)) return -1;
-    if (off) *off = smax < -kSkipEps || smin > c.nsm1 + kSkipEps;
+    *off = smax < -kSkipEps || smin > c.nsm1 + kSkipEps;
     int lo = static_cast<int>(floorf(smin)) - 2;
     int hi = static_cast<int>(floorf(smax)) + 3;
     const bool fits = hi - lo + 1 <= c.W;
@@ -175,317 +298,413 @@ __device__ int window_start(float2 vp, float x0, float x1, float y0, float y1, c
     return min(lo, c.ns);
 }
 
-// Forward FP32 tile kernel with cooperative (plain-load) staging: proj [na][ns]
-// -> img [ny][nx] (batch in grid.z).  t0/t1/t2: fan xpos/ypos/sincostbl,
-// parallel xcos/ysin/unused.  Used where the TMA kernel below does not apply
-// (windows wider than one 256-element box, unaligned buffers).
-template <Geo G>
-__global__ void __launch_bounds__(kBpThreads, 2)
-    bp_tile_f32_coop(const float* __restrict__ proj, float* __restrict__ img,
-                const double* __restrict__ t0, const double* __restrict__ t1,
-                const double* __restrict__ t2, const TileConst c)
+// FP64 1/x from the FP32 reciprocal and one Newton step (relative error
+// ~1e-14 for x within FP32 range).
+__device__ __forceinline__ double rcp_refined(double x)
 {
-    extern __shared__ float2 win[];  // [kViewBlock][W]
-    __shared__ float2 s_vp[kViewBlock];
-    __shared__ int s_lo[kViewBlock];
-    __shared__ int s_in[kViewBlock];
-
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int tx0 = blockIdx.x * kTileX, ty0 = blockIdx.y * kTileY;
-    const float* P = proj + blockIdx.z * c.proj_stride;
-
-    auto px = [&](int ix) -> float {
-        if constexpr (G == Geo::kFan) return static_cast<float>(t0[ix]);
-        else return static_cast<float>((ix - c.centx) * c.dx);
-    };
-    auto py = [&](int iy) -> float {
-        if constexpr (G == Geo::kFan) return static_cast<float>(t1[iy]);
-        else return static_cast<float>((c.centy - iy) * c.dy);
-    };
-    const int ixc = min(tx0 + lane, c.nx - 1);
-    const float x = px(ixc);
-    float y[kRowsPerThread], acc[kRowsPerThread];
-#pragma unroll
-    for (int r = 0; r < kRowsPerThread; ++r) {
-        y[r] = py(min(ty0 + warp * kRowsPerThread + r, c.ny - 1));
-        acc[r] = 0.0f;
-    }
-    const float cx0 = px(tx0), cx1 = px(min(tx0 + kTileX - 1, c.nx - 1));
-    const float cy0 = py(ty0), cy1 = py(min(ty0 + kTileY - 1, c.ny - 1));
-
-    for (int v0 = 0; v0 < c.na; v0 += kViewBlock) {
-        const int nv = min(kViewBlock, c.na - v0);
-        if (threadIdx.x < nv) {
-            const float2 vp = view_params<G>(t2, v0 + threadIdx.x, c);
-            bool inner;
-            s_vp[threadIdx.x] = vp;
-            s_lo[threadIdx.x] = window_start<G>(vp, cx0, cx1, cy0, cy1, c, &inner);
-            s_in[threadIdx.x] = inner;
-        }
-        __syncthreads();
-        for (int idx = threadIdx.x; idx < nv * c.W; idx += kBpThreads) {
-            const int j = idx / c.W, k = idx - j * c.W;
-            const int g = s_lo[j] + k;
-            const float* row = P + static_cast<size_t>(v0 + j) * c.ns;
-            const float p0 = (g >= 0 && g < c.ns) ? __ldg(row + g) : 0.0f;
-            const float p1 = (g + 1 >= 0 && g + 1 < c.ns) ? __ldg(row + g + 1) : 0.0f;
-            win[idx] = make_float2(p0, p1 - p0);
-        }
-        __syncthreads();
-        for (int j = 0; j < nv; ++j) {
-            const float2 vp = s_vp[j];
-            const int lo = s_lo[j];
-            const float2* wj = win + j * c.W;
-            if (s_in[j]) {
-                // every tap of the tile is on the detector and inside the window
-#pragma unroll
-                for (int r = 0; r < kRowsPerThread; ++r) {
-                    float w;
-                    const float s = channel_of<G>(x, y[r], vp, c, &w);
-                    const float fs = floorf(s);
-                    const float2 pv = wj[static_cast<int>(fs) - lo];
-                    const float v = fmaf(s - fs, pv.y, pv.x);
-                    if constexpr (G == Geo::kFan) acc[r] = fmaf(v, w, acc[r]);
-                    else acc[r] += v;
-                }
-            } else {
-#pragma unroll
-                for (int r = 0; r < kRowsPerThread; ++r) {
-                    float w, u;
-                    int k;
-                    const float s = channel_of<G>(x, y[r], vp, c, &w);
-                    const int iyc = min(ty0 + warp * kRowsPerThread + r, c.ny - 1);
-                    if (edge_tap<G>(s, ixc, iyc, v0 + j, lo, t0, t1, t2, c, &k, &u)) {
-                        const float2 pv = wj[k];
-                        const float v = fmaf(u, pv.y, pv.x);
-                        if constexpr (G == Geo::kFan) acc[r] = fmaf(v, w, acc[r]);
-                        else acc[r] += v;
-                    }
-                }
-            }
-        }
-        __syncthreads();
-    }
-    float* I = img + blockIdx.z * c.img_stride;
-    const int ix = tx0 + lane;
-#pragma unroll
-    for (int r = 0; r < kRowsPerThread; ++r) {
-        const int iy = ty0 + warp * kRowsPerThread + r;
-        if (ix < c.nx && iy < c.ny) I[static_cast<size_t>(iy) * c.nx + ix] = acc[r] * c.scale;
-    }
+    const double r = static_cast<double>(__frcp_rn(static_cast<float>(x)));
+    return fma(r, fma(-x, r, 1.0), r);
 }
 
-// ---- TMA-fed forward kernel ---------------------------------------------------
-//
-// Same tile as bp_tile_f32_coop, but a CTA runs two view groups of 256 threads
-// on the same 32x32 tile (each group takes half of every block of
-// 2*kViewBlock views; the two partial sums are added in a fixed order at the
-// end), and the detector windows reach shared memory through the TMA engine:
-// one cp.async.bulk copy per view (16-byte aligned start in the flattened
-// sinogram, a 128-byte aligned shared slot), issued two view blocks ahead
-// into double-buffered raw slots, each block completed on its own mbarrier
-// (waits are bounded and report kFlagWaitTimeout).  Once a slot
-// has landed, the CTA rewrites it as (q[k], d[k]) pairs, d[k] = p[k+1] - p[k]
-// and q[k] = p[k] - k d[k] (k the channel less the window start lo), zero off
-// the detector, so an interpolation at s' = s - lo in [k, k+1] is one 8-byte
-// shared load and one FMA, q[k] + s' d[k], with no fraction of s'.
-//
-// Interior fast path (every tap of the tile on the detector): s' comes out of
-// the position's last FMA with cents - lo in place of cents, its floor from
-// adding 2^23 - 0.5 (round-to-nearest of s' - 1/2 lands the integer part in
-// the low mantissa bits; s' in [1, 2^22)), and for the fan
-// atan(r/d) is one of the minimax polynomials below (the lowest degree whose
-// range covers |r/d| on the whole tile, up to 0.6), with an approximate
-// reciprocal of d.
-
-// atan(t) ~= t*P(t^2), minimax for relative error (Remez; gen_atan_poly.py),
-// four variants of about the same error: a tile takes the lowest degree whose
-// range covers all its pixels.  |t| <= 0.6: degree 5 in t^2, max relative error
-// 3.28e-08; |t| <= 0.45: degree 4, 3.87e-08; |t| <= 0.3: degree 3, 4.84e-08;
-// |t| <= 0.15: degree 2, 4.93e-08.
-constexpr int kAtanVariants = 4;
-__host__ __device__ constexpr float atan_tmax(int v)
+// atan(t) for |t| <= (kAtanTab - 1/2)/16 in FP64: the table value at the
+// nearest sixteenth, plus atan(delta) with delta = (t - t_j)/(1 + t t_j),
+// |delta| <= 1/32, as delta - delta^3/3 + delta^5/5 (the next term is below
+// 5e-12); the cubic and quintic terms (below 1.1e-5) are formed in FP32.
+__device__ __forceinline__ double atan_ref(double t, const TileConst& c)
 {
-    return v == 0 ? 0.6f : v == 1 ? 0.45f : v == 2 ? 0.3f : 0.15f;
-}
-constexpr double kAtanPoly[kAtanVariants][6] = {
-    {9.99999967214467378e-01, -3.33326573611355148e-01, 1.99772013637297047e-01, -1.39992597733896912e-01,
-     9.42086263445095634e-02, -4.04465160162714304e-02},
-    {9.99999961331696996e-01, -3.33323584754777580e-01, 1.99603534902473234e-01, -1.37111734158844867e-01,
-     7.55531535813081662e-02, 0.0},
-    {9.99999951640157425e-01, -3.33315939607756684e-01, 1.99016376594526256e-01, -1.24757817537760357e-01,
-     0.0, 0.0},
-    {9.99999950700421469e-01, -3.33293746601247498e-01, 1.95275580886984462e-01, 0.0, 0.0, 0.0}};
-constexpr float kMagic = 8388608.0f;       // 2^23
-constexpr float kMagicHalf = 8388607.5f;   // 2^23 - 1/2
-constexpr unsigned kMagicBits = 0x4B000000u;
-constexpr int kGroups = 2;
-constexpr int kBlockViews = kGroups * kViewBlock;
-constexpr int kTmaThreads = kGroups * kBpThreads;
-constexpr int kModeEdge = 0, kModeSkip = 1, kModeFast = 2;
-// A fast view's mode: a multiple of 8 (kModeFastBase, or the forward tile's
-// shared slot base) plus the atan variant in the low two bits.
-constexpr int kModeFastBase = 8;
-
-struct ViewP {
-    float2 vp;
-    int lo;     // first staged channel
-    int mode;   // kModeEdge, kModeSkip, or >= kModeFast: the interior fast path
-                // (the forward tile stores the view's shared slot base there)
-};
-// Parallel beam: also the channel position of the tile's first pixel less lo,
-// from FP64, so that fast-path positions add only in-tile offsets in FP32.
-struct ViewPar : ViewP {
-    float cen;
-    int pad;
-};
-template <Geo G> struct ViewSel { using type = ViewP; };
-template <> struct ViewSel<Geo::kPar> { using type = ViewPar; };
-template <Geo G> using ViewT = typename ViewSel<G>::type;
-constexpr size_t kViewBytesMax = sizeof(ViewPar);
-
-// Fast-path origin of positions less the window start: the detector centre
-// (fan) or the tile's first pixel (parallel).
-template <Geo G>
-__device__ __forceinline__ float view_cen(const ViewT<G>& P, const TileConst& c)
-{
-    if constexpr (G == Geo::kFan) return c.cents - static_cast<float>(P.lo);
-    else return P.cen;
-}
-
-__device__ __forceinline__ bool mode_fast(int m) { return static_cast<unsigned>(m) >= kModeFast; }
-
-__device__ __forceinline__ float2 lds_f2(unsigned addr)
-{
-    float2 v;
-    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
-    return v;
-}
-
-// Channel position on the interior fast path (shared by the forward and the
-// adjoint), relative to the tile's window start lo, from ViewP.cen.  Fan (x, y
-// absolute): xs = dso + x sin b, xc = x cos b, s - lo = K atan(r/d) + cen;
-// parallel (x, y offsets from the tile's first pixel): xs = x cos t / ds + cen,
-// s - lo = xs + y sin t / ds.  Returns s - lo (below the window length); *w is
-// the fan distance weight 1/(d^2+r^2).
-// V = the atan variant (fan; 0 for the parallel beam).
-template <Geo G, int V = 0>
-__device__ __forceinline__ float fast_s(float xs, float xc, float y, float2 vp, float cen,
-                                        const TileConst& c, float* w)
-{
-    if constexpr (G == Geo::kFan) {
-        constexpr int deg = 5 - V;
-        const float d = fmaf(-y, vp.y, xs);
-        const float rr = fmaf(y, vp.x, xc);
-        const float t = rr * rcp_approx(d);
-        const float z = t * t;
-        float p = c.poly[V][deg];
-#pragma unroll
-        for (int k = deg - 1; k >= 0; --k) p = fmaf(z, p, c.poly[V][k]);
-        *w = rcp_approx(fmaf(d, d, rr * rr));
-        return fmaf(t, p, cen);
-    } else {
-        *w = 1.0f;
-        return fmaf(y, vp.y, xs);
-    }
-}
-
-template <Geo G>
-__device__ __forceinline__ void fast_xs(float x, float2 vp, float cen, const TileConst& c, float* xs,
-                                        float* xc)
-{
-    if constexpr (G == Geo::kFan) {
-        *xs = fmaf(x, vp.x, c.dso);
-        *xc = x * vp.y;
-    } else {
-        *xs = fmaf(x, vp.x, cen);
-        *xc = 0.0f;
-    }
+    const double q = rint(t * 16.0);
+    const double tq = q * 0.0625;
+    const double delta = (t - tq) * rcp_refined(fma(t, tq, 1.0));
+    const float df = static_cast<float>(delta), d2 = df * df;
+    const float corr = df * d2 * fmaf(d2, 0.2f, -1.0f / 3.0f);
+    const int j = static_cast<int>(fabs(q));
+    const double base = q < 0.0 ? -c.atab[j] : c.atab[j];
+    return base + (delta + static_cast<double>(corr));
 }
 
 // Per-view parameters, window and path for one tile (thread-local).
 template <Geo G>
-__device__ ViewT<G> view_setup(const double* __restrict__ t0, const double* __restrict__ t1,
-                               const double* __restrict__ t2, int ia, int ix0, int iy0, float x0,
-                               float x1, float y0, float y1, const TileConst& c)
+__device__ ViewRec view_setup(const double* __restrict__ t0, const double* __restrict__ t1,
+                              const double* __restrict__ t2, int ia, const TileBox& B,
+                              const TileConst& c)
 {
-    ViewT<G> P;
-    if constexpr (G == Geo::kFan) {
-        P.vp = view_params<G>(t2, ia, c);
-    } else {
-        // FP32 slopes: on the fast path they multiply offsets within the tile
-        // only (the tile's origin comes from the FP64 tables below)
-        float sf, cf;
-        sincosf(static_cast<float>(c.orbit_start + ia * c.orbit), &sf, &cf);
-        const float ids = static_cast<float>(c.inv_ds);
-        P.vp = make_float2(cf * ids, sf * ids);
-    }
+    ViewRec P;
     bool inner, off;
-    P.lo = window_start<G>(P.vp, x0, x1, y0, y1, c, &inner, &off);
-    bool fast = inner;
-    if constexpr (G == Geo::kFan) {
-        // polynomial atan needs d > 0 and |r/d| <= atan_tmax(0) on the whole
-        // tile (r/d is a linear-fractional function: extremes at the corners);
-        // the tile takes the lowest-degree variant that covers it
-        const float xs[2] = {x0, x1}, ys[2] = {y0, y1};
-        float tmax = 0.0f;
-#pragma unroll
-        for (int i = 0; i < 2; ++i)
-#pragma unroll
-            for (int j = 0; j < 2; ++j) {
-                const float d = fmaf(-ys[j], P.vp.y, fmaf(xs[i], P.vp.x, c.dso));
-                const float r = fmaf(xs[i], P.vp.y, ys[j] * P.vp.x);
-                fast = fast && d > 0.0f && fabsf(r) <= atan_tmax(0) * d;
-                tmax = fmaxf(tmax, fabsf(r) / d);
-            }
-        int v = 0;
-#pragma unroll
-        for (int k = 1; k < kAtanVariants; ++k)
-            if (tmax <= atan_tmax(k)) v = k;
-        P.mode = fast ? kModeFastBase + v : (off ? kModeSkip : kModeEdge);
-    } else {
-        P.mode = fast ? kModeFastBase : (off ? kModeSkip : kModeEdge);
-    }
     if constexpr (G == Geo::kPar) {
-        // s(x0, y0) - lo in FP64 from the caller's x cos t / y sin t tables
-        // (src/bp_par_2d.cc:70), (ix0, iy0) the tile's first pixel: the fast
-        // path adds only offsets within the tile in FP32 (at most a tile's
-        // extent in channels)
-        P.cen = static_cast<float>((t0[static_cast<size_t>(ix0) * c.na + ia] +
-                                    t1[static_cast<size_t>(iy0) * c.na + ia]) * c.inv_ds +
-                                   c.cents_d - P.lo);
-        P.pad = 0;
+        // slopes from the caller's FP64 tables (differences of neighbouring
+        // pixels; the tables are x cos t and y sin t), reference position in
+        // FP64 (src/bp_par_2d.cc:70): FP32 then rounds only in-tile offsets
+        const size_t na = static_cast<size_t>(c.na);
+        const int ixn = B.ixm + 1 < c.nx ? B.ixm + 1 : B.ixm - 1;
+        const int iyn = B.iym + 1 < c.ny ? B.iym + 1 : B.iym - 1;
+        const double xc = t0[B.ixm * na + ia], ys = t1[B.iym * na + ia];
+        double cs = (c.nx > 1) ? (t0[ixn * na + ia] - xc) * c.inv_dx * (ixn > B.ixm ? 1.0 : -1.0) : 0.0;
+        double sn = (c.ny > 1) ? (ys - t1[iyn * na + ia]) * c.inv_dy * (iyn > B.iym ? 1.0 : -1.0) : 0.0;
+        if (c.nx == 1 || c.ny == 1) {
+            // a one-pixel-wide image has no neighbour: use the view angle
+            double sa, ca;
+            ::sincos(c.orbit_start + ia * c.orbit, &sa, &ca);
+            if (c.nx == 1) cs = ca;
+            if (c.ny == 1) sn = sa;
+        }
+        P.p0 = static_cast<float>(cs * c.inv_ds);
+        P.p1 = static_cast<float>(sn * c.inv_ds);
+        P.lo = window_start<G>(make_float2(P.p0, P.p1), B, c, &inner, &off);
+        P.cen = static_cast<float>((xc + ys) * c.inv_ds + c.cents_d - (P.lo + c.kc + 0.5));
+        P.e = 1.0f;
+        P.mode = inner ? kModeFastBase : (off ? kModeSkip : kModeEdgeRel);
+    } else {
+        const double sb = t2[2 * ia], cb = t2[2 * ia + 1];
+        const double X = t0[B.ixm], Y = t1[B.iym];
+        P.lo = window_start<G>(make_float2(static_cast<float>(sb), static_cast<float>(cb)), B, c, &inner, &off);
+        // source-to-reference-pixel vector in the view's frame
+        const double A = fma(c.dso_d, cb, -Y), Bv = fma(c.dso_d, sb, X);
+        const double d0 = fma(A, cb, Bv * sb), r0 = fma(Bv, cb, -(A * sb));
+        const double R2 = fma(A, A, Bv * Bv);
+        bool rel = d0 > 0.0 && R2 > 0.0 && fabs(r0) <= (kAtanTab - 0.5) / 16.0 * d0;
+        int v = 0;
+        if (rel) {
+            const double eR = rcp_refined(R2);
+            P.p0 = static_cast<float>(A * eR);
+            P.p1 = static_cast<float>(Bv * eR);
+            P.e = static_cast<float>(eR);
+            // largest |tau| over the tile: at a corner (the angle seen from the
+            // source is monotone along each edge of the convex tile)
+            float tmax = 0.0f;
+            const float oxs[2] = {B.ox0, B.ox1}, oys[2] = {B.oy0, B.oy1};
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    const float n = fmaf(oys[k], P.p1, oxs[i] * P.p0);
+                    const float dn = fmaf(-oys[k], P.p0, fmaf(oxs[i], P.p1, 1.0f));
+                    if (!(dn > 0.0f)) rel = false;
+                    tmax = fmaxf(tmax, fabsf(n) / dn);
+                }
+            v = -1;
+#pragma unroll
+            for (int k = 0; k < kRelVariants; ++k)
+                if (tmax <= rel_tmax(k)) v = k;
+            if (v < 0) rel = false;
+            if (rel) {
+                const double g0 = atan_ref(r0 * rcp_refined(d0), c);
+                P.cen = static_cast<float>(fma(g0, c.K_d, c.cents_d - (P.lo + c.kc + 0.5)));
+            }
+        }
+        if (!rel) {
+            P.p0 = static_cast<float>(sb);
+            P.p1 = static_cast<float>(cb);
+            P.cen = 0.0f;
+            P.e = 1.0f;
+        }
+        P.mode = off ? kModeSkip : (rel ? (inner ? kModeFastBase : kModeEdgeRel) + v : kModeEdgeAbs);
     }
     return P;
 }
 
-// Pixel coordinates on the fast path: absolute for the fan, offsets from the
-// tile's first pixel (x0, y0) for the parallel beam (exact: both are on the
-// pixel grid).
-template <Geo G>
-__device__ __forceinline__ float fast_coord(float v, float v0)
+// ---- channel positions (bit-identical wherever they are computed) ----------
+// Every operation below is an explicit round-to-nearest intrinsic, so the
+// forward kernels and the adjoint compute the same position for a
+// (pixel, view): the adjoint is then the exact transpose of the forward.
+
+// Parallel beam: sigma = cen + ox p0 + oy p1 (x part once per column).
+__device__ __forceinline__ float par_xpart(float ox, const FastRec& P) { return __fmaf_rn(ox, P.p0, P.cen); }
+__device__ __forceinline__ float par_sigma(float xs, float oy, const FastRec& P) { return __fmaf_rn(oy, P.p1, xs); }
+
+// Fan: x part (ox a, 1 + ox b) once per column; then per pixel
+// tau = n / dn, n = ox a + oy b, dn = 1 + ox b - oy a, sigma = cen +
+// (dsd/ds) atan(tau), weight w = 1/(dn^2 + n^2) (the view's 1/R^2 is in the
+// staged pairs).
+struct FanX {
+    float n, d;
+};
+__device__ __forceinline__ FanX fan_xpart(float ox, const FastRec& P)
 {
-    if constexpr (G == Geo::kFan) return v;
-    else return v - v0;
+    return FanX{__fmul_rn(ox, P.p0), __fmaf_rn(ox, P.p1, 1.0f)};
+}
+template <int V>
+__device__ __forceinline__ float fan_sigma(FanX X, float oy, const FastRec& P, const TileConst& c, float* w)
+{
+    constexpr int da = kRelAtanDeg[V];
+    const float n = __fmaf_rn(oy, P.p1, X.n);
+    const float dn = __fmaf_rn(-oy, P.p0, X.d);
+    const float t = __fmul_rn(n, rcp_approx(dn));
+    const float z = __fmul_rn(t, t);
+    float p = c.apoly[V][da];
+#pragma unroll
+    for (int k = da - 1; k >= 0; --k) p = __fmaf_rn(z, p, c.apoly[V][k]);
+    *w = rcp_approx(__fmaf_rn(dn, dn, __fmul_rn(n, n)));
+    return __fmaf_rn(t, p, P.cen);
 }
 
-// The fast-path taps of one view for a thread's R pixels (atan variant V).
+// round(sigma) as a float (exact).
+__device__ __forceinline__ float round_sigma(float sig) { return __fadd_rn(__fadd_rn(sig, kMagic), -kMagic); }
+
+// One tap on an edge view, relative position: inclusion decided as the
+// reference does (0 <= s <= ns-1, in FP64 within kEdgeEps of an end); returns
+// false when excluded, else the pair index j (in [0, W-2]) and *sig2, the
+// position relative to the window centre used for the interpolation
+// (q[j] + sig2 d[j]; the fraction beyond j is sig2 - (j - kc - 1/2)).
+template <Geo G>
+__device__ __forceinline__ bool edge_tap(float sig, int ix, int iy, int ia, int lo, const double* t0,
+                                         const double* t1, const double* t2, const TileConst& c,
+                                         int* j, float* sig2)
+{
+    const float s = __fadd_rn(sig, static_cast<float>(lo + c.kc) + 0.5f);  // absolute, FP32
+    if (fabsf(s) < kEdgeEps || fabsf(s - c.nsm1) < kEdgeEps) {
+        const double sd = channel_exact<G>(ix, iy, ia, t0, t1, t2, c);
+        if (!(sd >= 0.0 && sd <= static_cast<double>(c.ns - 1))) return false;
+        const double fd = floor(sd);
+        *j = static_cast<int>(fd) - lo;
+        *sig2 = static_cast<float>(sd - (lo + c.kc + 0.5));
+    } else {
+        if (!(s >= 0.0f && s <= c.nsm1)) return false;
+        *j = static_cast<int>(round_sigma(sig)) + c.kc;
+        *sig2 = sig;
+    }
+    if (*j < 0 || *j > c.W - 2) {
+        *j = min(max(*j, 0), c.W - 2);
+        *sig2 = fminf(fmaxf(*sig2, static_cast<float>(*j - c.kc) - 0.5f), static_cast<float>(*j - c.kc) + 0.5f);
+    }
+    return true;
+}
+
+// The same on an absolute FP32 position s (fan tiles the relative form does
+// not cover).
+template <Geo G>
+__device__ __forceinline__ bool edge_tap_abs(float s, int ix, int iy, int ia, int lo, const double* t0,
+                                             const double* t1, const double* t2, const TileConst& c,
+                                             int* j, float* sig2)
+{
+    double sd;
+    if (fabsf(s) < kEdgeEps || fabsf(s - c.nsm1) < kEdgeEps) {
+        sd = channel_exact<G>(ix, iy, ia, t0, t1, t2, c);
+        if (!(sd >= 0.0 && sd <= static_cast<double>(c.ns - 1))) return false;
+    } else {
+        if (!(s >= 0.0f && s <= c.nsm1)) return false;
+        sd = static_cast<double>(s);
+    }
+    const double fd = floor(sd);
+    *j = min(max(static_cast<int>(fd) - lo, 0), c.W - 2);
+    *sig2 = static_cast<float>(fmin(fmax(sd - (lo + c.kc + 0.5), (*j - c.kc) - 0.5), (*j - c.kc) + 0.5));
+    return true;
+}
+
+// Pair of staged window element k (channel lo + k): (q, d) scaled by e, with
+// d = p[k+1] - p[k] and q = p[k] - (k - kc - 1/2) d.
+__device__ __forceinline__ float2 make_pair(float p0, float p1, int k, int kc, float e)
+{
+    const float d = p1 - p0;
+    const float q = fmaf(-(static_cast<float>(k - kc) - 0.5f), d, p0);
+    return make_float2(q * e, d * e);
+}
+
+// ---- fast-path taps of the forward ------------------------------------------
+
+// The fast-path taps of one view for a thread's R pixels (fan variant V):
+// pixel r is at offsets (ox, oy[r]); base = the view's pair slot address
+// plus 8 kc, less 8 kMagicBits.
 template <Geo G, int V, int R>
-__device__ __forceinline__ void fast_rows(float xs, float xc, const float (&yf)[R], float2 vp, float cen,
+__device__ __forceinline__ void fast_rows(float ox, const float (&oy)[R], const FastRec& P,
                                           const TileConst& c, unsigned base, float (&part)[R])
 {
+    if constexpr (G == Geo::kFan) {
+        const FanX X = fan_xpart(ox, P);
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-        float w;
-        const float s = fast_s<G, V>(xs, xc, yf[r], vp, cen, c, &w);
-        const float2 pv = lds_f2(base + 8u * __float_as_uint(s + kMagicHalf));
-        if constexpr (G == Geo::kFan) part[r] = fmaf(fmaf(s, pv.y, pv.x), w, part[r]);
-        else part[r] += fmaf(s, pv.y, pv.x);
+        for (int r = 0; r < R; ++r) {
+            float w;
+            const float sig = fan_sigma<V>(X, oy[r], P, c, &w);
+            const float2 pv = lds_f2(base + 8u * __float_as_uint(__fadd_rn(sig, kMagic)));
+            part[r] = fmaf(fmaf(sig, pv.y, pv.x), w, part[r]);
+        }
+    } else {
+        const float xs = par_xpart(ox, P);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const float sig = par_sigma(xs, oy[r], P);
+            const float2 pv = lds_f2(base + 8u * __float_as_uint(__fadd_rn(sig, kMagic)));
+            part[r] += fmaf(sig, pv.y, pv.x);
+        }
     }
 }
 
+// Edge-path taps of one view (pairs of the view at wj) for a thread's R
+// pixels: column ixc at offset ox, rows iy0 + r (clamped to the image) at
+// offsets oy[r].
+template <int V, int R>
+__device__ __forceinline__ void edge_rows_fan(FanX X, const float (&oy)[R], int ixc, int iy0, int ia,
+                                              const ViewRec& P, const float2* wj, const double* t0,
+                                              const double* t1, const double* t2, const TileConst& c,
+                                              float (&part)[R])
+{
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        float w, sig2;
+        int j;
+        const float sig = fan_sigma<V>(X, oy[r], P, c, &w);
+        if (edge_tap<Geo::kFan>(sig, ixc, min(iy0 + r, c.ny - 1), ia, P.lo, t0, t1, t2, c, &j, &sig2)) {
+            const float2 pv = wj[j];
+            part[r] = fmaf(fmaf(sig2, pv.y, pv.x), w, part[r]);
+        }
+    }
+}
+
+template <Geo G, int R>
+__device__ __forceinline__ void edge_rows(float ox, const float (&oy)[R], int ixc, int iy0, int ia,
+                                          const ViewRec& P, const float2* wj, const double* t0,
+                                          const double* t1, const double* t2, const TileConst& c,
+                                          float (&part)[R])
+{
+    if constexpr (G == Geo::kFan) {
+        if (P.mode == kModeEdgeAbs) {
+            const float x = static_cast<float>(t0[ixc]);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int iyc = min(iy0 + r, c.ny - 1);
+                float w, sig2;
+                int j;
+                const float s = channel_abs<G>(x, static_cast<float>(t1[iyc]), make_float2(P.p0, P.p1), c, &w);
+                if (edge_tap_abs<G>(s, ixc, iyc, ia, P.lo, t0, t1, t2, c, &j, &sig2)) {
+                    const float2 pv = wj[j];
+                    part[r] = fmaf(fmaf(sig2, pv.y, pv.x), w, part[r]);
+                }
+            }
+            return;
+        }
+        const FanX X = fan_xpart(ox, P);
+        switch (mode_variant(P.mode)) {
+            case 0: edge_rows_fan<0, R>(X, oy, ixc, iy0, ia, P, wj, t0, t1, t2, c, part); break;
+            case 1: edge_rows_fan<1, R>(X, oy, ixc, iy0, ia, P, wj, t0, t1, t2, c, part); break;
+            default: edge_rows_fan<2, R>(X, oy, ixc, iy0, ia, P, wj, t0, t1, t2, c, part); break;
+        }
+    } else {
+        const float xs = par_xpart(ox, P);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            float sig2;
+            int j;
+            const float sig = par_sigma(xs, oy[r], P);
+            if (edge_tap<G>(sig, ixc, min(iy0 + r, c.ny - 1), ia, P.lo, t0, t1, t2, c, &j, &sig2)) {
+                const float2 pv = wj[j];
+                part[r] += fmaf(sig2, pv.y, pv.x);
+            }
+        }
+    }
+}
+
+// Fast-path taps of one view, dispatched on the fan variant.
+template <Geo G, int R>
+__device__ __forceinline__ void fast_view(float ox, const float (&oy)[R], const FastRec& P,
+                                          const TileConst& c, float (&part)[R])
+{
+    const unsigned base = static_cast<unsigned>(P.mode) & ~3u;
+    if constexpr (G == Geo::kFan) {
+        switch (mode_variant(P.mode)) {
+            case 0: fast_rows<G, 0, R>(ox, oy, P, c, base, part); break;
+            case 1: fast_rows<G, 1, R>(ox, oy, P, c, base, part); break;
+            default: fast_rows<G, 2, R>(ox, oy, P, c, base, part); break;
+        }
+    } else {
+        fast_rows<G, 0, R>(ox, oy, P, c, base, part);
+    }
+}
+
+// A fast view's mode: the shared address of its pair slot plus 8 kc, less
+// 8 kMagicBits, with the variant in the low bits (kModeEdgeRel + variant in
+// the unlikely case that the address falls below kModeFastBase).
+__device__ __forceinline__ int fast_mode(unsigned slot_addr, const TileConst& c, int mode)
+{
+    const unsigned base = slot_addr + 8u * static_cast<unsigned>(c.kc) - 8u * kMagicBits;
+    const int v = mode_variant(mode);
+    return base >= static_cast<unsigned>(kModeFastBase) ? static_cast<int>(base | static_cast<unsigned>(v))
+                                                        : kModeEdgeRel + v;
+}
+
+// Forward FP32 tile kernel with cooperative (plain-load) staging: proj [na][ns]
+// -> img [ny][nx] (batch in grid.z), tile 32 x kTileY.  t0/t1/t2: fan
+// xpos/ypos/sincostbl, parallel xcos/ysin/unused.  Used where the bulk-copy
+// kernel below does not apply (windows wider than its box, unaligned
+// buffers); same positions and pairs, so the same sums up to the order of
+// the view blocks.
+template <Geo G>
+__global__ void __launch_bounds__(kBpThreads, 2)
+    bp_tile_f32_coop(const float* __restrict__ proj, float* __restrict__ img,
+                     const double* __restrict__ t0, const double* __restrict__ t1,
+                     const double* __restrict__ t2, const TileConst c)
+{
+    constexpr int R = kRowsPerThread;
+    extern __shared__ __align__(16) float2 win[];  // [kViewBlock][W]
+    __shared__ ViewRec s_v[kViewBlock];
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const TileBox B = tile_box<G>(t0, t1, blockIdx.x, blockIdx.y, kTileY, c);
+    const float* P_ = proj + blockIdx.z * c.proj_stride;
+    const int ixc = min(B.tx0 + lane, c.nx - 1);
+    const int iy0 = B.ty0 + warp * R;
+    const float ox = off_x<G>(t0, ixc, B.ixm, c);
+    float oy[R], acc[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        oy[r] = off_y<G>(t1, min(iy0 + r, c.ny - 1), B.iym, c);
+        acc[r] = 0.0f;
+    }
+    const unsigned win_base = smem_u32(win);
+    for (int v0 = 0; v0 < c.na; v0 += kViewBlock) {
+        const int nv = min(kViewBlock, c.na - v0);
+        if (threadIdx.x < nv) {
+            ViewRec P = view_setup<G>(t0, t1, t2, v0 + threadIdx.x, B, c);
+            if (mode_fast(P.mode)) P.mode = fast_mode(win_base + 8u * threadIdx.x * c.W, c, P.mode);
+            s_v[threadIdx.x] = P;
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < nv * c.W; idx += kBpThreads) {
+            const int j = idx / c.W, k = idx - j * c.W;
+            const int g = s_v[j].lo + k;
+            const float* row = P_ + static_cast<size_t>(v0 + j) * c.ns;
+            const float p0 = (g >= 0 && g < c.ns) ? __ldg(row + g) : 0.0f;
+            const float p1 = (g + 1 >= 0 && g + 1 < c.ns) ? __ldg(row + g + 1) : 0.0f;
+            win[idx] = make_pair(p0, p1, k, c.kc, s_v[j].e);
+        }
+        __syncthreads();
+        float part[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) part[r] = 0.0f;
+        for (int j = 0; j < nv; ++j) {
+            const FastRec F = load_fast(s_v + j);
+            if (mode_fast(F.mode)) fast_view<G, R>(ox, oy, F, c, part);
+            else if (F.mode != kModeSkip)
+                edge_rows<G, R>(ox, oy, ixc, iy0, v0 + j, s_v[j], win + j * c.W, t0, t1, t2, c, part);
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) acc[r] += part[r];
+        __syncthreads();
+    }
+    float* I = img + blockIdx.z * c.img_stride;
+    const int ix = B.tx0 + lane;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int iy = iy0 + r;
+        if (ix < c.nx && iy < c.ny) I[static_cast<size_t>(iy) * c.nx + ix] = acc[r] * c.scale;
+    }
+}
+
+// ---- bulk-copy-fed forward kernel ---------------------------------------------
+//
+// A CTA runs NG view groups of 256 threads on one 32 x (8 R) tile (each
+// group takes its share of every block of NG*VB views; with two groups the
+// partial sums are added in a fixed order at the end), and the detector
+// windows reach shared memory through the TMA engine: one cp.async.bulk copy
+// per view (16-byte aligned start in the flattened sinogram, a 128-byte
+// aligned shared slot), issued two view blocks ahead into double-buffered raw
+// slots, each block completed on its own mbarrier (waits are bounded and
+// report kFlagWaitTimeout).  Once a slot has landed, the CTA rewrites it as
+// pairs (make_pair), zero off the detector.
+constexpr int kGroups = 2;
+constexpr int kBlockViews = kGroups * kViewBlock;
+constexpr int kTmaThreads = kGroups * kBpThreads;
+
 // One tile (tile_x, tile_y) of item `item`, over its view blocks
-// [b_begin, b_end) (b_end < 0: all); all 512 threads of the CTA call it.
+// [b_begin, b_end) (b_end < 0: all); all NG*256 threads of the CTA call it.
 // With `partial` null the scaled sums are stored to the image; otherwise the
 // unscaled sums of this range go to partial[row * kTileX + column] of the tile.
 // Re-entrant across calls of a persistent CTA: the mbarriers are
@@ -504,12 +723,12 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
     constexpr int kThreads = NG * kBpThreads;   // NG view groups of 256 threads
     // Dynamic shared memory, 128-byte aligned here: raw slots [2][kBV][WS]
     // (every slot stride a 128-byte multiple), pairs [2][kBV][W], then one
-    // view record (ViewT<G>) per view of the whole scan.
+    // view record per view of the whole scan.
     extern __shared__ __align__(128) unsigned char smem_dyn[];
     unsigned char* smem = smem_dyn + ((128u - (smem_u32(smem_dyn) & 127u)) & 127u);
     float* raw = reinterpret_cast<float*>(smem);
     float2* pairs = reinterpret_cast<float2*>(smem + 2 * kBV * c.WS * sizeof(float));
-    ViewT<G>* views = reinterpret_cast<ViewT<G>*>(pairs + 2 * kBV * c.W);
+    ViewRec* views = reinterpret_cast<ViewRec*>(pairs + 2 * kBV * c.W);
     __shared__ __align__(8) unsigned long long s_bar[2];
     __shared__ int s_ok;
 
@@ -517,20 +736,9 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
     const int group = tid / kBpThreads;
     const int lt = tid - group * kBpThreads;
     const int lane = lt & 31, warp = lt >> 5;
-    const int tx0 = tile_x * kTileX, ty0 = tile_y * kTY;
+    const TileBox B = tile_box<G>(t0, t1, tile_x, tile_y, kTY, c);
     const int nblocks = b_end < 0 ? (c.na + kBV - 1) / kBV : b_end;
     // double-buffer slots and barrier phases count from b_begin
-
-    auto px = [&](int ix) -> float {
-        if constexpr (G == Geo::kFan) return static_cast<float>(t0[ix]);
-        else return static_cast<float>((ix - c.centx) * c.dx);
-    };
-    auto py = [&](int iy) -> float {
-        if constexpr (G == Geo::kFan) return static_cast<float>(t1[iy]);
-        else return static_cast<float>((c.centy - iy) * c.dy);
-    };
-    const float cx0 = px(tx0), cx1 = px(min(tx0 + kTileX - 1, c.nx - 1));
-    const float cy0 = py(ty0), cy1 = py(min(ty0 + kTY - 1, c.ny - 1));
 
     // Slot j of block b receives sinogram elements [gx, gx + WB) of the flattened
     // array (gx = window start rounded down to 4 elements, so the source is
@@ -570,19 +778,14 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
     };
 
     // per-view parameters, windows and paths of this tile for the whole scan;
-    // a fast view keeps, in place of its mode, the shared address of its pair
-    // slot minus 8 * kMagicBits (a multiple of 8), so a tap's address is that
-    // plus 8 * bits(s' + 2^23 - 1/2), s' = s - lo; the low two bits keep the
-    // atan variant (values below kModeFastBase fall back to the edge path)
+    // a fast view keeps its pair slot's address base in place of its mode
     const unsigned pairs_base = smem_u32(pairs);
     const int ia_end = min(nblocks * kBV, c.na);
     for (int ia = b_begin * kBV + tid; ia < ia_end; ia += kThreads) {
-        ViewT<G> P = view_setup<G>(t0, t1, t2, ia, tx0, ty0, cx0, cx1, cy0, cy1, c);
+        ViewRec P = view_setup<G>(t0, t1, t2, ia, B, c);
         if (mode_fast(P.mode)) {
             const int slot = ((ia / kBV - b_begin) & 1) * kBV + ia % kBV;
-            const unsigned base = pairs_base + 8u * static_cast<unsigned>(slot * c.W) - 8u * kMagicBits;
-            P.mode = base >= static_cast<unsigned>(kModeFastBase) ? static_cast<int>(base | (P.mode & 3))
-                                                                 : kModeEdge;
+            P.mode = fast_mode(pairs_base + 8u * static_cast<unsigned>(slot * c.W), c, P.mode);
         }
         views[ia] = P;
     }
@@ -606,18 +809,17 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
         issue_block(b_begin + 1);
     }
 
-    const int ixc = min(tx0 + lane, c.nx - 1);
-    const float x = px(ixc);
-    const float xf = fast_coord<G>(x, cx0);
-    float y[R], yf[R], acc[R];
+    const int ixc = min(B.tx0 + lane, c.nx - 1);
+    const int iy0 = B.ty0 + warp * R;
+    const float ox = off_x<G>(t0, ixc, B.ixm, c);
+    float oy[R], acc[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-        y[r] = py(min(ty0 + warp * R + r, c.ny - 1));
-        yf[r] = fast_coord<G>(y[r], cy0);
+        oy[r] = off_y<G>(t1, min(iy0 + r, c.ny - 1), B.iym, c);
         acc[r] = 0.0f;
     }
 
-    const int wid = tid >> 5;  // warp of the CTA (0..15)
+    const int wid = tid >> 5;  // warp of the CTA
     for (int b = b_begin; b < nblocks; ++b) {
         const int lb = b - b_begin;
         // every thread waits for block b's copies (bounded); a timeout is
@@ -627,28 +829,23 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
         const int nv = min(kBV, c.na - b * kBV);
         const float* slot = raw + (lb & 1) * kBV * c.WS;
         float2* pb = pairs + (lb & 1) * kBV * c.W;
-        // one warp per view: rewrite the raw window as (p[k] - k d[k], d[k]) pairs,
-        // d[k] = p[k+1] - p[k], k the channel less lo (a tap at s' = s - lo in
-        // [k, k+1] is then one FMA: p[k] + (s' - k) d[k] = q[k] + s' d[k])
+        // one warp per view: rewrite the raw window as pairs
         for (int j = wid; j < nv; j += kThreads / 32) {
             const long long st = slot_start(b * kBV + j);
             const int lo = views[b * kBV + j].lo;
+            const float e = views[b * kBV + j].e;
             const float* src = slot + j * c.WS + static_cast<int>(st & 3ll);
             float2* dst = pb + j * c.W;
             if (lo >= 0 && lo + c.W < c.ns && st + c.W < c.total4) {
-                for (int k = lane; k < c.W; k += 32) {
-                    const float p0 = src[k], d = src[k + 1] - p0;
-                    dst[k] = make_float2(fmaf(-static_cast<float>(k), d, p0), d);
-                }
+                for (int k = lane; k < c.W; k += 32) dst[k] = make_pair(src[k], src[k + 1], k, c.kc, e);
             } else {  // a detector end or the array's ragged tail is in the window
                 for (int k = lane; k < c.W; k += 32) {
                     auto at = [&](int gg, long long ii, const float* sp) -> float {
                         if (gg < 0 || gg >= c.ns) return 0.0f;  // off the detector
                         return ii < c.total4 ? *sp : __ldg(proj + ii);
                     };
-                    const float p0 = at(lo + k, st + k, src + k);
-                    const float d = at(lo + k + 1, st + k + 1, src + k + 1) - p0;
-                    dst[k] = make_float2(fmaf(-static_cast<float>(k), d, p0), d);
+                    dst[k] = make_pair(at(lo + k, st + k, src + k), at(lo + k + 1, st + k + 1, src + k + 1), k,
+                                       c.kc, e);
                 }
             }
         }
@@ -662,39 +859,10 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
         for (int r = 0; r < R; ++r) part[r] = 0.0f;
         for (int j = jb; j < je; ++j) {
             const int ia = b * kBV + j;
-            const ViewT<G> P = views[ia];
-            if (mode_fast(P.mode)) {
-                // floor of s' = bits(fl(s' + 2^23 - 1/2)) - kMagicBits
-                const unsigned base = static_cast<unsigned>(P.mode) & ~3u;
-                const float cen = view_cen<G>(P, c);
-                float xs, xc;
-                fast_xs<G>(xf, P.vp, cen, c, &xs, &xc);
-                if constexpr (G == Geo::kFan) {
-                    switch (P.mode & 3) {
-                        case 0: fast_rows<G, 0, R>(xs, xc, yf, P.vp, cen, c, base, part); break;
-                        case 1: fast_rows<G, 1, R>(xs, xc, yf, P.vp, cen, c, base, part); break;
-                        case 2: fast_rows<G, 2, R>(xs, xc, yf, P.vp, cen, c, base, part); break;
-                        default: fast_rows<G, 3, R>(xs, xc, yf, P.vp, cen, c, base, part); break;
-                    }
-                } else {
-                    fast_rows<G, 0, R>(xs, xc, yf, P.vp, cen, c, base, part);
-                }
-            } else if (P.mode == kModeEdge) {
-                const float2* wj = pb + j * c.W;
-#pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    float w, u;
-                    int k;
-                    const float s = channel_of<G>(x, y[r], P.vp, c, &w);
-                    const int iyc = min(ty0 + warp * R + r, c.ny - 1);
-                    if (edge_tap<G>(s, ixc, iyc, ia, P.lo, t0, t1, t2, c, &k, &u)) {
-                        const float2 pv = wj[k];
-                        const float v = fmaf(u, pv.y, fmaf(static_cast<float>(k), pv.y, pv.x));
-                        if constexpr (G == Geo::kFan) part[r] = fmaf(v, w, part[r]);
-                        else part[r] += v;
-                    }
-                }
-            }
+            const FastRec F = load_fast(views + ia);
+            if (mode_fast(F.mode)) fast_view<G, R>(ox, oy, F, c, part);
+            else if (F.mode != kModeSkip)
+                edge_rows<G, R>(ox, oy, ixc, iy0, ia, views[ia], pb + j * c.W, t0, t1, t2, c, part);
         }
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[r] += part[r];
@@ -719,10 +887,10 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
             for (int r = 0; r < R; ++r) partial[(warp * R + r) * kTileX + lane] = acc[r];
         } else {
             float* I = img + static_cast<size_t>(item) * c.img_stride;
-            const int ix = tx0 + lane;
+            const int ix = B.tx0 + lane;
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                const int iy = ty0 + warp * R + r;
+                const int iy = iy0 + r;
                 if (ix < c.nx && iy < c.ny) I[static_cast<size_t>(iy) * c.nx + ix] = acc[r] * c.scale;
             }
         }
@@ -743,7 +911,7 @@ __global__ void __launch_bounds__(NG * kBpThreads, MinBlocks)
 //
 // A launch with few tiles (a 512^2 image is 128 tiles of 32 x 64) leaves SMs
 // idle when each CTA owns whole tiles.  Here the work is cut into units of
-// (tile, block of 2*VB views), tiles outer, and CTA c of G takes the
+// (tile, block of NG*VB views), tiles outer, and CTA c of G takes the
 // contiguous units [c*U/G, (c+1)*U/G): every SM gets the same number of view
 // blocks.  A tile whose units span several CTAs gets one unscaled partial sum
 // per CTA (segment) in `partial`; each CTA counts its segment in on the
@@ -826,6 +994,14 @@ int par_window(int ns, double ds, double dx, double dy, int tile_y = kTileY)
     const double span = std::sqrt(std::pow(kTileX * dx, 2) + std::pow(tile_y * dy, 2)) / ds;
     const int w = static_cast<int>(std::ceil(span)) + 8;
     return std::min(w, ns + 2);
+}
+
+// The window every single-geometry kernel uses for a geometry (forward,
+// either staging, and the adjoint): the same window centre gives the same
+// positions, so the adjoint transposes the forward exactly.
+inline int tile_window(int w)
+{
+    return std::max(w, 32);
 }
 
 }  // namespace

@@ -11,8 +11,18 @@
 // one output column for all staged rows, so a tap load is shared by kRows
 // multiply-adds.  The reference kernels have zero even taps (k != 0); when
 // the caller's table has that structure (checked in-kernel) only the odd
-// taps are visited.  Left and right halves accumulate
-// separately, which keeps FP32 partial sums small.
+// taps are visited.
+//
+// FP32 accuracy: the ramp taps sum to almost zero, so on a smooth sinogram
+// the output is a small difference of large partial sums.  The FP32 kernel
+// therefore accumulates h[o-j] (x[j] - c) with c a value of the row near the
+// thread's outputs, and adds back c (h[0] + sum of the taps that output o
+// sums), formed in FP64 from the FP64 taps (prefix sums by one extra warp
+// while the others start their sums):
+//   out[o] = h[0] (x[o] - c) + c D[o] + sum_j h[o-j] (x[j] - c),
+//   D[o] = h[0] + sum_{j of the other parity} h[o-j].
+// Partial sums then stay near the size of the result (on a 2304 x 1472 fan
+// sinogram: 1.3e-5 -> ~1e-6 from FP64).
 #include "ctr_common.cuh"
 
 namespace ctr {
@@ -88,6 +98,8 @@ int launch_fan_weighting(const ctr_fan_weighting_param* p, const T* in, T* out, 
 // cover 8 consecutive outputs (both parities).  Even taps other than 0, which
 // the ramp filters of the reference never have, take the generic loop.
 constexpr int kFilterMaxThreads = 1024;
+// Threads of the output tasks (the FP32 kernels add one warp, see filter_block).
+constexpr int kFilterTaskThreads = kFilterMaxThreads - 32;
 constexpr int kFilterPad = 16;   // zero taps beyond the ends of H
 constexpr int kFilterRowsPlain = 2;
 
@@ -95,12 +107,12 @@ constexpr int kFilterRowsPlain = 2;
 // CTA, each task's inputs are split in two halves run by two threads, whose
 // partial sums are added in a fixed order (halves the serial loop per thread).
 __host__ __device__ inline int filter_tasks(unsigned ns) { return static_cast<int>((ns + 7) / 8) * 2; }
-__host__ __device__ inline bool filter_split(unsigned ns) { return 2 * filter_tasks(ns) <= kFilterMaxThreads; }
+__host__ __device__ inline bool filter_split(unsigned ns) { return 2 * filter_tasks(ns) <= kFilterTaskThreads; }
 
 __host__ __device__ inline int filter_threads(unsigned ns)
 {
     const int t = filter_tasks(ns) * (filter_split(ns) ? 2 : 1);
-    return t < 32 ? 32 : (t > kFilterMaxThreads ? kFilterMaxThreads : (t + 31) / 32 * 32);
+    return t < 32 ? 32 : (t > kFilterTaskThreads ? kFilterTaskThreads : (t + 31) / 32 * 32);
 }
 
 // Tap storage: tap idx (offset d + ns - 1 + kFilterPad) lives at word
@@ -115,13 +127,22 @@ __host__ __device__ inline int tap_words(unsigned ns, int tg)
     return tap_slot(2 * static_cast<int>(ns) + 2 * kFilterPad, tg);
 }
 
-// Shared layout: the taps H[-(ns-1) - kFilterPad .. ns - 1 + kFilterPad] (taps *
-// ds), then xs[kRows][ns], then the second halves' sums [kRows][tasks][4].
+// Shared layout (FP32): the FP64 prefix sums of the odd taps [2 ns] (see
+// filter_rows), then the taps H[-(ns-1) - kFilterPad .. ns - 1 + kFilterPad]
+// (taps * ds), then xs[kRows][ns], then the second halves' sums
+// [kRows][tasks][4].  FP64 has no prefix sums.
 template <typename T>
 __host__ __device__ inline size_t filter_smem(unsigned ns, int rows, int tg)
 {
-    return sizeof(T) * (static_cast<size_t>(tap_words(ns, tg)) + static_cast<size_t>(rows) * ns +
+    return (sizeof(T) == 4 ? 2 * sizeof(double) * ns : 0) +
+           sizeof(T) * (static_cast<size_t>(tap_words(ns, tg)) + static_cast<size_t>(rows) * ns +
                         static_cast<size_t>(rows) * filter_tasks(ns) * 4);
+}
+// The FP32 kernels run one more warp, which forms the prefix sums.
+template <typename T>
+__host__ __device__ inline int filter_block(unsigned ns)
+{
+    return filter_threads(ns) + (sizeof(T) == 4 ? 32 : 0);
 }
 
 // The tap layout for a launch: skewed when it fits kFilterSmemMax.
@@ -142,14 +163,14 @@ __device__ __forceinline__ double fma_t(double a, double b, double c) { return f
 template <typename T, int kRows>
 __device__ __forceinline__ void filter_span(const T* __restrict__ xs, int n, int j0, int j1, int i0, int tg,
                                             const T* __restrict__ H0, T w0, T w1, T w2, T w3,
-                                            T (&acc)[kRows][4])
+                                            const T (&cr)[kRows], T (&acc)[kRows][4])
 {
     const int d0 = (n - 1) + kFilterPad;  // tap d sits at H0[tap_slot(d + d0, tg)]
 #pragma unroll 4
     for (int j = j0; j < j1; j += 2) {
 #pragma unroll
         for (int r = 0; r < kRows; ++r) {
-            const T xv = xs[r * n + j];
+            const T xv = xs[r * n + j] - cr[r];
             acc[r][0] += w0 * xv;
             acc[r][1] += w1 * xv;
             acc[r][2] += w2 * xv;
@@ -168,58 +189,115 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
                                             unsigned ns, unsigned long long r0, int nr, double ds,
                                             int tg, unsigned char* smem_raw)
 {
+    constexpr bool kCentred = sizeof(T) == 4;
     const int n = static_cast<int>(ns);
-    T* H0 = reinterpret_cast<T*>(smem_raw);
+    double* Ash = reinterpret_cast<double*>(smem_raw);  // FP32: prefix sums [2n]
+    T* H0 = reinterpret_cast<T*>(smem_raw + (kCentred ? 2 * sizeof(double) * n : 0));
     const int d0 = (n - 1) + kFilterPad;  // tap d sits at H0[tap_slot(d + d0, tg)]
     auto H = [&](int d) -> T { return H0[tap_slot(d + d0, tg)]; };
     T* xs = H0 + tap_words(ns, tg);
     __shared__ int s_even;
+    // the task threads; an FP32 block has one more warp (the prefix sums)
+    const int nthr = kCentred ? static_cast<int>(blockDim.x) - 32 : static_cast<int>(blockDim.x);
 
     const double* h = filter + ns;  // h[k], k in [-ns, ns]
     if (threadIdx.x == 0) s_even = 0;
     __syncthreads();
-    bool even = false;
-    // staging loops unrolled so that a thread's global loads are in flight together
+    {
+        bool even = false;
+        // staging loops unrolled so that a thread's global loads are in flight together
 #pragma unroll 4
-    for (int idx = threadIdx.x; idx < 2 * n + 2 * kFilterPad; idx += blockDim.x) {
-        const int d = idx - (n - 1) - kFilterPad;
-        double v = 0.0;
-        if (d > -n && d < n) v = kGrad ? h[-d] : h[d];
-        H0[tap_slot(idx, tg)] = static_cast<T>(v * ds);
-        if (d != 0 && (d & 1) == 0 && v != 0.0) even = true;
-    }
-    if (even) s_even = 1;
-#pragma unroll 4
-    for (int idx = threadIdx.x; idx < kRows * n; idx += blockDim.x) {
-        const int r = idx / n, j = idx - r * n;
-        T v = 0;
-        if (r < nr) {
-            v = in[(r0 + r) * ns + j];
-            if (weight) v = static_cast<T>(v * static_cast<T>(weight[j]));
+        for (int idx = threadIdx.x; idx < 2 * n + 2 * kFilterPad; idx += blockDim.x) {
+            const int d = idx - (n - 1) - kFilterPad;
+            double v = 0.0;
+            if (d > -n && d < n) v = kGrad ? h[-d] : h[d];
+            H0[tap_slot(idx, tg)] = static_cast<T>(v * ds);
+            if (d != 0 && (d & 1) == 0 && v != 0.0) even = true;
         }
-        xs[idx] = v;
+        if (even) s_even = 1;
+        if constexpr (kCentred) {
+            // Ash[m + 1] = the FP64 tap at offset k = m - (n-1) (odd k only),
+            // summed into prefix sums below
+#pragma unroll 4
+            for (int m = threadIdx.x; m < 2 * n - 1; m += blockDim.x) {
+                const int k = m - (n - 1);
+                Ash[m + 1] = (k & 1) ? (kGrad ? h[-k] : h[k]) * ds : 0.0;
+            }
+            if (threadIdx.x == 0) Ash[0] = 0.0;
+        }
+#pragma unroll 4
+        for (int idx = threadIdx.x; idx < kRows * n; idx += blockDim.x) {
+            const int r = idx / n, j = idx - r * n;
+            T v = 0;
+            if (r < nr) {
+                v = in[(r0 + r) * ns + j];
+                if (weight) v = static_cast<T>(v * static_cast<T>(weight[j]));
+            }
+            xs[idx] = v;
+        }
     }
     __syncthreads();
+    if (kCentred && static_cast<int>(threadIdx.x) >= nthr) {
+        // the extra warp: Ash[m] becomes the sum of the odd taps at offsets up
+        // to m - n (in FP64, from shared memory), while the task threads start
+        // their sums; then the taps output o sums (offsets o - n + 1 .. o) add
+        // up to Ash[o + n] - Ash[o]
+        const int lane = threadIdx.x & 31;
+        const int L = 2 * n - 1, C = (L + 31) / 32;
+        const int m0 = min(lane * C, L), m1 = min(m0 + C, L);
+        double sum = 0.0;
+        for (int m = m0; m < m1; ++m) sum += Ash[m + 1];
+        double p = sum;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const double v = __shfl_up_sync(0xffffffffu, p, off);
+            if (lane >= off) p += v;
+        }
+        p -= sum;  // exclusive: the sum of the earlier lanes' chunks
+        for (int m = m0; m < m1; ++m) {
+            p += Ash[m + 1];
+            Ash[m + 1] = p;
+        }
+    }
+    // the single-thread-per-task path writes outputs as it goes: it needs the
+    // sums first
+    if (kCentred && !filter_split(ns)) __syncthreads();
+    // output o of a thread whose reference value is c (FP32: centred sums)
+    const double h0d = kCentred ? h[0] * ds : 0.0;
+    auto finish = [&](int o, int r, T c, T acc) -> T {
+        if constexpr (kCentred) {
+            const T D = static_cast<T>(h0d + (Ash[o + n] - Ash[o]));
+            return fma_t(H(0), xs[r * n + o] - c, fma_t(c, D, acc));
+        } else {
+            return fma_t(H(0), xs[r * n + o], acc);
+        }
+    };
+    // reference value of a task's rows: the input next to its outputs
+    auto refs = [&](int i0, T (&cr)[kRows]) {
+#pragma unroll
+        for (int r = 0; r < kRows; ++r) cr[r] = kCentred ? xs[r * n + min(i0 + 3, n - 1)] : T(0);
+    };
     const int groups = filter_tasks(ns);  // thread tasks: (8-output block, parity)
     T* red = xs + kRows * n;              // [kRows][groups][4]
     if (!s_even && filter_split(ns)) {
-        // two threads per task (blockDim.x >= 2 * groups): inputs [jb, jm) and [jm, n)
+        // two threads per task (nthr >= 2 * groups): inputs [jb, jm) and [jm, n)
         const int task = threadIdx.x;
         const bool active = task < 2 * groups;
         const int half = task >= groups ? 1 : 0;
         const int g = task - half * groups;
         const int i0 = (g >> 1) * 8 + (g & 1);
-        T acc[kRows][4];
+        T acc[kRows][4], cr[kRows];
 #pragma unroll
         for (int r = 0; r < kRows; ++r)
 #pragma unroll
             for (int m = 0; m < 4; ++m) acc[r][m] = 0;
         if (active) {
+            refs(i0, cr);
             const int jb = (i0 + 1) & 1;  // inputs of the other parity
             const int jm = jb + 2 * ((n - jb + 1) / 4);
             const int j0 = half ? jm : jb, j1 = half ? n : jm;
             T w0 = H(i0 - j0), w1 = H(i0 + 2 - j0), w2 = H(i0 + 4 - j0), w3 = H(i0 + 6 - j0);
-            filter_span<T, kRows>(xs, n, j0, j1, i0, tg, H0, w0, w1, w2, w3, acc);
+            filter_span<T, kRows>(xs, n, j0, j1, i0, tg, H0, w0, w1, w2, w3, cr, acc);
             if (half) {
 #pragma unroll
                 for (int r = 0; r < kRows; ++r)
@@ -229,7 +307,6 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
         }
         __syncthreads();
         if (active && !half) {
-            const T t0 = H(0);
 #pragma unroll
             for (int m = 0; m < 4; ++m) {
                 const int o = i0 + 2 * m;
@@ -237,28 +314,28 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
 #pragma unroll
                 for (int r = 0; r < kRows; ++r)
                     if (r < nr)
-                        out[(r0 + r) * ns + o] = fma_t(t0, xs[r * n + o], acc[r][m] + red[(r * groups + g) * 4 + m]);
+                        out[(r0 + r) * ns + o] = finish(o, r, cr[r], acc[r][m] + red[(r * groups + g) * 4 + m]);
             }
         }
     } else if (!s_even) {
         for (int task = threadIdx.x; task < groups; task += blockDim.x) {
             const int i0 = (task >> 1) * 8 + (task & 1);
-            T acc[kRows][4];
+            T acc[kRows][4], cr[kRows];
 #pragma unroll
             for (int r = 0; r < kRows; ++r)
 #pragma unroll
                 for (int m = 0; m < 4; ++m) acc[r][m] = 0;
+            refs(i0, cr);
             const int jb = (i0 + 1) & 1;  // inputs of the other parity
             T w0 = H(i0 - jb), w1 = H(i0 + 2 - jb), w2 = H(i0 + 4 - jb), w3 = H(i0 + 6 - jb);
-            filter_span<T, kRows>(xs, n, jb, n, i0, tg, H0, w0, w1, w2, w3, acc);
-            const T t0 = H(0);
+            filter_span<T, kRows>(xs, n, jb, n, i0, tg, H0, w0, w1, w2, w3, cr, acc);
 #pragma unroll
             for (int m = 0; m < 4; ++m) {
                 const int o = i0 + 2 * m;
                 if (o >= n) continue;
 #pragma unroll
                 for (int r = 0; r < kRows; ++r)
-                    if (r < nr) out[(r0 + r) * ns + o] = fma_t(t0, xs[r * n + o], acc[r][m]);
+                    if (r < nr) out[(r0 + r) * ns + o] = finish(o, r, cr[r], acc[r][m]);
             }
         }
     } else {
@@ -324,7 +401,7 @@ int launch_ramp_filter(const ctr_filter_param* p, const T* in, const double* fil
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "filter smem: %s", cudaGetErrorString(e));
     const unsigned blocks = div_up(rows, kFilterRowsPlain);
-    kern<<<blocks, filter_threads(p->ns), smem, stream>>>(in, filter, out, weight, p->ns, rows, p->ds, tg);
+    kern<<<blocks, filter_block<T>(p->ns), smem, stream>>>(in, filter, out, weight, p->ns, rows, p->ds, tg);
     return check_launch("ramp_filter");
 }
 
@@ -348,7 +425,7 @@ int ramp_filter_batch_f32(const FilterJob* jobs, const int2* blocks, int n_block
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "filter smem: %s", cudaGetErrorString(e));
     if (n_blocks > 0)
-        ramp_filter_batch_kernel<<<n_blocks, filter_threads(max_ns), smem, stream>>>(jobs, blocks, tg);
+        ramp_filter_batch_kernel<<<n_blocks, filter_block<float>(max_ns), smem, stream>>>(jobs, blocks, tg);
     return check_launch("ramp_filter_batch");
 }
 

@@ -13,6 +13,9 @@ pytestmark = pytest.mark.gpu
 
 # largest |A - (A^T)^T| entry relative to the largest entry of A
 TOL_ENTRY = 1e-5
+# the FP32 backprojector adjoints sum in fixed point: a quantum of 2^-19 of the
+# tile's largest value (measured 1e-6 parallel, 2.8e-6 fan)
+TOL_ENTRY_BP = 5e-6
 
 
 def _matrices(op, in_shape, out_shape):
@@ -26,11 +29,11 @@ def _matrices(op, in_shape, out_shape):
     return fwd.cpu().numpy().astype(np.float64), adj.cpu().numpy().astype(np.float64).T
 
 
-def _check(fwd, adjT):
+def _check(fwd, adjT, tol=TOL_ENTRY):
     scale = np.abs(fwd).max()
     assert scale > 0
     err = np.abs(fwd - adjT).max() / scale
-    assert err <= TOL_ENTRY, err
+    assert err <= tol, err
 
 
 @pytest.mark.parametrize("name", ["fp_half", "fp_full_wrap"])
@@ -41,10 +44,10 @@ def test_fp_par_2d_transpose(name):
 
 def test_bp_par_2d_transpose():
     g = gc.load("par_rect_cw")["geom"]
-    _check(*_matrices(par_op(g), (g["na"], g["ns"]), (g["ny"], g["nx"])))
+    _check(*_matrices(par_op(g), (g["na"], g["ns"]), (g["ny"], g["nx"])), TOL_ENTRY_BP)
 
 
 @pytest.mark.parametrize("name", ["fan_full", "fan_short_cw"])
 def test_bp_fan_2d_transpose(name):
     g = gc.load(name)["geom"]
-    _check(*_matrices(fan_op(g), (g["na"], g["ns"]), (g["ny"], g["nx"])))
+    _check(*_matrices(fan_op(g), (g["na"], g["ns"]), (g["ny"], g["nx"])), TOL_ENTRY_BP)

@@ -129,22 +129,48 @@ def test_fp_distance_driven(name, sfx, dt):
 
 # ---- adjoint dot tests --------------------------------------------------------
 
-def _dot(op, x_shape, y_shape, dt, seed=0):
-    # |<Ax,y> - <x,A^T y>| / |<Ax,y>| on positive inputs: no cancellation in the
-    # inner products, so the ratio measures the operators' mismatch, not the
-    # FP32 rounding of a near-zero sum.  Exact transposition entry by entry is
-    # checked in test_adjoint_matrix_gpu.py.
+def _smooth_signed(shape, rng, sigma=6.0):
+    """A smooth random field of both signs (white noise low-passed by a
+    Gaussian of `sigma` samples), unit standard deviation."""
+    f = np.fft.rfft2(rng.standard_normal(shape))
+    ky = np.fft.fftfreq(shape[0])[:, None]
+    kx = np.fft.rfftfreq(shape[1])[None, :]
+    f *= np.exp(-2.0 * (np.pi * sigma) ** 2 * (kx ** 2 + ky ** 2))
+    v = np.fft.irfft2(f, s=shape)
+    return v / v.std()
+
+
+def _dot(op, x_shape, y_shape, dt, seed=0, kind="positive"):
+    """|<Ax,y> - <x,A^T y>| / |<Ax,y>|, both inner products in FP64.
+    kind: "positive" (values in [0.5, 1.5): no cancellation in the inner
+    products, so the ratio isolates the operators' mismatch), "smooth" (smooth
+    fields of both signs) or "signed" (white noise of both signs: the FP32
+    rounding of the kernels themselves then shows, about 1e-6 of the terms).
+    Exact transposition entry by entry is checked in test_adjoint_matrix_gpu.py."""
     rng = np.random.default_rng(seed)
-    x = (0.5 + rng.random(x_shape)).astype(dt)
-    y = (0.5 + rng.random(y_shape)).astype(dt)
+    if kind == "positive":
+        x = (0.5 + rng.random(x_shape)).astype(dt)
+        y = (0.5 + rng.random(y_shape)).astype(dt)
+    elif kind == "smooth":
+        x = _smooth_signed(x_shape, rng).astype(dt)
+        y = _smooth_signed(y_shape, rng).astype(dt)
+    else:
+        x = rng.standard_normal(x_shape).astype(dt)
+        y = rng.standard_normal(y_shape).astype(dt)
     ax = host(op.forward(cuda(x)))
     aty = host(op.adjoint(cuda(y)))
+    if kind == "signed":
+        # <Ax, y> of independent signed fields is ~ |Ax| |y| / sqrt(size) and may
+        # come near zero by chance: normalise by |Ax| |y| instead
+        lhs = float(np.vdot(ax.astype(np.float64), y.astype(np.float64)))
+        rhs = float(np.vdot(x.astype(np.float64), aty.astype(np.float64)))
+        return abs(lhs - rhs) / (np.linalg.norm(ax.astype(np.float64)) * np.linalg.norm(y.astype(np.float64)))
     return dot_rel(ax, y, x, aty)
 
 
 @pytest.mark.parametrize("sfx,dt", DT)
 def test_adjoint_dot(sfx, dt):
-    lim = 1e-6 if dt == np.float32 else 1e-10
+    lim = 1e-6 if dt == np.float32 else 1e-12
     c = gc.load("fan_full")["geom"]
     assert _dot(fan_op(c), (c["na"], c["ns"]), (c["ny"], c["nx"]), dt) < lim
     p = gc.load("par_rect_cw")["geom"]
@@ -153,6 +179,32 @@ def test_adjoint_dot(sfx, dt):
     assert _dot(fp_op(f), (f["ny"], f["nx"]), (f["na"], f["ns"]), dt) < lim
     assert _dot(ramp_op(c, c["na"], 1), (c["na"], c["ns"]), (c["na"], c["ns"]), dt) < lim
     assert _dot(weight_op(c, c["na"], 1), (c["na"], c["ns"]), (c["na"], c["ns"]), dt) < lim
+
+
+# Signed inputs at the benchmark sizes.  Smooth signed fields: FP32 kernels to
+# 1e-6 of <Ax, y>.  White noise of both signs, normalised by |Ax| |y|: FP64
+# kernels to 1e-13, FP32 to 1e-7 (the forward backprojector's interpolation
+# pairs hold p - (k - kc - 1/2) d in FP32, which rounds at up to W/2 = 40 times
+# the size of a white-noise difference d: about 1e-6 of <Ax, y>, 2e-8 of
+# |Ax| |y|).  An adjoint that is wrong by a sign or an offset is off by more
+# than 1e-3 in either measure.
+SIGNED_CASES = [
+    ("fan", lambda: __import__("ct_recon_extensions_gb300.synthetic", fromlist=["x"]).fan_config_1(), fan_op, False),
+    ("par", lambda: __import__("ct_recon_extensions_gb300.synthetic", fromlist=["x"]).parallel_config_2(), par_op, False),
+    ("fp", lambda: __import__("ct_recon_extensions_gb300.synthetic", fromlist=["x"]).parallel_config_2(), fp_op, True),
+]
+
+
+@pytest.mark.parametrize("name,geom,mk,image_in", SIGNED_CASES, ids=[c[0] for c in SIGNED_CASES])
+def test_adjoint_dot_signed(name, geom, mk, image_in):
+    d = geom()
+    sino = (d["na"], d["ns"])
+    img = (d["ny"], d["nx"])
+    xs, ys = (img, sino) if image_in else (sino, img)
+    op = mk(d)
+    assert _dot(op, xs, ys, np.float64, seed=1, kind="signed") < 1e-13
+    assert _dot(op, xs, ys, np.float32, seed=2, kind="smooth") < 1e-6
+    assert _dot(op, xs, ys, np.float32, seed=3, kind="signed") < 1e-7
 
 
 # ---- batching ----------------------------------------------------------------
@@ -215,6 +267,43 @@ def test_parallel_config2(oracle_port):
     assert rel_l2(rec, rec64) <= 1e-4
 
 
+def test_fan_config1_white_noise(oracle_port):
+    """Fan weighting + ramp(fan) + bp_fan_2d at config 1 (720 views x 736
+    channels -> 512^2) on a white-noise sinogram (detector differences as large
+    as the values: the worst case for FP32 channel positions) against the
+    reference's CPU algorithm, T=float and FP64."""
+    from oracle import Geom
+    from ct_recon_extensions_gb300 import synthetic as syn
+    d = syn.fan_config_1()
+    g = Geom.make(**d)
+    sino = np.random.default_rng(17).standard_normal((d["na"], d["ns"])).astype(np.float32)
+    w = weight_op(d, d["na"], 1).forward(cuda(sino))
+    rec = host(fan_op(d).forward(ramp_op(d, d["na"], 1).forward(w)))
+    assert rel_l2(rec, oracle_port.fbp_fan(sino, g)) <= 1e-5  # measured ~2.5e-6
+    assert rel_l2(rec, oracle_port.fbp_fan(sino.astype(np.float64), g)) <= 1e-5
+
+
+def test_ramp_filter_f32_config5(oracle_port):
+    """The FP32 ramp filter (fan) of a config-5 sinogram (2304 views x 1472
+    channels, analytic ellipses) against the oracle in FP64; its taps nearly
+    cancel on smooth data, the case that FP32 partial sums lose."""
+    from oracle import Geom
+    from ct_recon_extensions_gb300 import synthetic as syn
+    d = syn.large_config_5()
+    g = Geom.make(**d)
+    e = syn.random_ellipses(5000)
+    sino = syn.fan_sinogram(e, d["na"], d["ns"], d["ds"], d["orbit"], d["dso"], d["dsd"])
+    w = weight_op(d, d["na"], 1).forward(cuda(sino))
+    out = host(ramp_op(d, d["na"], 1).forward(w))
+    # the reference's T=float filter sums in double (src/filter.cc:77-89): FP64
+    # on the same FP32 weighted sinogram
+    ref = oracle_port.ramp_filter(host(w).astype(np.float64), g.ds, g.dsd, 1)
+    assert rel_l2(out, ref) <= 1e-5  # measured ~1e-6 (1.3e-5 with uncentred FP32 sums)
+    grad = host(ramp_op(d, d["na"], 1).adjoint(w))
+    gref = oracle_port.ramp_filter(host(w).astype(np.float64), g.ds, g.dsd, 1, grad=True)
+    assert rel_l2(grad, gref) <= 1e-5
+
+
 def test_parallel_config2_white_noise(oracle_port):
     """Ramp + bp_par_2d at 512^2 x 720 views x 729 bins on a white-noise sinogram
     (detector differences as large as the values: the worst case for the FP32
@@ -226,7 +315,7 @@ def test_parallel_config2_white_noise(oracle_port):
     sino = np.random.default_rng(7).standard_normal((d["na"], d["ns"])).astype(np.float32)
     rec = host(par_op(d).forward(ramp_op(d, d["na"], 0, dsd=-1.0).forward(cuda(sino))))
     ref = oracle_port.bp_par_2d(oracle_port.ramp_filter(sino, g.ds, -1.0, 0), g)
-    assert rel_l2(rec, ref) <= 1e-5  # measured 7.6e-6
+    assert rel_l2(rec, ref) <= 1e-5  # measured ~1.5e-6
 
 
 def test_fp_ray_casting_config2(oracle_port):
