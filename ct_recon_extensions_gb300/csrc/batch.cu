@@ -183,6 +183,8 @@ TileConst item_const(const ctr_fan_bp_param& g, int tile_y, int R, int VB)
     c.dsd_d = g.dsd;
     c.dx = g.dx;
     c.dy = g.dy;
+    c.dxf = static_cast<float>(g.dx);
+    c.dyf = static_cast<float>(g.dy);
     fill_fan_tables(c, g.dsd, g.ds);
     c.proj_stride = static_cast<size_t>(g.ns) * g.na;
     c.img_stride = static_cast<size_t>(g.nx) * g.ny;

@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(kBpThreads, 2)
                 if (F.mode == kModeSkip) continue;
                 const int ia = v0 + j;
                 const unsigned slot = win_base + 4u * static_cast<unsigned>(j * c.W);
-                const bool xmaj = fabsf(F.p0) * static_cast<float>(c.dx) >= fabsf(F.p1) * static_cast<float>(c.dy);
+                const bool xmaj = fabsf(F.p0) * c.dxf >= fabsf(F.p1) * c.dyf;
                 if (mode_fast(F.mode) && !any_bad) {
                     const FastRec& P = F;
                     const unsigned base = static_cast<unsigned>(P.mode) & ~3u;
@@ -666,6 +666,8 @@ TileConst fan_const(const FanArgs& a, double extra_scale)
     c.scale = static_cast<float>(a.dsd * a.dsd * extra_scale);
     c.dx = a.dx;
     c.dy = a.dy;
+    c.dxf = static_cast<float>(a.dx);
+    c.dyf = static_cast<float>(a.dy);
     c.ds_d = a.ds;
     c.cents_d = (a.ns - 1) / 2.0 + a.offset_s;
     c.dso_d = a.dso;
@@ -780,6 +782,8 @@ TileConst par_const(const ctr_par_param* p)
     c.centy = (p->ny - 1) / 2.0 + p->offset_y;
     c.dx = p->dx;
     c.dy = p->dy;
+    c.dxf = static_cast<float>(p->dx);
+    c.dyf = static_cast<float>(p->dy);
     c.ds_d = p->ds;
     c.cents_d = (p->ns - 1) / 2.0 + p->offset_s;
     c.fx_bits = adj_fx_bits(p->ds, p->dx, p->dy);

@@ -72,7 +72,8 @@ struct TileConst {
     double orbit_start, orbit;  // parallel: view angle = orbit_start + ia*orbit
     double inv_ds;         // parallel: 1/ds
     double inv_dx, inv_dy; // parallel: 1/dx, 1/dy
-    double centx, centy, dx, dy;  // parallel pixel grid
+    double centx, centy, dx, dy;  // pixel grid (centres: parallel)
+    float dxf, dyf;        // pixel pitch in FP32
     double ds_d, cents_d, dso_d, dsd_d, K_d;  // FP64 geometry
     float apoly[kRelVariants][5];  // fan: (dsd/ds) atan(t)/t in powers of t^2
     double atab[kAtanTab];
@@ -183,17 +184,19 @@ __device__ __forceinline__ double pix_y(const double* __restrict__ t1, int iy, c
     else return (c.centy - iy) * c.dy;
 }
 // Offsets of a pixel from the tile's reference pixel, rounded once to FP32.
+// (Fan: from the caller's FP64 position tables; parallel: the pixel pitch
+// times a small integer, in FP32.)
 template <Geo G>
 __device__ __forceinline__ float off_x(const double* __restrict__ t0, int ix, int ixm, const TileConst& c)
 {
     if constexpr (G == Geo::kFan) return static_cast<float>(t0[ix] - t0[ixm]);
-    else return static_cast<float>((ix - ixm) * c.dx);
+    else return static_cast<float>(ix - ixm) * c.dxf;
 }
 template <Geo G>
 __device__ __forceinline__ float off_y(const double* __restrict__ t1, int iy, int iym, const TileConst& c)
 {
     if constexpr (G == Geo::kFan) return static_cast<float>(t1[iy] - t1[iym]);
-    else return static_cast<float>((iym - iy) * c.dy);
+    else return static_cast<float>(iym - iy) * c.dyf;
 }
 
 template <Geo G>
@@ -609,6 +612,68 @@ __device__ __forceinline__ void fast_view(float ox, const float (&oy)[R], const 
     }
 }
 
+// The fan variant shared by every view of n records at vr when all of them
+// take the fast path, else -1 (warp-uniform; n <= 64).
+__device__ __forceinline__ int block_variant(const ViewRec* vr, int n)
+{
+    const int lane = threadIdx.x & 31;
+    const int v0 = mode_variant(vr[0].mode);
+    bool ok = true;
+    for (int j = lane; j < n; j += 32) {
+        const int m = vr[j].mode;
+        ok = ok && mode_fast(m) && mode_variant(m) == v0;
+    }
+    return __all_sync(0xffffffffu, ok) ? v0 : -1;
+}
+
+// n views (records at vr) that all take the fast path with variant V: no
+// per-view dispatch, two views per trip (same summation order as one by one).
+template <Geo G, int V, int R>
+__device__ __forceinline__ void fast_block(float ox, const float (&oy)[R], const ViewRec* vr, int n,
+                                           const TileConst& c, float (&part)[R])
+{
+    int j = 0;
+    for (; j + 2 <= n; j += 2) {
+        const FastRec F0 = load_fast(vr + j), F1 = load_fast(vr + j + 1);
+        fast_rows<G, V, R>(ox, oy, F0, c, static_cast<unsigned>(F0.mode) & ~3u, part);
+        fast_rows<G, V, R>(ox, oy, F1, c, static_cast<unsigned>(F1.mode) & ~3u, part);
+    }
+    if (j < n) {
+        const FastRec F0 = load_fast(vr + j);
+        fast_rows<G, V, R>(ox, oy, F0, c, static_cast<unsigned>(F0.mode) & ~3u, part);
+    }
+}
+
+// The taps of n views (records at vr, pairs of view j at w + j*W; view
+// index ia0 + j) for a thread's R pixels.
+template <Geo G, int R>
+__device__ __forceinline__ void block_taps(float ox, const float (&oy)[R], int ixc, int iy0, int ia0,
+                                           const ViewRec* vr, int n, const float2* w, const double* t0,
+                                           const double* t1, const double* t2, const TileConst& c,
+                                           float (&part)[R])
+{
+    if (n <= 0) return;
+    const int v = block_variant(vr, n);
+    if (v >= 0) {
+        if constexpr (G == Geo::kFan) {
+            switch (v) {
+                case 0: fast_block<G, 0, R>(ox, oy, vr, n, c, part); break;
+                case 1: fast_block<G, 1, R>(ox, oy, vr, n, c, part); break;
+                default: fast_block<G, 2, R>(ox, oy, vr, n, c, part); break;
+            }
+        } else {
+            fast_block<G, 0, R>(ox, oy, vr, n, c, part);
+        }
+        return;
+    }
+    for (int j = 0; j < n; ++j) {
+        const FastRec F = load_fast(vr + j);
+        if (mode_fast(F.mode)) fast_view<G, R>(ox, oy, F, c, part);
+        else if (F.mode != kModeSkip)
+            edge_rows<G, R>(ox, oy, ixc, iy0, ia0 + j, vr[j], w + j * c.W, t0, t1, t2, c, part);
+    }
+}
+
 // A fast view's mode: the shared address of its pair slot plus 8 kc, less
 // 8 kMagicBits, with the variant in the low bits (kModeEdgeRel + variant in
 // the unlikely case that the address falls below kModeFastBase).
@@ -669,12 +734,7 @@ __global__ void __launch_bounds__(kBpThreads, 2)
         float part[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) part[r] = 0.0f;
-        for (int j = 0; j < nv; ++j) {
-            const FastRec F = load_fast(s_v + j);
-            if (mode_fast(F.mode)) fast_view<G, R>(ox, oy, F, c, part);
-            else if (F.mode != kModeSkip)
-                edge_rows<G, R>(ox, oy, ixc, iy0, v0 + j, s_v[j], win + j * c.W, t0, t1, t2, c, part);
-        }
+        block_taps<G, R>(ox, oy, ixc, iy0, v0, s_v, nv, win, t0, t1, t2, c, part);
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[r] += part[r];
         __syncthreads();
@@ -857,13 +917,8 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
         float part[R];  // this block's partial sums (blocked summation)
 #pragma unroll
         for (int r = 0; r < R; ++r) part[r] = 0.0f;
-        for (int j = jb; j < je; ++j) {
-            const int ia = b * kBV + j;
-            const FastRec F = load_fast(views + ia);
-            if (mode_fast(F.mode)) fast_view<G, R>(ox, oy, F, c, part);
-            else if (F.mode != kModeSkip)
-                edge_rows<G, R>(ox, oy, ixc, iy0, ia, views[ia], pb + j * c.W, t0, t1, t2, c, part);
-        }
+        block_taps<G, R>(ox, oy, ixc, iy0, b * kBV + jb, views + b * kBV + jb, je - jb, pb + jb * c.W, t0, t1,
+                         t2, c, part);
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[r] += part[r];
     }
