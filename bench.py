@@ -237,14 +237,14 @@ class ParPipeline:
                                                 g["offset_s"], g["orbit_start"], g["nx"], g["ny"],
                                                 g["dx"], g["dy"], g["offset_x"], g["offset_y"],
                                                 g["fov"])
-        self.fpt = [ctypes.c_void_p(t.data_ptr()) for t in self.fp.tables(device)]
+        self.fplan = self.fp.plan(device, 1)  # per-geometry ray tables, built once
         self.taps = ctypes.c_void_p(self.ramp.taps(device).data_ptr())
         self.bpt = [ctypes.c_void_p(t.data_ptr()) for t in self.bp.tables(device)]
         f32 = dict(dtype=torch.float32, device=device)
         self.sino = torch.empty((g["na"], g["ns"]), **f32)
         self.filt = torch.empty((g["na"], g["ns"]), **f32)
         self.names = ["fp_par_2d", "ramp_filter", "bp_par_2d"]
-        # our kernels per call (fp_par_2d: ray set-up with the transposed copy, projector)
+        # our kernels per call (fp_par_2d: transposed copy, projector)
         self.kernels = {"fp_par_2d": 2, "ramp_filter": 1, "bp_par_2d": 1}
         # algorithmic FP32 FLOPs per launch (fixed conventions)
         self.flops = {"fp_par_2d": 6.0 * g["na"] * g["ns"] * g["ny"],
@@ -258,9 +258,8 @@ class ParPipeline:
     def launches(self, img, out, stream):
         L = self.lib
         s = ctypes.c_void_p(stream)
-        p = ctypes.byref(self.fp.p)
-        yield lambda: L.ctr_fp_par_2d_f32(p, ctypes.c_void_p(img.data_ptr()),
-                                          ctypes.c_void_p(self.sino.data_ptr()), *self.fpt, 1, s)
+        yield lambda: L.ctr_fp_par_2d_plan_run(self.fplan, ctypes.c_void_p(img.data_ptr()),
+                                               ctypes.c_void_p(self.sino.data_ptr()), 1, s)
         yield lambda: L.ctr_ramp_filter_f32(ctypes.byref(self.ramp.p),
                                             ctypes.c_void_p(self.sino.data_ptr()), self.taps,
                                             ctypes.c_void_p(self.filt.data_ptr()), 1, s)

@@ -109,6 +109,9 @@ PROTOTYPES = {
     "ctr_fbp_fan_plan_info": [c_void_p, _S(PlanInfo)],
     "ctr_fbp_fan_plan_destroy": [c_void_p],
     "ctr_fp_par_2d_f32_noalloc": [_S(ParParam), _P, _P, _P, _P, _P, c_int, _P],
+    "ctr_fp_par_2d_plan_create": [_S(ParParam), _P, _P, _P, c_int, ctypes.POINTER(c_void_p), _P],
+    "ctr_fp_par_2d_plan_run": [c_void_p, _P, _P, c_int, _P],
+    "ctr_fp_par_2d_plan_destroy": [c_void_p],
     "ctr_fp_par_2d_cast_prep": [_S(ParParam), c_double, _P, _P, _P, _P],
     "ctr_fp_par_2d_dd_prep": [_S(ParParam), _P, _P, _P, _P],
     "ctr_fp_par_2d_dd_grad_prep": [_S(ParParam), _P, _P, _P, _P],

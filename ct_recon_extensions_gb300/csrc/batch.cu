@@ -66,6 +66,8 @@ __global__ void __launch_bounds__(NG * kBpThreads, (R >= 8 ? 1 : 2) * (3 - NG))
 struct Config {
     int R, VB, NG;
 };
+// Dynamic shared memory a candidate may take (227 KB per CTA, less static use).
+constexpr size_t kBatchSmemMax = 220 * 1024;
 constexpr Config kConfigs[] = {{4, 16, 2}, {2, 16, 2}, {4, 8, 2}, {2, 8, 2}, {8, 16, 2},
                                {8, 8, 2},  {8, 16, 1}, {8, 32, 1}};
 constexpr int kNumConfigs = sizeof(kConfigs) / sizeof(kConfigs[0]);
@@ -192,6 +194,8 @@ TileConst item_const(const ctr_fan_bp_param& g, int tile_y, int R, int VB)
     return c;
 }
 
+// Builds candidate ci; a candidate whose windows or shared memory do not fit
+// is left out (n_work = 0), which is not an error unless every one is.
 int build_config(ctr_fbp_plan* P, int ci, int sm_count)
 {
     const int R = kConfigs[ci].R, VB = kConfigs[ci].VB, NG = kConfigs[ci].NG;
@@ -204,7 +208,10 @@ int build_config(ctr_fbp_plan* P, int ci, int sm_count)
         const ctr_fan_bp_param& g = P->geoms[i];
         ItemDev& it = D.h_items[i];
         it.c = item_const(g, ty, R, VB);
-        if (it.c.WB > 256) return fail(CTR_ERR_UNSUPPORTED, "item %d: detector window too wide", i);
+        if (it.c.WB > 256) {
+            D.n_work = 0;  // a window wider than the bulk-copy box
+            return CTR_OK;
+        }
         it.proj = P->h_jobs[i].out;
         it.img = nullptr;
         it.xpos = P->xpos[i]->p;
@@ -216,7 +223,7 @@ int build_config(ctr_fbp_plan* P, int ci, int sm_count)
         for (int t = 0; t < it.tiles_x * tiles_y; ++t) work.push_back({cost, make_int2(i, t)});
         smem = std::max(smem, 128 + 2 * static_cast<size_t>(bv) * it.c.WS * sizeof(float) +
                                   2 * static_cast<size_t>(bv) * it.c.W * sizeof(float2) +
-                                  static_cast<size_t>(g.na) * sizeof(ViewRec));
+                                  static_cast<size_t>(g.na) * kViewBytes);
     }
     // longest first; ties keep item order (tiles of one item stay together)
     std::stable_sort(work.begin(), work.end(),
@@ -225,14 +232,21 @@ int build_config(ctr_fbp_plan* P, int ci, int sm_count)
                      });
     std::vector<int2> wl(work.size());
     for (size_t k = 0; k < work.size(); ++k) wl[k] = work[k].second;
-    if (smem > 200 * 1024) return fail(CTR_ERR_UNSUPPORTED, "batch needs %zu bytes of shared memory", smem);
+    if (smem > kBatchSmemMax) {
+        D.n_work = 0;
+        return CTR_OK;
+    }
     void* kern = kernel_of(ci);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "batch smem: %s", cudaGetErrorString(e));
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NG * kBpThreads, smem);
-    if (e != cudaSuccess || per_sm < 1) return fail(CTR_ERR_UNSUPPORTED, "batch kernel does not fit an SM");
+    if (e != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        D.n_work = 0;
+        return CTR_OK;
+    }
     D.smem = smem;
     D.n_work = static_cast<int>(wl.size());
     D.grid = std::min(D.n_work, per_sm * sm_count);
@@ -403,6 +417,15 @@ int ctr_fbp_fan_plan_create(const ctr_fan_bp_param* geoms, int n_items, int weig
     for (int ci = 0; ci < kNumConfigs; ++ci) {
         st = build_config(P.get(), ci, sm_count);
         if (st) return st;
+    }
+    if (P->cfg[P->chosen].n_work == 0) {
+        for (int ci = 0; ci < kNumConfigs; ++ci)
+            if (P->cfg[ci].n_work > 0) {
+                P->chosen = ci;
+                break;
+            }
+        if (P->cfg[P->chosen].n_work == 0)
+            return fail(CTR_ERR_UNSUPPORTED, "no backprojection tile shape fits these items' windows");
     }
     if (cudaStreamSynchronize(P->stream) != cudaSuccess) return fail(CTR_ERR_CUDA, "plan setup");
     if (flags & CTR_PLAN_AUTOTUNE) {

@@ -105,7 +105,8 @@ __global__ void __launch_bounds__(kBpThreads, 2)
     constexpr int R = kRowsPerThread;
     extern __shared__ __align__(16) unsigned char adj_smem[];
     unsigned* win = reinterpret_cast<unsigned*>(adj_smem);  // [kViewBlock][W]
-    ViewRec* views = reinterpret_cast<ViewRec*>(adj_smem + (kViewBlock * c.W * 4 + 15) / 16 * 16);
+    FastRec* views = reinterpret_cast<FastRec*>(adj_smem + (kViewBlock * c.W * 4 + 15) / 16 * 16);
+    ViewAux* vaux = reinterpret_cast<ViewAux*>(views + kAdjChunkBlocks * kViewBlock);
     __shared__ unsigned s_max[kBpThreads / 32];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -178,13 +179,14 @@ __global__ void __launch_bounds__(kBpThreads, 2)
                     if (mode_fast(P.mode))
                         P.mode = adj_fast_mode(win_base + 4u * static_cast<unsigned>((ia % kViewBlock) * c.W), c,
                                                P.mode);
-                    views[ia - va] = P;
+                    store_view(views, vaux, ia - va, P);
                 }
                 __syncthreads();
             }
             const int v0 = b * kViewBlock;
             const int nv = min(kViewBlock, c.na - v0);
-            const ViewRec* vb = views + (b - b0) % kAdjChunkBlocks * kViewBlock;
+            const FastRec* vb = views + (b - b0) % kAdjChunkBlocks * kViewBlock;
+            const ViewAux* vab = vaux + (b - b0) % kAdjChunkBlocks * kViewBlock;
             for (int j = 0; j < nv; ++j) {
                 const FastRec F = load_fast(vb + j);
                 if (F.mode == kModeSkip) continue;
@@ -239,17 +241,18 @@ __global__ void __launch_bounds__(kBpThreads, 2)
                     }
                     continue;
                 }
-                const ViewRec P = vb[j];
+                const FastRec& P = F;
+                const int lo = vab[j].lo;
                 // edge views (and every view of a tile with non-finite values):
                 // x-major, the forward's inclusion decisions; fixed-point taps into
                 // the window, or FP32 taps straight into the sinogram
                 const bool direct = any_bad || (G == Geo::kFan && P.mode == kModeEdgeAbs);
-                float* Grow = Gs + static_cast<size_t>(ia) * c.ns + P.lo;
+                float* Grow = Gs + static_cast<size_t>(ia) * c.ns + lo;
                 auto tap = [&](int jj, float sig2, float t) {
                     const float u = __fadd_rn(sig2, -(static_cast<float>(jj - c.kc) - 0.5f));
                     if (direct) {
                         const float a1 = t * u;
-                        const int g = P.lo + jj;  // taps off the detector carry no weight
+                        const int g = lo + jj;  // taps off the detector carry no weight
                         if (t != 0.0f && g >= 0 && g < c.ns) atomicAdd(Grow + jj, t - a1);
                         if (t != 0.0f && g + 1 >= 0 && g + 1 < c.ns) atomicAdd(Grow + jj + 1, a1);
                     } else {
@@ -268,7 +271,7 @@ __global__ void __launch_bounds__(kBpThreads, 2)
                             float w, sig2;
                             int jj;
                             const float s = channel_abs<G>(x, static_cast<float>(t1[iyc]), make_float2(P.p0, P.p1), c, &w);
-                            if (edge_tap_abs<G>(s, ixx, iyc, ia, P.lo, t0, t1, t2, c, &jj, &sig2))
+                            if (edge_tap_abs<G>(s, ixx, iyc, ia, lo, t0, t1, t2, c, &jj, &sig2))
                                 tap(jj, sig2, (any_bad ? vx[r] : vx[r] * back) * w);
                         }
                         continue;
@@ -280,8 +283,8 @@ __global__ void __launch_bounds__(kBpThreads, 2)
                             float w, sig2;
                             int jj;
                             const float sig = fan_sigma<V>(X, oyx[r], P, c, &w);
-                            if (edge_tap<G>(sig, ixx, min(iy0 + r, c.ny - 1), ia, P.lo, t0, t1, t2, c, &jj, &sig2))
-                                tap(jj, sig2, any_bad ? vx[r] * (w * P.e) : __fmul_rn(vx[r], w));
+                            if (edge_tap<G>(sig, ixx, min(iy0 + r, c.ny - 1), ia, lo, t0, t1, t2, c, &jj, &sig2))
+                                tap(jj, sig2, any_bad ? vx[r] * (w * vab[j].e) : __fmul_rn(vx[r], w));
                         }
                     };
                     switch (mode_variant(P.mode)) {
@@ -295,7 +298,7 @@ __global__ void __launch_bounds__(kBpThreads, 2)
                         float sig2;
                         int jj;
                         const float sig = par_sigma(xs, oyx[r], P);
-                        if (edge_tap<G>(sig, ixx, min(iy0 + r, c.ny - 1), ia, P.lo, t0, t1, t2, c, &jj, &sig2))
+                        if (edge_tap<G>(sig, ixx, min(iy0 + r, c.ny - 1), ia, lo, t0, t1, t2, c, &jj, &sig2))
                             tap(jj, sig2, vx[r]);
                     }
                 }
@@ -307,7 +310,7 @@ __global__ void __launch_bounds__(kBpThreads, 2)
                 if (a == 0u) continue;
                 win[idx] = 0u;
                 const int j = idx / c.W, kk = idx - j * c.W;
-                const ViewRec& P = vb[j];
+                const ViewAux& P = vab[j];
                 const int g = P.lo + kk;
                 if (g >= 0 && g < c.ns)
                     atomicAdd(Gs + static_cast<size_t>(v0 + j) * c.ns + g,
@@ -506,7 +509,7 @@ int sm_count()
 inline size_t fwd_smem(const TileConst& ct, int VB, int NG = 1)
 {
     const size_t bv = static_cast<size_t>(NG) * VB;
-    return 128 + 2 * bv * ct.WS * sizeof(float) + 2 * bv * ct.W * sizeof(float2) + ct.na * sizeof(ViewRec);
+    return 128 + 2 * bv * ct.WS * sizeof(float) + 2 * bv * ct.W * sizeof(float2) + ct.na * kViewBytes;
 }
 
 // The bulk-copy kernel (one group of VB views, tiles of 32 x kTileY): stream-K
@@ -615,7 +618,7 @@ int launch_adjoint(const float* img, float* grad, const double* t0, const double
                    const TileConst& c, int batch, cudaStream_t stream, const char* what)
 {
     const size_t smem = (static_cast<size_t>(kViewBlock) * c.W * 4 + 15) / 16 * 16 +
-                        static_cast<size_t>(std::min(c.na, kAdjChunkBlocks * kViewBlock)) * sizeof(ViewRec);
+                        static_cast<size_t>(kAdjChunkBlocks * kViewBlock) * kViewBytes;
     if (smem > kTileSmemMax) return fail(CTR_ERR_UNSUPPORTED, "%s: window of %d channels too wide", what, c.W);
     const int tiles_x = static_cast<int>(div_up(c.nx, kTileX));
     const int tiles_y = static_cast<int>(div_up(c.ny, kTileY));

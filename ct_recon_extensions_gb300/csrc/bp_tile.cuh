@@ -148,15 +148,26 @@ struct __align__(16) FastRec {
     float cen;     // position of the reference pixel less (lo + kc + 1/2)
     int mode;      // kModeSkip / kModeEdgeAbs / kModeEdgeRel + variant, or a fast-path base
 };
-struct __align__(16) ViewRec : FastRec {
+// The rest of a record (kept in a second array: 24 bytes of shared memory a view).
+struct ViewAux {
     float e;       // fan relative: 1/R^2 (folded into the staged pairs); else 1
     int lo;        // first staged channel
 };
+struct ViewRec : FastRec {
+    float e;
+    int lo;
+};
+constexpr size_t kViewBytes = sizeof(FastRec) + sizeof(ViewAux);
 
-__device__ __forceinline__ FastRec load_fast(const ViewRec* v)
+__device__ __forceinline__ FastRec load_fast(const FastRec* v)
 {
     const float4 f = *reinterpret_cast<const float4*>(v);
     return FastRec{f.x, f.y, f.z, __float_as_int(f.w)};
+}
+__device__ __forceinline__ void store_view(FastRec* vf, ViewAux* va, int i, const ViewRec& P)
+{
+    vf[i] = FastRec{P.p0, P.p1, P.cen, P.mode};
+    va[i] = ViewAux{P.e, P.lo};
 }
 
 __device__ __forceinline__ bool mode_fast(int m) { return static_cast<unsigned>(m) >= kModeFastBase; }
@@ -536,7 +547,7 @@ __device__ __forceinline__ void fast_rows(float ox, const float (&oy)[R], const 
 // offsets oy[r].
 template <int V, int R>
 __device__ __forceinline__ void edge_rows_fan(FanX X, const float (&oy)[R], int ixc, int iy0, int ia,
-                                              const ViewRec& P, const float2* wj, const double* t0,
+                                              const FastRec& P, int lo, const float2* wj, const double* t0,
                                               const double* t1, const double* t2, const TileConst& c,
                                               float (&part)[R])
 {
@@ -545,7 +556,7 @@ __device__ __forceinline__ void edge_rows_fan(FanX X, const float (&oy)[R], int 
         float w, sig2;
         int j;
         const float sig = fan_sigma<V>(X, oy[r], P, c, &w);
-        if (edge_tap<Geo::kFan>(sig, ixc, min(iy0 + r, c.ny - 1), ia, P.lo, t0, t1, t2, c, &j, &sig2)) {
+        if (edge_tap<Geo::kFan>(sig, ixc, min(iy0 + r, c.ny - 1), ia, lo, t0, t1, t2, c, &j, &sig2)) {
             const float2 pv = wj[j];
             part[r] = fmaf(fmaf(sig2, pv.y, pv.x), w, part[r]);
         }
@@ -554,7 +565,7 @@ __device__ __forceinline__ void edge_rows_fan(FanX X, const float (&oy)[R], int 
 
 template <Geo G, int R>
 __device__ __forceinline__ void edge_rows(float ox, const float (&oy)[R], int ixc, int iy0, int ia,
-                                          const ViewRec& P, const float2* wj, const double* t0,
+                                          const FastRec& P, int lo, const float2* wj, const double* t0,
                                           const double* t1, const double* t2, const TileConst& c,
                                           float (&part)[R])
 {
@@ -567,7 +578,7 @@ __device__ __forceinline__ void edge_rows(float ox, const float (&oy)[R], int ix
                 float w, sig2;
                 int j;
                 const float s = channel_abs<G>(x, static_cast<float>(t1[iyc]), make_float2(P.p0, P.p1), c, &w);
-                if (edge_tap_abs<G>(s, ixc, iyc, ia, P.lo, t0, t1, t2, c, &j, &sig2)) {
+                if (edge_tap_abs<G>(s, ixc, iyc, ia, lo, t0, t1, t2, c, &j, &sig2)) {
                     const float2 pv = wj[j];
                     part[r] = fmaf(fmaf(sig2, pv.y, pv.x), w, part[r]);
                 }
@@ -576,9 +587,9 @@ __device__ __forceinline__ void edge_rows(float ox, const float (&oy)[R], int ix
         }
         const FanX X = fan_xpart(ox, P);
         switch (mode_variant(P.mode)) {
-            case 0: edge_rows_fan<0, R>(X, oy, ixc, iy0, ia, P, wj, t0, t1, t2, c, part); break;
-            case 1: edge_rows_fan<1, R>(X, oy, ixc, iy0, ia, P, wj, t0, t1, t2, c, part); break;
-            default: edge_rows_fan<2, R>(X, oy, ixc, iy0, ia, P, wj, t0, t1, t2, c, part); break;
+            case 0: edge_rows_fan<0, R>(X, oy, ixc, iy0, ia, P, lo, wj, t0, t1, t2, c, part); break;
+            case 1: edge_rows_fan<1, R>(X, oy, ixc, iy0, ia, P, lo, wj, t0, t1, t2, c, part); break;
+            default: edge_rows_fan<2, R>(X, oy, ixc, iy0, ia, P, lo, wj, t0, t1, t2, c, part); break;
         }
     } else {
         const float xs = par_xpart(ox, P);
@@ -587,7 +598,7 @@ __device__ __forceinline__ void edge_rows(float ox, const float (&oy)[R], int ix
             float sig2;
             int j;
             const float sig = par_sigma(xs, oy[r], P);
-            if (edge_tap<G>(sig, ixc, min(iy0 + r, c.ny - 1), ia, P.lo, t0, t1, t2, c, &j, &sig2)) {
+            if (edge_tap<G>(sig, ixc, min(iy0 + r, c.ny - 1), ia, lo, t0, t1, t2, c, &j, &sig2)) {
                 const float2 pv = wj[j];
                 part[r] += fmaf(sig2, pv.y, pv.x);
             }
@@ -614,7 +625,7 @@ __device__ __forceinline__ void fast_view(float ox, const float (&oy)[R], const 
 
 // The fan variant shared by every view of n records at vr when all of them
 // take the fast path, else -1 (warp-uniform; n <= 64).
-__device__ __forceinline__ int block_variant(const ViewRec* vr, int n)
+__device__ __forceinline__ int block_variant(const FastRec* vr, int n)
 {
     const int lane = threadIdx.x & 31;
     const int v0 = mode_variant(vr[0].mode);
@@ -629,7 +640,7 @@ __device__ __forceinline__ int block_variant(const ViewRec* vr, int n)
 // n views (records at vr) that all take the fast path with variant V: no
 // per-view dispatch, two views per trip (same summation order as one by one).
 template <Geo G, int V, int R>
-__device__ __forceinline__ void fast_block(float ox, const float (&oy)[R], const ViewRec* vr, int n,
+__device__ __forceinline__ void fast_block(float ox, const float (&oy)[R], const FastRec* vr, int n,
                                            const TileConst& c, float (&part)[R])
 {
     int j = 0;
@@ -644,11 +655,12 @@ __device__ __forceinline__ void fast_block(float ox, const float (&oy)[R], const
     }
 }
 
-// The taps of n views (records at vr, pairs of view j at w + j*W; view
-// index ia0 + j) for a thread's R pixels.
+// The taps of n views (records at vr and va, pairs of view j at w + j*W;
+// view index ia0 + j) for a thread's R pixels.
 template <Geo G, int R>
 __device__ __forceinline__ void block_taps(float ox, const float (&oy)[R], int ixc, int iy0, int ia0,
-                                           const ViewRec* vr, int n, const float2* w, const double* t0,
+                                           const FastRec* vr, const ViewAux* va, int n, const float2* w,
+                                           const double* t0,
                                            const double* t1, const double* t2, const TileConst& c,
                                            float (&part)[R])
 {
@@ -670,7 +682,7 @@ __device__ __forceinline__ void block_taps(float ox, const float (&oy)[R], int i
         const FastRec F = load_fast(vr + j);
         if (mode_fast(F.mode)) fast_view<G, R>(ox, oy, F, c, part);
         else if (F.mode != kModeSkip)
-            edge_rows<G, R>(ox, oy, ixc, iy0, ia0 + j, vr[j], w + j * c.W, t0, t1, t2, c, part);
+            edge_rows<G, R>(ox, oy, ixc, iy0, ia0 + j, F, va[j].lo, w + j * c.W, t0, t1, t2, c, part);
     }
 }
 
@@ -699,7 +711,8 @@ __global__ void __launch_bounds__(kBpThreads, 2)
 {
     constexpr int R = kRowsPerThread;
     extern __shared__ __align__(16) float2 win[];  // [kViewBlock][W]
-    __shared__ ViewRec s_v[kViewBlock];
+    __shared__ FastRec s_v[kViewBlock];
+    __shared__ ViewAux s_a[kViewBlock];
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const TileBox B = tile_box<G>(t0, t1, blockIdx.x, blockIdx.y, kTileY, c);
@@ -719,22 +732,22 @@ __global__ void __launch_bounds__(kBpThreads, 2)
         if (threadIdx.x < nv) {
             ViewRec P = view_setup<G>(t0, t1, t2, v0 + threadIdx.x, B, c);
             if (mode_fast(P.mode)) P.mode = fast_mode(win_base + 8u * threadIdx.x * c.W, c, P.mode);
-            s_v[threadIdx.x] = P;
+            store_view(s_v, s_a, threadIdx.x, P);
         }
         __syncthreads();
         for (int idx = threadIdx.x; idx < nv * c.W; idx += kBpThreads) {
             const int j = idx / c.W, k = idx - j * c.W;
-            const int g = s_v[j].lo + k;
+            const int g = s_a[j].lo + k;
             const float* row = P_ + static_cast<size_t>(v0 + j) * c.ns;
             const float p0 = (g >= 0 && g < c.ns) ? __ldg(row + g) : 0.0f;
             const float p1 = (g + 1 >= 0 && g + 1 < c.ns) ? __ldg(row + g + 1) : 0.0f;
-            win[idx] = make_pair(p0, p1, k, c.kc, s_v[j].e);
+            win[idx] = make_pair(p0, p1, k, c.kc, s_a[j].e);
         }
         __syncthreads();
         float part[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) part[r] = 0.0f;
-        block_taps<G, R>(ox, oy, ixc, iy0, v0, s_v, nv, win, t0, t1, t2, c, part);
+        block_taps<G, R>(ox, oy, ixc, iy0, v0, s_v, s_a, nv, win, t0, t1, t2, c, part);
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[r] += part[r];
         __syncthreads();
@@ -783,12 +796,13 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
     constexpr int kThreads = NG * kBpThreads;   // NG view groups of 256 threads
     // Dynamic shared memory, 128-byte aligned here: raw slots [2][kBV][WS]
     // (every slot stride a 128-byte multiple), pairs [2][kBV][W], then one
-    // view record per view of the whole scan.
+    // view record per view of the whole scan (FastRec array, then ViewAux).
     extern __shared__ __align__(128) unsigned char smem_dyn[];
     unsigned char* smem = smem_dyn + ((128u - (smem_u32(smem_dyn) & 127u)) & 127u);
     float* raw = reinterpret_cast<float*>(smem);
     float2* pairs = reinterpret_cast<float2*>(smem + 2 * kBV * c.WS * sizeof(float));
-    ViewRec* views = reinterpret_cast<ViewRec*>(pairs + 2 * kBV * c.W);
+    FastRec* views = reinterpret_cast<FastRec*>(pairs + 2 * kBV * c.W);
+    ViewAux* vaux = reinterpret_cast<ViewAux*>(views + c.na);
     __shared__ __align__(8) unsigned long long s_bar[2];
     __shared__ int s_ok;
 
@@ -806,7 +820,7 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
     // to 4 elements; the conversion below reads the clipped-away elements from
     // global directly.
     auto slot_start = [&](int ia) -> long long {
-        return (static_cast<long long>(item) * c.na + ia) * c.ns + views[ia].lo;
+        return (static_cast<long long>(item) * c.na + ia) * c.ns + vaux[ia].lo;
     };
     // Issued by warp 0, one lane per view (kBV <= 64: two rounds at most); lane 0
     // arms the barrier with the block's byte count (a warp sum) first.
@@ -847,7 +861,7 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
             const int slot = ((ia / kBV - b_begin) & 1) * kBV + ia % kBV;
             P.mode = fast_mode(pairs_base + 8u * static_cast<unsigned>(slot * c.W), c, P.mode);
         }
-        views[ia] = P;
+        store_view(views, vaux, ia, P);
     }
     if (tid == 0) {
         // every copy destination must be 128-byte aligned; check before issuing any
@@ -892,8 +906,8 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
         // one warp per view: rewrite the raw window as pairs
         for (int j = wid; j < nv; j += kThreads / 32) {
             const long long st = slot_start(b * kBV + j);
-            const int lo = views[b * kBV + j].lo;
-            const float e = views[b * kBV + j].e;
+            const int lo = vaux[b * kBV + j].lo;
+            const float e = vaux[b * kBV + j].e;
             const float* src = slot + j * c.WS + static_cast<int>(st & 3ll);
             float2* dst = pb + j * c.W;
             if (lo >= 0 && lo + c.W < c.ns && st + c.W < c.total4) {
@@ -917,8 +931,8 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
         float part[R];  // this block's partial sums (blocked summation)
 #pragma unroll
         for (int r = 0; r < R; ++r) part[r] = 0.0f;
-        block_taps<G, R>(ox, oy, ixc, iy0, b * kBV + jb, views + b * kBV + jb, je - jb, pb + jb * c.W, t0, t1,
-                         t2, c, part);
+        block_taps<G, R>(ox, oy, ixc, iy0, b * kBV + jb, views + b * kBV + jb, vaux + b * kBV + jb, je - jb,
+                         pb + jb * c.W, t0, t1, t2, c, part);
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[r] += part[r];
     }

@@ -24,7 +24,7 @@
 // FP64 kernels follow the reference's arithmetic (one thread per ray / pixel).
 #include <algorithm>
 #include <climits>
-#include <mutex>
+#include <memory>
 #include <numeric>
 
 #include "ctr_async.cuh"
@@ -199,6 +199,7 @@ struct FpxConst {
     long long total4;      // total rounded down to 4
     size_t proj_stride;
     float dx, dy;
+    int sms;               // SMs of the device
 };
 
 // Global tie entry (a ray the fixed-point rule could not settle).
@@ -210,6 +211,7 @@ struct FpxTie {
 
 // The per-call tables (scratch) written by fpx_setup.
 struct FpxRays {
+    float* vw;       // [na] ray weight of the view: dy/|cos| (row-marching) or dx/|sin|
     long long* X0;   // [na*ns] 32.32 position of sample 0
     long long* S;    // [na*ns] 32.32 step
     int* code;       // [na*ns] k0 | k1 << 15 | class << 30, or kFpxEmpty
@@ -224,7 +226,8 @@ __host__ __device__ inline size_t fpx_table_bytes(long long rays, int na, int ct
 {
     const size_t r = static_cast<size_t>(rays);
     const size_t views = 4 * (static_cast<size_t>(na) / 4 + 3);
-    return ((r * 24 + views * 4 + (static_cast<size_t>(ctas) + 2) * 4 + 63) & ~static_cast<size_t>(63)) +
+    const size_t vw = (static_cast<size_t>(na) * 4 + 255) & ~static_cast<size_t>(255);
+    return vw + ((r * 24 + views * 4 + (static_cast<size_t>(ctas) + 2) * 4 + 63) & ~static_cast<size_t>(63)) +
            64 + static_cast<size_t>(kFpxMaxTies) * sizeof(FpxTie);
 }
 
@@ -246,37 +249,58 @@ __device__ __forceinline__ void slot_ray(unsigned q, int lane, const FpxConst& c
     *is = slot_octet(q - quad * static_cast<unsigned>(c.octets), c) * 8 + (lane & 7);
 }
 
-// ---- set-up kernel: every ray once; block 0 the class lists and CTA cut ------
-// Blocks from `setup_blocks` on transpose the images instead (32 x 32 tiles):
-// the two jobs are independent, and the transpose blocks fill the SMs left idle
-// while the few tie rays of the set-up walk the reference's accumulation.
+// imgT[b][x][y] = img[b][y][x] for the 32 x 32 tile `tb` (tiles of every
+// item in a row); t is 32 x 33 floats of shared memory.
+__device__ __forceinline__ void fpx_transpose_tile(const float* __restrict__ img, float* __restrict__ imgT,
+                                                   int n, int tb, float (*t)[33])
+{
+    const int tid = threadIdx.x;
+    const int tiles = (n + 31) / 32;
+    const int item = tb / (tiles * tiles), tt = tb - item * tiles * tiles;
+    const int x0 = (tt % tiles) * 32, y0 = (tt / tiles) * 32;
+    const int tx = tid & 31, ty = tid >> 5;
+    const size_t off = static_cast<size_t>(item) * n * n;
+    for (int rr = ty; rr < 32; rr += kFpxSetupThreads / 32) {
+        const int y = y0 + rr, x = x0 + tx;
+        if (x < n && y < n) t[rr][tx] = img[off + static_cast<size_t>(y) * n + x];
+    }
+    __syncthreads();
+    for (int rr = ty; rr < 32; rr += kFpxSetupThreads / 32) {
+        const int x = x0 + rr, y = y0 + tx;
+        if (x < n && y < n) imgT[off + static_cast<size_t>(x) * n + y] = t[tx][rr];
+    }
+}
+
+// The transposed copy alone (the plan's calls: its ray tables already exist).
 __global__ void __launch_bounds__(kFpxSetupThreads)
-    fpx_setup(const double* __restrict__ bo, const int* __restrict__ usex, const FpxConst c,
-              const FpxRays r, int setup_blocks, const float* __restrict__ img, float* __restrict__ imgT)
+    fpx_transpose(const float* __restrict__ img, float* __restrict__ imgT, int n)
+{
+    __shared__ float t[32][33];
+    fpx_transpose_tile(img, imgT, n, static_cast<int>(blockIdx.x), t);
+}
+
+// ---- set-up kernel: every ray once; block 0 the class lists, CTA cut and view
+// weights.  Blocks from `setup_blocks` on transpose the images instead (32 x 32
+// tiles): the two jobs are independent, and the transpose blocks fill the SMs
+// left idle while the few tie rays of the set-up walk the reference's
+// accumulation.
+__global__ void __launch_bounds__(kFpxSetupThreads)
+    fpx_setup(const double* __restrict__ bo, const int* __restrict__ usex, const double* __restrict__ sincos,
+              const FpxConst c, const FpxRays r, int setup_blocks, const float* __restrict__ img,
+              float* __restrict__ imgT)
 {
     __shared__ int s_chunk[2049];  // block 0: row-marching views before each chunk of 32
     const int tid = threadIdx.x;
     if (static_cast<int>(blockIdx.x) >= setup_blocks) {
-        // imgT[b][x][y] = img[b][y][x]
-        float (*t)[33] = reinterpret_cast<float (*)[33]>(s_chunk);  // 32 x 33 floats
-        const int n = c.n, tiles = (n + 31) / 32;
-        const int tb = static_cast<int>(blockIdx.x) - setup_blocks;
-        const int item = tb / (tiles * tiles), tt = tb - item * tiles * tiles;
-        const int x0 = (tt % tiles) * 32, y0 = (tt / tiles) * 32;
-        const int tx = tid & 31, ty = tid >> 5;
-        const size_t off = static_cast<size_t>(item) * n * n;
-        for (int rr = ty; rr < 32; rr += kFpxSetupThreads / 32) {
-            const int y = y0 + rr, x = x0 + tx;
-            if (x < n && y < n) t[rr][tx] = img[off + static_cast<size_t>(y) * n + x];
-        }
-        __syncthreads();
-        for (int rr = ty; rr < 32; rr += kFpxSetupThreads / 32) {
-            const int x = x0 + rr, y = y0 + tx;
-            if (x < n && y < n) imgT[off + static_cast<size_t>(x) * n + y] = t[tx][rr];
-        }
+        fpx_transpose_tile(img, imgT, c.n, static_cast<int>(blockIdx.x) - setup_blocks,
+                           reinterpret_cast<float (*)[33]>(s_chunk));
         return;
     }
     if (blockIdx.x == 0) {
+        // ray weight of each view: the reference's dy/|cos| or dx/|sin|, in FP32
+        for (int ia = tid; ia < c.na; ia += kFpxSetupThreads)
+            r.vw[ia] = usex[ia] != 0 ? c.dy / fabsf(dbl2flt(sincos[2 * ia + 1]))
+                                     : c.dx / fabsf(dbl2flt(sincos[2 * ia]));
         // class lists with warp ballots over chunks of 32 views: row-marching
         // views (usex) first, then column-marching ones, each padded to quads
         constexpr int kWarps = kFpxSetupThreads / 32;
@@ -375,8 +399,7 @@ __global__ void __launch_bounds__(kFpxSetupThreads)
 
 __global__ void __launch_bounds__(kFpxThreads, 2)
     fp_proj_f32(const float* __restrict__ img, const float* __restrict__ imgT,
-                float* __restrict__ proj, const double* __restrict__ sincos,
-                const int* __restrict__ usex, const FpxConst c, const FpxRays r)
+                float* __restrict__ proj, const FpxConst c, const FpxRays r)
 {
     extern __shared__ __align__(128) unsigned char fpx_dyn[];
     float* stage = reinterpret_cast<float*>(fpx_dyn + ((128u - (smem_u32(fpx_dyn) & 127u)) & 127u));
@@ -564,9 +587,7 @@ __global__ void __launch_bounds__(kFpxThreads, 2)
                         v += p0 + u * (p1 - p0);
                     }
                 }
-                const float dw = cls1 ? c.dx / fabsf(dbl2flt(sincos[2 * ia]))
-                                      : c.dy / fabsf(dbl2flt(sincos[2 * ia + 1]));
-                proj[blockIdx.y * c.proj_stride + static_cast<size_t>(ia) * c.ns + is] = v * dw;
+                proj[blockIdx.y * c.proj_stride + static_cast<size_t>(ia) * c.ns + is] = v * r.vw[ia];
             }
         }
         g += c.nbands;
@@ -1196,7 +1217,11 @@ bool fpx_const(const ctr_par_param* p, const void* img, int batch, FpxConst* out
     const long long slots = static_cast<long long>(c.quads + 2) * c.octets;  // with class padding
     if (slots >= (1ll << 30) || static_cast<long long>(p->na) * p->ns >= (1ll << 31)) return false;
     // two CTAs an SM; more when the mean CTA would exceed 7/8 of a round
-    const long long ctas = std::max<long long>(div_up(slots * 8, kFpxRound * 7), 2 * kSmCount);
+    int dev = 0;
+    c.sms = kSmCount;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&c.sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        c.sms = kSmCount;
+    const long long ctas = std::max<long long>(div_up(slots * 8, kFpxRound * 7), 2ll * c.sms);
     c.ctas = static_cast<int>(std::min<long long>(ctas, slots));
     c.band = std::max(1, std::min(32, kFpxStageFloats / n));
     c.nbands = static_cast<int>(div_up(n, c.band));
@@ -1219,14 +1244,13 @@ size_t fpx_scratch_bytes(const FpxConst& c)
     return imgT + fpx_table_bytes(static_cast<long long>(c.na) * c.ns, c.na, c.ctas);
 }
 
-// Carves the tables out of `scratch` (256-byte aligned), after the transposed image.
-FpxRays fpx_rays(void* scratch, const FpxConst& c, float** imgT)
+// Carves the ray tables out of `b` (256-byte aligned).
+FpxRays fpx_tables(unsigned char* b, const FpxConst& c)
 {
     const size_t rays = static_cast<size_t>(c.na) * c.ns;
-    unsigned char* b = static_cast<unsigned char*>(scratch);
-    *imgT = reinterpret_cast<float*>(b);
-    b += (static_cast<size_t>(c.total) * sizeof(float) + 255) & ~static_cast<size_t>(255);
     FpxRays r;
+    r.vw = reinterpret_cast<float*>(b);
+    b += (static_cast<size_t>(c.na) * 4 + 255) & ~static_cast<size_t>(255);
     r.X0 = reinterpret_cast<long long*>(b);
     r.S = reinterpret_cast<long long*>(b + rays * 8);
     r.code = reinterpret_cast<int*>(b + rays * 16);
@@ -1241,30 +1265,52 @@ FpxRays fpx_rays(void* scratch, const FpxConst& c, float** imgT)
     return r;
 }
 
+// Carves the tables out of `scratch` (256-byte aligned), after the transposed image.
+FpxRays fpx_rays(void* scratch, const FpxConst& c, float** imgT)
+{
+    unsigned char* b = static_cast<unsigned char*>(scratch);
+    *imgT = reinterpret_cast<float*>(b);
+    b += (static_cast<size_t>(c.total) * sizeof(float) + 255) & ~static_cast<size_t>(255);
+    return fpx_tables(b, c);
+}
+
+// Ray set-up (and, when imgT_src is given, the transposed copy of it into
+// imgT) in one launch, set-up blocks first.
+int launch_fpx_setup(const FpxConst& c, const FpxRays& r, const double* sc, const double* bo, const int* usex,
+                     const float* img, float* imgT, int batch, cudaStream_t stream)
+{
+    cudaError_t e = cudaMemsetAsync(r.nties, 0, sizeof(int), stream);
+    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp_par_2d: %s", cudaGetErrorString(e));
+    const long long rays = static_cast<long long>(c.na) * c.ns;
+    const unsigned blocks = static_cast<unsigned>(
+        std::min<long long>(div_up(rays, kFpxSetupThreads), 8ll * c.sms));
+    const unsigned long long tblocks =
+        img ? static_cast<unsigned long long>(div_up(c.n, 32)) * div_up(c.n, 32) * batch : 0ull;
+    if (blocks + tblocks > 0x7FFFFFFFull) return fail(CTR_ERR_UNSUPPORTED, "fp_par_2d: batch too large");
+    fpx_setup<<<static_cast<unsigned>(blocks + tblocks), kFpxSetupThreads, 0, stream>>>(
+        bo, usex, sc, c, r, static_cast<int>(blocks), img, imgT);
+    return check_launch("fp_par_2d set-up");
+}
+
+int launch_fpx_proj(const FpxConst& c, size_t smem, const FpxRays& r, const float* img, const float* imgT,
+                    float* proj, int batch, cudaStream_t stream)
+{
+    cudaError_t e = cudaFuncSetAttribute(fp_proj_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp smem: %s", cudaGetErrorString(e));
+    fp_proj_f32<<<dim3(c.ctas, batch), kFpxThreads, smem, stream>>>(img, imgT, proj, c, r);
+    return check_launch("fp_par_2d");
+}
+
 // Transposed copy, ray set-up and the projector, in stream order, on `scratch`.
 int launch_fpx(const FpxConst& c, size_t smem, void* scratch, const float* img, float* proj,
                const double* sc, const double* bo, const int* usex, int batch, cudaStream_t stream)
 {
     float* imgT = nullptr;
     const FpxRays r = fpx_rays(scratch, c, &imgT);
-    const int n = c.n;
-    cudaError_t e = cudaMemsetAsync(r.nties, 0, sizeof(int), stream);
-    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp_par_2d: %s", cudaGetErrorString(e));
-    const long long rays = static_cast<long long>(c.na) * c.ns;
-    const unsigned blocks = static_cast<unsigned>(
-        std::min<long long>(div_up(rays, kFpxSetupThreads), 8 * kSmCount));
-    const unsigned long long tblocks = static_cast<unsigned long long>(div_up(n, 32)) * div_up(n, 32) * batch;
-    if (blocks + tblocks > 0x7FFFFFFFull) return fail(CTR_ERR_UNSUPPORTED, "fp_par_2d: batch too large");
-    // ray set-up and the transposed copy in one launch (set-up blocks first)
-    fpx_setup<<<static_cast<unsigned>(blocks + tblocks), kFpxSetupThreads, 0, stream>>>(
-        bo, usex, c, r, static_cast<int>(blocks), img, imgT);
-    int st = check_launch("fp_par_2d set-up");
+    int st = launch_fpx_setup(c, r, sc, bo, usex, img, imgT, batch, stream);
     if (st) return st;
-    e = cudaFuncSetAttribute(fp_proj_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(smem));
-    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp smem: %s", cudaGetErrorString(e));
-    fp_proj_f32<<<dim3(c.ctas, batch), kFpxThreads, smem, stream>>>(img, imgT, proj, sc, usex, c, r);
-    return check_launch("fp_par_2d");
+    return launch_fpx_proj(c, smem, r, img, imgT, proj, batch, stream);
 }
 
 template <typename T>
@@ -1413,29 +1459,16 @@ int fp_adjoint(const ctr_par_param* p, const T* proj, T* img, const double* w,
 constexpr long long kFpNoAllocBytes = 16ll << 20;
 static __device__ __align__(256) unsigned char g_fp_noalloc_scratch[kFpNoAllocBytes];
 
-constexpr int kNoAllocMaxDevices = 64;
-std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
-
-// The array's device address on the current device, looked up once per device
-// (cudaGetSymbolAddress; the first call on a device does this set-up).
+// The array's device address in the current context (cudaGetSymbolAddress on
+// every call: cheap once the module is loaded, and never stale after a device
+// reset or under another context; the first call in a context loads the module).
 int noalloc_scratch(void** out)
 {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return fail(CTR_ERR_DEVICE, "cudaGetDevice: %s", cudaGetErrorString(e));
-    if (dev < 0 || dev >= kNoAllocMaxDevices)
-        return fail(CTR_ERR_UNSUPPORTED, "device %d >= %d", dev, kNoAllocMaxDevices);
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-        void* ptr = nullptr;
-        e = cudaGetSymbolAddress(&ptr, g_fp_noalloc_scratch);
-        if (e != cudaSuccess || !ptr)
-            return fail(CTR_ERR_CUDA, "fp_par_2d_f32_noalloc scratch address: %s",
-                        cudaGetErrorString(e));
-        g_noalloc_ptr[dev] = ptr;
-    }
-    *out = g_noalloc_ptr[dev];
+    void* ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_fp_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+        return fail(CTR_ERR_CUDA, "fp_par_2d_f32_noalloc scratch address: %s", cudaGetErrorString(e));
+    *out = ptr;
     return CTR_OK;
 }
 
@@ -1464,9 +1497,89 @@ int fp_forward_noalloc(const ctr_par_param* p, const float* img, float* proj, co
 }  // namespace
 }  // namespace ctr
 
+// A per-geometry plan of the FP32 ray-driven projector: the ray tables (fixed-
+// point start and step, exact sample range and class of every ray, the
+// reference's decisions for its tie rays, view lists, CTA cut and view
+// weights) are built once from the caller's tables; a call then runs the
+// transposed copy and the projector only.
+struct ctr_fp_plan {
+    int device = 0;
+    int max_batch = 0;
+    ctr::FpxConst c{};
+    size_t smem = 0;
+    void* tables = nullptr;
+    float* imgT = nullptr;
+    ctr::FpxRays r{};
+    ~ctr_fp_plan()
+    {
+        if (tables) cudaFree(tables);
+        if (imgT) cudaFree(imgT);
+    }
+};
+
 using namespace ctr;
 
 extern "C" {
+
+int ctr_fp_par_2d_plan_create(const ctr_par_param* p, const double* sincostbl, const double* beginoffset,
+                              const int* usex, int max_batch, ctr_fp_plan** plan, cudaStream_t stream)
+{
+    if (!plan) return fail(CTR_ERR_INVALID_ARG, "null plan pointer");
+    *plan = nullptr;
+    int st = check_fp(p, sincostbl, beginoffset, sincostbl, beginoffset, usex, max_batch);
+    if (st) return st;
+    FpxConst c;
+    size_t smem = 0;
+    alignas(16) static const float probe[4] = {};  // the plan checks the caller's image per call
+    if (!fpx_const(p, probe, max_batch, &c, &smem))
+        return fail(CTR_ERR_UNSUPPORTED, "fp_par_2d plan: needs nx <= 8192 and fewer than 2^30 ray slots");
+    auto P = std::make_unique<ctr_fp_plan>();
+    cudaGetDevice(&P->device);
+    P->max_batch = max_batch;
+    P->c = c;
+    P->smem = smem;
+    const size_t tbytes = fpx_table_bytes(static_cast<long long>(c.na) * c.ns, c.na, c.ctas);
+    const size_t ibytes = static_cast<size_t>(max_batch) * c.n * c.n * sizeof(float);
+    if (cudaMalloc(&P->tables, tbytes) != cudaSuccess || cudaMalloc(&P->imgT, ibytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(CTR_ERR_CUDA, "fp_par_2d plan: %zu + %zu bytes", tbytes, ibytes);
+    }
+    P->r = fpx_tables(static_cast<unsigned char*>(P->tables), c);
+    st = launch_fpx_setup(c, P->r, sincostbl, beginoffset, usex, nullptr, nullptr, 1, stream);
+    if (st) return st;
+    const cudaError_t e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp_par_2d plan set-up: %s", cudaGetErrorString(e));
+    *plan = P.release();
+    return CTR_OK;
+}
+
+int ctr_fp_par_2d_plan_run(ctr_fp_plan* plan, const float* img, float* proj, int batch, cudaStream_t stream)
+{
+    if (!plan || !img || !proj) return fail(CTR_ERR_INVALID_ARG, "null argument");
+    int st = check_common(batch);
+    if (st) return st;
+    int dev = -1;
+    cudaGetDevice(&dev);
+    if (dev != plan->device) return fail(CTR_ERR_INVALID_ARG, "plan made on device %d, current %d", plan->device, dev);
+    if (batch > plan->max_batch) return fail(CTR_ERR_INVALID_ARG, "batch %d > the plan's %d", batch, plan->max_batch);
+    if (reinterpret_cast<uintptr_t>(img) % 16 != 0)
+        return fail(CTR_ERR_INVALID_ARG, "fp_par_2d plan: img must be 16-byte aligned");
+    FpxConst c = plan->c;
+    c.total = static_cast<long long>(batch) * c.n * c.n;
+    c.total4 = c.total & ~3ll;
+    const unsigned long long tiles = static_cast<unsigned long long>(div_up(c.n, 32)) * div_up(c.n, 32) * batch;
+    if (tiles > 0x7FFFFFFFull) return fail(CTR_ERR_UNSUPPORTED, "fp_par_2d: batch too large");
+    fpx_transpose<<<static_cast<unsigned>(tiles), kFpxSetupThreads, 0, stream>>>(img, plan->imgT, c.n);
+    st = check_launch("fp_par_2d transposed copy");
+    if (st) return st;
+    return launch_fpx_proj(c, plan->smem, plan->r, img, plan->imgT, proj, batch, stream);
+}
+
+int ctr_fp_par_2d_plan_destroy(ctr_fp_plan* plan)
+{
+    delete plan;
+    return CTR_OK;
+}
 
 int ctr_fp_par_2d_f32(const ctr_par_param* p, const float* img, float* proj,
                       const double* sincostbl, const double* beginoffset, const int* usex,

@@ -349,7 +349,10 @@ class ParallelProjection2DOp:
     no gradient, as in the reference) or "disdriven"
     (ParallelProjection2DDisDriven{Prep,,GradPrep,Grad},
     include/fp_par_2d.h:283-352; its adjoint is the reference's distance-driven
-    grad, which the reference op registers as the gradient)."""
+    grad, which the reference op registers as the gradient).  FP32 ray-driven
+    calls run through a per-geometry plan (ctr_fp_par_2d_plan_*): the ray
+    set-up runs once per device, a call is the transposed copy and the
+    projector."""
 
     def __init__(self, ns, na, ds, orbit, offset_s, orbit_start, nx, ny, dx, dy, offset_x,
                  offset_y, fov=-1.0, method="raydriven", step_size=0.125):
@@ -367,6 +370,38 @@ class ParallelProjection2DOp:
         self.ns, self.na, self.nx, self.ny = ns, na, nx, ny
         self._fwd_tables = _Tables()
         self._adj_tables = _Tables()
+        self._plans = {}  # device -> (ctr_fp_plan handle, max batch): FP32 ray driven
+        self._lib = _lib.load()
+
+    def plan(self, device, batch=1):
+        """The FP32 ray-driven projector's per-geometry plan on `device` (its
+        ray tables built once from this op's tables), grown to the largest
+        batch seen."""
+        dev = device.index if device.index is not None else torch.cuda.current_device()
+        cur = self._plans.get(dev)
+        if cur is None or cur[1] < batch:
+            with torch.cuda.device(dev):
+                if cur is not None:
+                    torch.cuda.current_stream().synchronize()
+                    self._lib.ctr_fp_par_2d_plan_destroy(cur[0])
+                    del self._plans[dev]
+                h = ctypes.c_void_p()
+                call("ctr_fp_par_2d_plan_create", ctypes.byref(self.p),
+                     *map(_ptr, self.tables(torch.device("cuda", dev))), int(batch), ctypes.byref(h),
+                     _stream())
+                self._plans[dev] = (h, batch)
+        return self._plans[dev][0]
+
+    def close(self):
+        for h, _ in self._plans.values():
+            self._lib.ctr_fp_par_2d_plan_destroy(h)
+        self._plans.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
     def tables(self, device):
         if self.method == "raycasting":
@@ -417,6 +452,9 @@ class ParallelProjection2DOp:
         elif self.method == "disdriven":
             call(f"ctr_fp_par_2d_dd_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(proj),
                  *map(_ptr, self.tables(xb.device)), xb.shape[0], _stream())
+        elif xb.dtype == torch.float32 and xb.data_ptr() % 16 == 0 and self.nx <= 8192:
+            call("ctr_fp_par_2d_plan_run", self.plan(xb.device, xb.shape[0]), _ptr(xb), _ptr(proj),
+                 xb.shape[0], _stream())
         else:
             call(f"ctr_fp_par_2d_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(proj),
                  *map(_ptr, self.tables(xb.device)), xb.shape[0], _stream())

@@ -253,6 +253,25 @@ int ctr_fp_par_2d_grad_f64(const ctr_par_param* p, const double* proj, double* i
                            const double* weights, const double* pos, const int* usex,
                            int batch, cudaStream_t stream);
 
+/* ---- ray-driven FP32 projection with a per-geometry plan (no counterpart
+ *      in the reference: ParallelProjection2DRayDriven<float>::calculate_on_gpu,
+ *      include/fp_par_2d.h:227-244, with the per-call ray set-up done once) ----
+ * ctr_fp_par_2d_plan_create builds, from the prep tables above (read on
+ * `stream`, which it synchronises; the tables may be freed afterwards), every
+ * ray's fixed-point start and step, exact sample range and class, the
+ * reference's decisions for rays that end within a rounding of the image
+ * border, and a transposed-image workspace for max_batch images.  A run then
+ * gives the same results as ctr_fp_par_2d_f32 with two launches (transposed
+ * copy, projector) and no allocation; img must be 16-byte aligned.  A plan
+ * serves one stream at a time, on the device it was made on. */
+typedef struct ctr_fp_plan ctr_fp_plan;
+int ctr_fp_par_2d_plan_create(const ctr_par_param* p, const double* sincostbl,
+                              const double* beginoffset, const int* usex, int max_batch,
+                              ctr_fp_plan** plan, cudaStream_t stream);
+int ctr_fp_par_2d_plan_run(ctr_fp_plan* plan, const float* img, float* proj, int batch,
+                           cudaStream_t stream);
+int ctr_fp_par_2d_plan_destroy(ctr_fp_plan* plan);
+
 /* ---- parallel-beam ray-casting forward projection
  *      (reference include/fp_par_2d.h:155-203, src/fp_par_2d.cc:18-145) ----
  * Prep (ParallelProjection2DRayCastingPrepare, its step_size argument):
@@ -305,11 +324,12 @@ int ctr_fp_par_2d_dd_grad_f64(const ctr_par_param* p, const double* proj, double
  * image pixel of the batch plus about 400 KB within 16 MiB (720 views x 729
  * bins with up to 3 images of 512 x 512), nx at most 8192, img 16-byte
  * aligned; otherwise CTR_ERR_UNSUPPORTED.
- * The first call on each device looks up the array's address
- * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture.  All calls on a device share the array: calls
- * ordered on one stream are fine, calls that may overlap (other streams,
- * other host threads) race on it. */
+ * Every call looks up the array's address in the current context
+ * (cudaGetSymbolAddress: cheap once the library's module is loaded, and
+ * never stale after a device reset); the first call in a context loads the
+ * module, so make it before any stream capture.  All calls on a device share
+ * the array: calls ordered on one stream are fine, calls that may overlap
+ * (other streams, other host threads) race on it. */
 int ctr_fp_par_2d_f32_noalloc(const ctr_par_param* p, const float* img, float* proj,
                               const double* sincostbl, const double* beginoffset,
                               const int* usex, int batch, cudaStream_t stream);

@@ -359,6 +359,32 @@ def test_fp_distance_driven_config2(oracle_port):
     assert np.array_equal(outs[1], host(op.forward(cuda(stack[1]))))
 
 
+def test_fp_plan_matches_per_call_path():
+    """The per-geometry plan (ray tables built once) gives bit-identical
+    results to the per-call entry point at config 2, for one image and a batch
+    of three, and calls after a plan has grown keep doing so."""
+    import ctypes
+    import torch
+    from ct_recon_extensions_gb300 import _lib
+    from ct_recon_extensions_gb300 import synthetic as syn
+    from ct_recon_extensions_gb300.torch_ctrecon import _ptr, _stream
+    d = syn.parallel_config_2()
+    op = fp_op(d)
+    rng = np.random.default_rng(21)
+    imgs = cuda(np.stack([syn.rasterize(syn.random_ellipses(2400), 512, 512, 0.5, 0.5),
+                          rng.standard_normal((512, 512)).astype(np.float32),
+                          rng.random((512, 512)).astype(np.float32)]))
+    ref = torch.empty((3, d["na"], d["ns"]), dtype=torch.float32, device="cuda")
+    _lib.call("ctr_fp_par_2d_f32", ctypes.byref(op.p), _ptr(imgs), _ptr(ref),
+              *map(_ptr, op.tables(imgs.device)), 3, _stream())
+    one = op.forward(imgs[0])           # plan for one image
+    three = op.forward(imgs)            # plan grown to three
+    torch.cuda.synchronize()
+    assert torch.equal(one, ref[0])
+    assert torch.equal(three, ref)
+    assert torch.equal(op.forward(imgs[1]), ref[1])
+
+
 def test_fp_adjoint_config2_batch(oracle_port):
     """The FP adjoint at 512^2 x 720 views x 729 bins: against the oracle, and a
     batch of 7 (image groups of the gather plus a remainder) equal to its items."""

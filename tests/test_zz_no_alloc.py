@@ -2,10 +2,14 @@
 
 Called through the C ABI and compared with ctr_fp_par_2d_f32 (stream-ordered
 scratch) on the same inputs, twice in a row on one stream, and with the
-reference's golden output.  The file sorts last so it also runs after every
-other GPU test in one process.
+reference's golden output.  That it allocates nothing is read off the
+device's default memory pool: its high watermark of memory in use does not
+move during a call (and does move during an allocating ctr_fp_par_2d_f32 call,
+which shows the probe sees the library's allocations).  The file sorts last
+so it also runs after every other GPU test in one process.
 """
 import ctypes
+import ctypes.util
 
 import numpy as np
 import pytest
@@ -68,3 +72,49 @@ def test_noalloc_rejects_oversize():
     img = torch.zeros((1, d["ny"], d["nx"]), dtype=torch.float32, device="cuda")
     with pytest.raises(CtrError, match="16 MiB"):
         _run("ctr_fp_par_2d_f32_noalloc", op, img)
+
+
+def _cudart():
+    """The CUDA runtime as a shared library, only to read the device's default
+    memory pool (a driver object that the library's own, statically linked,
+    runtime allocates from too)."""
+    for name in ("libcudart.so.13", "libcudart.so", "/usr/local/cuda/lib64/libcudart.so",
+                 ctypes.util.find_library("cudart")):
+        if not name:
+            continue
+        try:
+            return ctypes.CDLL(name)
+        except OSError:
+            pass
+    pytest.skip("no libcudart to read the default memory pool")
+
+
+def test_noalloc_allocates_nothing():
+    import torch
+    from ct_recon_extensions_gb300._lib import call
+    from ct_recon_extensions_gb300 import synthetic as syn
+    from ct_recon_extensions_gb300.torch_ctrecon import _ptr, _stream
+    used_now, used_high = 7, 8  # cudaMemPoolAttrUsedMemCurrent, cudaMemPoolAttrUsedMemHigh
+    rt = _cudart()
+    pool = ctypes.c_void_p()
+    assert rt.cudaDeviceGetDefaultMemPool(ctypes.byref(pool), torch.cuda.current_device()) == 0
+    d = syn.parallel_config_2()
+    op = fp_op(d)
+    img = cuda(np.random.default_rng(3).standard_normal((1, d["ny"], d["nx"])).astype(np.float32))
+    proj = torch.empty((1, d["na"], d["ns"]), dtype=torch.float32, device="cuda")
+    tables = [_ptr(t) for t in op.tables(img.device)]
+
+    def peak_growth(name):
+        torch.cuda.synchronize()
+        zero, now, high = ctypes.c_uint64(0), ctypes.c_uint64(), ctypes.c_uint64()
+        assert rt.cudaMemPoolSetAttribute(pool, used_high, ctypes.byref(zero)) == 0
+        assert rt.cudaMemPoolGetAttribute(pool, used_now, ctypes.byref(now)) == 0
+        call(name, ctypes.byref(op.p), _ptr(img), _ptr(proj), *tables, 1, _stream())
+        torch.cuda.synchronize()
+        assert rt.cudaMemPoolGetAttribute(pool, used_high, ctypes.byref(high)) == 0
+        return high.value - now.value
+
+    for _ in range(2):
+        assert peak_growth("ctr_fp_par_2d_f32_noalloc") == 0
+    # the allocating entry point's stream-ordered scratch shows up in the same probe
+    assert peak_growth("ctr_fp_par_2d_f32") > 0
