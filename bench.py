@@ -13,9 +13,15 @@ so every step reads its input from HBM.
 Reported: slices/s (value) and pixel-view updates/s; ``e2e`` repeats the
 workload through the C ABI with the slice copied from pinned host memory and
 the reconstruction read back every step; ``roofline`` is the dominant
-kernel's algorithmic FP32 FLOP/s (per-launch CUDA-event durations inside the
-timed region) against the FP32 peak; ``cpu_baseline`` times the oracle port
+kernel's algorithmic FP32 FLOP/s (per-kernel pass below) against the FP32
+peak; ``cpu_baseline`` times the oracle port
 (the reference's CPU algorithm restated in C) on this host's cores.
+
+``roofline.kernel_ms`` comes from a per-kernel pass after the timed region
+(each stage 100 times from a CUDA graph, CUDA events around the replay);
+``roofline.hbm`` gives the same kernel's algorithmic bytes against the
+measured HBM bandwidth; ``roofline.traffic`` is the ncu DRAM traffic per call
+recorded in profiles/ncu_traffic.txt.
 
 ``extra`` (``--legs`` selects): ``fan_fbp_config1`` the fan FBP at its
 headline size (fan weighting -> ramp(fan) -> bp_fan_2d, 720 x 736 -> 512x512);
@@ -29,7 +35,10 @@ error against the FP64 oracle on image strips when the CPU-baseline leg runs;
 driven, beside ray driven; ``helical`` 360LI / 180LI rebinning of a
 clinical-size helical scan (736 channels x 64 rows, 1152 views per rotation,
 pitch 1, 128 slices) with its algorithmic bytes against the measured HBM
-bandwidth and the oracle port beside it.
+bandwidth and the oracle port beside it; ``adjoints`` the FP32 adjoints of
+bp_fan_2d (config 1) and bp_par_2d (config 2) beside their forwards, and the
+fan FBP chain's sinogram gradient; ``bp_par_2d_sv`` the single-view
+backprojection at config 2 (write-bound) against the HBM bandwidth.
 
 ``--impl reference`` times the reference's CPU implementation of the same
 workload on this host (the compiled reference when its build is present,
@@ -59,7 +68,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "FBP slices/s and pixel-view updates/s at rel-L2<=1e-4 vs FP64; batched vs plain"
 SM_COUNT = 152
-LEGS = ("fan", "batched", "gd", "lowp", "fpmethods", "helical")
+LEGS = ("fan", "batched", "gd", "lowp", "fpmethods", "helical", "adjoints", "sv")
 FP32_LANES_PER_SM = 128
 
 
@@ -392,6 +401,170 @@ def run_device(pipe, pool_dev, outs, steps, warmup, dist, per_kernel=True):
     return secs, kern, sum(pipe.kernels.values()) * steps
 
 
+KERNEL_REPS = 100  # back-to-back launches per stage in the per-kernel pass
+
+
+def stage_ms(launch, reps=KERNEL_REPS):
+    """Mean device time of one call of `launch(k, stream)` (k = repetition
+    index, so callers can cycle their inputs): `reps` calls captured in a CUDA
+    graph, the graph replayed once untimed and once between CUDA events on the
+    replay stream, so the mean has no host gaps.  Where capture fails (a call
+    that cannot be captured), the calls are issued directly between events."""
+    import torch
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        for k in range(3):
+            launch(k, s.cuda_stream)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    try:
+        with torch.cuda.graph(g, stream=s):
+            for k in range(reps):
+                launch(k, s.cuda_stream)
+        captured = True
+    except Exception:
+        torch.cuda.synchronize()
+        captured = False
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(s):
+        if captured:
+            g.replay()
+            e0.record(s)
+            g.replay()
+            e1.record(s)
+        else:
+            e0.record(s)
+            for k in range(reps):
+                launch(k, s.cuda_stream)
+            e1.record(s)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps, captured
+
+
+def pipeline_kernel_pass(pipe, pool_dev, outs):
+    """Per-stage mean time of the pipeline (pipe.names order): the first stage
+    cycles through the input pool (as the timed steps do), later stages read
+    the pipeline's own intermediate buffers."""
+    res, graphs = {}, []
+    P = len(pool_dev)
+    for i, name in enumerate(pipe.names):
+        def launch(k, sp, i=i, name=name):
+            fn = list(pipe.launches(pool_dev[k % P], outs[k % len(outs)], sp))[i]
+            if fn() != 0:
+                raise RuntimeError(f"{name}: {pipe.lib.ctr_last_error().decode()}")
+        ms, cap = stage_ms(launch)
+        res[name] = ms
+        graphs.append(cap)
+    return res, all(graphs)
+
+
+def op_call(op, which, x, out, sp):
+    """One C-ABI call of a torch_ctrecon operator's forward, adjoint or single
+    view into a preallocated output, on stream handle sp (one item)."""
+    from ct_recon_extensions_gb300 import torch_ctrecon as tc
+    from ct_recon_extensions_gb300._lib import call
+    s = ctypes.c_void_p(sp)
+    p = ctypes.byref(op.p)
+    xi, oi = ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr())
+    if isinstance(op, tc.FanBackprojection2DOp):
+        t = [ctypes.c_void_p(a.data_ptr()) for a in op.tables(x.device)]
+        call("ctr_bp_fan_2d_f32" if which == "forward" else "ctr_bp_fan_2d_grad_f32", p, xi, oi, *t, 1, s)
+    elif isinstance(op, tc.ParallelBackprojection2DOp):
+        t = [ctypes.c_void_p(a.data_ptr()) for a in op.tables(x.device)]
+        if which == "forward":
+            call("ctr_bp_par_2d_f32", p, xi, oi, *t, None, 1, s)
+        elif which == "adjoint":
+            call("ctr_bp_par_2d_grad_f32", p, xi, oi, *t, 1, s)
+        else:
+            call("ctr_bp_par_2d_sv_f32", p, xi, oi, *t, None, 1, s)
+    elif isinstance(op, tc.RampFilterOp):
+        taps = ctypes.c_void_p(op.taps(x.device).data_ptr())
+        call("ctr_ramp_filter_f32" if which == "forward" else "ctr_ramp_filter_grad_f32", p, xi, taps, oi, 1, s)
+    elif isinstance(op, tc.FanWeightingOp):
+        call("ctr_fan_weighting_f32" if which == "forward" else "ctr_fan_weighting_grad_f32", p, xi, oi, 1, s)
+    else:
+        raise TypeError(type(op))
+
+
+def run_adjoints(device, dist):
+    """The FP32 adjoints beside their forwards, one image per call: bp_fan_2d
+    and its exact adjoint at config 1 (720 x 736 -> 512^2), bp_par_2d and its
+    adjoint at config 2 (720 x 729 -> 512^2), and the sinogram gradient of the
+    fan FBP chain (bp_fan_2d adjoint -> ramp-filter adjoint -> fan-weighting
+    adjoint, the reference's TF gradient wiring), with FP32-pipe throughput
+    (the forward's algorithmic FLOPs: 32 per fan update, 9 per parallel one)."""
+    import torch
+    from ct_recon_extensions_gb300 import synthetic as syn
+    from ct_recon_extensions_gb300 import torch_ctrecon as tc
+    rng = np.random.default_rng(5)
+    out = {}
+    gf, gp = syn.fan_config_1(), syn.parallel_config_2()
+    fan = tc.FanBackprojection2DOp(gf["ns"], gf["na"], gf["ds"], gf["orbit"], gf["offset_s"],
+                                   gf["orbit_start"], gf["nx"], gf["ny"], gf["dx"], gf["dy"],
+                                   gf["offset_x"], gf["offset_y"], gf["dso"], gf["dsd"], gf["fov"])
+    par = tc.ParallelBackprojection2DOp(gp["ns"], gp["na"], gp["ds"], gp["orbit"], gp["offset_s"],
+                                        gp["orbit_start"], gp["nx"], gp["ny"], gp["dx"], gp["dy"],
+                                        gp["offset_x"], gp["offset_y"], gp["fov"])
+    w = tc.FanWeightingOp(gf["ns"], gf["na"], gf["ds"], gf["offset_s"], gf["dso"], gf["dsd"], 1)
+    ramp = tc.RampFilterOp(gf["ns"], gf["na"], gf["ds"], gf["dsd"], 1)
+    f32 = dict(dtype=torch.float32, device=device)
+    pool = 40  # 40 distinct inputs of 1-2 MB: more than L2 per cycle
+
+    def randn(shape):
+        return torch.from_numpy(rng.standard_normal(shape).astype(np.float32)).to(device)
+
+    for name, op, g, fl in (("bp_fan_2d", fan, gf, 32.0), ("bp_par_2d", par, gp, 9.0)):
+        sinos = [randn((g["na"], g["ns"])) for _ in range(pool)]
+        imgs = [randn((g["ny"], g["nx"])) for _ in range(pool)]
+        img_out = torch.empty((g["ny"], g["nx"]), **f32)
+        sino_out = torch.empty((g["na"], g["ns"]), **f32)
+        flops = fl * g["nx"] * g["ny"] * g["na"]
+        ms_f, _ = stage_ms(lambda k, sp: op_call(op, "forward", sinos[k % pool], img_out, sp))
+        ms_a, _ = stage_ms(lambda k, sp: op_call(op, "adjoint", imgs[k % pool], sino_out, sp))
+        out[name] = {"forward_ms": ms_f, "adjoint_ms": ms_a, "adjoint_over_forward": ms_a / ms_f,
+                     "forward_tflops": flops / ms_f / 1e9, "adjoint_tflops": flops / ms_a / 1e9}
+    imgs = [randn((gf["ny"], gf["nx"])) for _ in range(pool)]
+    t1, t2, t3 = (torch.empty((gf["na"], gf["ns"]), **f32) for _ in range(3))
+
+    def chain(k, sp):
+        op_call(fan, "adjoint", imgs[k % pool], t1, sp)
+        op_call(ramp, "adjoint", t1, t2, sp)
+        op_call(w, "adjoint", t2, t3, sp)
+    ms_c, _ = stage_ms(chain)
+    out["fan_chain_grad"] = {"ms": ms_c, "kernels": 4,
+                             "workload": "d loss / d sinogram of fan_weighting -> ramp(fan) -> "
+                                         "bp_fan_2d, 720 x 736 -> 512^2"}
+    out["workload"] = ("FP32 adjoints vs forwards, one image per call, 100 calls replayed from a "
+                       "CUDA graph, inputs cycled over 40 distinct buffers")
+    return out
+
+
+def run_single_view(device, dist):
+    """bp_par_2d_sv at config 2: 720 x 729 -> 512 x 512 x 720 FP32 (755 MB out,
+    write-bound), one sinogram per call, against the measured HBM bandwidth."""
+    import torch
+    from ct_recon_extensions_gb300 import synthetic as syn
+    from ct_recon_extensions_gb300 import torch_ctrecon as tc
+    g = syn.parallel_config_2()
+    op = tc.ParallelBackprojection2DOp(g["ns"], g["na"], g["ds"], g["orbit"], g["offset_s"],
+                                       g["orbit_start"], g["nx"], g["ny"], g["dx"], g["dy"],
+                                       g["offset_x"], g["offset_y"], g["fov"])
+    rng = np.random.default_rng(9)
+    sinos = [torch.from_numpy(rng.standard_normal((g["na"], g["ns"])).astype(np.float32)).to(device)
+             for _ in range(4)]
+    out = torch.empty((g["ny"], g["nx"], g["na"]), dtype=torch.float32, device=device)
+    ms, _ = stage_ms(lambda k, sp: op_call(op, "single_view", sinos[k % 4], out, sp), reps=20)
+    wbytes = 4.0 * g["nx"] * g["ny"] * g["na"]
+    rbytes = 4.0 * g["na"] * g["ns"] + 8.0 * g["na"] * (g["nx"] + g["ny"])  # sinogram + FP64 tables
+    gbs = (wbytes + rbytes) / ms / 1e6
+    peak = hbm_peak_gbs()
+    return {"workload": "bp_par_2d_sv 720 views x 729 bins -> 512 x 512 x 720 (FP32), one sinogram per call",
+            "ms_per_call": ms, "algorithmic_bytes": wbytes + rbytes, "achieved_gbs": gbs,
+            "hbm_peak_gbs": peak, "hbm_frac": gbs / peak, "calls": 20}
+
+
 def run_batched(device, steps, warmup, dist):
     """The uneven fan batch (64 items, image 256^2..1024^2, 360..2304 views,
     512..1024 channels): one plan run (batched filter launch + one persistent
@@ -431,14 +604,20 @@ def run_batched(device, steps, warmup, dist):
     info = plan.info()
     pipes = [FanPipeline(g, device) for g in geoms]
     sp = stream.cuda_stream
+    outs_plain = [torch.empty_like(o) for o in outs]
 
     def plain():
-        for pipe, s, o in zip(pipes, sinos, outs):
+        for pipe, s, o in zip(pipes, sinos, outs_plain):
             for fn in pipe.launches(s, o, sp):
                 if fn() != 0:
                     raise RuntimeError(pipe.lib.ctr_last_error().decode())
 
     p_secs = timed(plain, k)
+    # the plan's images against the plain per-item path's (separate buffers)
+    plan.run(sinos, outs)
+    plain()
+    torch.cuda.synchronize()
+    diffs = [rel_l2(a.cpu().numpy(), b.cpu().numpy()) for a, b in zip(outs, outs_plain)]
     n = len(geoms)
     plan.close()
     return {
@@ -446,6 +625,7 @@ def run_batched(device, steps, warmup, dist):
                     "512-1024 channels): weighting -> ramp(fan) -> bp_fan_2d",
         "slices_per_s": n * k / b_secs, "updates_per_s": updates * k / b_secs,
         "plain_slices_per_s": n * k / p_secs, "speedup_vs_plain": p_secs / b_secs,
+        "rel_l2_plan_vs_plain_max": max(diffs),
         "plan": {key: info[key] for key in ("tile_rows", "view_block", "ctas", "autotuned",
                                             "tuned_ms", "graph", "launches_per_run")},
         "gpu_launches": int(info["launches_per_run"]) * k, "runs": k,
@@ -1064,6 +1244,8 @@ def main():
     clocks = clk.stop([(t_a, time.perf_counter())])
     secs = dist.max(secs)
     value = replica_value(ws, args.steps, secs)
+    # per-kernel pass after the timed region: each stage 100x from a CUDA graph
+    kpass, kpass_graph = pipeline_kernel_pass(pipe, pool_dev, outs)
 
     # ---- e2e through the C ABI with pinned host buffers ----
     pool_host = [t.cpu().pin_memory() for t in pool_dev[:32]]
@@ -1083,14 +1265,17 @@ def main():
         fouts = [torch.empty((gf["ny"], gf["nx"]), dtype=torch.float32, device=device) for _ in range(4)]
         f_secs, f_kern, f_launches = run_device(fpipe, fpool, fouts, args.steps, args.warmup, dist)
         f_secs = dist.max(f_secs)
-        fdom = max(f_kern, key=f_kern.get)
+        f_pass, _ = pipeline_kernel_pass(fpipe, fpool, fouts)
+        fdom = max(f_pass, key=f_pass.get)
         extra["fan_fbp_config1"] = {
             "workload": "fan_weighting -> ramp(fan) -> bp_fan_2d, 720 views x 736 ch -> 512x512",
             "slices_per_s": ws * args.steps / f_secs,
             "updates_per_s": ws * args.steps / f_secs * fpipe.updates,
-            "kernel_ms": f_kern,
+            "ms_per_step": 1e3 * f_secs / args.steps,
+            "kernel_ms": f_pass,
+            "kernel_ms_in_run": f_kern,
             "dominant": fdom,
-            "dominant_tflops": fpipe.flops[fdom] / (f_kern[fdom] / 1e3) / 1e12,
+            "dominant_tflops": fpipe.flops[fdom] / (f_pass[fdom] / 1e3) / 1e12,
             "gpu_launches": f_launches,
         }
 
@@ -1111,6 +1296,14 @@ def main():
         extra["helical"] = run_helical(device, args.steps, args.warmup, dist,
                                        rank == 0 and not args.no_cpu_baseline)
 
+    # ---- FP32 adjoints beside their forwards, and the fan chain's gradient ----
+    if "adjoints" in args.legs:
+        extra["adjoints"] = run_adjoints(device, dist)
+
+    # ---- single-view backprojection (write-bound) ----
+    if "sv" in args.legs:
+        extra["bp_par_2d_sv"] = run_single_view(device, dist)
+
     # ---- reduced-precision large slice (config 5); its FP64 check is CPU
     #      oracle work on rank 0, part of the CPU-baseline leg ----
     if "lowp" in args.legs:
@@ -1121,19 +1314,30 @@ def main():
     peak_meas = fp32_peak_tflops(device)
     clk_max = clocks.get("sm_max_mhz") or 2070.0
     peak_nominal = SM_COUNT * FP32_LANES_PER_SM * 2 * clk_max * 1e6 / 1e12
-    dom = max(kern, key=kern.get)
-    achieved = pipe.flops[dom] / (kern[dom] / 1e3) / 1e12
+    dom = max(kpass, key=kpass.get)
+    achieved = pipe.flops[dom] / (kpass[dom] / 1e3) / 1e12
     traffic = read_traffic()
     plausible = peak_meas <= 1.1 * peak_nominal
     peak = peak_meas if plausible else peak_nominal
+    hbm = hbm_peak_gbs()
+    gbs = pipe.bytes[dom] / (kpass[dom] / 1e3) / 1e9
     roofline = {
         "bound": "fp32", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
         "frac": achieved / peak, "traffic": traffic.get(dom),
+        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per call, "
+                          "profiles/ncu_traffic.txt (not measured in this run)",
         "algorithmic_bytes": pipe.bytes[dom],
         "peak_source": ("measured: cuBLAS SGEMM 8192^3, TF32 off, best of 5" if plausible else
                         "nominal: 152 SMs x 128 FP32 lanes x 2 x max SM clock"),
         "peak_nominal": peak_nominal,
-        "kernel_ms": kern,
+        "hbm": {"achieved_gbs": gbs, "peak_gbs": hbm, "frac": gbs / hbm,
+                "peak_source": "measured: MEASURED_PEAKS.json hbm_gbs (copy)"},
+        "kernel_ms": kpass,
+        "kernel_ms_source": "per-stage pass after the timed region: 100 calls per stage replayed "
+                            "from a CUDA graph, CUDA events around the replay"
+                            + ("" if kpass_graph else " (some stage not capturable: issued directly)"),
+        "kernel_sum_ms": sum(kpass.values()),
+        "kernel_ms_in_run": kern,
     }
     if rank == 0:
         cpu = None

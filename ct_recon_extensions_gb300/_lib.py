@@ -98,6 +98,7 @@ PROTOTYPES = {
     "ctr_version": [],
     "ctr_device_check": [],
     "ctr_kernel_flags": [ctypes.POINTER(c_uint), c_int],
+    "ctr_selftest_wait_timeout": [ctypes.c_ulonglong, _P],
     "ctr_ramp_filter_prep": [_S(FilterParam), _P, _P],
     "ctr_bp_fan_2d_prep": [_S(FanBpParam), _P, _P, _P, _P],
     "ctr_bp_fan_2d_angle_prep": [_S(FanBpAngleParam), _P, _P, _P, _P, _P],

@@ -62,13 +62,17 @@ __device__ __forceinline__ unsigned long long global_ns()
     return t;
 }
 
-// Waits for an mbarrier phase for at most ~1 s; false on timeout.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity)
+// The limit of every bounded wait of the library's kernels.
+constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s
+
+// Waits for an mbarrier phase for at most limit_ns (~1 s); false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity,
+                                                  unsigned long long limit_ns = kWaitLimitNs)
 {
     if (mbar_try_wait(bar, parity)) return true;
     const unsigned long long t0 = global_ns();
     while (!mbar_try_wait(bar, parity)) {
-        if (global_ns() - t0 > 1000000000ull) return false;
+        if (global_ns() - t0 > limit_ns) return false;
     }
     return true;
 }

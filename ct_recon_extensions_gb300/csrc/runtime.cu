@@ -9,6 +9,7 @@
 #include <cstring>
 #include <vector>
 
+#include "ctr_async.cuh"
 #include "ctr_common.cuh"
 #include "host_geometry.h"
 
@@ -173,6 +174,52 @@ int ctr_device_check(void)
     if (prop.major != 10 || prop.minor != 3)
         return fail(CTR_ERR_DEVICE, "device %d is sm_%d%d; this library needs sm_103", dev,
                     prop.major, prop.minor);
+    return CTR_OK;
+}
+
+// Self-test of the bounded-wait error path (see the header): one CTA arms an
+// mbarrier for a 16-byte copy that is never issued, as a producer that
+// skipped its stage would, and waits on it with the library's bounded wait
+// under `limit_ns`; the wait runs out, the kernel raises kFlagWaitTimeout and
+// returns.  No copy is in flight when it exits.
+__global__ void selftest_wait_kernel(unsigned long long limit_ns, int* waited_out)
+{
+    __shared__ __align__(8) unsigned long long bar;
+    if (threadIdx.x == 0) {
+        mbar_init(smem_u32(&bar), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) mbar_expect_tx(smem_u32(&bar), 16);  // the copy that never comes
+    __syncthreads();
+    const bool ok = mbar_wait_bounded(smem_u32(&bar), 0, limit_ns);
+    if (!ok && threadIdx.x == 0) {
+        raise_flag(kFlagWaitTimeout);
+        *waited_out = 1;
+    }
+}
+
+int ctr_selftest_wait_timeout(unsigned long long limit_ns, cudaStream_t stream)
+{
+    if (limit_ns == 0 || limit_ns > kWaitLimitNs) return fail(CTR_ERR_INVALID_ARG, "limit_ns must be in (0, 1 s]");
+    int* waited = nullptr;
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&waited), sizeof(int), stream);
+    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "self-test: %s", cudaGetErrorString(e));
+    e = cudaMemsetAsync(waited, 0, sizeof(int), stream);
+    if (e == cudaSuccess) {
+        selftest_wait_kernel<<<1, 64, 0, stream>>>(limit_ns, waited);
+        e = cudaGetLastError();
+    }
+    int h = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, waited, sizeof(int), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    cudaFreeAsync(waited, stream);
+    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "self-test: %s", cudaGetErrorString(e));
+    unsigned int flags = 0;
+    int st = ctr_kernel_flags(&flags, 0);
+    if (st) return st;
+    if (h && (flags & kFlagWaitTimeout))
+        return fail(CTR_ERR_KERNEL, "a bounded wait gave up after %llu ns (kernel flags 0x%x)", limit_ns, flags);
     return CTR_OK;
 }
 

@@ -759,3 +759,51 @@ def fan_backprojection_2d_angle(proj, angles, img_shape, img_space, proj_shape, 
                                     float(img_offset[1]), float(img_offset[0]), float(dso),
                                     float(dsd), float(fov))
     return apply(op, proj)
+
+
+# ---- the reference's PyTorch extension functions (pytorch/bp_par_2d_ops.cc) ----
+
+_BPPAR2D_METHOD_ERROR = "Unrecognised backprojection method. Only pixdriven is available now."
+
+
+def bppar2d_prep_forward(method, ns, na, ds, orbit, offset_s, orbit_start, nx, ny, dx, dy,
+                         offset_x, offset_y, fov, device=None):
+    """ParallelBackprojection2DPixDrivenPrep as the reference's PyTorch
+    extension exposes it (pytorch/bp_par_2d_ops.cc:17-48): returns [buffer1,
+    buffer2, buffer3] = [x cos(t) double [nx][na], y sin(t) double [ny][na],
+    the prep's unused int buffer (one int)].  Same arguments and the same error
+    for any method other than "pixdriven".  The buffers are built on the CUDA
+    device (`device`, default the current one): this library has no CPU
+    implementation, where the reference extension ran the prep on the CPU."""
+    if method != "pixdriven":
+        raise RuntimeError(_BPPAR2D_METHOD_ERROR)
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+    p = ParParam(ns, na, ds, orbit, offset_s, orbit_start, nx, ny, dx, dy, offset_x, offset_y, fov)
+    buf1 = torch.empty((nx, na), dtype=torch.float64, device=dev)
+    buf2 = torch.empty((ny, na), dtype=torch.float64, device=dev)
+    buf3 = torch.zeros((1,), dtype=torch.int32, device=dev)
+    with torch.cuda.device(dev):
+        call("ctr_bp_par_2d_prep", ctypes.byref(p), _ptr(buf1), _ptr(buf2), _ptr(buf3), _stream())
+    return [buf1, buf2, buf3]
+
+
+def bppar2d_forward(input, buffer1, buffer2, buffer3, method, ns, na, ds, orbit, offset_s,
+                    orbit_start, nx, ny, dx, dy, offset_x, offset_y, fov):
+    """ParallelBackprojection2DPixDriven through the reference's PyTorch
+    extension signature (pytorch/bp_par_2d_ops.cc:50-73): `input` is a
+    sinogram [na][ns] or a batch [B][na][ns] (float32 or float64, CUDA), the
+    buffers are bppar2d_prep_forward's; returns the image [ny][nx] (or
+    [B][ny][nx]).  Raises RuntimeError for a method other than "pixdriven"."""
+    if method != "pixdriven":
+        raise RuntimeError(_BPPAR2D_METHOD_ERROR)
+    p = ParParam(ns, na, ds, orbit, offset_s, orbit_start, nx, ny, dx, dy, offset_x, offset_y, fov)
+    xb, restore = _as_batch(input, na, ns, "bppar2d_forward")
+    for b, shape in ((buffer1, (nx, na)), (buffer2, (ny, na))):
+        if (b.dtype != torch.float64 or tuple(b.shape) != shape or b.device != xb.device
+                or not b.is_contiguous()):
+            raise ValueError(f"bppar2d_forward: buffer of shape {tuple(b.shape)} {b.dtype} on "
+                             f"{b.device}; expected a contiguous {shape} float64 on {xb.device}")
+    img = torch.empty((xb.shape[0], ny, nx), dtype=xb.dtype, device=xb.device)
+    call(f"ctr_bp_par_2d_{_sfx(xb)}", ctypes.byref(p), _ptr(xb), _ptr(img), _ptr(buffer1),
+         _ptr(buffer2), _ptr(buffer3), xb.shape[0], _stream())
+    return restore(img)

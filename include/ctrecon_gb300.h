@@ -58,6 +58,15 @@ int ctr_device_check(void);
  * failed its alignment check (the kernel then skips its work).  Synchronises
  * the device. */
 int ctr_kernel_flags(unsigned int* flags, int reset);
+/* Self-test of the bounded-wait error path (no counterpart in the reference,
+ * whose GPU calls report failure as a false return after
+ * cudaDeviceSynchronize, cuda/bp_fan_2d.cu:229-230): a one-CTA kernel waits,
+ * with the same bounded mbarrier wait as the bulk-copy pipelines but a limit
+ * of limit_ns (at most 1 s), for a copy that is never issued.  The wait runs
+ * out, the kernel sets flag bit 2 and returns; the call returns
+ * CTR_ERR_KERNEL and the context stays usable.  It leaves the flag set (read
+ * and clear it with ctr_kernel_flags). */
+int ctr_selftest_wait_timeout(unsigned long long limit_ns, cudaStream_t stream);
 
 /* ---- parameter structs (field order of the reference Param structs) ---- */
 

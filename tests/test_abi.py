@@ -57,6 +57,11 @@ def test_host_validation_without_gpu(lib):
     from ct_recon_extensions_gb300 import _lib as L
     # null parameter / null buffers are rejected before any CUDA call
     assert lib.ctr_fan_weighting_f32(None, None, None, 1, None) == 1
+    assert lib.ctr_selftest_wait_timeout(0, None) == 1
+    assert lib.ctr_fp_par_2d_plan_run(None, None, None, 1, None) == 1
+    plan = ctypes.c_void_p(1)
+    assert lib.ctr_fp_par_2d_plan_create(None, None, None, None, 1, ctypes.byref(plan), None) == 1
+    assert plan.value is None
     p = L.FanWeightingParam(8, 4, 1.0, 0.0, 500.0, 1000.0, 3)
     dummy = ctypes.c_void_p(16)
     assert lib.ctr_fan_weighting_f32(ctypes.byref(p), dummy, dummy, 1, None) == 1  # bad type

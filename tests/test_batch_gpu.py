@@ -77,3 +77,37 @@ def test_batch_against_oracle():
     outs = FanFBPBatch(geoms).run(sinos)
     for o, r in zip(outs, refs):
         assert rel_l2(host(o), r) <= 1e-5
+
+
+def test_batch_config3_sizes():
+    """The plan at the batched benchmark's sizes (items of syn.batched_config_3:
+    image 256^2-1024^2, 360-2304 views, 512-1024 channels): the largest item,
+    the smallest and three others, each against the oracle's T=float FBP on two
+    strips of 16 image rows and against the single-item path on the whole
+    image."""
+    import os
+    from ct_recon_extensions_gb300 import synthetic as syn
+    from ct_recon_extensions_gb300.batch import FanFBPBatch
+    from oracle import Geom, Oracle
+    port = Oracle("port", threads=os.cpu_count() or 1)
+    items = syn.batched_config_3()
+    cost = [it["nx"] * it["ny"] * it["na"] for it in items]
+    pick = sorted({int(np.argmax(cost)), int(np.argmin(cost)), 7, 23, 41})
+    geoms = [{k: v for k, v in items[i].items() if k != "seed"} for i in pick]
+    hosts = [syn.fan_sinogram(syn.random_ellipses(items[i]["seed"]), g["na"], g["ns"], g["ds"],
+                              g["orbit"], g["dso"], g["dsd"]) for i, g in zip(pick, geoms)]
+    outs = FanFBPBatch(geoms).run([cuda(s) for s in hosts])
+    for g, s, o in zip(geoms, hosts, outs):
+        img = host(o)
+        w = weight_op(g, g["na"], 1).forward(cuda(s))
+        single = host(fan_op(g).forward(ramp_op(g, g["na"], 1).forward(w)))
+        assert rel_l2(img, single) <= TOL_PATHS
+        f = port.ramp_filter(port.fan_weighting(s, g["ds"], g["offset_s"], g["dso"], g["dsd"], 1),
+                             g["ds"], g["dsd"], 1)
+        for r0 in (g["ny"] // 4, (3 * g["ny"]) // 4):
+            k = 16
+            off_y = (g["ny"] - 1) / 2 + g["offset_y"] - r0 - (k - 1) / 2
+            gs = Geom.make(g["ns"], g["na"], g["ds"], g["orbit"], g["nx"], k, g["dx"], g["dy"],
+                           g["offset_s"], g["orbit_start"], g["offset_x"], off_y, g["dso"],
+                           g["dsd"], g["fov"])
+            assert rel_l2(img[r0:r0 + k], port.bp_fan_2d(f, gs)) <= TOL_PATHS

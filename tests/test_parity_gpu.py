@@ -73,6 +73,26 @@ def test_par_bp(name, sfx, dt):
 
 
 @pytest.mark.parametrize("sfx,dt", DT)
+def test_bppar2d_torch_binding(sfx, dt):
+    """The reference's PyTorch extension functions (pytorch/bp_par_2d_ops.cc):
+    bppar2d_prep_forward's buffers into bppar2d_forward, against the golden
+    backprojection; any method but "pixdriven" raises its error."""
+    from ct_recon_extensions_gb300 import torch_ctrecon as tc
+    c = gc.load("par")
+    g = c["geom"]
+    args = (g["ns"], g["na"], g["ds"], g["orbit"], g["offset_s"], g["orbit_start"], g["nx"],
+            g["ny"], g["dx"], g["dy"], g["offset_x"], g["offset_y"], g["fov"])
+    bufs = tc.bppar2d_prep_forward("pixdriven", *args)
+    assert tuple(bufs[0].shape) == (g["nx"], g["na"]) and tuple(bufs[1].shape) == (g["ny"], g["na"])
+    img = tc.bppar2d_forward(cuda(c[f"filtered_{sfx}"]), *bufs, "pixdriven", *args)
+    assert rel_l2(host(img), c[f"bp_{sfx}"]) <= tol(dt)
+    with pytest.raises(RuntimeError, match="Only pixdriven is available now"):
+        tc.bppar2d_prep_forward("raydriven", *args)
+    with pytest.raises(RuntimeError, match="Only pixdriven is available now"):
+        tc.bppar2d_forward(cuda(c[f"filtered_{sfx}"]), *bufs, "raydriven", *args)
+
+
+@pytest.mark.parametrize("sfx,dt", DT)
 def test_single_view(sfx, dt):
     c = gc.load("sv")
     g = c["geom"]
