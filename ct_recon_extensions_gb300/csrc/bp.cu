@@ -96,6 +96,20 @@ __device__ __forceinline__ void adj_taps(unsigned addr, float sig, float t)
     red_shared_u32(addr + 4u, static_cast<unsigned>(q1));
 }
 
+// The two taps of a parallel-beam pixel whose fixed-point value tq is an
+// integer, tb = bits(tq + 1.5*2^23) (both formed once per tile): q1 =
+// round(tq u) at j + 1 and tq - q1 at j, u = sig - round(sig) + 1/2 with the
+// half folded into the rounding constant of the FMA.
+__device__ __forceinline__ void adj_taps_int(unsigned base, float sig, float tq, unsigned tb)
+{
+    const float vb = __fadd_rn(sig, kMagic);
+    const unsigned addr = base + 4u * __float_as_uint(vb);
+    const float d = __fadd_rn(sig, -__fadd_rn(vb, -kMagic));
+    const unsigned q1b = __float_as_uint(__fmaf_rn(tq, d, __fmaf_rn(tq, 0.5f, kMagic)));
+    red_shared_u32(addr, tb - q1b);
+    red_shared_u32(addr + 4u, q1b - kMagicBits);
+}
+
 template <Geo G>
 __global__ void __launch_bounds__(kBpThreads, 2)
     bp_tile_adj(const float* __restrict__ img, float* __restrict__ grad, const double* __restrict__ t0,
@@ -159,12 +173,20 @@ __global__ void __launch_bounds__(kBpThreads, 2)
         int ex = 0;
         frexpf(__uint_as_float(m), &ex);
         const int sh = c.fx_bits - ex;  // values * 2^sh are below 2^fx_bits
-        // per pixel: the scaled value; the parallel beam also keeps round(t)
-        // as an integer (its taps do not depend on the view)
+        // per pixel: the scaled value; the parallel beam rounds it to an
+        // integer once (its taps do not depend on the view) and keeps the
+        // rounding's bit pattern
+        unsigned tbx[R], tby[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             vx[r] = any_bad ? vx[r] * c.scale : ldexpf(vx[r], sh);
             vy[r] = any_bad ? vy[r] * c.scale : ldexpf(vy[r], sh);
+            tbx[r] = __float_as_uint(__fadd_rn(vx[r], kMagic));
+            tby[r] = __float_as_uint(__fadd_rn(vy[r], kMagic));
+            if (G == Geo::kPar && !any_bad) {
+                vx[r] = __fadd_rn(__uint_as_float(tbx[r]), -kMagic);
+                vy[r] = __fadd_rn(__uint_as_float(tby[r]), -kMagic);
+            }
         }
         const float back = ldexpf(c.scale, -sh);  // fixed point -> sinogram units
 
@@ -187,7 +209,63 @@ __global__ void __launch_bounds__(kBpThreads, 2)
             const int nv = min(kViewBlock, c.na - v0);
             const FastRec* vb = views + (b - b0) % kAdjChunkBlocks * kViewBlock;
             const ViewAux* vab = vaux + (b - b0) % kAdjChunkBlocks * kViewBlock;
-            for (int j = 0; j < nv; ++j) {
+            // every view of the block on the fast path (one variant): no per-view dispatch
+            const int fv = any_bad ? -1 : block_variant(vb, nv);
+            if (fv >= 0) {
+                if constexpr (G == Geo::kPar) {
+                    for (int j = 0; j < nv; ++j) {
+                        const FastRec P = load_fast(vb + j);
+                        const unsigned base = static_cast<unsigned>(P.mode) & ~3u;
+                        if (fabsf(P.p0) * c.dxf >= fabsf(P.p1) * c.dyf) {
+                            const float xs = par_xpart(oxx, P);
+#pragma unroll
+                            for (int r = 0; r < R; ++r) adj_taps_int(base, par_sigma(xs, oyx[r], P), vx[r], tbx[r]);
+                        } else {
+                            float xs[4];
+#pragma unroll
+                            for (int q = 0; q < 4; ++q) xs[q] = par_xpart(oxy[q], P);
+#pragma unroll
+                            for (int r = 0; r < R; ++r)
+                                adj_taps_int(base, par_sigma(xs[r & 3], oyy[r >> 2], P), vy[r], tby[r]);
+                        }
+                    }
+                } else {
+                    auto fan_block = [&](auto vc) {
+                        constexpr int V = decltype(vc)::value;
+                        for (int j = 0; j < nv; ++j) {
+                            const FastRec P = load_fast(vb + j);
+                            const unsigned base = static_cast<unsigned>(P.mode) & ~3u;
+                            if (fabsf(P.p0) * c.dxf >= fabsf(P.p1) * c.dyf) {
+                                const FanX X = fan_xpart(oxx, P);
+#pragma unroll
+                                for (int r = 0; r < R; ++r) {
+                                    float w;
+                                    const float sig = fan_sigma<V>(X, oyx[r], P, c, &w);
+                                    adj_taps(base + 4u * __float_as_uint(__fadd_rn(sig, kMagic)), sig,
+                                             __fmul_rn(vx[r], w));
+                                }
+                            } else {
+                                FanX X[4];
+#pragma unroll
+                                for (int q = 0; q < 4; ++q) X[q] = fan_xpart(oxy[q], P);
+#pragma unroll
+                                for (int r = 0; r < R; ++r) {
+                                    float w;
+                                    const float sig = fan_sigma<V>(X[r & 3], oyy[r >> 2], P, c, &w);
+                                    adj_taps(base + 4u * __float_as_uint(__fadd_rn(sig, kMagic)), sig,
+                                             __fmul_rn(vy[r], w));
+                                }
+                            }
+                        }
+                    };
+                    switch (fv) {
+                        case 0: fan_block(std::integral_constant<int, 0>{}); break;
+                        case 1: fan_block(std::integral_constant<int, 1>{}); break;
+                        default: fan_block(std::integral_constant<int, 2>{}); break;
+                    }
+                }
+            }
+            for (int j = 0; j < (fv >= 0 ? 0 : nv); ++j) {
                 const FastRec F = load_fast(vb + j);
                 if (F.mode == kModeSkip) continue;
                 const int ia = v0 + j;
@@ -200,16 +278,11 @@ __global__ void __launch_bounds__(kBpThreads, 2)
                         if (xmaj) {
                             const float xs = par_xpart(oxx, P);
 #pragma unroll
-                            for (int r = 0; r < R; ++r) {
-                                const float sig = par_sigma(xs, oyx[r], P);
-                                adj_taps(base + 4u * __float_as_uint(__fadd_rn(sig, kMagic)), sig, vx[r]);
-                            }
+                            for (int r = 0; r < R; ++r) adj_taps_int(base, par_sigma(xs, oyx[r], P), vx[r], tbx[r]);
                         } else {
 #pragma unroll
-                            for (int r = 0; r < R; ++r) {
-                                const float sig = par_sigma(par_xpart(oxy[r & 3], P), oyy[r >> 2], P);
-                                adj_taps(base + 4u * __float_as_uint(__fadd_rn(sig, kMagic)), sig, vy[r]);
-                            }
+                            for (int r = 0; r < R; ++r)
+                                adj_taps_int(base, par_sigma(par_xpart(oxy[r & 3], P), oyy[r >> 2], P), vy[r], tby[r]);
                         }
                     } else {
                         auto fan_fast = [&](auto vc) {
@@ -487,6 +560,82 @@ __global__ void __launch_bounds__(kSvThreads)
             }
         }
         O[(static_cast<size_t>(iy) * nx + ix) * na + ia] = out;
+    }
+}
+
+// FP32 single-view BP: write-bound (na outputs per pixel).  A CTA owns 32
+// consecutive views (one per lane) and a band of image rows; it stages the 32
+// sinogram rows in shared memory (row stride odd, so lanes at similar
+// channels fall in different banks).  A warp task is a row segment of up to
+// kSvSeg pixels: each lane forms its view's channel position at the
+// segment's middle pixel in FP64 from the caller's tables (integer part and
+// FP32 fraction), then steps through the segment in FP32 with the view's
+// slope, so every store of the warp writes 32 consecutive views of one pixel
+// (128 contiguous bytes).  The reference's inclusion rule 0 <= s <= ns-1 is
+// decided in FP64 (src/bp_par_2d_sv.cc:55-92 arithmetic) for positions within
+// a channel of a detector end; farther out the output is 0, farther in the
+// FP32 position (within ~4e-6 channels) interpolates.
+constexpr int kSvFastThreads = 256;
+constexpr int kSvViews = 32;
+constexpr int kSvSeg = 64;
+constexpr int kSvRowsPerCta = 16;
+
+__global__ void __launch_bounds__(kSvFastThreads, 2)
+    bp_par_sv_f32(const float* __restrict__ proj, float* __restrict__ img, const double* __restrict__ xcos,
+                  const double* __restrict__ ysin, int ns, int na, int nx, int ny, double ds, double inv_ds,
+                  double cents, int stride, size_t proj_stride, size_t img_stride)
+{
+    extern __shared__ float sv_rows[];  // [kSvViews][stride]
+    const int v0 = blockIdx.x * kSvViews;
+    const int nv = min(kSvViews, na - v0);
+    const float* P = proj + blockIdx.z * proj_stride + static_cast<size_t>(v0) * ns;
+    for (int idx = threadIdx.x; idx < nv * ns; idx += kSvFastThreads) {
+        const int v = idx / ns, k = idx - v * ns;
+        sv_rows[v * stride + k] = __ldg(P + idx);
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane >= nv) return;  // no barrier follows
+    const int ia = v0 + lane;
+    const float* R = sv_rows + lane * stride;
+    // the view's channel step per pixel along x, from the caller's x cos t table
+    const float px = nx > 1 ? static_cast<float>((xcos[static_cast<size_t>(na) + ia] - xcos[ia]) * inv_ds) : 0.0f;
+    float* O = img + blockIdx.z * img_stride + ia;
+    const int y0 = blockIdx.y * kSvRowsPerCta, y1 = min(ny, y0 + kSvRowsPerCta);
+    const int segs = (nx + kSvSeg - 1) / kSvSeg;
+    for (int task = warp; task < (y1 - y0) * segs; task += kSvFastThreads / 32) {
+        const int iy = y0 + task / segs;
+        const int xs0 = (task % segs) * kSvSeg, xs1 = min(nx, xs0 + kSvSeg);
+        const int xm = (xs0 + xs1) / 2;
+        const double ys = ysin[static_cast<size_t>(iy) * na + ia];
+        const double sd0 = (xcos[static_cast<size_t>(xm) * na + ia] + ys) * inv_ds + cents;
+        const double fl0 = floor(sd0);
+        const int i0 = static_cast<int>(fl0);
+        const float f0 = static_cast<float>(sd0 - fl0);
+        float* Or = O + static_cast<size_t>(iy) * nx * na;
+        for (int ix = xs0; ix < xs1; ++ix) {
+            const float sr = fmaf(static_cast<float>(ix - xm), px, f0);
+            const float fr = floorf(sr);
+            int j = i0 + static_cast<int>(fr);
+            float u = sr - fr;
+            float out = 0.0f;
+            bool in = j >= 1 && j <= ns - 3;
+            if (!in && j >= -1 && j <= ns) {
+                // within a channel of an end: the reference's FP64 decision
+                const double sd = (xcos[static_cast<size_t>(ix) * na + ia] + ys) / ds + cents;
+                in = sd >= 0.0 && sd <= static_cast<double>(ns - 1);
+                if (in) {
+                    const double f = floor(sd);
+                    j = static_cast<int>(f);
+                    u = static_cast<float>(sd - f);
+                }
+            }
+            if (in) {
+                const float a = R[j], b = R[min(j + 1, ns - 1)];
+                out = fmaf(u, b - a, a);
+            }
+            Or[static_cast<size_t>(ix) * na] = out;
+        }
     }
 }
 
@@ -844,6 +993,20 @@ int par_single_view(const ctr_par_param* p, const T* proj, T* img, const double*
     int st = check_par(p, proj, img, xcos, ysin, batch);
     if (st) return st;
     const double cents = (p->ns - 1) / 2.0 + p->offset_s;
+    if constexpr (sizeof(T) == 4) {
+        const int stride = static_cast<int>(p->ns) | 1;
+        const size_t smem = sizeof(float) * kSvViews * static_cast<size_t>(stride);
+        if (smem <= 220 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(bp_par_sv_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 static_cast<int>(smem));
+            if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "bp_par_2d_sv: %s", cudaGetErrorString(e));
+            dim3 g2(div_up(p->na, kSvViews), div_up(p->ny, kSvRowsPerCta), batch);
+            bp_par_sv_f32<<<g2, kSvFastThreads, smem, stream>>>(
+                proj, img, xcos, ysin, p->ns, p->na, p->nx, p->ny, p->ds, 1.0 / p->ds, cents, stride,
+                static_cast<size_t>(p->ns) * p->na, static_cast<size_t>(p->nx) * p->ny * p->na);
+            return check_launch("bp_par_2d_sv");
+        }
+    }
     dim3 grid(div_up(p->nx, kSvPix), p->ny, batch);
     bp_par_sv<T><<<grid, kSvThreads, 0, stream>>>(proj, img, xcos, ysin, p->ns, p->na, p->nx,
                                                   p->ny, p->ds, cents,

@@ -338,6 +338,30 @@ def test_parallel_config2_white_noise(oracle_port):
     assert rel_l2(rec, ref) <= 1e-5  # measured ~1.5e-6
 
 
+def test_single_view_config2_strips(oracle_port):
+    """bp_par_2d_sv at config 2 (720 views x 729 bins -> 512 x 512 x 720) on a
+    white-noise sinogram: two strips of 8 image rows against the reference's
+    CPU algorithm (T=float), plus the image's outer rows, where pixels reach
+    the detector ends."""
+    import torch
+    from oracle import Geom
+    from ct_recon_extensions_gb300 import synthetic as syn
+    d = syn.parallel_config_2()
+    sino = np.random.default_rng(19).standard_normal((d["na"], d["ns"])).astype(np.float32)
+    out = par_op(d).single_view(cuda(sino))[0]
+    for r0 in (0, 200, 504):
+        k = 8
+        off_y = (d["ny"] - 1) / 2 + d["offset_y"] - r0 - (k - 1) / 2
+        gs = Geom.make(d["ns"], d["na"], d["ds"], d["orbit"], d["nx"], k, d["dx"], d["dy"], d["offset_s"],
+                       d["orbit_start"], d["offset_x"], off_y, -1.0, -1.0, d["fov"])
+        ref = oracle_port.bp_par_2d_sv(sino, gs)
+        got = out[r0:r0 + k].cpu().numpy()
+        assert got.shape == ref.shape
+        assert rel_l2(got, ref) <= 1e-5
+    del out
+    torch.cuda.empty_cache()
+
+
 def test_fp_ray_casting_config2(oracle_port):
     """Ray casting at 512^2 (0.5 mm) -> 720 views x 729 bins over pi, FoV radius
     128 mm, step 0.125 pixel, against the oracle (~1.7e9 samples), and a batch
