@@ -575,7 +575,7 @@ __global__ void __launch_bounds__(kSvThreads)
 // decided in FP64 (src/bp_par_2d_sv.cc:55-92 arithmetic) for positions within
 // a channel of a detector end; farther out the output is 0, farther in the
 // FP32 position (within ~4e-6 channels) interpolates.
-constexpr int kSvFastThreads = 256;
+constexpr int kSvFastThreads = 512;
 constexpr int kSvViews = 32;
 constexpr int kSvSeg = 64;
 constexpr int kSvRowsPerCta = 16;
@@ -601,6 +601,7 @@ __global__ void __launch_bounds__(kSvFastThreads, 2)
     // the view's channel step per pixel along x, from the caller's x cos t table
     const float px = nx > 1 ? static_cast<float>((xcos[static_cast<size_t>(na) + ia] - xcos[ia]) * inv_ds) : 0.0f;
     float* O = img + blockIdx.z * img_stride + ia;
+    const size_t ostep = static_cast<size_t>(na);
     const int y0 = blockIdx.y * kSvRowsPerCta, y1 = min(ny, y0 + kSvRowsPerCta);
     const int segs = (nx + kSvSeg - 1) / kSvSeg;
     for (int task = warp; task < (y1 - y0) * segs; task += kSvFastThreads / 32) {
@@ -611,13 +612,33 @@ __global__ void __launch_bounds__(kSvFastThreads, 2)
         const double sd0 = (xcos[static_cast<size_t>(xm) * na + ia] + ys) * inv_ds + cents;
         const double fl0 = floor(sd0);
         const int i0 = static_cast<int>(fl0);
-        const float f0 = static_cast<float>(sd0 - fl0);
-        float* Or = O + static_cast<size_t>(iy) * nx * na;
-        for (int ix = xs0; ix < xs1; ++ix) {
-            const float sr = fmaf(static_cast<float>(ix - xm), px, f0);
-            const float fr = floorf(sr);
-            int j = i0 + static_cast<int>(fr);
-            float u = sr - fr;
+        // positions less (i0 + 1/2), so that rounding gives the floor
+        const float fh = static_cast<float>(sd0 - fl0) - 0.5f;
+        float* Or = O + (static_cast<size_t>(iy) * nx + xs0) * ostep;
+        // the position is linear along the segment: interior when both ends are
+        // at least a channel inside the detector
+        const float ka = static_cast<float>(xs0 - xm), kb = static_cast<float>(xs1 - 1 - xm);
+        const int ja = i0 + static_cast<int>(floorf(fmaf(ka, px, fh) + 0.5f));
+        const int jb = i0 + static_cast<int>(floorf(fmaf(kb, px, fh) + 0.5f));
+        if (min(ja, jb) >= 1 && max(ja, jb) <= ns - 3) {
+            float kf = ka;
+#pragma unroll 4
+            for (int ix = xs0; ix < xs1; ++ix, kf += 1.0f, Or += ostep) {
+                const float sr = fmaf(kf, px, fh);
+                const float vb = __fadd_rn(sr, kMagic);
+                const int j = i0 + static_cast<int>(__float_as_uint(vb) - kMagicBits);
+                const float u = __fadd_rn(__fadd_rn(sr, -__fadd_rn(vb, -kMagic)), 0.5f);
+                const float a = R[j], b = R[j + 1];
+                *Or = fmaf(u, b - a, a);
+            }
+            continue;
+        }
+        float kf = ka;
+        for (int ix = xs0; ix < xs1; ++ix, kf += 1.0f, Or += ostep) {
+            const float sr = fmaf(kf, px, fh);
+            const float vb = __fadd_rn(sr, kMagic);
+            int j = i0 + static_cast<int>(__float_as_uint(vb) - kMagicBits);
+            float u = __fadd_rn(__fadd_rn(sr, -__fadd_rn(vb, -kMagic)), 0.5f);
             float out = 0.0f;
             bool in = j >= 1 && j <= ns - 3;
             if (!in && j >= -1 && j <= ns) {
@@ -634,7 +655,7 @@ __global__ void __launch_bounds__(kSvFastThreads, 2)
                 const float a = R[j], b = R[min(j + 1, ns - 1)];
                 out = fmaf(u, b - a, a);
             }
-            Or[static_cast<size_t>(ix) * na] = out;
+            *Or = out;
         }
     }
 }
