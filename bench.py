@@ -1182,7 +1182,7 @@ def run_reference(args):
         return
     import oracle
     try:
-        oracle.build(ref=False)
+        oracle.build(ref_src="")
     except Exception as e:  # pragma: no cover
         print(json.dumps({"impl": "reference", "unavailable": f"oracle build failed: {e}"}))
         return

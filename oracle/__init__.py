@@ -32,7 +32,6 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(_HERE, "libctr_oracle.so")
 REF_LIB = os.path.join(_HERE, "_ref", "libctr_ref.so")
-REFERENCE_SRC = "/root/reference"
 
 _c_uint = ctypes.c_uint
 _c_double = ctypes.c_double
@@ -93,12 +92,15 @@ class HelicalError(RuntimeError):
         self.code = code
 
 
-def build(ref: bool | None = None, quiet: bool = True) -> None:
-    """Compile the port (always) and the reference build (when the reference
-    checkout exists, or when ``ref`` is True)."""
+def build(ref_src: str | None = None, quiet: bool = True) -> None:
+    """Compile the port (always) and, when ``ref_src`` (default: the
+    environment variable CTR_REFERENCE_SRC) names a reference checkout with its
+    ``src/`` directory, the reference build from that checkout."""
+    if ref_src is None:
+        ref_src = os.environ.get("CTR_REFERENCE_SRC")
     targets = ["all"]
-    if ref or (ref is None and os.path.isdir(os.path.join(REFERENCE_SRC, "src"))):
-        targets.append("ref")
+    if ref_src and os.path.isdir(os.path.join(ref_src, "src")):
+        targets += ["ref", f"REF={ref_src}"]
     out = subprocess.run(["make", "-C", _HERE, *targets], capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
