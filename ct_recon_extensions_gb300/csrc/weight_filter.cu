@@ -17,10 +17,15 @@
 // the output is a small difference of large partial sums.  The FP32 kernel
 // therefore accumulates h[o-j] (x[j] - c) with c a value of the row near the
 // thread's outputs, and adds back c (h[0] + sum of the taps that output o
-// sums), formed in FP64 from the FP64 taps (prefix sums by one extra warp
-// while the others start their sums):
+// sums):
 //   out[o] = h[0] (x[o] - c) + c D[o] + sum_j h[o-j] (x[j] - c),
-//   D[o] = h[0] + sum_{j of the other parity} h[o-j].
+//   D[o] = h[0] + sum_{j of the other parity} h[o-j]
+//        = C - P(o+1) - Q(n-o),
+// C = h[0] + the sum of every odd tap the filter reaches (offsets up to
+// n-1 either way; it nearly cancels: formed in FP64 from the caller's taps),
+// P(a) and Q(b) the sums of the odd taps at offsets >= a and <= -b (tails of
+// small same-signed taps: FP32 suffix sums of the staged taps).  One extra
+// warp forms C, P and Q while the others start their sums.
 // Partial sums then stay near the size of the result (on a 2304 x 1472 fan
 // sinogram: 1.3e-5 -> ~1e-6 from FP64).
 #include "ctr_common.cuh"
@@ -127,18 +132,19 @@ __host__ __device__ inline int tap_words(unsigned ns, int tg)
     return tap_slot(2 * static_cast<int>(ns) + 2 * kFilterPad, tg);
 }
 
-// Shared layout (FP32): the FP64 prefix sums of the odd taps [2 ns] (see
-// filter_rows), then the taps H[-(ns-1) - kFilterPad .. ns - 1 + kFilterPad]
-// (taps * ds), then xs[kRows][ns], then the second halves' sums
-// [kRows][tasks][4].  FP64 has no prefix sums.
+// Shared layout (FP32): the tail sums P and Q of the odd taps [2][ns/2 + 2]
+// and C (see filter_rows), then the taps H[-(ns-1) - kFilterPad .. ns - 1 +
+// kFilterPad] (taps * ds), then xs[kRows][ns], then the second halves' sums
+// [kRows][tasks][4].  FP64 has no tail sums.
+__host__ __device__ inline size_t filter_tail_bytes(unsigned ns) { return (2 * (ns / 2 + 2) + 4) * sizeof(float); }
 template <typename T>
 __host__ __device__ inline size_t filter_smem(unsigned ns, int rows, int tg)
 {
-    return (sizeof(T) == 4 ? 2 * sizeof(double) * ns : 0) +
+    return (sizeof(T) == 4 ? filter_tail_bytes(ns) : 0) +
            sizeof(T) * (static_cast<size_t>(tap_words(ns, tg)) + static_cast<size_t>(rows) * ns +
                         static_cast<size_t>(rows) * filter_tasks(ns) * 4);
 }
-// The FP32 kernels run one more warp, which forms the prefix sums.
+// The FP32 kernels run one more warp, which forms C and the tail sums.
 template <typename T>
 __host__ __device__ inline int filter_block(unsigned ns)
 {
@@ -191,13 +197,17 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
 {
     constexpr bool kCentred = sizeof(T) == 4;
     const int n = static_cast<int>(ns);
-    double* Ash = reinterpret_cast<double*>(smem_raw);  // FP32: prefix sums [2n]
-    T* H0 = reinterpret_cast<T*>(smem_raw + (kCentred ? 2 * sizeof(double) * n : 0));
+    // FP32: the tail sums P [ns/2 + 2], Q [ns/2 + 2], then C
+    const int nodd = n / 2;  // odd offsets in [1, n-1]
+    float* Pt = reinterpret_cast<float*>(smem_raw);
+    float* Qt = Pt + nodd + 2;
+    float* Cs = Qt + nodd + 2;
+    T* H0 = reinterpret_cast<T*>(smem_raw + (kCentred ? filter_tail_bytes(ns) : 0));
     const int d0 = (n - 1) + kFilterPad;  // tap d sits at H0[tap_slot(d + d0, tg)]
     auto H = [&](int d) -> T { return H0[tap_slot(d + d0, tg)]; };
     T* xs = H0 + tap_words(ns, tg);
     __shared__ int s_even;
-    // the task threads; an FP32 block has one more warp (the prefix sums)
+    // the task threads; an FP32 block has one more warp (C and the tail sums)
     const int nthr = kCentred ? static_cast<int>(blockDim.x) - 32 : static_cast<int>(blockDim.x);
 
     const double* h = filter + ns;  // h[k], k in [-ns, ns]
@@ -215,16 +225,6 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
             if (d != 0 && (d & 1) == 0 && v != 0.0) even = true;
         }
         if (even) s_even = 1;
-        if constexpr (kCentred) {
-            // Ash[m + 1] = the FP64 tap at offset k = m - (n-1) (odd k only),
-            // summed into prefix sums below
-#pragma unroll 4
-            for (int m = threadIdx.x; m < 2 * n - 1; m += blockDim.x) {
-                const int k = m - (n - 1);
-                Ash[m + 1] = (k & 1) ? (kGrad ? h[-k] : h[k]) * ds : 0.0;
-            }
-            if (threadIdx.x == 0) Ash[0] = 0.0;
-        }
 #pragma unroll 4
         for (int idx = threadIdx.x; idx < kRows * n; idx += blockDim.x) {
             const int r = idx / n, j = idx - r * n;
@@ -238,39 +238,51 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
     }
     __syncthreads();
     if (kCentred && static_cast<int>(threadIdx.x) >= nthr) {
-        // the extra warp: Ash[m] becomes the sum of the odd taps at offsets up
-        // to m - n (in FP64, from shared memory), while the task threads start
-        // their sums; then the taps output o sums (offsets o - n + 1 .. o) add
-        // up to Ash[o + n] - Ash[o]
-        const int lane = threadIdx.x & 31;
-        const int L = 2 * n - 1, C = (L + 31) / 32;
-        const int m0 = min(lane * C, L), m1 = min(m0 + C, L);
-        double sum = 0.0;
-        for (int m = m0; m < m1; ++m) sum += Ash[m + 1];
-        double p = sum;
+        // the extra warp, while the task threads start their sums.  Lanes 0-15
+        // form P (positive offsets), lanes 16-31 Q (negative offsets): entry i
+        // is the sum of the staged taps at odd offsets +-(2i+1) .. +-(n-1),
+        // added from the far (small) end; entry nodd is 0.
+        const int lane = threadIdx.x & 31, sl = lane & 15;
+        const int sg = lane < 16 ? 1 : -1;
+        float* A = lane < 16 ? Pt : Qt;
+        const int C16 = (nodd + 15) / 16;
+        const int i0 = min(sl * C16, nodd), i1 = min(i0 + C16, nodd);
+        float tot = 0.0f;
+        for (int i = i1 - 1; i >= i0; --i) tot += H(sg * (2 * i + 1));
+        float suf = tot;  // inclusive suffix over this half's lanes
 #pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            const double v = __shfl_up_sync(0xffffffffu, p, off);
-            if (lane >= off) p += v;
+        for (int off = 1; off < 16; off <<= 1) {
+            const float v = __shfl_down_sync(0xffffffffu, suf, off, 16);
+            if (sl + off < 16) suf += v;
         }
-        p -= sum;  // exclusive: the sum of the earlier lanes' chunks
-        for (int m = m0; m < m1; ++m) {
-            p += Ash[m + 1];
-            Ash[m + 1] = p;
+        suf -= tot;
+        for (int i = i1 - 1; i >= i0; --i) {
+            suf += H(sg * (2 * i + 1));
+            A[i] = suf;
         }
+        if (sl == 0) A[nodd] = A[nodd + 1] = 0.0f;
+        // C in FP64 from the caller's taps
+        double cs = 0.0;
+        for (int i = lane; i < nodd; i += 32) {
+            const int k = 2 * i + 1;
+            cs += kGrad ? h[-k] + h[k] : h[k] + h[-k];
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) cs += __shfl_xor_sync(0xffffffffu, cs, off);
+        if (lane == 0) Cs[0] = static_cast<float>((h[0] + cs) * ds);
     }
     // the single-thread-per-task path writes outputs as it goes: it needs the
     // sums first
     if (kCentred && !filter_split(ns)) __syncthreads();
+    // D[o] (FP32 kernels), once per output
+    auto dcorr = [&](int o) -> T {
+        if constexpr (kCentred) return Cs[0] - Pt[(o + 1) / 2] - Qt[(n - o) / 2];
+        else return T(0);
+    };
     // output o of a thread whose reference value is c (FP32: centred sums)
-    const double h0d = kCentred ? h[0] * ds : 0.0;
-    auto finish = [&](int o, int r, T c, T acc) -> T {
-        if constexpr (kCentred) {
-            const T D = static_cast<T>(h0d + (Ash[o + n] - Ash[o]));
-            return fma_t(H(0), xs[r * n + o] - c, fma_t(c, D, acc));
-        } else {
-            return fma_t(H(0), xs[r * n + o], acc);
-        }
+    auto finish = [&](int o, int r, T c, T D, T acc) -> T {
+        if constexpr (kCentred) return fma_t(H(0), xs[r * n + o] - c, fma_t(c, D, acc));
+        else return fma_t(H(0), xs[r * n + o], acc);
     };
     // reference value of a task's rows: the input next to its outputs
     auto refs = [&](int i0, T (&cr)[kRows]) {
@@ -311,10 +323,11 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
             for (int m = 0; m < 4; ++m) {
                 const int o = i0 + 2 * m;
                 if (o >= n) continue;
+                const T D = dcorr(o);
 #pragma unroll
                 for (int r = 0; r < kRows; ++r)
                     if (r < nr)
-                        out[(r0 + r) * ns + o] = finish(o, r, cr[r], acc[r][m] + red[(r * groups + g) * 4 + m]);
+                        out[(r0 + r) * ns + o] = finish(o, r, cr[r], D, acc[r][m] + red[(r * groups + g) * 4 + m]);
             }
         }
     } else if (!s_even) {
@@ -333,9 +346,10 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
             for (int m = 0; m < 4; ++m) {
                 const int o = i0 + 2 * m;
                 if (o >= n) continue;
+                const T D = dcorr(o);
 #pragma unroll
                 for (int r = 0; r < kRows; ++r)
-                    if (r < nr) out[(r0 + r) * ns + o] = finish(o, r, cr[r], acc[r][m]);
+                    if (r < nr) out[(r0 + r) * ns + o] = finish(o, r, cr[r], D, acc[r][m]);
             }
         }
     } else {
