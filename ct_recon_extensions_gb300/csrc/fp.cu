@@ -54,6 +54,27 @@ __device__ __forceinline__ float frac_of(long long X)
     return __uint_as_float(0x3F800000u | (static_cast<unsigned>(X) >> 9)) - 1.0f;
 }
 
+// 1 + frac(X) on the FMA pipe: the fraction's top 23 bits as a mantissa in
+// one integer multiply-add, (lo * 2^23) >> 32 plus the bits of 1.0.  `m` (2^23)
+// and `one` (0x3F800000) are run-time registers (see fpx_regs), so the multiply
+// is not turned back into a shift on the half-rate integer ALU pipe, which the
+// 64-bit position step and the address already load.
+__device__ __forceinline__ float one_plus_frac(long long X, unsigned m, unsigned one)
+{
+    unsigned b;
+    asm("mad.hi.u32 %0, %1, %2, %3;" : "=r"(b) : "r"(static_cast<unsigned>(X)), "r"(m), "r"(one));
+    return __uint_as_float(b);
+}
+
+// Packed FP32 pairs: __fadd2_rn / __ffma2_rn (Blackwell FADD2 / FFMA2, two
+// IEEE round-to-nearest operations in one instruction, independent halves).
+// A difference is an FMA with -1 (exact negation, one rounding: the same as
+// a subtraction).
+__device__ __forceinline__ float2 f2_sub(float2 a, float2 b)
+{
+    return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
+}
+
 // A CTA projects `views` consecutive views (all channels).  Rays of row-marching
 // views (usex) and of column-marching views are run in separate passes; each
 // pass stages the image in bands of `band` rows (or columns, stored transposed)
@@ -158,31 +179,39 @@ __global__ void __launch_bounds__(kFpThreads)
 // consecutive channels, one ray per lane (lane = 8*view + channel), so a
 // warp's 32 samples of one row fall within a few pixels of each other.  Slots
 // are ordered view quad by view quad, and within a quad the channel octets in
-// a strided order (slot_octet), so a contiguous range of slots mixes long
-// central rays and short edge rays.  Each class gets CTAs in proportion to its
-// views and cuts its slots into equal ranges, and a CTA deals its slots, sorted
-// by their exact sample counts, to its warps in snake order.  A round holds up
-// to kFpxRound slots (one more round streams the image again; rare).
+// a strided order (slot_octet).  Each class gets CTAs (one an SM) in
+// proportion to its views, and the G CTAs of a class take its slots in turn
+// (CTA i: slots i, i + G, ...), so each CTA holds long central and short edge
+// rays of views across the class's whole angular range; a CTA deals its
+// slots, sorted by their exact sample counts, to its warps in snake order.  A
+// round holds up to kFpxRound slots (one more round streams the image again;
+// rare).
 //
 // Pipeline: a producer lane copies band t (one contiguous range of the staged
 // row-major array, one TMA bulk copy) into stage t % 3 once every consumer
 // warp has released that stage, so warps drift up to two bands apart instead
-// of meeting at a CTA barrier per band.  Within a band a sample costs one
-// 64-bit add, the address, two shared loads, the fraction and two FP32
-// operations: the position's high word indexes the stage directly
-// (S2 = S + n * 2^32 steps one row down).
+// of meeting at a CTA barrier per band.  One CTA of 19 consumer warps (6
+// slots each) and a producer warp runs on each SM, with three 64 KB stages.
+// Within a band a sample costs one 64-bit add, the address, two shared loads,
+// the fraction (one integer multiply-add on the FMA pipe) and two FP32
+// operations, packed two rows to an instruction: the position's high word
+// indexes the stage directly (S2 = S + n * 2^32 steps one row down).  A band
+// is walked in chunks of CH rows, slot by slot, with warp-uniform decisions: a slot none of whose rays
+// reaches the band is skipped, a chunk every ray of the slot covers runs
+// unrolled without tests, and only chunks where some ray starts or ends test
+// each row against the lane's range.
 //
 // Ties: a ray whose end sample lies within a hair of the image border (where
 // the fixed-point rule might differ from the reference's accumulated FP64
 // one) streams only its certain samples; the set-up decides its few border
 // samples by the reference's accumulation (acc_advance) and the ray's lane
 // adds the ones found inside, read from global memory, before writing.
-constexpr int kFpxWarps = 9;                         // consumer warps
+constexpr int kFpxWarps = 19;                        // consumer warps (one CTA an SM)
 constexpr int kFpxThreads = (kFpxWarps + 1) * 32;    // + one producer warp
-constexpr int kFpxSlots = 8;                         // ray slots per consumer lane and round
+constexpr int kFpxSlots = 6;                         // ray slots per consumer lane and round
 constexpr int kFpxRound = kFpxWarps * kFpxSlots;     // slots per round
 constexpr int kFpxStages = 3;
-constexpr int kFpxStageFloats = 8192;                // nominal stage: 32 KB
+constexpr int kFpxStageFloats = 16384;               // nominal stage: 64 KB
 constexpr int kFpxEmpty = 3 << 30;                   // ray code of a ray with no sample
 constexpr int kFpxMaxTies = 8192;                    // tie rays per call
 constexpr int kFpxSetupThreads = 256;
@@ -200,6 +229,8 @@ struct FpxConst {
     size_t proj_stride;
     float dx, dy;
     int sms;               // SMs of the device
+    unsigned frac_mul;     // 2^23 (one_plus_frac)
+    unsigned frac_one;     // 0x3F800000, the bits of 1.0f (one_plus_frac)
 };
 
 // Global tie entry (a ray the fixed-point rule could not settle).
@@ -217,7 +248,7 @@ struct FpxRays {
     int* code;       // [na*ns] k0 | k1 << 15 | class << 30, or kFpxEmpty
     int* tie;        // [na*ns] index into ties, or -1
     int* views;      // [4 * (quads + 2)] views of class 0, then of class 1, -1 padded to quads
-    int* cuts;       // [ctas + 1] first slot of every CTA; cuts[ctas + 1] = CTAs of class 0
+    int* cuts;       // [3]: CTAs of class 0, slots of class 0, slots of class 1
     FpxTie* ties;    // [kFpxMaxTies]
     int* nties;      // count (zeroed before fpx_setup)
 };
@@ -338,21 +369,19 @@ __global__ void __launch_bounds__(kFpxSetupThreads)
         }
         for (int i = N0 + tid; i < 4 * Q0; i += kFpxSetupThreads) r.views[i] = -1;
         for (int i = 4 * Q0 + N1 + tid; i < 4 * Qt; i += kFpxSetupThreads) r.views[i] = -1;
-        // CTAs per class in proportion to its views, each class cut into equal
-        // slot ranges (a view costs about the same at every angle: fewer samples
-        // at 45 degrees, but longer shared-memory and lane waits)
+        // CTAs per class in proportion to its views; a class's CTAs take its
+        // slots in turn (CTA i of G: slots i, i + G, i + 2G, ...), so every CTA
+        // holds views of the class's whole angular range (the samples of a
+        // view scale with |cos| or |sin| of its angle) and all CTAs carry about
+        // the same work
         int G0 = 0;
         if (N0 > 0) G0 = N1 > 0 ? static_cast<int>(rintf(static_cast<float>(c.ctas) * N0 / c.na)) : c.ctas;
         if (N0 > 0 && N1 > 0) G0 = max(1, min(c.ctas - 1, G0));
-        const int G1 = c.ctas - G0;
-        for (int i = tid; i <= c.ctas; i += kFpxSetupThreads) {
-            const bool cls1 = i > G0 || (i == G0 && G0 == 0);
-            const long long gi = cls1 ? i - G0 : i, G = cls1 ? G1 : G0;
-            const long long s0 = static_cast<long long>(cls1 ? Q0 : 0) * c.octets;
-            const long long ns_ = static_cast<long long>(cls1 ? Q1 : Q0) * c.octets;
-            r.cuts[i] = static_cast<int>(s0 + (G > 0 ? (gi * ns_) / G : 0));
+        if (tid == 0) {
+            r.cuts[0] = G0;
+            r.cuts[1] = Q0 * c.octets;  // slots of class 0 (class 1 starts there)
+            r.cuts[2] = Q1 * c.octets;  // slots of class 1
         }
-        if (tid == 0) r.cuts[c.ctas + 1] = G0;
     }
     const int rays = c.na * c.ns;
     for (int ray = blockIdx.x * kFpxSetupThreads + tid; ray < rays; ray += setup_blocks * kFpxSetupThreads) {
@@ -397,7 +426,8 @@ __global__ void __launch_bounds__(kFpxSetupThreads)
     }
 }
 
-__global__ void __launch_bounds__(kFpxThreads, 2)
+template <int CH>
+__global__ void __launch_bounds__(kFpxThreads, 1)
     fp_proj_f32(const float* __restrict__ img, const float* __restrict__ imgT,
                 float* __restrict__ proj, const FpxConst c, const FpxRays r)
 {
@@ -412,8 +442,12 @@ __global__ void __launch_bounds__(kFpxThreads, 2)
     const int n = c.n;
     const long long item0 = static_cast<long long>(blockIdx.y) * n * n;
     const float* I = img + item0;
-    const int q_lo = r.cuts[blockIdx.x], q_hi = r.cuts[blockIdx.x + 1];
-    const bool cls1 = static_cast<int>(blockIdx.x) >= r.cuts[c.ctas + 1];
+    // this CTA's slots: ci, ci + G, ci + 2G, ... of its class (count of them)
+    const int G0 = r.cuts[0];
+    const bool cls1 = static_cast<int>(blockIdx.x) >= G0;
+    const int G = cls1 ? c.ctas - G0 : G0, ci = static_cast<int>(blockIdx.x) - (cls1 ? G0 : 0);
+    const int s0 = (cls1 ? r.cuts[1] : 0) + ci, ncls = cls1 ? r.cuts[2] : r.cuts[1];
+    const int count = ci < ncls ? (ncls - 1 - ci) / G + 1 : 0;
     const float* src = cls1 ? imgT : img;  // the staged array: rows are the marched lines
     if (tid == 0) {
         s_abort = 0;
@@ -425,14 +459,14 @@ __global__ void __launch_bounds__(kFpxThreads, 2)
     }
 
     int g = 0;  // band instances so far (producer and consumers count alike)
-    for (int base = q_lo; base < q_hi; base += kFpxRound) {
-        const int m = min(kFpxRound, q_hi - base);
+    for (int base = 0; base < count; base += kFpxRound) {
+        const int m = min(kFpxRound, count - base);
         for (int i = tid; i < kFpxRound; i += kFpxThreads) (&s_assign[0][0])[i] = -1;
         // ---- sample counts of the round's slots
         if (warp < kFpxWarps) {
             for (int t = warp; t < m; t += kFpxWarps) {
                 int ia, is, cnt = 0;
-                slot_ray(static_cast<unsigned>(base + t), lane, c, r.views, &ia, &is);
+                slot_ray(static_cast<unsigned>(s0 + (base + t) * G), lane, c, r.views, &ia, &is);
                 if (ia >= 0 && is < c.ns) {
                     const int code = r.code[ia * c.ns + is];
                     if (code != kFpxEmpty) cnt = ((code >> 15) & 0x7FFF) - (code & 0x7FFF) + 1;
@@ -503,7 +537,7 @@ __global__ void __launch_bounds__(kFpxThreads, 2)
                 const int t = s_assign[warp][j];
                 if (t >= 0) {
                     int ia, is;
-                    slot_ray(static_cast<unsigned>(base + t), lane, c, r.views, &ia, &is);
+                    slot_ray(static_cast<unsigned>(s0 + (base + t) * G), lane, c, r.views, &ia, &is);
                     if (ia >= 0 && is < c.ns) {
                         const int ray = ia * c.ns + is;
                         code[j] = r.code[ray];
@@ -514,6 +548,11 @@ __global__ void __launch_bounds__(kFpxThreads, 2)
             }
             int g1 = g;
             bool alive = true;
+            // constants of one_plus_frac held in registers: a value that came
+            // through a shuffle is not re-read from the constant bank per use
+            const unsigned fm = __shfl_sync(0xffffffffu, c.frac_mul, 0);
+            const unsigned f1 = __shfl_sync(0xffffffffu, c.frac_one, 0);
+            const float2 mone2 = make_float2(-1.0f, -1.0f);
             for (int t = 0; t < c.nbands; ++t, ++g1) {
                 const int s = g1 % kFpxStages;
                 int ok = 1;
@@ -532,21 +571,55 @@ __global__ void __launch_bounds__(kFpxThreads, 2)
                 const float* bb = stage + s * c.stage_floats + (g0 & 3ll);
 #pragma unroll
                 for (int j = 0; j < kFpxSlots; ++j) {
+                    // the lane's ray range [k0, k1] (empty: k0 above every row)
                     const int cj = code[j];
-                    if (cj == kFpxEmpty) continue;
-                    const int ka = max(cj & 0x7FFF, b0), kb = min((cj >> 15) & 0x7FFF, b1);
-                    if (ka > kb) continue;
-                    long long x = X0[j] + static_cast<long long>(ka) * S[j] +
-                                  (static_cast<long long>((ka - b0) * n) << 32);
+                    const int k0 = cj == kFpxEmpty ? 0x7FFF : (cj & 0x7FFF), k1 = (cj >> 15) & 0x7FFF;
+                    if (!__any_sync(0xffffffffu, k0 <= b1 && k1 >= b0)) continue;
+                    // sample b0 at row 0 of the band; a row step adds n to the word
+                    // offset, so the integer part is the staged index
+                    long long x = X0[j] + static_cast<long long>(b0) * S[j];
                     const long long S2 = S[j] + (static_cast<long long>(n) << 32);
                     float a = 0.0f, b = 0.0f;  // this band's partial sums (blocked summation)
+                    for (int r0 = b0; r0 <= b1; r0 += CH) {
+                        if (__all_sync(0xffffffffu, k0 <= r0 && k1 >= r0 + CH - 1)) {
+                            // every lane's ray covers the chunk: no per-sample test.
+                            // Even and odd rows run as two independent chains
+                            // (positions and sums) whose FP32 work is packed in
+                            // pairs (even row in .x), unrolled by 4 row pairs only:
+                            // every slot's fully unrolled chunk would outgrow the
+                            // instruction cache.
+                            long long xo = x + S2;
+                            const long long S4 = S2 + S2;
+                            float2 a2 = make_float2(0.0f, 0.0f), b2 = a2;
 #pragma unroll 4
-                    for (int k = ka; k <= kb; ++k) {
-                        const float* p = bb + static_cast<int>(x >> 32);
-                        const float p0 = p[0], p1 = p[1];
-                        a += p0;
-                        b = fmaf(frac_of(x), p1 - p0, b);
-                        x += S2;
+                            for (int r = 0; r < CH; r += 2) {
+                                const float* pe = bb + static_cast<int>(x >> 32);
+                                const float* po = bb + static_cast<int>(xo >> 32);
+                                const float2 p0 = make_float2(pe[0], po[0]);
+                                const float2 p1 = make_float2(pe[1], po[1]);
+                                const float2 u = __fadd2_rn(
+                                    make_float2(one_plus_frac(x, fm, f1), one_plus_frac(xo, fm, f1)), mone2);
+                                a2 = __fadd2_rn(a2, p0);
+                                b2 = __ffma2_rn(u, f2_sub(p1, p0), b2);
+                                x += S4;
+                                xo += S4;
+                            }
+                            a += a2.x + a2.y;
+                            b += b2.x + b2.y;
+                        } else {
+                            // the lane's own rows of the chunk (a divergent loop)
+                            const int ka = max(k0, r0), kb = min(k1, r0 + CH - 1);
+                            long long y = x + static_cast<long long>(ka - r0) * S2;
+#pragma unroll 1
+                            for (int k = ka; k <= kb; ++k) {
+                                const float* p = bb + static_cast<int>(y >> 32);
+                                const float p0 = p[0], p1 = p[1];
+                                a += p0;
+                                b = fmaf(one_plus_frac(y, fm, f1) - 1.0f, p1 - p0, b);
+                                y += S2;
+                            }
+                            x += static_cast<long long>(CH) * S2;
+                        }
                     }
                     sum[j] += a + b;
                 }
@@ -559,7 +632,7 @@ __global__ void __launch_bounds__(kFpxThreads, 2)
                 const int t = s_assign[warp][j];
                 if (!alive || t < 0) continue;
                 int ia, is;
-                slot_ray(static_cast<unsigned>(base + t), lane, c, r.views, &ia, &is);
+                slot_ray(static_cast<unsigned>(s0 + (base + t) * G), lane, c, r.views, &ia, &is);
                 if (ia < 0 || is >= c.ns) continue;
                 float v = sum[j];
                 const int gi = r.tie[ia * c.ns + is];
@@ -1216,14 +1289,18 @@ bool fpx_const(const ctr_par_param* p, const void* img, int batch, FpxConst* out
     c.quads = static_cast<int>(div_up(p->na, 4));
     const long long slots = static_cast<long long>(c.quads + 2) * c.octets;  // with class padding
     if (slots >= (1ll << 30) || static_cast<long long>(p->na) * p->ns >= (1ll << 31)) return false;
-    // two CTAs an SM; more when the mean CTA would exceed 7/8 of a round
+    // one CTA an SM while every CTA's slots fit one round; else enough CTAs
+    // for rounds 7/8 full
     int dev = 0;
     c.sms = kSmCount;
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&c.sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         c.sms = kSmCount;
-    const long long ctas = std::max<long long>(div_up(slots * 8, kFpxRound * 7), 2ll * c.sms);
+    const long long ctas = div_up(slots, c.sms) <= kFpxRound ? static_cast<long long>(c.sms) : div_up(slots * 8, kFpxRound * 7);
     c.ctas = static_cast<int>(std::min<long long>(ctas, slots));
+    // rows per stage: a multiple of the projector's chunk (16 or 8 rows) where
+    // 8 rows fit the nominal stage
     c.band = std::max(1, std::min(32, kFpxStageFloats / n));
+    c.band = c.band >= 16 ? c.band / 16 * 16 : (c.band >= 8 ? 8 : c.band);
     c.nbands = static_cast<int>(div_up(n, c.band));
     c.stage_floats = (c.band * n + 8 + 31) / 32 * 32;
     c.total = static_cast<long long>(batch) * n * n;
@@ -1231,6 +1308,8 @@ bool fpx_const(const ctr_par_param* p, const void* img, int batch, FpxConst* out
     c.proj_stride = static_cast<size_t>(p->ns) * p->na;
     c.dx = static_cast<float>(p->dx);
     c.dy = static_cast<float>(p->dy);
+    c.frac_mul = 1u << 23;
+    c.frac_one = 0x3F800000u;
     *smem = 128 + static_cast<size_t>(kFpxStages) * c.stage_floats * sizeof(float);
     if (*smem > 200 * 1024) return false;
     *out = c;
@@ -1295,10 +1374,10 @@ int launch_fpx_setup(const FpxConst& c, const FpxRays& r, const double* sc, cons
 int launch_fpx_proj(const FpxConst& c, size_t smem, const FpxRays& r, const float* img, const float* imgT,
                     float* proj, int batch, cudaStream_t stream)
 {
-    cudaError_t e = cudaFuncSetAttribute(fp_proj_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
+    auto kern = c.band % 16 == 0 ? fp_proj_f32<16> : (c.band % 8 == 0 ? fp_proj_f32<8> : fp_proj_f32<1>);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp smem: %s", cudaGetErrorString(e));
-    fp_proj_f32<<<dim3(c.ctas, batch), kFpxThreads, smem, stream>>>(img, imgT, proj, c, r);
+    kern<<<dim3(c.ctas, batch), kFpxThreads, smem, stream>>>(img, imgT, proj, c, r);
     return check_launch("fp_par_2d");
 }
 
