@@ -212,7 +212,9 @@ constexpr int kFpxSlots = 6;                         // ray slots per consumer l
 constexpr int kFpxRound = kFpxWarps * kFpxSlots;     // slots per round
 constexpr int kFpxStages = 3;
 constexpr int kFpxStageFloats = 16384;               // nominal stage: 64 KB
-constexpr int kFpxEmpty = 3 << 30;                   // ray code of a ray with no sample
+constexpr int kFpxEmpty = 0x7FFF;                    // ray code of a ray with no sample (k0 > k1)
+constexpr unsigned kFpxExc = 1u << 31;               // ray code flag: own line and tie in the per-ray tables
+constexpr long long kFpxLineTol = 256;               // |model - own line start| allowed, units of 2^-32 px
 constexpr int kFpxMaxTies = 8192;                    // tie rays per call
 constexpr int kFpxSetupThreads = 256;
 
@@ -240,12 +242,15 @@ struct FpxTie {
     int amb[4];   // ambiguous samples next to the certain range
 };
 
-// The per-call tables (scratch) written by fpx_setup.
+// The per-call tables (scratch) written by fpx_setup.  The projector reads a
+// ray's 4-byte code and its view's line; only rays flagged kFpxExc (ties, the
+// FP64 path, a line off the view's model) read X0, S and tie.
 struct FpxRays {
     float* vw;       // [na] ray weight of the view: dy/|cos| (row-marching) or dx/|sin|
+    long long* line; // [na][3] the view's model: sample 0 of channel is at x0 + is*d2, step S
     long long* X0;   // [na*ns] 32.32 position of sample 0
     long long* S;    // [na*ns] 32.32 step
-    int* code;       // [na*ns] k0 | k1 << 15 | class << 30, or kFpxEmpty
+    int* code;       // [na*ns] k0 | k1 << 15 | class << 30 | kFpxExc (empty: k0 > k1)
     int* tie;        // [na*ns] index into ties, or -1
     int* views;      // [4 * (quads + 2)] views of class 0, then of class 1, -1 padded to quads
     int* cuts;       // [3]: CTAs of class 0, slots of class 0, slots of class 1
@@ -258,7 +263,8 @@ __host__ __device__ inline size_t fpx_table_bytes(long long rays, int na, int ct
     const size_t r = static_cast<size_t>(rays);
     const size_t views = 4 * (static_cast<size_t>(na) / 4 + 3);
     const size_t vw = (static_cast<size_t>(na) * 4 + 255) & ~static_cast<size_t>(255);
-    return vw + ((r * 24 + views * 4 + (static_cast<size_t>(ctas) + 2) * 4 + 63) & ~static_cast<size_t>(63)) +
+    const size_t line = (static_cast<size_t>(na) * 24 + 255) & ~static_cast<size_t>(255);
+    return vw + line + ((r * 24 + views * 4 + (static_cast<size_t>(ctas) + 2) * 4 + 63) & ~static_cast<size_t>(63)) +
            64 + static_cast<size_t>(kFpxMaxTies) * sizeof(FpxTie);
 }
 
@@ -308,6 +314,16 @@ __global__ void __launch_bounds__(kFpxSetupThreads)
 {
     __shared__ float t[32][33];
     fpx_transpose_tile(img, imgT, n, static_cast<int>(blockIdx.x), t);
+}
+
+// A begin the view model may take (|v| < 2^20 px, fix32's exact range; NaN
+// and infinities fail).
+__device__ __forceinline__ bool line_ok(double v) { return fabs(v) < 1048576.0; }
+
+// a / b rounded to nearest (ties away from zero), b > 0.
+__device__ __forceinline__ long long round_div(long long a, long long b)
+{
+    return a >= 0 ? (a + b / 2) / b : -((-a + b / 2) / b);
 }
 
 // ---- set-up kernel: every ray once; block 0 the class lists, CTA cut and view
@@ -389,7 +405,8 @@ __global__ void __launch_bounds__(kFpxSetupThreads)
         const double begin = bo[2 * static_cast<size_t>(ray)], step = bo[2 * static_cast<size_t>(ray) + 1];
         long long X0 = 0, S = 0;
         int k0, k1, tie = -1;
-        if (!ray_fixed(begin, step, c.n, &X0, &S, &k0, &k1)) {
+        const bool plain = ray_fixed(begin, step, c.n, &X0, &S, &k0, &k1);
+        if (!plain) {
             int amb[4], namb = 0;
             bool done = false;
             if (ray_split(begin, step, c.n, &X0, &S, &k0, &k1, amb, &namb)) {
@@ -418,10 +435,26 @@ __global__ void __launch_bounds__(kFpxSetupThreads)
             }
             if (!done) ray_fp64(begin, step, c.n, &X0, &S, &k0, &k1);
         }
+        // the view's linear model, from its first and last channels (every
+        // ray of the view computes it alike): x0 + is * d2, step Sv
+        const int is = ray - ia * c.ns;
+        const double* bv = bo + 2 * static_cast<size_t>(ia) * c.ns;
+        const double bl = bv[2 * static_cast<size_t>(c.ns - 1)];
+        const bool model = line_ok(bv[0]) && line_ok(bl) && fabs(bv[1]) < 4.0;
+        const long long x0 = model ? fix32(bv[0]) : 0, Sv = model ? fix32(bv[1]) : 0;
+        const long long d2 = model && c.ns > 1 ? round_div(fix32(bl) - x0, c.ns - 1) : 0;
+        if (is == 0) {
+            r.line[3 * static_cast<size_t>(ia)] = x0;
+            r.line[3 * static_cast<size_t>(ia) + 1] = d2;
+            r.line[3 * static_cast<size_t>(ia) + 2] = Sv;
+        }
+        const long long dev = x0 + static_cast<long long>(is) * d2 - X0;
+        const bool own = !model || tie >= 0 || !plain || S != Sv || dev > kFpxLineTol || dev < -kFpxLineTol;
         const int cls = usex[ia] != 0 ? 0 : 1;
         r.X0[ray] = X0;
         r.S[ray] = S;
-        r.code[ray] = k0 <= k1 ? (k0 | (k1 << 15) | (cls << 30)) : kFpxEmpty;
+        r.code[ray] = (k0 <= k1 ? (k0 | (k1 << 15)) : kFpxEmpty) | (cls << 30) |
+                      static_cast<int>(own ? kFpxExc : 0u);
         r.tie[ray] = tie;
     }
 }
@@ -469,7 +502,7 @@ __global__ void __launch_bounds__(kFpxThreads, 1)
                 slot_ray(static_cast<unsigned>(s0 + (base + t) * G), lane, c, r.views, &ia, &is);
                 if (ia >= 0 && is < c.ns) {
                     const int code = r.code[ia * c.ns + is];
-                    if (code != kFpxEmpty) cnt = ((code >> 15) & 0x7FFF) - (code & 0x7FFF) + 1;
+                    cnt = max(0, ((code >> 15) & 0x7FFF) - (code & 0x7FFF) + 1);
                 }
                 const unsigned tot = __reduce_add_sync(0xffffffffu, static_cast<unsigned>(cnt));
                 if (lane == 0) s_work[t] = static_cast<int>(tot);
@@ -541,8 +574,14 @@ __global__ void __launch_bounds__(kFpxThreads, 1)
                     if (ia >= 0 && is < c.ns) {
                         const int ray = ia * c.ns + is;
                         code[j] = r.code[ray];
-                        X0[j] = r.X0[ray];
-                        S[j] = r.S[ray];
+                        if (static_cast<unsigned>(code[j]) & kFpxExc) {
+                            X0[j] = r.X0[ray];
+                            S[j] = r.S[ray];
+                        } else {  // the view's model line
+                            const long long* L = r.line + 3 * static_cast<size_t>(ia);
+                            X0[j] = L[0] + static_cast<long long>(is) * L[1];
+                            S[j] = L[2];
+                        }
                     }
                 }
             }
@@ -573,7 +612,7 @@ __global__ void __launch_bounds__(kFpxThreads, 1)
                 for (int j = 0; j < kFpxSlots; ++j) {
                     // the lane's ray range [k0, k1] (empty: k0 above every row)
                     const int cj = code[j];
-                    const int k0 = cj == kFpxEmpty ? 0x7FFF : (cj & 0x7FFF), k1 = (cj >> 15) & 0x7FFF;
+                    const int k0 = cj & 0x7FFF, k1 = (cj >> 15) & 0x7FFF;
                     if (!__any_sync(0xffffffffu, k0 <= b1 && k1 >= b0)) continue;
                     // sample b0 at row 0 of the band; a row step adds n to the word
                     // offset, so the integer part is the staged index
@@ -635,7 +674,7 @@ __global__ void __launch_bounds__(kFpxThreads, 1)
                 slot_ray(static_cast<unsigned>(s0 + (base + t) * G), lane, c, r.views, &ia, &is);
                 if (ia < 0 || is >= c.ns) continue;
                 float v = sum[j];
-                const int gi = r.tie[ia * c.ns + is];
+                const int gi = (static_cast<unsigned>(code[j]) & kFpxExc) ? r.tie[ia * c.ns + is] : -1;
                 if (gi >= 0) {
                     // border samples of a tie ray found inside by the reference's
                     // rule: read directly
@@ -1330,6 +1369,8 @@ FpxRays fpx_tables(unsigned char* b, const FpxConst& c)
     FpxRays r;
     r.vw = reinterpret_cast<float*>(b);
     b += (static_cast<size_t>(c.na) * 4 + 255) & ~static_cast<size_t>(255);
+    r.line = reinterpret_cast<long long*>(b);
+    b += (static_cast<size_t>(c.na) * 24 + 255) & ~static_cast<size_t>(255);
     r.X0 = reinterpret_cast<long long*>(b);
     r.S = reinterpret_cast<long long*>(b + rays * 8);
     r.code = reinterpret_cast<int*>(b + rays * 16);
