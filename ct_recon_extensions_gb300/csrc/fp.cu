@@ -235,6 +235,15 @@ struct FpxConst {
     unsigned frac_one;     // 0x3F800000, the bits of 1.0f (one_plus_frac)
 };
 
+// A view's model line: sample 0 of channel is at x0 + is*d2, step S (32.32),
+// with FP32 estimates of where channel is crosses the image's ends,
+// t0 = a + is*b and t1 = t0 + c samples.
+struct FpxLine {
+    long long x0, d2, S;
+    float a, b, c;
+    int pad;
+};
+
 // Global tie entry (a ray the fixed-point rule could not settle).
 struct FpxTie {
     int namb;
@@ -242,12 +251,15 @@ struct FpxTie {
     int amb[4];   // ambiguous samples next to the certain range
 };
 
-// The per-call tables (scratch) written by fpx_setup.  The projector reads a
-// ray's 4-byte code and its view's line; only rays flagged kFpxExc (ties, the
-// FP64 path, a line off the view's model) read X0, S and tie.
+// The per-call tables (scratch) written by fpx_setup.  The projector derives
+// a ray's line and sample range from its view's model line (24 bytes a view)
+// and reads one exception bit; only flagged rays (ties, the FP64 path, a line
+// or range off the view's model) read their code, X0, S and tie.
 struct FpxRays {
     float* vw;       // [na] ray weight of the view: dy/|cos| (row-marching) or dx/|sin|
-    long long* line; // [na][3] the view's model: sample 0 of channel is at x0 + is*d2, step S
+    FpxLine* line;   // [na] the views' model lines
+    unsigned* exc;   // [na * octets bits, in words] bit 8*(ia*octets + octet) + c: channel
+                     // 8*octet + c of view ia is flagged kFpxExc (zeroed before fpx_setup)
     long long* X0;   // [na*ns] 32.32 position of sample 0
     long long* S;    // [na*ns] 32.32 step
     int* code;       // [na*ns] k0 | k1 << 15 | class << 30 | kFpxExc (empty: k0 > k1)
@@ -258,13 +270,20 @@ struct FpxRays {
     int* nties;      // count (zeroed before fpx_setup)
 };
 
+// Bytes of the exception bitmap: one byte per (view, channel octet).
+__host__ __device__ inline size_t fpx_exc_bytes(long long rays, int na)
+{
+    const size_t octets = na > 0 ? (static_cast<size_t>(rays / na) + 7) / 8 : 0;
+    return (static_cast<size_t>(na) * octets + 255) & ~static_cast<size_t>(255);
+}
+
 __host__ __device__ inline size_t fpx_table_bytes(long long rays, int na, int ctas)
 {
     const size_t r = static_cast<size_t>(rays);
     const size_t views = 4 * (static_cast<size_t>(na) / 4 + 3);
     const size_t vw = (static_cast<size_t>(na) * 4 + 255) & ~static_cast<size_t>(255);
-    const size_t line = (static_cast<size_t>(na) * 24 + 255) & ~static_cast<size_t>(255);
-    return vw + line + ((r * 24 + views * 4 + (static_cast<size_t>(ctas) + 2) * 4 + 63) & ~static_cast<size_t>(63)) +
+    const size_t line = (static_cast<size_t>(na) * sizeof(FpxLine) + 255) & ~static_cast<size_t>(255);
+    return vw + line + fpx_exc_bytes(rays, na) + ((r * 24 + views * 4 + (static_cast<size_t>(ctas) + 2) * 4 + 63) & ~static_cast<size_t>(63)) +
            64 + static_cast<size_t>(kFpxMaxTies) * sizeof(FpxTie);
 }
 
@@ -324,6 +343,57 @@ __device__ __forceinline__ bool line_ok(double v) { return fabs(v) < 1048576.0; 
 __device__ __forceinline__ long long round_div(long long a, long long b)
 {
     return a >= 0 ? (a + b / 2) / b : -((-a + b / 2) / b);
+}
+
+// The FP32 constants of a view's crossing estimates (view_range): channel
+// is crosses 0 at sample -(x0 + is*d2)/S and n-1 at ((n-1)*2^32 - x0 - is*d2)/S.
+__device__ __forceinline__ FpxLine view_line(long long x0, long long d2, long long S, int n)
+{
+    FpxLine l{x0, d2, S, 0.0f, 0.0f, 0.0f, 0};
+    if (S != 0) {
+        const float s = fix_to_float(S);
+        l.a = -fix_to_float(x0) / s;
+        l.b = -fix_to_float(d2) / s;
+        l.c = static_cast<float>(n - 1) / s;
+    }
+    return l;
+}
+
+// The sample range [*k0, *k1] (empty: k0 = kFpxEmpty, k1 = 0) of channel is
+// of a view's model line, X(k) = x0 + is*d2 + k*S inside [0, (n-1)*2^32]: the
+// FP32 crossing estimates settled by up to three exact steps at each end.  A
+// ray keeps the range derived this way only where the set-up found it equal
+// to the exact one (every other ray is flagged and reads its own code).
+__device__ __forceinline__ void view_range(const FpxLine& l, int is, int n, int* k0o, int* k1o)
+{
+    const long long L = static_cast<long long>(n - 1) << 32;
+    const long long X0 = l.x0 + static_cast<long long>(is) * l.d2, S = l.S;
+    auto inside = [&](int k) {
+        const long long x = X0 + static_cast<long long>(k) * S;
+        return x >= 0 && x <= L;
+    };
+    int k0, k1;
+    if (S == 0) {
+        k0 = 0;
+        k1 = inside(0) ? n - 1 : -1;
+    } else {
+        const float t0 = fmaf(static_cast<float>(is), l.b, l.a), t1 = t0 + l.c;
+        const float lim = static_cast<float>(n + 2);
+        const float ta = fminf(fmaxf(fminf(t0, t1), -2.0f), lim);
+        const float tb = fminf(fmaxf(fmaxf(t0, t1), -2.0f), lim);
+        k0 = max(0, static_cast<int>(ceilf(ta)));
+        k1 = min(n - 1, static_cast<int>(floorf(tb)));
+        for (int it = 0; it < 3 && k0 > 0 && inside(k0 - 1); ++it) --k0;
+        for (int it = 0; it < 3 && k0 <= k1 && !inside(k0); ++it) ++k0;
+        for (int it = 0; it < 3 && k1 < n - 1 && inside(k1 + 1); ++it) ++k1;
+        for (int it = 0; it < 3 && k1 >= k0 && !inside(k1); ++it) --k1;
+    }
+    if (k0 > k1) {
+        k0 = kFpxEmpty;
+        k1 = 0;
+    }
+    *k0o = k0;
+    *k1o = k1;
 }
 
 // ---- set-up kernel: every ray once; block 0 the class lists, CTA cut and view
@@ -443,13 +513,21 @@ __global__ void __launch_bounds__(kFpxSetupThreads)
         const bool model = line_ok(bv[0]) && line_ok(bl) && fabs(bv[1]) < 4.0;
         const long long x0 = model ? fix32(bv[0]) : 0, Sv = model ? fix32(bv[1]) : 0;
         const long long d2 = model && c.ns > 1 ? round_div(fix32(bl) - x0, c.ns - 1) : 0;
-        if (is == 0) {
-            r.line[3 * static_cast<size_t>(ia)] = x0;
-            r.line[3 * static_cast<size_t>(ia) + 1] = d2;
-            r.line[3 * static_cast<size_t>(ia) + 2] = Sv;
-        }
+        const FpxLine vl = view_line(x0, d2, Sv, c.n);
+        if (is == 0) r.line[ia] = vl;
         const long long dev = x0 + static_cast<long long>(is) * d2 - X0;
-        const bool own = !model || tie >= 0 || !plain || S != Sv || dev > kFpxLineTol || dev < -kFpxLineTol;
+        bool own = !model || tie >= 0 || !plain || S != Sv || dev > kFpxLineTol || dev < -kFpxLineTol;
+        if (!own) {
+            // the projector derives the range from the model line: keep it
+            // only where that gives the exact range
+            int m0, m1;
+            view_range(vl, is, c.n, &m0, &m1);
+            own = k0 <= k1 ? (m0 != k0 || m1 != k1) : m0 <= m1;
+        }
+        if (own) {
+            const long long bit = (static_cast<long long>(ia) * c.octets + (is >> 3)) * 8 + (is & 7);
+            atomicOr(r.exc + (bit >> 5), 1u << (bit & 31));
+        }
         const int cls = usex[ia] != 0 ? 0 : 1;
         r.X0[ray] = X0;
         r.S[ray] = S;
@@ -457,6 +535,25 @@ __global__ void __launch_bounds__(kFpxSetupThreads)
                       static_cast<int>(own ? kFpxExc : 0u);
         r.tie[ray] = tie;
     }
+}
+
+// Barrier 1 over the projector's consumer warps only (the producer warp runs on).
+__device__ __forceinline__ void consumer_sync()
+{
+    asm volatile("bar.sync 1, %0;" ::"n"(kFpxWarps * 32) : "memory");
+}
+
+// The code of ray (ia, is): its own (flagged kFpxExc) where the exception
+// bitmap says so, else the range of its view's model line.
+__device__ __forceinline__ int ray_code(const FpxRays& r, const FpxConst& c, int ia, int is)
+{
+    const long long bit = (static_cast<long long>(ia) * c.octets + (is >> 3)) * 8 + (is & 7);
+    const unsigned w = r.exc[bit >> 5];
+    const FpxLine l = r.line[ia];
+    if ((w >> (bit & 31)) & 1u) return r.code[static_cast<size_t>(ia) * c.ns + is];
+    int k0, k1;
+    view_range(l, is, c.n, &k0, &k1);
+    return k0 | (k1 << 15);
 }
 
 template <int CH>
@@ -468,6 +565,7 @@ __global__ void __launch_bounds__(kFpxThreads, 1)
     float* stage = reinterpret_cast<float*>(fpx_dyn + ((128u - (smem_u32(fpx_dyn) & 127u)) & 127u));
     __shared__ __align__(8) unsigned long long s_full[kFpxStages], s_empty[kFpxStages];
     __shared__ int s_work[kFpxRound];
+    __shared__ int s_code[kFpxRound][32];           // ray codes of the round's slots
     __shared__ int s_assign[kFpxWarps][kFpxSlots];  // slot of the round, or -1
     __shared__ int s_abort;
 
@@ -491,38 +589,54 @@ __global__ void __launch_bounds__(kFpxThreads, 1)
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
 
+    // zero the stages once: the few slack elements past a band read as finite
+    // (later bands leave image values there)
+    for (int i = tid; i < kFpxStages * c.stage_floats; i += kFpxThreads) stage[i] = 0.0f;
+    __syncthreads();
+
     int g = 0;  // band instances so far (producer and consumers count alike)
     for (int base = 0; base < count; base += kFpxRound) {
         const int m = min(kFpxRound, count - base);
-        for (int i = tid; i < kFpxRound; i += kFpxThreads) (&s_assign[0][0])[i] = -1;
-        // ---- sample counts of the round's slots
         if (warp < kFpxWarps) {
-            for (int t = warp; t < m; t += kFpxWarps) {
-                int ia, is, cnt = 0;
-                slot_ray(static_cast<unsigned>(s0 + (base + t) * G), lane, c, r.views, &ia, &is);
-                if (ia >= 0 && is < c.ns) {
-                    const int code = r.code[ia * c.ns + is];
-                    cnt = max(0, ((code >> 15) & 0x7FFF) - (code & 0x7FFF) + 1);
-                }
+            // the consumers prepare the round while the producer fills the stages
+            for (int i = tid; i < kFpxRound; i += kFpxWarps * 32) (&s_assign[0][0])[i] = -1;
+            // ---- ray codes and sample counts of the round's slots (slot warp + i *
+            // kFpxWarps; the steps run over all of a warp's slots at once, so
+            // their global loads overlap)
+            int ia_[kFpxSlots], is_[kFpxSlots], code_[kFpxSlots];
+#pragma unroll
+            for (int i = 0; i < kFpxSlots; ++i) {
+                const int t = warp + i * kFpxWarps;
+                ia_[i] = -1;
+                is_[i] = 0;
+                if (t < m) slot_ray(static_cast<unsigned>(s0 + (base + t) * G), lane, c, r.views, &ia_[i], &is_[i]);
+            }
+#pragma unroll
+            for (int i = 0; i < kFpxSlots; ++i)
+                code_[i] = ia_[i] >= 0 && is_[i] < c.ns ? ray_code(r, c, ia_[i], is_[i]) : kFpxEmpty;
+#pragma unroll
+            for (int i = 0; i < kFpxSlots; ++i) {
+                const int t = warp + i * kFpxWarps;
+                if (t >= m) continue;
+                s_code[t][lane] = code_[i];
+                const int cnt = max(0, ((code_[i] >> 15) & 0x7FFF) - (code_[i] & 0x7FFF) + 1);
                 const unsigned tot = __reduce_add_sync(0xffffffffu, static_cast<unsigned>(cnt));
                 if (lane == 0) s_work[t] = static_cast<int>(tot);
             }
-        }
-        __syncthreads();
-        // ---- deal the slots, largest first, to the warps in snake order
-        if (tid < m) {
-            const int wt = s_work[tid];
-            int rk = 0;
-            for (int u = 0; u < m; ++u) {
-                const int wu = s_work[u];
-                rk += (wu > wt || (wu == wt && u < tid)) ? 1 : 0;
+            consumer_sync();
+            // ---- deal the slots, largest first, to the warps in snake order
+            if (tid < m) {
+                const int wt = s_work[tid];
+                int rk = 0;
+                for (int u = 0; u < m; ++u) {
+                    const int wu = s_work[u];
+                    rk += (wu > wt || (wu == wt && u < tid)) ? 1 : 0;
+                }
+                const int k = rk / kFpxWarps, pos = rk - k * kFpxWarps;
+                s_assign[(k & 1) ? kFpxWarps - 1 - pos : pos][k] = tid;
             }
-            const int k = rk / kFpxWarps, pos = rk - k * kFpxWarps;
-            s_assign[(k & 1) ? kFpxWarps - 1 - pos : pos][k] = tid;
+            consumer_sync();
         }
-        // zero the stages: the few slack elements past a band read as finite
-        for (int i = tid; i < kFpxStages * c.stage_floats; i += kFpxThreads) stage[i] = 0.0f;
-        __syncthreads();
 
         if (warp == kFpxWarps) {
             // ---- producer: one lane issues every band
@@ -573,14 +687,14 @@ __global__ void __launch_bounds__(kFpxThreads, 1)
                     slot_ray(static_cast<unsigned>(s0 + (base + t) * G), lane, c, r.views, &ia, &is);
                     if (ia >= 0 && is < c.ns) {
                         const int ray = ia * c.ns + is;
-                        code[j] = r.code[ray];
+                        code[j] = s_code[t][lane];
                         if (static_cast<unsigned>(code[j]) & kFpxExc) {
                             X0[j] = r.X0[ray];
                             S[j] = r.S[ray];
                         } else {  // the view's model line
-                            const long long* L = r.line + 3 * static_cast<size_t>(ia);
-                            X0[j] = L[0] + static_cast<long long>(is) * L[1];
-                            S[j] = L[2];
+                            const FpxLine& l = r.line[ia];
+                            X0[j] = l.x0 + static_cast<long long>(is) * l.d2;
+                            S[j] = l.S;
                         }
                     }
                 }
@@ -1369,8 +1483,10 @@ FpxRays fpx_tables(unsigned char* b, const FpxConst& c)
     FpxRays r;
     r.vw = reinterpret_cast<float*>(b);
     b += (static_cast<size_t>(c.na) * 4 + 255) & ~static_cast<size_t>(255);
-    r.line = reinterpret_cast<long long*>(b);
-    b += (static_cast<size_t>(c.na) * 24 + 255) & ~static_cast<size_t>(255);
+    r.line = reinterpret_cast<FpxLine*>(b);
+    b += (static_cast<size_t>(c.na) * sizeof(FpxLine) + 255) & ~static_cast<size_t>(255);
+    r.exc = reinterpret_cast<unsigned*>(b);
+    b += fpx_exc_bytes(static_cast<long long>(c.na) * c.ns, c.na);
     r.X0 = reinterpret_cast<long long*>(b);
     r.S = reinterpret_cast<long long*>(b + rays * 8);
     r.code = reinterpret_cast<int*>(b + rays * 16);
@@ -1400,6 +1516,8 @@ int launch_fpx_setup(const FpxConst& c, const FpxRays& r, const double* sc, cons
                      const float* img, float* imgT, int batch, cudaStream_t stream)
 {
     cudaError_t e = cudaMemsetAsync(r.nties, 0, sizeof(int), stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(r.exc, 0, fpx_exc_bytes(static_cast<long long>(c.na) * c.ns, c.na), stream);
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp_par_2d: %s", cudaGetErrorString(e));
     const long long rays = static_cast<long long>(c.na) * c.ns;
     const unsigned blocks = static_cast<unsigned>(
