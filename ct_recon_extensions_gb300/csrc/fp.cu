@@ -537,6 +537,24 @@ __global__ void __launch_bounds__(kFpxSetupThreads)
     }
 }
 
+// Bounded wait until *p >= target (acquire, GPU scope); false after the
+// wait limit.
+__device__ __forceinline__ bool wait_count(const unsigned long long* p, unsigned long long target)
+{
+    auto ld = [&]() {
+        unsigned long long v;
+        asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+        return v;
+    };
+    if (ld() >= target) return true;
+    const unsigned long long t0 = global_ns();
+    while (ld() < target) {
+        if (global_ns() - t0 > kWaitLimitNs) return false;
+        __nanosleep(100);
+    }
+    return true;
+}
+
 // Barrier 1 over the projector's consumer warps only (the producer warp runs on).
 __device__ __forceinline__ void consumer_sync()
 {
@@ -558,8 +576,9 @@ __device__ __forceinline__ int ray_code(const FpxRays& r, const FpxConst& c, int
 
 template <int CH>
 __global__ void __launch_bounds__(kFpxThreads, 1)
-    fp_proj_f32(const float* __restrict__ img, const float* __restrict__ imgT,
-                float* __restrict__ proj, const FpxConst c, const FpxRays r)
+    fp_proj_f32(const float* __restrict__ img, float* __restrict__ imgT,
+                float* __restrict__ proj, const FpxConst c, const FpxRays r,
+                unsigned long long* __restrict__ tsync, unsigned long long ttarget)
 {
     extern __shared__ __align__(128) unsigned char fpx_dyn[];
     float* stage = reinterpret_cast<float*>(fpx_dyn + ((128u - (smem_u32(fpx_dyn) & 127u)) & 127u));
@@ -593,6 +612,34 @@ __global__ void __launch_bounds__(kFpxThreads, 1)
     // (later bands leave image values there)
     for (int i = tid; i < kFpxStages * c.stage_floats; i += kFpxThreads) stage[i] = 0.0f;
     __syncthreads();
+
+    if (tsync != nullptr && warp < kFpxWarps) {
+        // Fused transposed copy (one image, cooperative launch): this CTA's
+        // 32 x 32 tiles (blockIdx.x, + gridDim.x, ...) through shared memory,
+        // then one count on tsync.  Column-marching CTAs stream imgT once the
+        // count reaches ttarget (every CTA's tiles written).
+        float(*t)[33] = reinterpret_cast<float(*)[33]>(&s_code[0][0]);
+        const int tiles = (n + 31) / 32;
+        for (int tb = blockIdx.x; tb < tiles * tiles; tb += gridDim.x) {
+            const int x0 = (tb % tiles) * 32, y0 = (tb / tiles) * 32;
+            for (int rr = warp; rr < 32; rr += kFpxWarps) {
+                const int y = y0 + rr, x = x0 + lane;
+                if (x < n && y < n) t[rr][lane] = img[static_cast<size_t>(y) * n + x];
+            }
+            consumer_sync();
+            for (int rr = warp; rr < 32; rr += kFpxWarps) {
+                const int x = x0 + rr, y = y0 + lane;
+                if (x < n && y < n) imgT[static_cast<size_t>(x) * n + y] = t[lane][rr];
+            }
+            consumer_sync();
+        }
+        if (tid == 0) {
+            // the copy's generic writes, released to the readers' bulk copies
+            asm volatile("fence.proxy.async.global;" ::: "memory");
+            __threadfence();
+            atomicAdd(tsync, 1ull);
+        }
+    }
 
     int g = 0;  // band instances so far (producer and consumers count alike)
     for (int base = 0; base < count; base += kFpxRound) {
@@ -642,8 +689,16 @@ __global__ void __launch_bounds__(kFpxThreads, 1)
             // ---- producer: one lane issues every band
             if (lane == 0) {
                 bool alive = true;
+                if (tsync != nullptr && cls1 && base == 0) {
+                    // the fused transposed copy must be complete
+                    if (!wait_count(tsync, ttarget)) {
+                        raise_flag(kFlagWaitTimeout);
+                        alive = false;
+                    }
+                    asm volatile("fence.proxy.async.global;" ::: "memory");
+                }
                 int g1 = g;
-                for (int t = 0; t < c.nbands; ++t, ++g1) {
+                for (int t = 0; alive && t < c.nbands; ++t, ++g1) {
                     const int s = g1 % kFpxStages;
                     const int use = g1 / kFpxStages;
                     if (use > 0 && !mbar_wait_bounded(smem_u32(&s_empty[s]), (use - 1) & 1)) {
@@ -1530,13 +1585,59 @@ int launch_fpx_setup(const FpxConst& c, const FpxRays& r, const double* sc, cons
     return check_launch("fp_par_2d set-up");
 }
 
-int launch_fpx_proj(const FpxConst& c, size_t smem, const FpxRays& r, const float* img, const float* imgT,
+using FpxKernel = void (*)(const float*, float*, float*, FpxConst, FpxRays, unsigned long long*,
+                           unsigned long long);
+
+FpxKernel fpx_kernel(const FpxConst& c, size_t smem, cudaError_t* e)
+{
+    const FpxKernel k = c.band % 16 == 0 ? fp_proj_f32<16> : (c.band % 8 == 0 ? fp_proj_f32<8> : fp_proj_f32<1>);
+    *e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    return k;
+}
+
+// The projector on an existing transposed copy imgT.
+int launch_fpx_proj(const FpxConst& c, size_t smem, const FpxRays& r, const float* img, float* imgT,
                     float* proj, int batch, cudaStream_t stream)
 {
-    auto kern = c.band % 16 == 0 ? fp_proj_f32<16> : (c.band % 8 == 0 ? fp_proj_f32<8> : fp_proj_f32<1>);
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    cudaError_t e;
+    const FpxKernel kern = fpx_kernel(c, smem, &e);
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp smem: %s", cudaGetErrorString(e));
-    kern<<<dim3(c.ctas, batch), kFpxThreads, smem, stream>>>(img, imgT, proj, c, r);
+    kern<<<dim3(c.ctas, batch), kFpxThreads, smem, stream>>>(img, imgT, proj, c, r, nullptr, 0ull);
+    return check_launch("fp_par_2d");
+}
+
+// Whether one image's projector can make its own transposed copy: a
+// cooperative launch (every CTA resident at once, so the column-marching
+// CTAs may wait for the others' tiles).
+bool fpx_fusable(const FpxConst& c, size_t smem)
+{
+    int dev = 0, coop = 0, per_sm = 0;
+    cudaError_t e;
+    const FpxKernel kern = fpx_kernel(c, smem, &e);
+    if (e != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFpxThreads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return static_cast<long long>(per_sm) * c.sms >= c.ctas;
+}
+
+// One image with the fused transposed copy: count `tsync` reaches ttarget
+// once every CTA has written its tiles of imgT.
+int launch_fpx_proj_fused(const FpxConst& c, size_t smem, const FpxRays& r, const float* img, float* imgT,
+                          float* proj, unsigned long long* tsync, unsigned long long ttarget,
+                          cudaStream_t stream)
+{
+    cudaError_t e;
+    const FpxKernel kern = fpx_kernel(c, smem, &e);
+    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp smem: %s", cudaGetErrorString(e));
+    FpxConst cc = c;
+    FpxRays rr = r;
+    void* args[] = {const_cast<float**>(&img), &imgT, &proj, &cc, &rr, &tsync, &ttarget};
+    e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kern), dim3(c.ctas, 1), dim3(kFpxThreads),
+                                    args, smem, stream);
+    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fp_par_2d (cooperative): %s", cudaGetErrorString(e));
     return check_launch("fp_par_2d");
 }
 
@@ -1748,10 +1849,14 @@ struct ctr_fp_plan {
     void* tables = nullptr;
     float* imgT = nullptr;
     ctr::FpxRays r{};
+    bool fused = false;                  // one-image calls make their own transposed copy
+    unsigned long long* tsync = nullptr; // the fused copy's CTA count (never reset)
+    unsigned long long calls = 0;        // fused calls so far: count target = calls * ctas
     ~ctr_fp_plan()
     {
         if (tables) cudaFree(tables);
         if (imgT) cudaFree(imgT);
+        if (tsync) cudaFree(tsync);
     }
 };
 
@@ -1783,6 +1888,12 @@ int ctr_fp_par_2d_plan_create(const ctr_par_param* p, const double* sincostbl, c
         return fail(CTR_ERR_CUDA, "fp_par_2d plan: %zu + %zu bytes", tbytes, ibytes);
     }
     P->r = fpx_tables(static_cast<unsigned char*>(P->tables), c);
+    P->fused = fpx_fusable(c, smem);
+    if (P->fused && (cudaMalloc(&P->tsync, sizeof(unsigned long long)) != cudaSuccess ||
+                     cudaMemsetAsync(P->tsync, 0, sizeof(unsigned long long), stream) != cudaSuccess)) {
+        cudaGetLastError();
+        return fail(CTR_ERR_CUDA, "fp_par_2d plan: sync counter");
+    }
     st = launch_fpx_setup(c, P->r, sincostbl, beginoffset, usex, nullptr, nullptr, 1, stream);
     if (st) return st;
     const cudaError_t e = cudaStreamSynchronize(stream);
@@ -1805,6 +1916,11 @@ int ctr_fp_par_2d_plan_run(ctr_fp_plan* plan, const float* img, float* proj, int
     FpxConst c = plan->c;
     c.total = static_cast<long long>(batch) * c.n * c.n;
     c.total4 = c.total & ~3ll;
+    if (batch == 1 && plan->fused) {
+        ++plan->calls;
+        return launch_fpx_proj_fused(c, plan->smem, plan->r, img, plan->imgT, proj, plan->tsync,
+                                     plan->calls * static_cast<unsigned long long>(c.ctas), stream);
+    }
     const unsigned long long tiles = static_cast<unsigned long long>(div_up(c.n, 32)) * div_up(c.n, 32) * batch;
     if (tiles > 0x7FFFFFFFull) return fail(CTR_ERR_UNSUPPORTED, "fp_par_2d: batch too large");
     fpx_transpose<<<static_cast<unsigned>(tiles), kFpxSetupThreads, 0, stream>>>(img, plan->imgT, c.n);
