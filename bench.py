@@ -253,8 +253,9 @@ class ParPipeline:
         self.sino = torch.empty((g["na"], g["ns"]), **f32)
         self.filt = torch.empty((g["na"], g["ns"]), **f32)
         self.names = ["fp_par_2d", "ramp_filter", "bp_par_2d"]
-        # our kernels per call (fp_par_2d: transposed copy, projector)
-        self.kernels = {"fp_par_2d": 2, "ramp_filter": 1, "bp_par_2d": 1}
+        # our kernels per call (fp_par_2d: the plan's one-image projector makes
+        # its own transposed copy)
+        self.kernels = {"fp_par_2d": 1, "ramp_filter": 1, "bp_par_2d": 1}
         # algorithmic FP32 FLOPs per launch (fixed conventions)
         self.flops = {"fp_par_2d": 6.0 * g["na"] * g["ns"] * g["ny"],
                       "ramp_filter": 2.0 * g["ns"] * g["na"] * g["ns"],
