@@ -110,6 +110,99 @@ __device__ __forceinline__ void adj_taps_int(unsigned base, float sig, float tq,
     red_shared_u32(addr + 4u, q1b - kMagicBits);
 }
 
+// adj_taps_int for two pixels, the FP32 steps packed (same roundings as two
+// calls).
+__device__ __forceinline__ void adj_taps_int2(unsigned base, float2 sig, float2 tq, unsigned tb0, unsigned tb1)
+{
+    const float2 vb = __fadd2_rn(sig, dup2(kMagic));
+    const float2 d = sub2(sig, __fadd2_rn(vb, dup2(-kMagic)));
+    const float2 q = __ffma2_rn(tq, d, __ffma2_rn(tq, dup2(0.5f), dup2(kMagic)));
+    const unsigned a0 = base + 4u * __float_as_uint(vb.x), a1 = base + 4u * __float_as_uint(vb.y);
+    const unsigned q0 = __float_as_uint(q.x), q1 = __float_as_uint(q.y);
+    red_shared_u32(a0, tb0 - q0);
+    red_shared_u32(a0 + 4u, q0 - kMagicBits);
+    red_shared_u32(a1, tb1 - q1);
+    red_shared_u32(a1 + 4u, q1 - kMagicBits);
+}
+
+// adj_taps for two pixels (fixed-point values t), the FP32 steps packed.
+__device__ __forceinline__ void adj_taps2(unsigned base, float2 sig, float2 t)
+{
+    const float2 vb = __fadd2_rn(sig, dup2(kMagic));  // round(sig) in its bits: the address
+    const float2 r = __fadd2_rn(vb, dup2(-kMagic));
+    const float2 u = __fadd2_rn(sub2(sig, r), dup2(0.5f));
+    const float2 q = __ffma2_rn(t, u, dup2(kMagic));
+    const float2 tr = __fadd2_rn(t, dup2(kMagic));
+    const unsigned a0 = base + 4u * __float_as_uint(vb.x), a1 = base + 4u * __float_as_uint(vb.y);
+    const int q1a = static_cast<int>(__float_as_uint(q.x) - kMagicBits);
+    const int q1b = static_cast<int>(__float_as_uint(q.y) - kMagicBits);
+    const int q0a = static_cast<int>(__float_as_uint(tr.x) - kMagicBits) - q1a;
+    const int q0b = static_cast<int>(__float_as_uint(tr.y) - kMagicBits) - q1b;
+    red_shared_u32(a0, static_cast<unsigned>(q0a));
+    red_shared_u32(a0 + 4u, static_cast<unsigned>(q1a));
+    red_shared_u32(a1, static_cast<unsigned>(q0b));
+    red_shared_u32(a1 + 4u, static_cast<unsigned>(q1b));
+}
+
+// The fast-path taps of one view for a thread's pixels, parallel beam: the
+// x-major mapping (column oxx, rows oyx) or the y-major one (columns oxy[r &
+// 3], rows oyy[r >> 2]); pixel pairs (r, r+1) packed.
+template <int R>
+__device__ __forceinline__ void adj_par_view(const FastRec& P, unsigned base, bool xmaj, float oxx,
+                                             const float (&oyx)[R], const float (&oxy)[4],
+                                             const float (&oyy)[R / 4], const float (&vx)[R],
+                                             const float (&vy)[R], const unsigned (&tbx)[R],
+                                             const unsigned (&tby)[R])
+{
+    const float2 p1 = dup2(P.p1);
+    if (xmaj) {
+        const float2 xs = dup2(par_xpart(oxx, P));
+#pragma unroll
+        for (int r = 0; r < R; r += 2)
+            adj_taps_int2(base, __ffma2_rn(make_float2(oyx[r], oyx[r + 1]), p1, xs), make_float2(vx[r], vx[r + 1]),
+                          tbx[r], tbx[r + 1]);
+    } else {
+        const float2 p0 = dup2(P.p0), cen = dup2(P.cen);
+        const float2 xs01 = __ffma2_rn(make_float2(oxy[0], oxy[1]), p0, cen);
+        const float2 xs23 = __ffma2_rn(make_float2(oxy[2], oxy[3]), p0, cen);
+#pragma unroll
+        for (int r = 0; r < R; r += 2)
+            adj_taps_int2(base, __ffma2_rn(dup2(oyy[r >> 2]), p1, (r & 3) ? xs23 : xs01),
+                          make_float2(vy[r], vy[r + 1]), tby[r], tby[r + 1]);
+    }
+}
+
+// The same for the fan beam (variant V), pixel pairs packed.
+template <int V, int R>
+__device__ __forceinline__ void adj_fan_view(const FastRec& P, unsigned base, bool xmaj, float oxx,
+                                             const float (&oyx)[R], const float (&oxy)[4],
+                                             const float (&oyy)[R / 4], const float (&vx)[R],
+                                             const float (&vy)[R], const TileConst& c)
+{
+    if (xmaj) {
+        const FanX X = fan_xpart(oxx, P);
+        const float2 xn = dup2(X.n), xd = dup2(X.d);
+#pragma unroll
+        for (int r = 0; r < R; r += 2) {
+            float2 w;
+            const float2 sig = fan_sigma2<V>(xn, xd, make_float2(oyx[r], oyx[r + 1]), P, c, &w);
+            adj_taps2(base, sig, __fmul2_rn(make_float2(vx[r], vx[r + 1]), w));
+        }
+    } else {
+        FanX X[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) X[q] = fan_xpart(oxy[q], P);
+#pragma unroll
+        for (int r = 0; r < R; r += 2) {
+            const int q = r & 3;
+            float2 w;
+            const float2 sig = fan_sigma2<V>(make_float2(X[q].n, X[q + 1].n), make_float2(X[q].d, X[q + 1].d),
+                                             dup2(oyy[r >> 2]), P, c, &w);
+            adj_taps2(base, sig, __fmul2_rn(make_float2(vy[r], vy[r + 1]), w));
+        }
+    }
+}
+
 template <Geo G>
 __global__ void __launch_bounds__(kBpThreads, 2)
     bp_tile_adj(const float* __restrict__ img, float* __restrict__ grad, const double* __restrict__ t0,
@@ -215,47 +308,18 @@ __global__ void __launch_bounds__(kBpThreads, 2)
                 if constexpr (G == Geo::kPar) {
                     for (int j = 0; j < nv; ++j) {
                         const FastRec P = load_fast(vb + j);
-                        const unsigned base = static_cast<unsigned>(P.mode) & ~3u;
-                        if (fabsf(P.p0) * c.dxf >= fabsf(P.p1) * c.dyf) {
-                            const float xs = par_xpart(oxx, P);
-#pragma unroll
-                            for (int r = 0; r < R; ++r) adj_taps_int(base, par_sigma(xs, oyx[r], P), vx[r], tbx[r]);
-                        } else {
-                            float xs[4];
-#pragma unroll
-                            for (int q = 0; q < 4; ++q) xs[q] = par_xpart(oxy[q], P);
-#pragma unroll
-                            for (int r = 0; r < R; ++r)
-                                adj_taps_int(base, par_sigma(xs[r & 3], oyy[r >> 2], P), vy[r], tby[r]);
-                        }
+                        adj_par_view<R>(P, static_cast<unsigned>(P.mode) & ~3u,
+                                        fabsf(P.p0) * c.dxf >= fabsf(P.p1) * c.dyf, oxx, oyx, oxy, oyy, vx, vy,
+                                        tbx, tby);
                     }
                 } else {
                     auto fan_block = [&](auto vc) {
                         constexpr int V = decltype(vc)::value;
                         for (int j = 0; j < nv; ++j) {
                             const FastRec P = load_fast(vb + j);
-                            const unsigned base = static_cast<unsigned>(P.mode) & ~3u;
-                            if (fabsf(P.p0) * c.dxf >= fabsf(P.p1) * c.dyf) {
-                                const FanX X = fan_xpart(oxx, P);
-#pragma unroll
-                                for (int r = 0; r < R; ++r) {
-                                    float w;
-                                    const float sig = fan_sigma<V>(X, oyx[r], P, c, &w);
-                                    adj_taps(base + 4u * __float_as_uint(__fadd_rn(sig, kMagic)), sig,
-                                             __fmul_rn(vx[r], w));
-                                }
-                            } else {
-                                FanX X[4];
-#pragma unroll
-                                for (int q = 0; q < 4; ++q) X[q] = fan_xpart(oxy[q], P);
-#pragma unroll
-                                for (int r = 0; r < R; ++r) {
-                                    float w;
-                                    const float sig = fan_sigma<V>(X[r & 3], oyy[r >> 2], P, c, &w);
-                                    adj_taps(base + 4u * __float_as_uint(__fadd_rn(sig, kMagic)), sig,
-                                             __fmul_rn(vy[r], w));
-                                }
-                            }
+                            adj_fan_view<V, R>(P, static_cast<unsigned>(P.mode) & ~3u,
+                                               fabsf(P.p0) * c.dxf >= fabsf(P.p1) * c.dyf, oxx, oyx, oxy, oyy, vx,
+                                               vy, c);
                         }
                     };
                     switch (fv) {
@@ -275,41 +339,12 @@ __global__ void __launch_bounds__(kBpThreads, 2)
                     const FastRec& P = F;
                     const unsigned base = static_cast<unsigned>(P.mode) & ~3u;
                     if constexpr (G == Geo::kPar) {
-                        if (xmaj) {
-                            const float xs = par_xpart(oxx, P);
-#pragma unroll
-                            for (int r = 0; r < R; ++r) adj_taps_int(base, par_sigma(xs, oyx[r], P), vx[r], tbx[r]);
-                        } else {
-#pragma unroll
-                            for (int r = 0; r < R; ++r)
-                                adj_taps_int(base, par_sigma(par_xpart(oxy[r & 3], P), oyy[r >> 2], P), vy[r], tby[r]);
-                        }
+                        adj_par_view<R>(P, base, xmaj, oxx, oyx, oxy, oyy, vx, vy, tbx, tby);
                     } else {
-                        auto fan_fast = [&](auto vc) {
-                            constexpr int V = decltype(vc)::value;
-                            if (xmaj) {
-                                const FanX X = fan_xpart(oxx, P);
-#pragma unroll
-                                for (int r = 0; r < R; ++r) {
-                                    float w;
-                                    const float sig = fan_sigma<V>(X, oyx[r], P, c, &w);
-                                    adj_taps(base + 4u * __float_as_uint(__fadd_rn(sig, kMagic)), sig,
-                                             __fmul_rn(vx[r], w));
-                                }
-                            } else {
-#pragma unroll
-                                for (int r = 0; r < R; ++r) {
-                                    float w;
-                                    const float sig = fan_sigma<V>(fan_xpart(oxy[r & 3], P), oyy[r >> 2], P, c, &w);
-                                    adj_taps(base + 4u * __float_as_uint(__fadd_rn(sig, kMagic)), sig,
-                                             __fmul_rn(vy[r], w));
-                                }
-                            }
-                        };
                         switch (mode_variant(P.mode)) {
-                            case 0: fan_fast(std::integral_constant<int, 0>{}); break;
-                            case 1: fan_fast(std::integral_constant<int, 1>{}); break;
-                            default: fan_fast(std::integral_constant<int, 2>{}); break;
+                            case 0: adj_fan_view<0, R>(P, base, xmaj, oxx, oyx, oxy, oyy, vx, vy, c); break;
+                            case 1: adj_fan_view<1, R>(P, base, xmaj, oxx, oyx, oxy, oyy, vx, vy, c); break;
+                            default: adj_fan_view<2, R>(P, base, xmaj, oxx, oyx, oxy, oyy, vx, vy, c); break;
                         }
                     }
                     continue;

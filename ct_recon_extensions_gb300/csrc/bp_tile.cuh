@@ -520,9 +520,30 @@ __device__ __forceinline__ float2 make_pair(float p0, float p1, int k, int kc, f
 // plus 8 kc, less 8 kMagicBits.
 // Rows are taken in pairs: the position arithmetic of rows r and r+1 runs as
 // packed FP32 pairs (FFMA2 / FADD2 / FMUL2, each half rounded as the scalar
-// operation, so positions are bit-identical to fan_sigma / par_sigma and to
-// the adjoint's).
+// operation, so positions are bit-identical to fan_sigma / par_sigma and the
+// forward's and adjoint's taps agree).
 __device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
+
+// a - b per half (an FMA with -1: exact negation, one rounding).
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, dup2(-1.0f), a); }
+
+// fan_sigma for two pixels (x parts xn, xd; y offsets o), with their weights.
+template <int V>
+__device__ __forceinline__ float2 fan_sigma2(float2 xn, float2 xd, float2 o, const FastRec& P,
+                                             const TileConst& c, float2* w)
+{
+    constexpr int da = kRelAtanDeg[V];
+    const float2 n = __ffma2_rn(o, dup2(P.p1), xn);
+    const float2 dn = __ffma2_rn(o, dup2(-P.p0), xd);  // -oy p0 + d
+    const float2 t = __fmul2_rn(n, make_float2(rcp_approx(dn.x), rcp_approx(dn.y)));
+    const float2 z = __fmul2_rn(t, t);
+    float2 pp = dup2(c.apoly[V][da]);
+#pragma unroll
+    for (int k = da - 1; k >= 0; --k) pp = __ffma2_rn(z, pp, dup2(c.apoly[V][k]));
+    const float2 q = __ffma2_rn(dn, dn, __fmul2_rn(n, n));
+    *w = make_float2(rcp_approx(q.x), rcp_approx(q.y));
+    return __ffma2_rn(t, pp, dup2(P.cen));
+}
 
 template <Geo G, int V, int R>
 __device__ __forceinline__ void fast_rows(float ox, const float (&oy)[R], const FastRec& P,
@@ -531,26 +552,17 @@ __device__ __forceinline__ void fast_rows(float ox, const float (&oy)[R], const 
     static_assert(R % 2 == 0, "rows are taken in pairs");
     const float2 mag = dup2(kMagic);
     if constexpr (G == Geo::kFan) {
-        constexpr int da = kRelAtanDeg[V];
         const FanX X = fan_xpart(ox, P);
-        const float2 xn = dup2(X.n), xd = dup2(X.d), p1 = dup2(P.p1), mp0 = dup2(-P.p0), cen = dup2(P.cen);
+        const float2 xn = dup2(X.n), xd = dup2(X.d);
 #pragma unroll
         for (int r = 0; r < R; r += 2) {
-            const float2 o = make_float2(oy[r], oy[r + 1]);
-            const float2 n = __ffma2_rn(o, p1, xn);
-            const float2 dn = __ffma2_rn(o, mp0, xd);  // -oy p0 + d, as fan_sigma
-            const float2 t = __fmul2_rn(n, make_float2(rcp_approx(dn.x), rcp_approx(dn.y)));
-            const float2 z = __fmul2_rn(t, t);
-            float2 pp = dup2(c.apoly[V][da]);
-#pragma unroll
-            for (int k = da - 1; k >= 0; --k) pp = __ffma2_rn(z, pp, dup2(c.apoly[V][k]));
-            const float2 q = __ffma2_rn(dn, dn, __fmul2_rn(n, n));
-            const float2 sig = __ffma2_rn(t, pp, cen);
+            float2 w;
+            const float2 sig = fan_sigma2<V>(xn, xd, make_float2(oy[r], oy[r + 1]), P, c, &w);
             const float2 tm = __fadd2_rn(sig, mag);
             const float2 pa = lds_f2(base + 8u * __float_as_uint(tm.x));
             const float2 pb = lds_f2(base + 8u * __float_as_uint(tm.y));
-            part[r] = fmaf(fmaf(sig.x, pa.y, pa.x), rcp_approx(q.x), part[r]);
-            part[r + 1] = fmaf(fmaf(sig.y, pb.y, pb.x), rcp_approx(q.y), part[r + 1]);
+            part[r] = fmaf(fmaf(sig.x, pa.y, pa.x), w.x, part[r]);
+            part[r + 1] = fmaf(fmaf(sig.y, pb.y, pb.x), w.y, part[r + 1]);
         }
     } else {
         const float2 xs = dup2(par_xpart(ox, P)), p1 = dup2(P.p1);
