@@ -702,13 +702,7 @@ constexpr int kTileCtasPerSm = 2;
 // Shared memory one tile CTA may take (two CTAs per SM).
 constexpr size_t kTileSmemMax = 110 * 1024;
 
-int sm_count()
-{
-    int dev = 0, sms = kSmCount;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return sms;
-}
+int sm_count() { return device_sms(); }
 
 // Shared bytes of the bulk-copy forward kernel with NG groups of VB views.
 inline size_t fwd_smem(const TileConst& ct, int VB, int NG = 1)

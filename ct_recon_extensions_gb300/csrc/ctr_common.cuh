@@ -40,6 +40,18 @@ __device__ __forceinline__ void raise_flag(unsigned int f) { atomicOr(&g_kernel_
 // ---- launch geometry --------------------------------------------------------
 constexpr int kSmCount = 152;  // GB300: 2 dies x 76 SMs
 
+// SMs of the current device (kSmCount when the query fails).
+inline int device_sms()
+{
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) {
+        cudaGetLastError();
+        return kSmCount;
+    }
+    return sms;
+}
+
 inline unsigned int div_up(unsigned long long a, unsigned long long b)
 {
     return static_cast<unsigned int>((a + b - 1) / b);

@@ -107,6 +107,7 @@ constexpr int kFilterMaxThreads = 1024;
 constexpr int kFilterTaskThreads = kFilterMaxThreads - 32;
 constexpr int kFilterPad = 16;   // zero taps beyond the ends of H
 constexpr int kFilterRowsPlain = 2;
+constexpr int kFilterRowsSpread = 3;
 
 // Thread tasks of a row: (8-output block, parity).  When twice that fits one
 // CTA, each task's inputs are split in two halves run by two threads, whose
@@ -371,16 +372,25 @@ __device__ __forceinline__ void filter_rows(const T* __restrict__ in, const doub
     __syncthreads();  // shared buffers are free for the caller's next call
 }
 
-template <typename T, bool kGrad>
+// kRows rows a CTA; with `spread` the rows are instead dealt evenly over the
+// grid (CTA i: rows [i*rows/G, (i+1)*rows/G), at most kRows), so a grid of
+// exactly the resident CTAs finishes in one wave.
+template <typename T, bool kGrad, int kRows>
 __global__ void __launch_bounds__(kFilterMaxThreads)
     ramp_filter_kernel(const T* __restrict__ in, const double* __restrict__ filter,
                        T* __restrict__ out, const float* __restrict__ weight, unsigned ns,
-                       unsigned long long rows, double ds, int tg)
+                       unsigned long long rows, double ds, int tg, int spread)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const unsigned long long r0 = static_cast<unsigned long long>(blockIdx.x) * kFilterRowsPlain;
-    const int nr = static_cast<int>(rows - r0 < kFilterRowsPlain ? rows - r0 : kFilterRowsPlain);
-    filter_rows<T, kFilterRowsPlain, kGrad>(in, filter, out, weight, ns, r0, nr, ds, tg, smem_raw);
+    unsigned long long r0, r1;
+    if (spread) {
+        r0 = static_cast<unsigned long long>(blockIdx.x) * rows / gridDim.x;
+        r1 = static_cast<unsigned long long>(blockIdx.x + 1) * rows / gridDim.x;
+    } else {
+        r0 = static_cast<unsigned long long>(blockIdx.x) * kRows;
+        r1 = rows - r0 < kRows ? rows : r0 + kRows;
+    }
+    filter_rows<T, kRows, kGrad>(in, filter, out, weight, ns, r0, static_cast<int>(r1 - r0), ds, tg, smem_raw);
 }
 
 // Batched FP32 filtering with pre-weighting: one CTA per (job, row block).
@@ -406,16 +416,39 @@ int launch_ramp_filter(const ctr_filter_param* p, const T* in, const double* fil
     if (p->ns < 1 || p->nrow < 1) return fail(CTR_ERR_INVALID_ARG, "empty sinogram");
     if (in == out) return fail(CTR_ERR_INVALID_ARG, "ramp filter cannot run in place");
     const unsigned long long rows = static_cast<unsigned long long>(p->nrow) * batch;
+    const int threads = filter_block<T>(p->ns);
+    // Up to kFilterRowsSpread rows a CTA dealt over the resident CTAs (one
+    // wave, CTAs within a row of each other); more rows take CTAs of
+    // kFilterRowsPlain rows in waves.
+    {
+        const int tg = filter_layout<T>(p->ns, kFilterRowsSpread);
+        const size_t smem = filter_smem<T>(p->ns, kFilterRowsSpread, tg);
+        auto kern = ramp_filter_kernel<T, kGrad, kFilterRowsSpread>;
+        int per_sm = 0;
+        if (smem <= kFilterSmemMax &&
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) ==
+                cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) == cudaSuccess &&
+            per_sm > 0) {
+            const unsigned long long resident = static_cast<unsigned long long>(per_sm) * device_sms();
+            if (rows <= kFilterRowsSpread * resident) {
+                const unsigned blocks = static_cast<unsigned>(rows < resident ? rows : resident);
+                kern<<<blocks, threads, smem, stream>>>(in, filter, out, weight, p->ns, rows, p->ds, tg, 1);
+                return check_launch("ramp_filter");
+            }
+        }
+        cudaGetLastError();
+    }
     const int tg = filter_layout<T>(p->ns, kFilterRowsPlain);
     const size_t smem = filter_smem<T>(p->ns, kFilterRowsPlain, tg);
     if (smem > kFilterSmemMax)
         return fail(CTR_ERR_UNSUPPORTED, "ns=%u exceeds the filter's shared-memory tile", p->ns);
-    auto kern = ramp_filter_kernel<T, kGrad>;
+    auto kern = ramp_filter_kernel<T, kGrad, kFilterRowsPlain>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "filter smem: %s", cudaGetErrorString(e));
     const unsigned blocks = div_up(rows, kFilterRowsPlain);
-    kern<<<blocks, filter_block<T>(p->ns), smem, stream>>>(in, filter, out, weight, p->ns, rows, p->ds, tg);
+    kern<<<blocks, threads, smem, stream>>>(in, filter, out, weight, p->ns, rows, p->ds, tg, 0);
     return check_launch("ramp_filter");
 }
 
