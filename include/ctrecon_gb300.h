@@ -267,12 +267,14 @@ int ctr_fp_par_2d_grad_f64(const ctr_par_param* p, const double* proj, double* i
  *      include/fp_par_2d.h:227-244, with the per-call ray set-up done once) ----
  * ctr_fp_par_2d_plan_create builds, from the prep tables above (read on
  * `stream`, which it synchronises; the tables may be freed afterwards), every
- * ray's fixed-point start and step, exact sample range and class, the
- * reference's decisions for rays that end within a rounding of the image
- * border, and a transposed-image workspace for max_batch images.  A run then
- * gives the same results as ctr_fp_par_2d_f32 with two launches (transposed
- * copy, projector) and no allocation; img must be 16-byte aligned.  A plan
- * serves one stream at a time, on the device it was made on. */
+ * ray's fixed-point start and step, exact sample range and class (as a model
+ * line per view plus the rays that differ from it), the reference's decisions
+ * for rays that end within a rounding of the image border, and a
+ * transposed-image workspace for max_batch images.  A run then gives the same
+ * results as ctr_fp_par_2d_f32 bit for bit with no allocation: one launch for
+ * one image (the projector makes its own transposed copy; a cooperative
+ * launch), two for a batch (transposed copy, projector); img must be 16-byte
+ * aligned.  A plan serves one stream at a time, on the device it was made on. */
 typedef struct ctr_fp_plan ctr_fp_plan;
 int ctr_fp_par_2d_plan_create(const ctr_par_param* p, const double* sincostbl,
                               const double* beginoffset, const int* usex, int max_batch,
