@@ -1209,6 +1209,10 @@ def run_reference(args):
         "e2e": {"value": v, "unit": "slices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "updates_per_s": v * g["nx"] * g["ny"] * g["na"],
     }
+    if k == "port":
+        line["cpu_baseline"]["note"] = ("the reference's own src/ was not built on this host (its checkout is "
+                                        "absent), so the oracle port runs: the reference's CPU algorithm "
+                                        "restated in C, bit-exact to fixtures made by the reference build")
     print(json.dumps(line))
 
 
