@@ -580,6 +580,7 @@ __global__ void __launch_bounds__(kFpxThreads, 1)
                 float* __restrict__ proj, const FpxConst c, const FpxRays r,
                 unsigned long long* __restrict__ tsync, unsigned long long ttarget)
 {
+    static_assert(CH >= 2 && CH % 2 == 0, "a chunk's rows are taken in pairs");
     extern __shared__ __align__(128) unsigned char fpx_dyn[];
     float* stage = reinterpret_cast<float*>(fpx_dyn + ((128u - (smem_u32(fpx_dyn) & 127u)) & 127u));
     __shared__ __align__(8) unsigned long long s_full[kFpxStages], s_empty[kFpxStages];
@@ -1505,10 +1506,11 @@ bool fpx_const(const ctr_par_param* p, const void* img, int batch, FpxConst* out
         c.sms = kSmCount;
     const long long ctas = div_up(slots, c.sms) <= kFpxRound ? static_cast<long long>(c.sms) : div_up(slots * 8, kFpxRound * 7);
     c.ctas = static_cast<int>(std::min<long long>(ctas, slots));
-    // rows per stage: a multiple of the projector's chunk (16 or 8 rows) where
-    // 8 rows fit the nominal stage
+    // rows per stage: a multiple of the projector's chunk of 16, 8 or 2 rows
+    // (the chunk's rows are taken in pairs, so never fewer than 2)
     c.band = std::max(1, std::min(32, kFpxStageFloats / n));
-    c.band = c.band >= 16 ? c.band / 16 * 16 : (c.band >= 8 ? 8 : c.band);
+    c.band = c.band >= 16 ? c.band / 16 * 16 : (c.band >= 8 ? 8 : c.band & ~1);
+    if (c.band < 2) return false;
     c.nbands = static_cast<int>(div_up(n, c.band));
     c.stage_floats = (c.band * n + 8 + 31) / 32 * 32;
     c.total = static_cast<long long>(batch) * n * n;
@@ -1590,7 +1592,7 @@ using FpxKernel = void (*)(const float*, float*, float*, FpxConst, FpxRays, unsi
 
 FpxKernel fpx_kernel(const FpxConst& c, size_t smem, cudaError_t* e)
 {
-    const FpxKernel k = c.band % 16 == 0 ? fp_proj_f32<16> : (c.band % 8 == 0 ? fp_proj_f32<8> : fp_proj_f32<1>);
+    const FpxKernel k = c.band % 16 == 0 ? fp_proj_f32<16> : (c.band % 8 == 0 ? fp_proj_f32<8> : fp_proj_f32<2>);
     *e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     return k;
 }

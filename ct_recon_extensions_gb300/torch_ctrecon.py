@@ -351,7 +351,8 @@ class ParallelProjection2DOp:
     include/fp_par_2d.h:283-352; its adjoint is the reference's distance-driven
     grad, which the reference op registers as the gradient).  FP32 ray-driven
     calls run through a per-geometry plan (ctr_fp_par_2d_plan_*): the ray
-    set-up runs once per device, a call is the transposed copy and the
+    set-up runs once per device; a one-image call is one projector launch
+    (which makes its own transposed copy), a batch the transposed copy and the
     projector."""
 
     def __init__(self, ns, na, ds, orbit, offset_s, orbit_start, nx, ny, dx, dy, offset_x,

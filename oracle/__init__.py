@@ -305,10 +305,13 @@ class Oracle:
         self._fn("fp_par_2d_grad_prep")(ctypes.byref(g), _p(w), _p(pos), _p(usex))
         return w, pos, usex
 
-    def fp_par_2d(self, img, g: Geom):
+    def fp_par_2d(self, img, g: Geom, tables=None):
+        """Ray-driven projection; `tables` = (sincos, beginoffset, usex) in
+        place of the prep's own (a caller's table, as the reference's op takes)."""
         img = self._c(img)
         assert img.shape == (g.ny, g.nx)
-        sc, bo, usex = self.fp_par_2d_tables(g)
+        sc, bo, usex = self.fp_par_2d_tables(g) if tables is None else (
+            self._c(tables[0], np.float64), self._c(tables[1], np.float64), self._c(tables[2], np.int32))
         proj = np.empty((g.na, g.ns), dtype=img.dtype)
         if self.kind == "reference":
             self._fn(f"fp_par_2d_{_sfx(img.dtype)}")(ctypes.byref(g), _p(img), _p(proj), _p(sc),
