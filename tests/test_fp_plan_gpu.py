@@ -5,8 +5,9 @@
   per-call entry point matches the oracle run on the same table, and the plan
   (one image: the projector makes its own transposed copy; a batch: a separate
   copy) matches the per-call entry point bit for bit.
-* Images whose bands take the projector's 8-row and 1-row chunk kernels (nx
-  above 1024 and above 2048) match the oracle.
+* Images whose bands take the projector's 8-row and 2-row chunk kernels (nx
+  above 1024 and above 2048) match the oracle, and so does a geometry with
+  more ray slots than one round of one CTA per SM.
 Reference: src/fp_par_2d.cc:149-280 (the table and the ray march).
 """
 import ctypes
@@ -96,8 +97,8 @@ def test_fp_rays_off_the_view_model(oracle_port):
 
 @pytest.mark.parametrize("n", [1100, 2100])
 def test_fp_chunk_paths_vs_oracle(oracle_port, n):
-    """nx = 1100 takes 8-row bands and chunks, nx = 2100 7-row bands and
-    1-row chunks; the FoV-covering detector keeps every ray range exact."""
+    """nx = 1100 takes 8-row bands and chunks, nx = 2100 6-row bands and
+    2-row chunks; the FoV-covering detector keeps every ray range exact."""
     import torch
     from oracle import Geom
     d = _geom(n, 36)
@@ -110,3 +111,24 @@ def test_fp_chunk_paths_vs_oracle(oracle_port, n):
     ref = _per_call(op, cuda(img)[None], op.tables(torch.device("cuda")))
     torch.cuda.synchronize()
     assert np.array_equal(out, host(ref[0]))
+
+
+def test_fp_many_slots_vs_oracle(oracle_port):
+    """720 views x 1501 channels on a 256^2 image: more slots than one CTA per
+    SM holds in a round, so the projector runs more CTAs than SMs and the plan
+    keeps the separate transposed copy."""
+    import torch
+    from oracle import Geom
+    d = dict(ns=1501, na=720, ds=0.25, orbit=math.pi / 720, offset_s=0.0, orbit_start=0.0,
+             nx=256, ny=256, dx=0.5, dy=0.5, offset_x=0.0, offset_y=0.0, fov=-1.0)
+    g = Geom.make(**d)
+    op = fp_op(d)
+    rng = np.random.default_rng(77)
+    imgs = cuda(np.stack([rng.random((256, 256)), rng.standard_normal((256, 256))]).astype(np.float32))
+    out = host(op.forward(imgs))
+    for k in range(2):
+        assert rel_l2(out[k], oracle_port.fp_par_2d(host(imgs[k]), g)) <= 1e-5
+    ref = _per_call(op, imgs, op.tables(torch.device("cuda")))
+    torch.cuda.synchronize()
+    assert np.array_equal(out, host(ref))
+    assert np.array_equal(host(op.forward(imgs[1])), out[1])
