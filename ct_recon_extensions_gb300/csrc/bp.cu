@@ -83,35 +83,12 @@ __device__ __forceinline__ int round_int(float x)
     return static_cast<int>(__float_as_uint(__fadd_rn(x, kMagic)) - kMagicBits);
 }
 
-// The two taps of one pixel with fixed-point value t at window-relative
-// position sig (j = round(sig) + kc, accumulator address addr of j):
-// (round(t) - q1) at j and q1 = round(t u) at j + 1, u = sig - round(sig) + 1/2.
-__device__ __forceinline__ void adj_taps(unsigned addr, float sig, float t)
-{
-    const float r = round_sigma(sig);
-    const float u = __fadd_rn(__fadd_rn(sig, -r), 0.5f);
-    const int q1 = static_cast<int>(__float_as_uint(__fmaf_rn(t, u, kMagic)) - kMagicBits);
-    const int q0 = round_int(t) - q1;
-    red_shared_u32(addr, static_cast<unsigned>(q0));
-    red_shared_u32(addr + 4u, static_cast<unsigned>(q1));
-}
-
-// The two taps of a parallel-beam pixel whose fixed-point value tq is an
-// integer, tb = bits(tq + 1.5*2^23) (both formed once per tile): q1 =
-// round(tq u) at j + 1 and tq - q1 at j, u = sig - round(sig) + 1/2 with the
-// half folded into the rounding constant of the FMA.
-__device__ __forceinline__ void adj_taps_int(unsigned base, float sig, float tq, unsigned tb)
-{
-    const float vb = __fadd_rn(sig, kMagic);
-    const unsigned addr = base + 4u * __float_as_uint(vb);
-    const float d = __fadd_rn(sig, -__fadd_rn(vb, -kMagic));
-    const unsigned q1b = __float_as_uint(__fmaf_rn(tq, d, __fmaf_rn(tq, 0.5f, kMagic)));
-    red_shared_u32(addr, tb - q1b);
-    red_shared_u32(addr + 4u, q1b - kMagicBits);
-}
-
-// adj_taps_int for two pixels, the FP32 steps packed (same roundings as two
-// calls).
+// The two taps of two parallel-beam pixels whose fixed-point values tq are
+// integers, tb = bits(tq + 1.5*2^23) (formed once per tile), at window-relative
+// positions sig (j = round(sig) + kc, accumulator address base + 4 bits(sig +
+// 1.5*2^23)): q1 = round(tq u) at j + 1 and tq - q1 at j, u = sig - round(sig)
+// + 1/2 with the half folded into the rounding constant of the FMA.  The FP32
+// steps of the two pixels run as packed pairs.
 __device__ __forceinline__ void adj_taps_int2(unsigned base, float2 sig, float2 tq, unsigned tb0, unsigned tb1)
 {
     const float2 vb = __fadd2_rn(sig, dup2(kMagic));
@@ -125,7 +102,9 @@ __device__ __forceinline__ void adj_taps_int2(unsigned base, float2 sig, float2 
     red_shared_u32(a1 + 4u, q1 - kMagicBits);
 }
 
-// adj_taps for two pixels (fixed-point values t), the FP32 steps packed.
+// The two taps of two pixels with fixed-point values t at window-relative
+// positions sig: (round(t) - q1) at j = round(sig) + kc and q1 = round(t u) at
+// j + 1, u = sig - round(sig) + 1/2.  The FP32 steps run as packed pairs.
 __device__ __forceinline__ void adj_taps2(unsigned base, float2 sig, float2 t)
 {
     const float2 vb = __fadd2_rn(sig, dup2(kMagic));  // round(sig) in its bits: the address
