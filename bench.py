@@ -248,7 +248,7 @@ class ParPipeline:
                                                 g["fov"])
         self.fplan = self.fp.plan(device, 1)  # per-geometry ray tables, built once
         self.taps = ctypes.c_void_p(self.ramp.taps(device).data_ptr())
-        self.bpt = [ctypes.c_void_p(t.data_ptr()) for t in self.bp.tables(device)]
+        self.bplan = self.bp.plan(device, 1)  # per-geometry tables, scratch and view constants
         f32 = dict(dtype=torch.float32, device=device)
         self.sino = torch.empty((g["na"], g["ns"]), **f32)
         self.filt = torch.empty((g["na"], g["ns"]), **f32)
@@ -273,9 +273,8 @@ class ParPipeline:
         yield lambda: L.ctr_ramp_filter_f32(ctypes.byref(self.ramp.p),
                                             ctypes.c_void_p(self.sino.data_ptr()), self.taps,
                                             ctypes.c_void_p(self.filt.data_ptr()), 1, s)
-        yield lambda: L.ctr_bp_par_2d_f32(ctypes.byref(self.bp.p),
-                                          ctypes.c_void_p(self.filt.data_ptr()),
-                                          ctypes.c_void_p(out.data_ptr()), *self.bpt, None, 1, s)
+        yield lambda: L.ctr_bp_plan_run(self.bplan, ctypes.c_void_p(self.filt.data_ptr()),
+                                        ctypes.c_void_p(out.data_ptr()), 1, s)
 
 
 class FanPipeline:
@@ -293,7 +292,7 @@ class FanPipeline:
                                            g["orbit_start"], g["nx"], g["ny"], g["dx"], g["dy"],
                                            g["offset_x"], g["offset_y"], g["dso"], g["dsd"], g["fov"])
         self.taps = ctypes.c_void_p(self.ramp.taps(device).data_ptr())
-        self.bpt = [ctypes.c_void_p(t.data_ptr()) for t in self.bp.tables(device)]
+        self.bplan = self.bp.plan(device, 1)  # per-geometry tables, scratch and view constants
         f32 = dict(dtype=torch.float32, device=device)
         self.wt = torch.empty((g["na"], g["ns"]), **f32)
         self.filt = torch.empty((g["na"], g["ns"]), **f32)
@@ -314,8 +313,8 @@ class FanPipeline:
                                               ctypes.c_void_p(self.wt.data_ptr()), 1, s)
         yield lambda: L.ctr_ramp_filter_f32(ctypes.byref(self.ramp.p), ctypes.c_void_p(self.wt.data_ptr()),
                                             self.taps, ctypes.c_void_p(self.filt.data_ptr()), 1, s)
-        yield lambda: L.ctr_bp_fan_2d_f32(ctypes.byref(self.bp.p), ctypes.c_void_p(self.filt.data_ptr()),
-                                          ctypes.c_void_p(out.data_ptr()), *self.bpt, 1, s)
+        yield lambda: L.ctr_bp_plan_run(self.bplan, ctypes.c_void_p(self.filt.data_ptr()),
+                                        ctypes.c_void_p(out.data_ptr()), 1, s)
 
 
 class LowpFanPipeline:
@@ -336,7 +335,7 @@ class LowpFanPipeline:
         self.bp = tc.FanBackprojection2DOp(g["ns"], g["na"], g["ds"], g["orbit"], g["offset_s"],
                                            g["orbit_start"], g["nx"], g["ny"], g["dx"], g["dy"],
                                            g["offset_x"], g["offset_y"], g["dso"], g["dsd"], g["fov"])
-        self.bpt = [ctypes.c_void_p(t.data_ptr()) for t in self.bp.tables(device)]
+        self.bplan = self.bp.plan(device, 1)  # per-geometry tables, scratch and view constants
         self.filt = torch.empty((g["na"], g["ns"]), dtype=torch.float32, device=device)
         self.names = ["ramp_filter_tc", "bp_fan_2d"]
         self.kernels = {"ramp_filter_tc": 2, "bp_fan_2d": 1}
@@ -350,8 +349,8 @@ class LowpFanPipeline:
         s = ctypes.c_void_p(stream)
         yield lambda: L.ctr_ramp_filter_tc_run(self.plan, self.dt, ctypes.c_void_p(sino.data_ptr()),
                                                ctypes.c_void_p(self.filt.data_ptr()), 1, s)
-        yield lambda: L.ctr_bp_fan_2d_f32(ctypes.byref(self.bp.p), ctypes.c_void_p(self.filt.data_ptr()),
-                                          ctypes.c_void_p(out.data_ptr()), *self.bpt, 1, s)
+        yield lambda: L.ctr_bp_plan_run(self.bplan, ctypes.c_void_p(self.filt.data_ptr()),
+                                        ctypes.c_void_p(out.data_ptr()), 1, s)
 
 
 # per-kernel CUDA events are recorded on every KERNEL_EVERY-th timed step only,
@@ -471,13 +470,16 @@ def op_call(op, which, x, out, sp):
     xi, oi = ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr())
     if isinstance(op, tc.FanBackprojection2DOp):
         t = [ctypes.c_void_p(a.data_ptr()) for a in op.tables(x.device)]
-        call("ctr_bp_fan_2d_f32" if which == "forward" else "ctr_bp_fan_2d_grad_f32", p, xi, oi, *t, 1, s)
+        if which == "forward":
+            call("ctr_bp_plan_run", op.plan(x.device, 1), xi, oi, 1, s)
+        else:
+            call("ctr_bp_plan_run_grad", op.plan(x.device, 1), xi, oi, 1, s)
     elif isinstance(op, tc.ParallelBackprojection2DOp):
         t = [ctypes.c_void_p(a.data_ptr()) for a in op.tables(x.device)]
         if which == "forward":
-            call("ctr_bp_par_2d_f32", p, xi, oi, *t, None, 1, s)
+            call("ctr_bp_plan_run", op.plan(x.device, 1), xi, oi, 1, s)
         elif which == "adjoint":
-            call("ctr_bp_par_2d_grad_f32", p, xi, oi, *t, 1, s)
+            call("ctr_bp_plan_run_grad", op.plan(x.device, 1), xi, oi, 1, s)
         else:
             call("ctr_bp_par_2d_sv_f32", p, xi, oi, *t, None, 1, s)
     elif isinstance(op, tc.RampFilterOp):

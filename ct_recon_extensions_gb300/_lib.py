@@ -113,6 +113,11 @@ PROTOTYPES = {
     "ctr_fp_par_2d_plan_create": [_S(ParParam), _P, _P, _P, c_int, ctypes.POINTER(c_void_p), _P],
     "ctr_fp_par_2d_plan_run": [c_void_p, _P, _P, c_int, _P],
     "ctr_fp_par_2d_plan_destroy": [c_void_p],
+    "ctr_bp_par_2d_plan_create": [_S(ParParam), _P, _P, c_int, ctypes.POINTER(c_void_p), _P],
+    "ctr_bp_fan_2d_plan_create": [_S(FanBpParam), _P, _P, _P, c_int, ctypes.POINTER(c_void_p), _P],
+    "ctr_bp_plan_run": [c_void_p, _P, _P, c_int, _P],
+    "ctr_bp_plan_run_grad": [c_void_p, _P, _P, c_int, _P],
+    "ctr_bp_plan_destroy": [c_void_p],
     "ctr_fp_par_2d_cast_prep": [_S(ParParam), c_double, _P, _P, _P, _P],
     "ctr_fp_par_2d_dd_prep": [_S(ParParam), _P, _P, _P, _P],
     "ctr_fp_par_2d_dd_grad_prep": [_S(ParParam), _P, _P, _P, _P],

@@ -25,6 +25,7 @@
 // src/bp_par_2d.cc:51-90, src/bp_par_2d_sv.cc:55-92).  The FP64 adjoint uses
 // global atomics per tap.
 #include <cfloat>
+#include <memory>
 #include <type_traits>
 
 #include "bp_tile.cuh"
@@ -63,6 +64,8 @@ struct AdjUnits {
     long long units;  // tiles x nb
     int nb;           // view blocks per tile
     int tiles_x, tiles_per_item;
+    const FastRec* rec;  // a plan's per-(tile, view) records, or null (set up here)
+    const ViewAux* aux;
 };
 
 constexpr int kAdjChunkBlocks = 64;  // view records set up per chunk of blocks
@@ -269,7 +272,20 @@ __global__ void __launch_bounds__(kBpThreads, 2)
                 const int vb = min(min(b1, b + kAdjChunkBlocks) * kViewBlock, c.na);
                 __syncthreads();
                 for (int ia = va + tid; ia < vb; ia += kBpThreads) {
-                    ViewRec P = view_setup<G>(t0, t1, t2, ia, B, c);
+                    ViewRec P;
+                    if (k.rec) {
+                        const size_t ti = static_cast<size_t>(tl) * c.na + ia;
+                        const FastRec F = k.rec[ti];
+                        const ViewAux A = k.aux[ti];
+                        P.p0 = F.p0;
+                        P.p1 = F.p1;
+                        P.cen = F.cen;
+                        P.mode = F.mode;
+                        P.e = A.e;
+                        P.lo = A.lo;
+                    } else {
+                        P = view_setup<G>(t0, t1, t2, ia, B, c);
+                    }
                     if (mode_fast(P.mode))
                         P.mode = adj_fast_mode(win_base + 4u * static_cast<unsigned>((ia % kViewBlock) * c.W), c,
                                                P.mode);
@@ -690,42 +706,99 @@ inline size_t fwd_smem(const TileConst& ct, int VB, int NG = 1)
     return 128 + 2 * bv * ct.WS * sizeof(float) + 2 * bv * ct.W * sizeof(float2) + ct.na * kViewBytes;
 }
 
-// The bulk-copy kernel (one group of VB views, tiles of 32 x kTileY): stream-K
-// over (tile, view block) units when the launch has fewer than 4 waves of
-// tiles, one CTA per tile otherwise.
+// A backprojection plan's device resources (ctr_bp_plan): stream-K scratch
+// whose tile counters (at its start) stay zero between launches, as the CTA
+// completing a tile resets its counter, and the geometry's per-(tile, view)
+// records (or null: the kernels set them up).
+struct BpPlanRes {
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    long long max_tiles = 0;  // counters at the start of scratch
+    const FastRec* rec = nullptr;
+    const ViewAux* aux = nullptr;
+};
+
+// Stream-K launch shape of the bulk-copy kernel for `batch` items: whether it
+// applies (fewer than 4 waves of tiles and more than one view block), its CTAs
+// and scratch bytes (counters first, then the partial sums).
+struct SkShape {
+    bool on = false;
+    int ctas = 0;
+    SkConst k{};
+    size_t bytes = 0;
+};
+
 template <Geo G, int VB>
-int launch_tma(const float* proj, float* img, const double* t0, const double* t1, const double* t2,
-               const TileConst& ct, int batch, cudaStream_t stream, const char* what)
+SkShape sk_shape(const TileConst& ct, int batch)
 {
-    constexpr int kR = kRowsPerThread;
+    SkShape sh;
     const size_t smem = fwd_smem(ct, VB);
     const int tiles_x = static_cast<int>(div_up(ct.nx, kTileX));
     const int tiles_y = static_cast<int>(div_up(ct.ny, kTileY));
     const long long tiles = static_cast<long long>(tiles_x) * tiles_y * batch;
     const int nb = static_cast<int>(div_up(ct.na, VB));
     const int sms = sm_count();
-    if (tiles < 4ll * sms * kTileCtasPerSm && nb > 1) {
-        SkConst k{};
-        k.units = tiles * nb;
-        k.nb = nb;
-        k.tiles_x = tiles_x;
-        k.tiles_per_item = tiles_x * tiles_y;
+    if (!(tiles < 4ll * sms * kTileCtasPerSm && nb > 1)) return sh;
+    auto kern = bp_tile_tma_sk<G, kRowsPerThread, VB, 1, kTileCtasPerSm>;
+    int per_sm = 1;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBpThreads, smem) != cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        return sh;
+    }
+    sh.on = true;
+    sh.k.units = tiles * nb;
+    sh.k.nb = nb;
+    sh.k.tiles_x = tiles_x;
+    sh.k.tiles_per_item = tiles_x * tiles_y;
+    sh.ctas = static_cast<int>(std::min<long long>(sh.k.units, static_cast<long long>(sms) * per_sm));
+    sh.k.maxseg = sk_max_segments(tiles, nb, sh.ctas);
+    const size_t counters = (sizeof(int) * static_cast<size_t>(tiles) + 255) & ~static_cast<size_t>(255);
+    sh.bytes = counters + static_cast<size_t>(tiles) * sh.k.maxseg * kTileX * kTileY * sizeof(float);
+    return sh;
+}
+
+// The bulk-copy kernel (one group of VB views, tiles of 32 x kTileY): stream-K
+// over (tile, view block) units when the launch has fewer than 4 waves of
+// tiles, one CTA per tile otherwise.  With a plan's resources the stream-K
+// scratch is the plan's (no allocation, no counter reset) and the view records
+// come from its table.
+template <Geo G, int VB>
+int launch_tma(const float* proj, float* img, const double* t0, const double* t1, const double* t2,
+               const TileConst& ct, int batch, cudaStream_t stream, const char* what,
+               const BpPlanRes* pr = nullptr)
+{
+    constexpr int kR = kRowsPerThread;
+    const size_t smem = fwd_smem(ct, VB);
+    const int tiles_x = static_cast<int>(div_up(ct.nx, kTileX));
+    const int tiles_y = static_cast<int>(div_up(ct.ny, kTileY));
+    const FastRec* rec = pr ? pr->rec : nullptr;
+    const ViewAux* aux = pr ? pr->aux : nullptr;
+    SkShape sh = sk_shape<G, VB>(ct, batch);
+    if (sh.on) {
         auto kern = bp_tile_tma_sk<G, kR, VB, 1, kTileCtasPerSm>;
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             static_cast<int>(smem));
-        int per_sm = 1;
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBpThreads, smem);
-        if (e != cudaSuccess || per_sm < 1) return fail(CTR_ERR_CUDA, "%s: occupancy", what);
-        const int ctas = static_cast<int>(std::min<long long>(k.units, static_cast<long long>(sms) * per_sm));
-        k.maxseg = sk_max_segments(tiles, nb, ctas);
-        const size_t part_bytes = static_cast<size_t>(tiles) * k.maxseg * kTileX * kTileY * sizeof(float);
+        const long long tiles = sh.k.units / sh.k.nb;
+        const size_t counters = (sizeof(int) * static_cast<size_t>(tiles) + 255) & ~static_cast<size_t>(255);
+        sh.k.rec = rec;
+        sh.k.aux = aux;
+        const size_t plan_counters =
+            pr ? (sizeof(int) * static_cast<size_t>(pr->max_tiles) + 255) & ~static_cast<size_t>(255) : 0;
+        if (pr && pr->scratch && tiles <= pr->max_tiles &&
+            plan_counters + (sh.bytes - counters) <= pr->scratch_bytes) {
+            sh.k.counter = static_cast<int*>(pr->scratch);
+            sh.k.partial = reinterpret_cast<float*>(static_cast<char*>(pr->scratch) + plan_counters);
+            kern<<<sh.ctas, kBpThreads, smem, stream>>>(proj, img, t0, t1, t2, ct, sh.k);
+            return check_launch(what);
+        }
         void* scratch = nullptr;
-        if (cudaMallocAsync(&scratch, part_bytes + sizeof(int) * tiles, stream) == cudaSuccess) {
-            k.partial = static_cast<float*>(scratch);
-            k.counter = reinterpret_cast<int*>(static_cast<char*>(scratch) + part_bytes);
-            e = cudaMemsetAsync(k.counter, 0, sizeof(int) * tiles, stream);
+        if (cudaMallocAsync(&scratch, sh.bytes, stream) == cudaSuccess) {
+            sh.k.counter = static_cast<int*>(scratch);
+            sh.k.partial = reinterpret_cast<float*>(static_cast<char*>(scratch) + counters);
+            cudaError_t e = cudaMemsetAsync(sh.k.counter, 0, sizeof(int) * static_cast<size_t>(tiles), stream);
             if (e == cudaSuccess) {
-                kern<<<ctas, kBpThreads, smem, stream>>>(proj, img, t0, t1, t2, ct, k);
+                kern<<<sh.ctas, kBpThreads, smem, stream>>>(proj, img, t0, t1, t2, ct, sh.k);
                 e = cudaGetLastError();
             }
             cudaFreeAsync(scratch, stream);
@@ -739,7 +812,7 @@ int launch_tma(const float* proj, float* img, const double* t0, const double* t1
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
     dim3 grid(tiles_x, tiles_y, batch);
-    kern<<<grid, kBpThreads, smem, stream>>>(proj, img, t0, t1, t2, ct);
+    kern<<<grid, kBpThreads, smem, stream>>>(proj, img, t0, t1, t2, ct, rec, aux);
     return check_launch(what);
 }
 
@@ -750,7 +823,8 @@ int launch_tma(const float* proj, float* img, const double* t0, const double* t1
 // positions as the adjoint.
 template <Geo G>
 int launch_forward(const float* proj, float* img, const double* t0, const double* t1,
-                   const double* t2, TileConst c, int batch, cudaStream_t stream, const char* what)
+                   const double* t2, TileConst c, int batch, cudaStream_t stream, const char* what,
+                   const BpPlanRes* pr = nullptr)
 {
     const unsigned long long total = static_cast<unsigned long long>(c.proj_stride) * batch;
     c.total4 = static_cast<long long>(total & ~3ull);
@@ -759,9 +833,9 @@ int launch_forward(const float* proj, float* img, const double* t0, const double
         // parallel: 32 views per block halve the block barriers of its short
         // per-view work; the fan keeps 16
         if (G == Geo::kPar && fwd_smem(c, 32) <= kTileSmemMax)
-            return launch_tma<G, 32>(proj, img, t0, t1, t2, c, batch, stream, what);
+            return launch_tma<G, 32>(proj, img, t0, t1, t2, c, batch, stream, what, pr);
         if (fwd_smem(c, 16) <= kTileSmemMax)
-            return launch_tma<G, 16>(proj, img, t0, t1, t2, c, batch, stream, what);
+            return launch_tma<G, 16>(proj, img, t0, t1, t2, c, batch, stream, what, pr);
     }
     const size_t smem = static_cast<size_t>(kViewBlock) * c.W * sizeof(float2);
     if (smem > 160 * 1024) return fail(CTR_ERR_UNSUPPORTED, "%s: window of %d channels too wide", what, c.W);
@@ -793,7 +867,8 @@ int adj_fx_bits(double pitch_mm, double dx, double dy)
 // resident.
 template <Geo G>
 int launch_adjoint(const float* img, float* grad, const double* t0, const double* t1, const double* t2,
-                   const TileConst& c, int batch, cudaStream_t stream, const char* what)
+                   const TileConst& c, int batch, cudaStream_t stream, const char* what,
+                   const BpPlanRes* pr = nullptr)
 {
     const size_t smem = (static_cast<size_t>(kViewBlock) * c.W * 4 + 15) / 16 * 16 +
                         static_cast<size_t>(kAdjChunkBlocks * kViewBlock) * kViewBytes;
@@ -805,6 +880,8 @@ int launch_adjoint(const float* img, float* grad, const double* t0, const double
     k.tiles_x = tiles_x;
     k.tiles_per_item = tiles_x * tiles_y;
     k.units = static_cast<long long>(k.tiles_per_item) * batch * k.nb;
+    k.rec = pr ? pr->rec : nullptr;
+    k.aux = pr ? pr->aux : nullptr;
     auto kern = bp_tile_adj<G>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     int per_sm = 1;
@@ -1044,12 +1121,206 @@ int par_single_view(const ctr_par_param* p, const T* proj, T* img, const double*
     return check_launch("bp_par_2d_sv");
 }
 
+// Largest record table a plan keeps (beyond it the kernels set views up).
+constexpr size_t kBpPlanRecMax = 64ull << 20;
+
+}  // namespace
+}  // namespace ctr
+
+// A backprojection plan: the geometry's tables (copies), the constants, the
+// stream-K scratch and the per-(tile, view) records, for the FP32 forward.
+struct ctr_bp_plan {
+    int device = 0;
+    int max_batch = 0;
+    bool fan = false;
+    ctr::TileConst c{};
+    double* tabs = nullptr;
+    const double* t0 = nullptr;
+    const double* t1 = nullptr;
+    const double* t2 = nullptr;
+    ctr::BpPlanRes res{};
+    void* rec_mem = nullptr;
+    ~ctr_bp_plan()
+    {
+        if (tabs) cudaFree(tabs);
+        if (res.scratch) cudaFree(res.scratch);
+        if (rec_mem) cudaFree(rec_mem);
+    }
+};
+
+namespace ctr {
+namespace {
+
+// The view block the forward dispatch picks for a geometry (0: not the
+// bulk-copy kernels).
+template <Geo G>
+int plan_view_block(const TileConst& c)
+{
+    if (!(c.WB <= 256 && c.na <= 4096)) return 0;
+    if (G == Geo::kPar && fwd_smem(c, 32) <= kTileSmemMax) return 32;
+    return fwd_smem(c, 16) <= kTileSmemMax ? 16 : 0;
+}
+
+template <Geo G, int VB>
+void plan_scratch_need(const TileConst& c, int max_batch, long long* max_tiles, size_t* part_max)
+{
+    for (int b = 1; b <= max_batch; ++b) {
+        const SkShape sh = sk_shape<G, VB>(c, b);
+        if (!sh.on) continue;
+        const long long tiles = sh.k.units / sh.k.nb;
+        const size_t counters = (sizeof(int) * static_cast<size_t>(tiles) + 255) & ~static_cast<size_t>(255);
+        *max_tiles = std::max(*max_tiles, tiles);
+        *part_max = std::max(*part_max, sh.bytes - counters);
+    }
+}
+
+// Copies the tables (n[i] doubles from src[i]), sizes and zeroes the stream-K
+// scratch for every batch up to max_batch, and writes the records.
+template <Geo G>
+int bp_plan_make(ctr_bp_plan* P, const double* const src[3], const size_t n[3], cudaStream_t stream)
+{
+    const size_t total = n[0] + n[1] + n[2];
+    if (cudaMalloc(&P->tabs, total * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(CTR_ERR_CUDA, "bp plan: %zu bytes of tables", total * sizeof(double));
+    }
+    size_t off = 0;
+    const double** dst[3] = {&P->t0, &P->t1, &P->t2};
+    for (int i = 0; i < 3; ++i) {
+        *dst[i] = n[i] ? P->tabs + off : nullptr;
+        if (n[i] && cudaMemcpyAsync(P->tabs + off, src[i], n[i] * sizeof(double), cudaMemcpyDeviceToDevice,
+                                    stream) != cudaSuccess)
+            return fail(CTR_ERR_CUDA, "bp plan: table copy");
+        off += n[i];
+    }
+    const TileConst& c = P->c;
+    const int vb = plan_view_block<G>(c);
+    if (vb == 0) return cudaStreamSynchronize(stream) == cudaSuccess ? CTR_OK : fail(CTR_ERR_CUDA, "bp plan");
+    long long max_tiles = 0;
+    size_t part = 0;
+    if (vb == 32) plan_scratch_need<G, 32>(c, P->max_batch, &max_tiles, &part);
+    else plan_scratch_need<G, 16>(c, P->max_batch, &max_tiles, &part);
+    if (max_tiles > 0) {
+        const size_t counters = (sizeof(int) * static_cast<size_t>(max_tiles) + 255) & ~static_cast<size_t>(255);
+        if (cudaMalloc(&P->res.scratch, counters + part) != cudaSuccess ||
+            cudaMemsetAsync(P->res.scratch, 0, counters, stream) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(CTR_ERR_CUDA, "bp plan: %zu bytes of scratch", counters + part);
+        }
+        P->res.scratch_bytes = counters + part;
+        P->res.max_tiles = max_tiles;
+    }
+    const int tiles_x = static_cast<int>(div_up(c.nx, kTileX));
+    const int tiles = tiles_x * static_cast<int>(div_up(c.ny, kTileY));
+    const size_t nrec = static_cast<size_t>(tiles) * c.na;
+    if (nrec * kViewBytes <= kBpPlanRecMax) {
+        if (cudaMalloc(&P->rec_mem, nrec * kViewBytes) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(CTR_ERR_CUDA, "bp plan: %zu bytes of view records", nrec * kViewBytes);
+        }
+        FastRec* rec = static_cast<FastRec*>(P->rec_mem);
+        ViewAux* aux = reinterpret_cast<ViewAux*>(rec + nrec);
+        const unsigned blocks = static_cast<unsigned>(std::min<size_t>(div_up(nrec, 256), 8ull * sm_count()));
+        bp_view_records<G><<<blocks, 256, 0, stream>>>(P->t0, P->t1, P->t2, c, tiles_x, tiles, rec, aux);
+        const int st = check_launch("bp plan records");
+        if (st) return st;
+        P->res.rec = rec;
+        P->res.aux = aux;
+    }
+    const cudaError_t e = cudaStreamSynchronize(stream);
+    return e == cudaSuccess ? CTR_OK : fail(CTR_ERR_CUDA, "bp plan set-up: %s", cudaGetErrorString(e));
+}
+
 }  // namespace
 }  // namespace ctr
 
 using namespace ctr;
 
 extern "C" {
+
+int ctr_bp_par_2d_plan_create(const ctr_par_param* p, const double* xcos, const double* ysin, int max_batch,
+                              ctr_bp_plan** plan, cudaStream_t stream)
+{
+    if (!plan) return fail(CTR_ERR_INVALID_ARG, "null plan pointer");
+    *plan = nullptr;
+    int st = check_par(p, xcos, ysin, xcos, ysin, max_batch);
+    if (st) return st;
+    auto P = std::make_unique<ctr_bp_plan>();
+    cudaGetDevice(&P->device);
+    P->max_batch = max_batch;
+    P->fan = false;
+    P->c = par_const(p);
+    const double* src[3] = {xcos, ysin, nullptr};
+    const size_t n[3] = {static_cast<size_t>(p->nx) * p->na, static_cast<size_t>(p->ny) * p->na, 0};
+    st = bp_plan_make<Geo::kPar>(P.get(), src, n, stream);
+    if (st) return st;
+    *plan = P.release();
+    return CTR_OK;
+}
+
+int ctr_bp_fan_2d_plan_create(const ctr_fan_bp_param* p, const double* xpos, const double* ypos,
+                              const double* sincostbl, int max_batch, ctr_bp_plan** plan,
+                              cudaStream_t stream)
+{
+    if (!plan) return fail(CTR_ERR_INVALID_ARG, "null plan pointer");
+    *plan = nullptr;
+    if (!p) return fail(CTR_ERR_INVALID_ARG, "null argument");
+    const FanArgs a = fan_args(p);
+    int st = check_fan(a, xpos, ypos, xpos, ypos, sincostbl, max_batch);
+    if (st) return st;
+    auto P = std::make_unique<ctr_bp_plan>();
+    cudaGetDevice(&P->device);
+    P->max_batch = max_batch;
+    P->fan = true;
+    P->c = fan_const(a, a.scale);
+    const double* src[3] = {xpos, ypos, sincostbl};
+    const size_t n[3] = {p->nx, p->ny, 2 * static_cast<size_t>(p->na)};
+    st = bp_plan_make<Geo::kFan>(P.get(), src, n, stream);
+    if (st) return st;
+    *plan = P.release();
+    return CTR_OK;
+}
+
+int ctr_bp_plan_run(ctr_bp_plan* plan, const float* proj, float* img, int batch, cudaStream_t stream)
+{
+    if (!plan || !proj || !img) return fail(CTR_ERR_INVALID_ARG, "null argument");
+    int st = check_common(batch);
+    if (st) return st;
+    int dev = -1;
+    cudaGetDevice(&dev);
+    if (dev != plan->device) return fail(CTR_ERR_INVALID_ARG, "plan made on device %d, current %d", plan->device, dev);
+    if (batch > plan->max_batch) return fail(CTR_ERR_INVALID_ARG, "batch %d > the plan's %d", batch, plan->max_batch);
+    if (plan->fan)
+        return launch_forward<Geo::kFan>(proj, img, plan->t0, plan->t1, plan->t2, plan->c, batch, stream,
+                                         "bp_fan_2d", &plan->res);
+    return launch_forward<Geo::kPar>(proj, img, plan->t0, plan->t1, plan->t2, plan->c, batch, stream, "bp_par_2d",
+                                     &plan->res);
+}
+
+int ctr_bp_plan_run_grad(ctr_bp_plan* plan, const float* img, float* grad, int batch, cudaStream_t stream)
+{
+    if (!plan || !img || !grad) return fail(CTR_ERR_INVALID_ARG, "null argument");
+    int st = check_common(batch);
+    if (st) return st;
+    int dev = -1;
+    cudaGetDevice(&dev);
+    if (dev != plan->device) return fail(CTR_ERR_INVALID_ARG, "plan made on device %d, current %d", plan->device, dev);
+    if (batch > plan->max_batch) return fail(CTR_ERR_INVALID_ARG, "batch %d > the plan's %d", batch, plan->max_batch);
+    const cudaError_t e = cudaMemsetAsync(grad, 0, sizeof(float) * plan->c.proj_stride * batch, stream);
+    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "zero grad: %s", cudaGetErrorString(e));
+    if (plan->fan)
+        return launch_adjoint<Geo::kFan>(img, grad, plan->t0, plan->t1, plan->t2, plan->c, batch, stream,
+                                         "bp_fan_2d_grad", &plan->res);
+    return launch_adjoint<Geo::kPar>(img, grad, plan->t0, plan->t1, plan->t2, plan->c, batch, stream,
+                                     "bp_par_2d_grad", &plan->res);
+}
+
+int ctr_bp_plan_destroy(ctr_bp_plan* plan)
+{
+    delete plan;
+    return CTR_OK;
+}
+
 
 int ctr_bp_fan_2d_f32(const ctr_fan_bp_param* p, const float* proj, float* img,
                       const double* xpos, const double* ypos, const double* sincostbl,

@@ -825,7 +825,9 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
                                              const double* __restrict__ t1,
                                              const double* __restrict__ t2, const TileConst& c,
                                              int tile_x, int tile_y, int item, int b_begin = 0,
-                                             int b_end = -1, float* __restrict__ partial = nullptr)
+                                             int b_end = -1, float* __restrict__ partial = nullptr,
+                                             const FastRec* __restrict__ rec = nullptr,
+                                             const ViewAux* __restrict__ aux = nullptr)
 {
     constexpr int kTY = (kBpThreads / 32) * R;  // tile height
     constexpr int kBV = NG * VB;                // views per staged block
@@ -892,7 +894,20 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
     const unsigned pairs_base = smem_u32(pairs);
     const int ia_end = min(nblocks * kBV, c.na);
     for (int ia = b_begin * kBV + tid; ia < ia_end; ia += kThreads) {
-        ViewRec P = view_setup<G>(t0, t1, t2, ia, B, c);
+        ViewRec P;
+        if (rec) {  // a plan's record of this (tile, view)
+            const size_t ti = (static_cast<size_t>(tile_y) * ((c.nx + kTileX - 1) / kTileX) + tile_x) * c.na + ia;
+            const FastRec F = rec[ti];
+            const ViewAux A = aux[ti];
+            P.p0 = F.p0;
+            P.p1 = F.p1;
+            P.cen = F.cen;
+            P.mode = F.mode;
+            P.e = A.e;
+            P.lo = A.lo;
+        } else {
+            P = view_setup<G>(t0, t1, t2, ia, B, c);
+        }
         if (mode_fast(P.mode)) {
             const int slot = ((ia / kBV - b_begin) & 1) * kBV + ia % kBV;
             P.mode = fast_mode(pairs_base + 8u * static_cast<unsigned>(slot * c.W), c, P.mode);
@@ -1007,9 +1022,27 @@ template <Geo G, int R, int MinBlocks, int VB, int NG>
 __global__ void __launch_bounds__(NG * kBpThreads, MinBlocks)
     bp_tile_tma_f32(const float* __restrict__ proj, float* __restrict__ img,
                     const double* __restrict__ t0, const double* __restrict__ t1,
-                    const double* __restrict__ t2, const TileConst c)
+                    const double* __restrict__ t2, const TileConst c,
+                    const FastRec* __restrict__ rec = nullptr, const ViewAux* __restrict__ aux = nullptr)
 {
-    tile_forward<G, R, VB, NG>(proj, img, t0, t1, t2, c, blockIdx.x, blockIdx.y, blockIdx.z);
+    tile_forward<G, R, VB, NG>(proj, img, t0, t1, t2, c, blockIdx.x, blockIdx.y, blockIdx.z, 0, -1, nullptr,
+                               rec, aux);
+}
+
+// A plan's per-(tile, view) records (tiles of 32 x kTileY, [tile][view], the
+// mode before its pair-slot base): one thread each.
+template <Geo G>
+__global__ void __launch_bounds__(256)
+    bp_view_records(const double* __restrict__ t0, const double* __restrict__ t1,
+                    const double* __restrict__ t2, const TileConst c, int tiles_x, int tiles,
+                    FastRec* __restrict__ rec, ViewAux* __restrict__ aux)
+{
+    const long long n = static_cast<long long>(tiles) * c.na;
+    for (long long i = blockIdx.x * 256ll + threadIdx.x; i < n; i += gridDim.x * 256ll) {
+        const int t = static_cast<int>(i / c.na), ia = static_cast<int>(i - static_cast<long long>(t) * c.na);
+        const TileBox B = tile_box<G>(t0, t1, t % tiles_x, t / tiles_x, kTileY, c);
+        store_view(rec, aux, static_cast<int>(i), view_setup<G>(t0, t1, t2, ia, B, c));
+    }
 }
 
 // ---- stream-K split of small launches ----------------------------------------
@@ -1028,7 +1061,9 @@ struct SkConst {
     int tiles_x, tiles_per_item;
     int maxseg;            // segments per tile, at most
     float* partial;        // [tiles][maxseg][kTileX x tile height]
-    int* counter;          // [tiles], zero at launch
+    int* counter;          // [tiles], zero at launch; the CTA completing a tile resets it
+    const FastRec* rec;    // a plan's per-(tile, view) records, or null (set up here)
+    const ViewAux* aux;
 };
 
 template <Geo G, int R, int VB, int NG, int MinBlocks>
@@ -1053,11 +1088,12 @@ __global__ void __launch_bounds__(NG * kBpThreads, MinBlocks)
         const int tx = tl % k.tiles_x, ty = tl / k.tiles_x;
         const int first = sk_cta_of(tu, ctas, U), last = sk_cta_of(tu + k.nb - 1, ctas, U);
         if (first == last) {  // the whole tile is this CTA's
-            if (!tile_forward<G, R, VB, NG>(proj, img, t0, t1, t2, c, tx, ty, item)) return;
+            if (!tile_forward<G, R, VB, NG>(proj, img, t0, t1, t2, c, tx, ty, item, 0, -1, nullptr, k.rec, k.aux))
+                return;
             continue;
         }
         float* seg = k.partial + (static_cast<size_t>(t) * k.maxseg + (blockIdx.x - first)) * kTilePix;
-        if (!tile_forward<G, R, VB, NG>(proj, img, t0, t1, t2, c, tx, ty, item, b0, b1, seg)) return;
+        if (!tile_forward<G, R, VB, NG>(proj, img, t0, t1, t2, c, tx, ty, item, b0, b1, seg, k.rec, k.aux)) return;
         __threadfence();  // this segment is visible before it is counted
         __syncthreads();
         if (threadIdx.x == 0) s_last = atomicAdd(k.counter + t, 1) == last - first;
@@ -1072,6 +1108,7 @@ __global__ void __launch_bounds__(NG * kBpThreads, MinBlocks)
                 for (int sg = 1; sg <= last - first; ++sg) v += __ldcg(base + sg * kTilePix + idx);
                 if (ix < c.nx && iy < c.ny) I[static_cast<size_t>(iy) * c.nx + ix] = v * c.scale;
             }
+            if (threadIdx.x == 0) k.counter[t] = 0;  // zero again for the next launch
         }
     }
 }

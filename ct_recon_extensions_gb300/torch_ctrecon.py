@@ -225,9 +225,44 @@ class RampFilterTCOp:
             pass
 
 
+class _BpPlans:
+    """Per-device FP32 backprojection plans (ctr_bp_*_plan_create: the tables,
+    the stream-split scratch and the per-(tile, view) constants kept), grown to
+    the largest batch seen."""
+
+    def __init__(self, create):
+        self._create = create  # (device, max_batch) -> plan handle
+        self._plans = {}
+        self._lib = _lib.load()
+
+    def get(self, device, batch):
+        dev = device.index if device.index is not None else torch.cuda.current_device()
+        cur = self._plans.get(dev)
+        if cur is None or cur[1] < batch:
+            with torch.cuda.device(dev):
+                if cur is not None:
+                    torch.cuda.current_stream().synchronize()
+                    self._lib.ctr_bp_plan_destroy(cur[0])
+                    del self._plans[dev]
+                self._plans[dev] = (self._create(torch.device("cuda", dev), batch), batch)
+        return self._plans[dev][0]
+
+    def close(self):
+        for h, _ in self._plans.values():
+            self._lib.ctr_bp_plan_destroy(h)
+        self._plans.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class FanBackprojection2DOp:
     """FanBackprojection2DPixDriven{Prep,,GradPrep,Grad} (reference
-    include/bp_fan_2d.h:151-225)."""
+    include/bp_fan_2d.h:151-225).  FP32 calls (forward and adjoint) run
+    through a per-geometry plan (ctr_bp_fan_2d_plan_*)."""
 
     def __init__(self, ns, na, ds, orbit, offset_s, orbit_start, nx, ny, dx, dy, offset_x,
                  offset_y, dso, dsd, fov=-1.0):
@@ -235,6 +270,17 @@ class FanBackprojection2DOp:
                             offset_y, dso, dsd, fov)
         self.ns, self.na, self.nx, self.ny = ns, na, nx, ny
         self._tables = _Tables()
+        self._plans = _BpPlans(self._make_plan)
+
+    def _make_plan(self, device, batch):
+        h = ctypes.c_void_p()
+        call("ctr_bp_fan_2d_plan_create", ctypes.byref(self.p), *map(_ptr, self.tables(device)), int(batch),
+             ctypes.byref(h), _stream())
+        return h
+
+    def plan(self, device, batch=1):
+        """The FP32 forward's plan handle on `device` (for the C ABI)."""
+        return self._plans.get(device, batch)
 
     def tables(self, device):
         def build(dev):
@@ -251,6 +297,10 @@ class FanBackprojection2DOp:
     def forward(self, proj):
         xb, restore = _as_batch(proj, self.na, self.ns, self._fwd)
         img = torch.empty((xb.shape[0], self.ny, self.nx), dtype=xb.dtype, device=xb.device)
+        if self._fwd == "bp_fan_2d" and xb.dtype == torch.float32:
+            call("ctr_bp_plan_run", self._plans.get(xb.device, xb.shape[0]), _ptr(xb), _ptr(img),
+                 xb.shape[0], _stream())
+            return restore(img)
         t = self.tables(xb.device)
         call(f"ctr_{self._fwd}_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(img),
              *map(_ptr, t), xb.shape[0], _stream())
@@ -259,6 +309,10 @@ class FanBackprojection2DOp:
     def adjoint(self, img):
         xb, restore = _as_batch(img, self.ny, self.nx, self._adj)
         grad = torch.empty((xb.shape[0], self.na, self.ns), dtype=xb.dtype, device=xb.device)
+        if self._adj == "bp_fan_2d_grad" and xb.dtype == torch.float32:
+            call("ctr_bp_plan_run_grad", self._plans.get(xb.device, xb.shape[0]), _ptr(xb), _ptr(grad),
+                 xb.shape[0], _stream())
+            return restore(grad)
         t = self.tables(xb.device)
         call(f"ctr_{self._adj}_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(grad),
              *map(_ptr, t), xb.shape[0], _stream())
@@ -280,6 +334,7 @@ class FanBackprojection2DAngleOp(FanBackprojection2DOp):
                                  dsd, fov)
         self.ns, self.na, self.nx, self.ny = ns, na, nx, ny
         self._tables = _Tables()
+        self._plans = None  # no plan form: the angle op's forward is unscaled
 
     def tables(self, device):
         def build(dev):
@@ -295,7 +350,8 @@ class FanBackprojection2DAngleOp(FanBackprojection2DOp):
 
 class ParallelBackprojection2DOp:
     """ParallelBackprojection2DPixDriven (reference include/bp_par_2d.h) and its
-    exact adjoint."""
+    exact adjoint.  FP32 calls (forward and adjoint) run through a
+    per-geometry plan (ctr_bp_par_2d_plan_*)."""
 
     def __init__(self, ns, na, ds, orbit, offset_s, orbit_start, nx, ny, dx, dy, offset_x,
                  offset_y, fov=-1.0):
@@ -303,6 +359,18 @@ class ParallelBackprojection2DOp:
                           offset_y, fov)
         self.ns, self.na, self.nx, self.ny = ns, na, nx, ny
         self._tables = _Tables()
+        self._plans = _BpPlans(self._make_plan)
+
+    def _make_plan(self, device, batch):
+        h = ctypes.c_void_p()
+        xcos, ysin = self.tables(device)
+        call("ctr_bp_par_2d_plan_create", ctypes.byref(self.p), _ptr(xcos), _ptr(ysin), int(batch),
+             ctypes.byref(h), _stream())
+        return h
+
+    def plan(self, device, batch=1):
+        """The FP32 forward's plan handle on `device` (for the C ABI)."""
+        return self._plans.get(device, batch)
 
     def tables(self, device):
         def build(dev):
@@ -316,6 +384,10 @@ class ParallelBackprojection2DOp:
     def forward(self, proj):
         xb, restore = _as_batch(proj, self.na, self.ns, "bp_par_2d")
         img = torch.empty((xb.shape[0], self.ny, self.nx), dtype=xb.dtype, device=xb.device)
+        if xb.dtype == torch.float32:
+            call("ctr_bp_plan_run", self._plans.get(xb.device, xb.shape[0]), _ptr(xb), _ptr(img),
+                 xb.shape[0], _stream())
+            return restore(img)
         xcos, ysin = self.tables(xb.device)
         call(f"ctr_bp_par_2d_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(img), _ptr(xcos),
              _ptr(ysin), None, xb.shape[0], _stream())
@@ -324,6 +396,10 @@ class ParallelBackprojection2DOp:
     def adjoint(self, img):
         xb, restore = _as_batch(img, self.ny, self.nx, "bp_par_2d_grad")
         grad = torch.empty((xb.shape[0], self.na, self.ns), dtype=xb.dtype, device=xb.device)
+        if xb.dtype == torch.float32:
+            call("ctr_bp_plan_run_grad", self._plans.get(xb.device, xb.shape[0]), _ptr(xb), _ptr(grad),
+                 xb.shape[0], _stream())
+            return restore(grad)
         xcos, ysin = self.tables(xb.device)
         call(f"ctr_bp_par_2d_grad_{_sfx(xb)}", ctypes.byref(self.p), _ptr(xb), _ptr(grad),
              _ptr(xcos), _ptr(ysin), xb.shape[0], _stream())

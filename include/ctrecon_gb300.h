@@ -228,6 +228,32 @@ int ctr_bp_par_2d_grad_f64(const ctr_par_param* p, const double* img, double* gr
                            const double* xcos, const double* ysin, int batch,
                            cudaStream_t stream);
 
+/* ---- FP32 backprojection plans (in the reference:
+ *      ParallelBackprojection2DPixDriven<float>::calculate_on_gpu,
+ *      include/bp_par_2d.h:170-185, and FanBackprojection2DPixDriven<float>::
+ *      calculate_on_gpu, include/bp_fan_2d.h:175-190, with the per-call set-up
+ *      done once) ----
+ * A plan copies the prep tables (read on `stream`, which it synchronises; the
+ * caller's tables may be freed afterwards), and keeps the stream-split
+ * scratch and each (32 x 64 tile, view)'s channel window and position
+ * constants, so a run allocates nothing and starts with the taps.  Forward
+ * results equal ctr_bp_par_2d_f32 / ctr_bp_fan_2d_f32 bit for bit.  A plan serves one
+ * stream at a time, on the device it was made on; after a failed run destroy
+ * it. */
+typedef struct ctr_bp_plan ctr_bp_plan;
+int ctr_bp_par_2d_plan_create(const ctr_par_param* p, const double* xcos, const double* ysin,
+                              int max_batch, ctr_bp_plan** plan, cudaStream_t stream);
+int ctr_bp_fan_2d_plan_create(const ctr_fan_bp_param* p, const double* xpos, const double* ypos,
+                              const double* sincostbl, int max_batch, ctr_bp_plan** plan,
+                              cudaStream_t stream);
+int ctr_bp_plan_run(ctr_bp_plan* plan, const float* proj, float* img, int batch,
+                    cudaStream_t stream);
+/* The exact adjoint (ctr_bp_par_2d_grad_f32 / ctr_bp_fan_2d_grad_f32, bit for
+ * bit up to the order of its float atomics), img [ny][nx] -> grad [na][ns]. */
+int ctr_bp_plan_run_grad(ctr_bp_plan* plan, const float* img, float* grad, int batch,
+                         cudaStream_t stream);
+int ctr_bp_plan_destroy(ctr_bp_plan* plan);
+
 /* ---- parallel-beam single-view backprojection
  *      (reference include/bp_par_2d_sv.h:112-138) ----
  * proj [na][ns] -> img [ny][nx][na]: the interpolated value of every view,
