@@ -126,6 +126,22 @@ __device__ __forceinline__ void adj_taps2(unsigned base, float2 sig, float2 t)
     red_shared_u32(a1 + 4u, static_cast<unsigned>(q1b));
 }
 
+// Whether a view walks the tile x-major (its channel changes faster along x).
+__device__ __forceinline__ bool adj_xmaj(const FastRec& P, const TileConst& c)
+{
+    return fabsf(P.p0) * c.dxf >= fabsf(P.p1) * c.dyf;
+}
+
+// 1 when every one of the n (<= 32) views at vr is x-major, 0 when every one
+// is y-major, else -1 (warp-uniform).
+__device__ __forceinline__ int block_major(const FastRec* vr, int n, const TileConst& c)
+{
+    const int lane = threadIdx.x & 31;
+    const bool m = lane < n ? adj_xmaj(load_fast(vr + lane), c) : true;
+    const bool yes = lane < n ? !m : true;
+    return __all_sync(0xffffffffu, m) ? 1 : (__all_sync(0xffffffffu, yes) ? 0 : -1);
+}
+
 // The fast-path taps of one view for a thread's pixels, parallel beam: the
 // x-major mapping (column oxx, rows oyx) or the y-major one (columns oxy[r &
 // 3], rows oyy[r >> 2]); pixel pairs (r, r+1) packed.
@@ -300,22 +316,34 @@ __global__ void __launch_bounds__(kBpThreads, 2)
             // every view of the block on the fast path (one variant): no per-view dispatch
             const int fv = any_bad ? -1 : block_variant(vb, nv);
             if (fv >= 0) {
+                // views of one walk direction (the usual case): no per-view test
+                const int bm = block_major(vb, nv, c);
                 if constexpr (G == Geo::kPar) {
-                    for (int j = 0; j < nv; ++j) {
-                        const FastRec P = load_fast(vb + j);
-                        adj_par_view<R>(P, static_cast<unsigned>(P.mode) & ~3u,
-                                        fabsf(P.p0) * c.dxf >= fabsf(P.p1) * c.dyf, oxx, oyx, oxy, oyy, vx, vy,
-                                        tbx, tby);
-                    }
+                    auto par_block = [&](auto mc) {
+                        constexpr int M = decltype(mc)::value;
+                        for (int j = 0; j < nv; ++j) {
+                            const FastRec P = load_fast(vb + j);
+                            adj_par_view<R>(P, static_cast<unsigned>(P.mode) & ~3u, M < 0 ? adj_xmaj(P, c) : M == 1,
+                                            oxx, oyx, oxy, oyy, vx, vy, tbx, tby);
+                        }
+                    };
+                    if (bm == 1) par_block(std::integral_constant<int, 1>{});
+                    else if (bm == 0) par_block(std::integral_constant<int, 0>{});
+                    else par_block(std::integral_constant<int, -1>{});
                 } else {
                     auto fan_block = [&](auto vc) {
                         constexpr int V = decltype(vc)::value;
-                        for (int j = 0; j < nv; ++j) {
-                            const FastRec P = load_fast(vb + j);
-                            adj_fan_view<V, R>(P, static_cast<unsigned>(P.mode) & ~3u,
-                                               fabsf(P.p0) * c.dxf >= fabsf(P.p1) * c.dyf, oxx, oyx, oxy, oyy, vx,
-                                               vy, c);
-                        }
+                        auto run = [&](auto mc) {
+                            constexpr int M = decltype(mc)::value;
+                            for (int j = 0; j < nv; ++j) {
+                                const FastRec P = load_fast(vb + j);
+                                adj_fan_view<V, R>(P, static_cast<unsigned>(P.mode) & ~3u,
+                                                   M < 0 ? adj_xmaj(P, c) : M == 1, oxx, oyx, oxy, oyy, vx, vy, c);
+                            }
+                        };
+                        if (bm == 1) run(std::integral_constant<int, 1>{});
+                        else if (bm == 0) run(std::integral_constant<int, 0>{});
+                        else run(std::integral_constant<int, -1>{});
                     };
                     switch (fv) {
                         case 0: fan_block(std::integral_constant<int, 0>{}); break;
@@ -329,7 +357,7 @@ __global__ void __launch_bounds__(kBpThreads, 2)
                 if (F.mode == kModeSkip) continue;
                 const int ia = v0 + j;
                 const unsigned slot = win_base + 4u * static_cast<unsigned>(j * c.W);
-                const bool xmaj = fabsf(F.p0) * c.dxf >= fabsf(F.p1) * c.dyf;
+                const bool xmaj = adj_xmaj(F, c);
                 if (mode_fast(F.mode) && !any_bad) {
                     const FastRec& P = F;
                     const unsigned base = static_cast<unsigned>(P.mode) & ~3u;
@@ -407,17 +435,20 @@ __global__ void __launch_bounds__(kBpThreads, 2)
                 }
             }
             __syncthreads();
-            // flush: window entries -> sinogram (and back to zero)
-            for (int idx = tid; idx < nv * c.W; idx += kBpThreads) {
-                const unsigned a = win[idx];
-                if (a == 0u) continue;
-                win[idx] = 0u;
-                const int j = idx / c.W, kk = idx - j * c.W;
-                const ViewAux& P = vab[j];
-                const int g = P.lo + kk;
-                if (g >= 0 && g < c.ns)
-                    atomicAdd(Gs + static_cast<size_t>(v0 + j) * c.ns + g,
-                              static_cast<float>(static_cast<int>(a)) * (back * P.e));
+            // flush: window entries -> sinogram (and back to zero); a warp
+            // takes whole views, its lanes the window's channels
+            for (int j = warp; j < nv; j += kBpThreads / 32) {
+                const ViewAux P = vab[j];
+                const float sc = back * P.e;
+                unsigned* wrow = win + j * c.W;
+                float* grow = Gs + static_cast<size_t>(v0 + j) * c.ns + P.lo;
+                for (int kk = lane; kk < c.W; kk += 32) {
+                    const unsigned a = wrow[kk];
+                    if (a == 0u) continue;
+                    wrow[kk] = 0u;
+                    const int g = P.lo + kk;
+                    if (g >= 0 && g < c.ns) atomicAdd(grow + kk, static_cast<float>(static_cast<int>(a)) * sc);
+                }
             }
             __syncthreads();
         }

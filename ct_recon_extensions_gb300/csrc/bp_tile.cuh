@@ -521,7 +521,8 @@ __device__ __forceinline__ float2 make_pair(float p0, float p1, int k, int kc, f
 // Rows are taken in pairs: the position arithmetic of rows r and r+1 runs as
 // packed FP32 pairs (FFMA2 / FADD2 / FMUL2, each half rounded as the scalar
 // operation, so positions are bit-identical to fan_sigma / par_sigma and the
-// forward's and adjoint's taps agree).
+// forward's and adjoint's taps agree), and so do the running sums (the fan's
+// weighted add, the parallel beam's add): each half is the scalar update.
 __device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
 
 // a - b per half (an FMA with -1: exact negation, one rounding).
@@ -561,8 +562,10 @@ __device__ __forceinline__ void fast_rows(float ox, const float (&oy)[R], const 
             const float2 tm = __fadd2_rn(sig, mag);
             const float2 pa = lds_f2(base + 8u * __float_as_uint(tm.x));
             const float2 pb = lds_f2(base + 8u * __float_as_uint(tm.y));
-            part[r] = fmaf(fmaf(sig.x, pa.y, pa.x), w.x, part[r]);
-            part[r + 1] = fmaf(fmaf(sig.y, pb.y, pb.x), w.y, part[r + 1]);
+            const float2 acc = __ffma2_rn(make_float2(fmaf(sig.x, pa.y, pa.x), fmaf(sig.y, pb.y, pb.x)), w,
+                                          make_float2(part[r], part[r + 1]));
+            part[r] = acc.x;
+            part[r + 1] = acc.y;
         }
     } else {
         const float2 xs = dup2(par_xpart(ox, P)), p1 = dup2(P.p1);
@@ -572,8 +575,10 @@ __device__ __forceinline__ void fast_rows(float ox, const float (&oy)[R], const 
             const float2 tm = __fadd2_rn(sig, mag);
             const float2 pa = lds_f2(base + 8u * __float_as_uint(tm.x));
             const float2 pb = lds_f2(base + 8u * __float_as_uint(tm.y));
-            part[r] += fmaf(sig.x, pa.y, pa.x);
-            part[r + 1] += fmaf(sig.y, pb.y, pb.x);
+            const float2 acc = __fadd2_rn(make_float2(part[r], part[r + 1]),
+                                          make_float2(fmaf(sig.x, pa.y, pa.x), fmaf(sig.y, pb.y, pb.x)));
+            part[r] = acc.x;
+            part[r + 1] = acc.y;
         }
     }
 }
@@ -679,15 +684,17 @@ template <Geo G, int V, int R>
 __device__ __forceinline__ void fast_block(float ox, const float (&oy)[R], const FastRec* vr, int n,
                                            const TileConst& c, float (&part)[R])
 {
+    // a parallel-beam mode has no variant bits: it is the base itself
+    constexpr unsigned kMask = G == Geo::kPar ? ~0u : ~3u;
     int j = 0;
     for (; j + 2 <= n; j += 2) {
         const FastRec F0 = load_fast(vr + j), F1 = load_fast(vr + j + 1);
-        fast_rows<G, V, R>(ox, oy, F0, c, static_cast<unsigned>(F0.mode) & ~3u, part);
-        fast_rows<G, V, R>(ox, oy, F1, c, static_cast<unsigned>(F1.mode) & ~3u, part);
+        fast_rows<G, V, R>(ox, oy, F0, c, static_cast<unsigned>(F0.mode) & kMask, part);
+        fast_rows<G, V, R>(ox, oy, F1, c, static_cast<unsigned>(F1.mode) & kMask, part);
     }
     if (j < n) {
         const FastRec F0 = load_fast(vr + j);
-        fast_rows<G, V, R>(ox, oy, F0, c, static_cast<unsigned>(F0.mode) & ~3u, part);
+        fast_rows<G, V, R>(ox, oy, F0, c, static_cast<unsigned>(F0.mode) & kMask, part);
     }
 }
 
@@ -962,7 +969,14 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
             const float* src = slot + j * c.WS + static_cast<int>(st & 3ll);
             float2* dst = pb + j * c.W;
             if (lo >= 0 && lo + c.W < c.ns && st + c.W < c.total4) {
-                for (int k = lane; k < c.W; k += 32) dst[k] = make_pair(src[k], src[k + 1], k, c.kc, e);
+                // make_pair with (k - kc - 1/2) carried as a float (exact) and,
+                // for the parallel beam, its unit scale left out
+                float fk = static_cast<float>(lane - c.kc) - 0.5f;
+                for (int k = lane; k < c.W; k += 32, fk += 32.0f) {
+                    const float p0 = src[k], d = src[k + 1] - p0;
+                    const float q = fmaf(-fk, d, p0);
+                    dst[k] = G == Geo::kPar ? make_float2(q, d) : make_float2(q * e, d * e);
+                }
             } else {  // a detector end or the array's ragged tail is in the window
                 for (int k = lane; k < c.W; k += 32) {
                     auto at = [&](int gg, long long ii, const float* sp) -> float {
