@@ -687,6 +687,14 @@ __device__ __forceinline__ void fast_block(float ox, const float (&oy)[R], const
     // a parallel-beam mode has no variant bits: it is the base itself
     constexpr unsigned kMask = G == Geo::kPar ? ~0u : ~3u;
     int j = 0;
+    for (; j + 4 <= n; j += 4) {
+        const FastRec F0 = load_fast(vr + j), F1 = load_fast(vr + j + 1);
+        const FastRec F2 = load_fast(vr + j + 2), F3 = load_fast(vr + j + 3);
+        fast_rows<G, V, R>(ox, oy, F0, c, static_cast<unsigned>(F0.mode) & kMask, part);
+        fast_rows<G, V, R>(ox, oy, F1, c, static_cast<unsigned>(F1.mode) & kMask, part);
+        fast_rows<G, V, R>(ox, oy, F2, c, static_cast<unsigned>(F2.mode) & kMask, part);
+        fast_rows<G, V, R>(ox, oy, F3, c, static_cast<unsigned>(F3.mode) & kMask, part);
+    }
     for (; j + 2 <= n; j += 2) {
         const FastRec F0 = load_fast(vr + j), F1 = load_fast(vr + j + 1);
         fast_rows<G, V, R>(ox, oy, F0, c, static_cast<unsigned>(F0.mode) & kMask, part);
