@@ -321,11 +321,17 @@ __global__ void __launch_bounds__(kBpThreads, 2)
                 if constexpr (G == Geo::kPar) {
                     auto par_block = [&](auto mc) {
                         constexpr int M = decltype(mc)::value;
-                        for (int j = 0; j < nv; ++j) {
-                            const FastRec P = load_fast(vb + j);
+                        auto one = [&](const FastRec& P) {
                             adj_par_view<R>(P, static_cast<unsigned>(P.mode) & ~3u, M < 0 ? adj_xmaj(P, c) : M == 1,
                                             oxx, oyx, oxy, oyy, vx, vy, tbx, tby);
+                        };
+                        int j = 0;
+                        for (; j + 2 <= nv; j += 2) {  // two views per trip
+                            const FastRec P0 = load_fast(vb + j), P1 = load_fast(vb + j + 1);
+                            one(P0);
+                            one(P1);
                         }
+                        if (j < nv) one(load_fast(vb + j));
                     };
                     if (bm == 1) par_block(std::integral_constant<int, 1>{});
                     else if (bm == 0) par_block(std::integral_constant<int, 0>{});
@@ -335,11 +341,17 @@ __global__ void __launch_bounds__(kBpThreads, 2)
                         constexpr int V = decltype(vc)::value;
                         auto run = [&](auto mc) {
                             constexpr int M = decltype(mc)::value;
-                            for (int j = 0; j < nv; ++j) {
-                                const FastRec P = load_fast(vb + j);
+                            auto one = [&](const FastRec& P) {
                                 adj_fan_view<V, R>(P, static_cast<unsigned>(P.mode) & ~3u,
                                                    M < 0 ? adj_xmaj(P, c) : M == 1, oxx, oyx, oxy, oyy, vx, vy, c);
+                            };
+                            int j = 0;
+                            for (; j + 2 <= nv; j += 2) {  // two views per trip
+                                const FastRec P0 = load_fast(vb + j), P1 = load_fast(vb + j + 1);
+                                one(P0);
+                                one(P1);
                             }
+                            if (j < nv) one(load_fast(vb + j));
                         };
                         if (bm == 1) run(std::integral_constant<int, 1>{});
                         else if (bm == 0) run(std::integral_constant<int, 0>{});
