@@ -904,6 +904,9 @@ __device__ __forceinline__ bool tile_forward(const float* __restrict__ proj, flo
         }
     };
 
+    // a persistent CTA calls this tile after tile: every warp must be done
+    // reading the previous tile's view records before they are overwritten
+    __syncthreads();
     // per-view parameters, windows and paths of this tile for the whole scan;
     // a fast view keeps its pair slot's address base in place of its mode
     const unsigned pairs_base = smem_u32(pairs);
