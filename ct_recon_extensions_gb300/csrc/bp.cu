@@ -832,7 +832,9 @@ int launch_tma(const float* proj, float* img, const double* t0, const double* t1
             plan_counters + (sh.bytes - counters) <= pr->scratch_bytes) {
             sh.k.counter = static_cast<int*>(pr->scratch);
             sh.k.partial = reinterpret_cast<float*>(static_cast<char*>(pr->scratch) + plan_counters);
-            kern<<<sh.ctas, kBpThreads, smem, stream>>>(proj, img, t0, t1, t2, ct, sh.k);
+            const cudaError_t e =
+                launch_dependent(kern, dim3(sh.ctas), dim3(kBpThreads), smem, stream, proj, img, t0, t1, t2, ct, sh.k);
+            if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
             return check_launch(what);
         }
         void* scratch = nullptr;
@@ -855,7 +857,8 @@ int launch_tma(const float* proj, float* img, const double* t0, const double* t1
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
     dim3 grid(tiles_x, tiles_y, batch);
-    kern<<<grid, kBpThreads, smem, stream>>>(proj, img, t0, t1, t2, ct, rec, aux);
+    e = launch_dependent(kern, grid, dim3(kBpThreads), smem, stream, proj, img, t0, t1, t2, ct, rec, aux);
+    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
     return check_launch(what);
 }
 

@@ -1050,6 +1050,7 @@ __global__ void __launch_bounds__(NG * kBpThreads, MinBlocks)
                     const double* __restrict__ t2, const TileConst c,
                     const FastRec* __restrict__ rec = nullptr, const ViewAux* __restrict__ aux = nullptr)
 {
+    grid_dep_wait();  // launched as a dependent of the kernel before it
     tile_forward<G, R, VB, NG>(proj, img, t0, t1, t2, c, blockIdx.x, blockIdx.y, blockIdx.z, 0, -1, nullptr,
                                rec, aux);
 }
@@ -1100,6 +1101,7 @@ __global__ void __launch_bounds__(NG * kBpThreads, MinBlocks)
     constexpr int kTY = (kBpThreads / 32) * R;
     constexpr int kTilePix = kTileX * kTY;
     __shared__ int s_last;
+    grid_dep_wait();  // launched as a dependent of the kernel before it
     const int ctas = static_cast<int>(gridDim.x);
     const long long U = k.units;
     const long long u0 = sk_unit_begin(blockIdx.x, ctas, U);

@@ -57,6 +57,32 @@ inline unsigned int div_up(unsigned long long a, unsigned long long b)
     return static_cast<unsigned int>((a + b - 1) / b);
 }
 
+// ---- programmatic dependent launch ------------------------------------------
+// A kernel launched with launch_dependent may be scheduled while the kernel
+// before it in the stream drains (its CTAs take the SMs the earlier grid
+// frees), which hides the launch gap between consecutive operators.  Such a
+// kernel calls grid_dep_wait() before it touches global memory: it returns
+// once the earlier grid has completed and its writes are visible (at once
+// when there is no earlier grid, or when the kernel was launched normally).
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_dependent(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                             Args&&... args)
+{
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, static_cast<Args&&>(args)...);
+}
+
 // ---- batched filtering (weight_filter.cu) -----------------------------------
 // One item of a batched weighting + ramp-filter launch.
 struct FilterJob {

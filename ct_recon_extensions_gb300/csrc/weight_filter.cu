@@ -55,6 +55,9 @@ __global__ void __launch_bounds__(kWeightThreads)
         s_w[threadIdx.x] = type == 2 ? dso * fabs(cos(atan2(s, dsd))) / dsd : dso * fabs(cos(s / dsd)) / dsd;
     }
     __syncthreads();
+    // launched as a dependent: the weights (kernel arguments only) are formed
+    // while the kernel before it drains; global memory only after this wait
+    grid_dep_wait();
     const unsigned long long r0 = static_cast<unsigned long long>(blockIdx.y) * kWeightRows;
     T v[kWeightPer];
 #pragma unroll
@@ -87,8 +90,9 @@ int launch_fan_weighting(const ctr_fan_weighting_param* p, const T* in, T* out, 
     const double cents = static_cast<double>(p->ns - 1) / 2 + p->offset;
     dim3 grid(div_up(p->ns, kWeightChannels), div_up(rows, kWeightRows));
     if (grid.y > 65535u) return fail(CTR_ERR_UNSUPPORTED, "too many rows for one launch");
-    fan_weight_kernel<T><<<grid, kWeightThreads, 0, stream>>>(in, out, p->ns, rows, p->ds, cents,
-                                                              p->dso, p->dsd, p->type);
+    const cudaError_t e = launch_dependent(fan_weight_kernel<T>, grid, dim3(kWeightThreads), 0, stream, in, out,
+                                           p->ns, rows, p->ds, cents, p->dso, p->dsd, p->type);
+    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "fan_weighting: %s", cudaGetErrorString(e));
     return check_launch("fan_weighting");
 }
 
@@ -382,6 +386,7 @@ __global__ void __launch_bounds__(kFilterMaxThreads)
                        unsigned long long rows, double ds, int tg, int spread)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    grid_dep_wait();  // launched as a dependent of the kernel before it
     unsigned long long r0, r1;
     if (spread) {
         r0 = static_cast<unsigned long long>(blockIdx.x) * rows / gridDim.x;
@@ -433,7 +438,9 @@ int launch_ramp_filter(const ctr_filter_param* p, const T* in, const double* fil
             const unsigned long long resident = static_cast<unsigned long long>(per_sm) * device_sms();
             if (rows <= kFilterRowsSpread * resident) {
                 const unsigned blocks = static_cast<unsigned>(rows < resident ? rows : resident);
-                kern<<<blocks, threads, smem, stream>>>(in, filter, out, weight, p->ns, rows, p->ds, tg, 1);
+                const cudaError_t e = launch_dependent(kern, dim3(blocks), dim3(threads), smem, stream, in, filter,
+                                                       out, weight, p->ns, rows, p->ds, tg, 1);
+                if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "ramp_filter: %s", cudaGetErrorString(e));
                 return check_launch("ramp_filter");
             }
         }
@@ -448,7 +455,9 @@ int launch_ramp_filter(const ctr_filter_param* p, const T* in, const double* fil
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "filter smem: %s", cudaGetErrorString(e));
     const unsigned blocks = div_up(rows, kFilterRowsPlain);
-    kern<<<blocks, threads, smem, stream>>>(in, filter, out, weight, p->ns, rows, p->ds, tg, 0);
+    e = launch_dependent(kern, dim3(blocks), dim3(threads), smem, stream, in, filter, out, weight, p->ns, rows,
+                         p->ds, tg, 0);
+    if (e != cudaSuccess) return fail(CTR_ERR_CUDA, "ramp_filter: %s", cudaGetErrorString(e));
     return check_launch("ramp_filter");
 }
 
