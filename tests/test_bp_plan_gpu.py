@@ -81,3 +81,25 @@ def test_bp_plan_adjoint_matches_per_call(geo):
     torch.cuda.synchronize()
     for k in range(3):
         assert rel_l2(host(got[k]), host(want[k])) <= 1e-6
+
+
+@pytest.mark.parametrize("geo", ["par", "fan"])
+def test_bp_stream_split_whole_tiles_vs_oracle(geo):
+    """Three 512^2 images in one call: 384 tiles, still a stream-split launch
+    (fewer than four waves of tiles), with more of a tile's view blocks per CTA
+    than one tile holds, so CTAs finish whole tiles and go on to the next one
+    (re-using their shared view records).  Each image against the oracle."""
+    import os
+    from oracle import Geom, Oracle
+    from ct_recon_extensions_gb300 import synthetic as syn
+    from gpu_helpers import host, rel_l2
+    d = syn.parallel_config_2() if geo == "par" else syn.fan_config_1()
+    g = Geom.make(**d)
+    op = par_op(d) if geo == "par" else fan_op(d)
+    port = Oracle("port", threads=os.cpu_count() or 1)
+    rng = np.random.default_rng(11)
+    stack = rng.standard_normal((3, d["na"], d["ns"])).astype(np.float32)
+    got = host(op.forward(cuda(stack)))
+    for k in range(3):
+        want = port.bp_par_2d(stack[k], g) if geo == "par" else port.bp_fan_2d(stack[k], g)
+        assert rel_l2(got[k], want) <= 1e-5, k
